@@ -1,0 +1,15 @@
+"""GB300-native (sm_103a) implementation of GPUSteer's per-step agent update.
+
+The compute runs in libgpusteer.so (CUDA kernels behind the C ABI declared in
+include/gpusteer.h); this package is the host-side mirror of the reference's
+group API (AgentGroup, KNNData, KNNBinData, WallGroup and the
+GroupSteerLibrary free functions), seeded scenarios and the build step.
+"""
+from ._lib import GpuSteerError, load  # noqa: F401
+from .groups import (  # noqa: F401
+    AgentGroup, KNNBinData, KNNData, WallGroup, antiPenetrationAgents, findKNearestNeighbors,
+    findKNearestNeighborsBruteForce, step, step_host, steerForAlignment, steerForCohesion,
+    steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, updateGroup,
+    updateKNNDatabase, wrapWorld)
+from .scenario import StepParams  # noqa: F401
+from .state import AgentState  # noqa: F401

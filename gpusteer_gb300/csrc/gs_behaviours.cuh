@@ -1,0 +1,251 @@
+// Per-agent steering behaviours and integration, shared by the per-behaviour
+// (drop-in) kernels and the fused step kernels.
+//
+// A behaviour is split into an accumulation over the agent's KNN list (one
+// call per neighbour, in list order) and a finalisation that applies the
+// weight, the applied-kernel bit and the add into the steering vector, exactly
+// as the reference kernel does for that agent.  The fused kernels run all
+// accumulations in a single pass over the neighbours and then finalise the
+// behaviours in the scenario's order; each accumulator sees the same operands
+// in the same order as the reference's separate kernel, so the results are
+// identical.
+#pragma once
+
+#include "gs_math.cuh"
+
+namespace gs {
+
+struct Self {
+    V3 pos, dir, side, up;
+    float speed, radius, max_speed, max_force, mass;
+};
+
+// ---- flocking: SteerFor{Separation,Alignment,Cohesion}CUDAKernel.cu -------------
+struct FlockAcc {
+    V3 sum;
+    unsigned n;
+};
+struct FlockParams {
+    float min_d, max_d, cos_max, w;
+    unsigned mask;
+};
+
+GS_HD void flock_init(FlockAcc& a) {
+    a.sum = v3(0.f, 0.f, 0.f);
+    a.n = 0;
+}
+// SteerForSeparationCUDAKernel.cu:109-116
+GS_HD void separation_add(FlockAcc& a, const FlockParams& p, V3 dir, V3 offset, float dsq,
+                          float d) {
+    if (in_boid_neighborhood(dir, offset, d, p.min_d, p.max_d, p.cos_max)) {
+        a.sum = add(a.sum, dvd(offset, -dsq));
+        a.n++;
+    }
+}
+// SteerForCohesionCUDAKernel.cu:109-117
+GS_HD void cohesion_add(FlockAcc& a, const FlockParams& p, V3 dir, V3 offset, float d, V3 bpos) {
+    if (in_boid_neighborhood(dir, offset, d, p.min_d, p.max_d, p.cos_max)) {
+        a.sum = add(a.sum, bpos);
+        a.n++;
+    }
+}
+// SteerForAlignmentCUDAKernel.cu:110-118
+GS_HD void alignment_add(FlockAcc& a, const FlockParams& p, V3 dir, V3 offset, float d, V3 bdir) {
+    if (in_boid_neighborhood(dir, offset, d, p.min_d, p.max_d, p.cos_max)) {
+        a.sum = add(a.sum, bdir);
+        a.n++;
+    }
+}
+// kind 0 separation, 1 alignment, 2 cohesion (…CUDAKernel.cu:119-134 of each).
+GS_HD void flock_finish(int kind, const FlockAcc& a, const FlockParams& p, const Self& s,
+                        unsigned& applied, V3& steer) {
+    if (applied & p.mask) return;
+    V3 r = a.sum;
+    if (a.n > 0) {
+        const V3 mean = dvd(a.sum, float(a.n));
+        if (kind == 0) r = normalize(mean);
+        else if (kind == 1) r = normalize(sub(mean, s.dir));
+        else r = normalize(sub(mean, s.pos));
+    }
+    r = mul(r, p.w);
+    const unsigned bit = kind == 0 ? SEPARATION_BIT : kind == 1 ? ALIGNMENT_BIT : COHESION_BIT;
+    if (!is_zero(r)) applied |= bit;
+    steer = add(r, steer);
+}
+
+// ---- SteerForSeekCUDAKernel.cu:41-71 ------------------------------------------------
+GS_HD void seek_finish(V3 target, float w, unsigned mask, const Self& s, unsigned& applied,
+                       V3& steer) {
+    if (applied & mask) return;
+    const V3 desired = sub(target, s.pos);
+    V3 r = sub(desired, s.dir);
+    r = mul(normalize(r), w);
+    if (!is_zero(r)) applied |= SEEK_BIT;
+    steer = add(r, steer);
+}
+
+// ---- SteerToAvoidCloseNeighborsCUDAKernel (SteerToAvoidNeighborsCUDAKernel.cu:93-187)
+struct CloseAcc {
+    bool found;
+    V3 steer;
+};
+GS_HD void close_init(CloseAcc& a) {
+    a.found = false;
+    a.steer = v3(0.f, 0.f, 0.f);
+}
+// knn_dist is the KNN distance of this list entry, not a recomputed one.
+GS_HD void close_add(CloseAcc& a, const Self& s, float min_sep, float knn_dist, V3 bpos,
+                     float bradius) {
+    if (a.found) return;
+    const float sum_radii = s.radius + bradius;
+    const float min_c2c = min_sep + sum_radii;
+    if (knn_dist < min_c2c) {
+        const V3 offset = sub(bpos, s.pos);
+        a.steer = perpendicular_component(neg(offset), s.dir);
+        a.found = true;
+    }
+}
+GS_HD void close_finish(const CloseAcc& a, float w, unsigned mask, unsigned& applied, V3& steer) {
+    if (applied & mask) return;
+    const V3 r = mul(normalize(a.steer), w);
+    if (!is_zero(r)) applied |= AVOID_CLOSE_NEIGHBORS_BIT;
+    steer = add(r, steer);
+}
+
+// ---- SteerToAvoidNeighborsCUDAKernel (SteerToAvoidNeighborsCUDAKernel.cu:259-401) ---
+struct AvoidAcc {
+    float min_t;
+    unsigned threat;
+    V3 threat_at, threat_dir, threat_pos;
+    float threat_speed;
+};
+GS_HD void avoid_init(AvoidAcc& a, float min_time) {
+    a.min_t = min_time;
+    a.threat = UINT_MAX;
+    a.threat_at = a.threat_dir = a.threat_pos = v3(0.f, 0.f, 0.f);
+    a.threat_speed = 0.f;
+}
+// `threat_at` keeps the nearest-approach position of the last candidate that
+// passed the time test, as in the reference (:330-340).
+GS_HD void avoid_add(AvoidAcc& a, const Self& s, unsigned bid, V3 bpos, V3 bdir, float bspeed,
+                     float bradius) {
+    const float danger = s.radius + bradius;
+    const float time = nearest_approach_time(s.pos, s.dir, s.speed, bpos, bdir, bspeed);
+    if (time >= 0.f && time < a.min_t) {
+        if (nearest_approach_positions(s.pos, s.dir, s.speed, bpos, bdir, bspeed, time,
+                                       a.threat_at) < danger) {
+            a.min_t = time;
+            a.threat = bid;
+            a.threat_dir = bdir;
+            a.threat_speed = bspeed;
+            a.threat_pos = bpos;  // the reference reads an uninitialised variable here
+        }
+    }
+}
+GS_HD void avoid_finish(const AvoidAcc& a, float w, unsigned mask, const Self& s,
+                        unsigned& applied, V3& steer) {
+    if (applied & (mask | AVOID_CLOSE_NEIGHBORS_BIT)) return;  // SteerToAvoidNeighborsCUDA.cu:159
+    if (a.threat == UINT_MAX) return;
+    const float parallelness = dot(s.dir, a.threat_dir);
+    const float angle = 0.707f;
+    float st = 0.f;
+    if (parallelness < -angle) {
+        const V3 offset = sub(a.threat_at, s.pos);
+        st = (dot(offset, s.side) > 0.f) ? -1.f : 1.f;
+    } else if (parallelness > angle) {
+        const V3 offset = sub(a.threat_pos, s.pos);
+        st = (dot(offset, s.side) > 0.f) ? -1.f : 1.f;
+    } else if (s.speed <= a.threat_speed) {
+        const float side_dot = dot(s.side, mul(a.threat_dir, a.threat_speed));
+        st = (side_dot > 0.f) ? -1.f : 1.f;
+    }
+    V3 r = mul(s.side, st);
+    r = mul(normalize(r), w);
+    if (!is_zero(r)) applied |= AVOID_NEIGHBORS_BIT;
+    steer = add(r, steer);
+}
+
+// ---- SteerToAvoidWallsCUDAKernel (AvoidWallsCUDAKernel.cu:89-244) -----------------
+struct WallAcc {
+    V3 feelers[3];
+    unsigned feeler_index;
+    float nearest_d;
+    unsigned nearest_line;
+    V3 nearest_ip, nearest_normal;
+    bool touching;
+};
+GS_HD void walls_init(WallAcc& a, const Self& s, float min_time) {
+    const float fl = 4.f * s.radius;  // FEELER_LENGTH * radius (AvoidWallsCUDAKernel.cu:41)
+    const V3 vel = mul(s.dir, s.speed);
+    a.feelers[0] = add(s.pos, mul(vel, min_time));
+    a.feelers[1] = add(s.pos, add(mul(s.side, fl), mul(s.dir, fl)));
+    a.feelers[2] = add(s.pos, add(mul(neg(s.side), fl), mul(s.dir, fl)));
+    a.feeler_index = 0;
+    a.nearest_d = FLT_MAX;
+    a.nearest_line = UINT_MAX;
+    a.nearest_ip = a.nearest_normal = v3(0.f, 0.f, 0.f);
+    a.touching = false;
+}
+GS_HD void walls_add(WallAcc& a, const Self& s, unsigned line, V3 ls, V3 le, V3 ln) {
+    V3 ip = v3(0.f, 0.f, 0.f);
+    const V3 closest = add(s.pos, mul(neg(ln), s.radius));
+    if (lines_intersect(s.pos, closest, ls, le, ip)) {
+        a.touching = true;
+        a.nearest_normal = ln;
+        a.nearest_d = distance(s.pos, ip);
+    }
+#pragma unroll
+    for (unsigned f = 0; f < 3; ++f) {
+        if (lines_intersect(s.pos, a.feelers[f], ls, le, ip)) {
+            const float d = distance(s.pos, ip);
+            if (d < a.nearest_d) {
+                a.nearest_d = d;
+                a.nearest_line = line;
+                a.nearest_ip = ip;
+                a.feeler_index = f;
+                a.nearest_normal = ln;
+            }
+        }
+    }
+}
+// Applies the result: may move the agent (anti-penetration) and adds the
+// weighted wall steering.  Returns false when masked (nothing changes).
+GS_HD bool walls_finish(const WallAcc& a, float w, unsigned mask, Self& s, unsigned& applied,
+                        V3& steer) {
+    if (applied & mask) return false;
+    V3 r = v3(0.f, 0.f, 0.f);
+    if (a.touching) {
+        const float pen = s.radius - a.nearest_d;
+        s.pos = add(s.pos, mul(a.nearest_normal, pen));
+        s.dir = normalize(perpendicular_component(s.dir, a.nearest_normal));
+        applied |= ANTI_PENETRATION_WALL;
+    } else if (a.nearest_line != UINT_MAX) {
+        const V3 f = a.feeler_index == 0 ? a.feelers[0]
+                     : a.feeler_index == 1 ? a.feelers[1] : a.feelers[2];
+        const float pen = length(sub(f, a.nearest_ip));
+        r = mul(a.nearest_normal, pen);
+        applied |= AVOID_WALLS_BIT;
+    }
+    r = mul(r, w);
+    steer = add(r, steer);
+    return true;
+}
+
+// ---- UpdateCUDAKernel.cu:78-123 -----------------------------------------------------
+// A new speed of 0 keeps the previous side vector (the reference writes back
+// uninitialised shared memory there).
+GS_HD void integrate(Self& s, V3 steer, float dt) {
+    steer = truncate_length(steer, s.max_force);
+    const V3 acc = dvd(steer, s.mass);
+    V3 vel = add(mul(s.dir, s.speed), mul(acc, dt));
+    vel = truncate_length(vel, s.max_speed);
+    s.speed = length(vel);
+    if (s.speed > 0.f) {
+        s.dir = dvd(vel, s.speed);
+        s.side = normalize(cross(s.dir, s.up));
+        s.up = cross(s.side, s.dir);
+    }
+    s.pos = add(s.pos, mul(vel, dt));
+}
+
+}  // namespace gs

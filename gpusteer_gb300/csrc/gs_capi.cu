@@ -1,0 +1,906 @@
+// C ABI of libgpusteer (include/gpusteer.h): handle management, host <-> device
+// transfers, the GroupSteerLibrary.cuh free functions and the fused step.
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <list>
+#include <new>
+#include <string>
+
+#include "gs_launch.h"
+
+namespace gs {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+gs_status fail(gs_status s, const std::string& msg) {
+    set_error(msg);
+    return s;
+}
+
+gs_status cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return GS_ERR_CUDA;
+}
+
+static GroupView view(gs_group g) {
+    return GroupView{g->position, g->direction, g->steering, g->side, g->up, g->speed,
+                     g->max_speed, g->max_force, g->radius, g->mass, g->applied, g->n};
+}
+static OtherView other_view(gs_group g) {
+    return OtherView{g->position, g->direction, g->speed, g->radius, g->applied, g->n};
+}
+
+static void release_fused(gs_group g) {
+    for (int j = 0; j < 6; ++j) {
+        dfree(g->A.f[j]);
+        dfree(g->B.f[j]);
+    }
+    dfree(g->cellrank);
+    dfree(g->w0);
+    dfree(g->w1);
+    dfree(g->w2);
+    dfree(g->knn_slot);
+    dfree(g->knn_dist);
+    dfree(g->d_scene);
+    db_release(g->fdb);
+    g->fused_k_alloc = 0;
+}
+
+// Brings the reference-layout arrays up to date after fused steps.
+static gs_status ensure_reference(gs_group g) {
+    if (!g->fused_current) return GS_OK;
+    GS_TRY(fused_to_reference(g->A, g->n, g->d_scene, view(g), g->stream));
+    g->fused_current = false;
+    g->db.valid = false;
+    return GS_OK;
+}
+
+// Marks the reference-layout arrays as modified by a per-function call.
+static void touched(gs_group g) {
+    g->fused_current = false;
+    g->accum_dirty = true;
+}
+
+static bool finite3(const float* v) {
+    return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
+}
+
+static gs_status check_grid(const unsigned wc[3], const float ws[3], Grid& g, unsigned& cells) {
+    unsigned long long c = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (wc[a] == 0) return fail(GS_ERR_INVALID_ARG, "world cells must be positive");
+        if (!(ws[a] > 0.f) || !std::isfinite(ws[a]))
+            return fail(GS_ERR_INVALID_ARG, "world size must be positive and finite");
+        c *= wc[a];
+        g.wc[a] = wc[a];
+        g.ws[a] = ws[a];
+    }
+    if (c > (1ull << 30)) return fail(GS_ERR_INVALID_ARG, "too many cells");
+    cells = unsigned(c);
+    return GS_OK;
+}
+
+// ---- walls: WallGroupData::LoadFromFile / SplitWalls --------------------------------
+struct Segment {
+    V3 s, m, e, n;
+};
+
+// WallGroupData::intersects (WallGroupData.cu:28-71): entry point of a
+// segment into an axis-aligned box, or false.
+static bool enters_box(V3 start, V3 end, V3 lo, V3 hi, V3& ip) {
+    const float si[3] = {start.x, start.y, start.z}, ei[3] = {end.x, end.y, end.z};
+    const float bmin[3] = {lo.x, lo.y, lo.z}, bmax[3] = {hi.x, hi.y, hi.z};
+    float fst = 0.f, fet = 1.f;
+    for (int a = 0; a < 3; ++a) {
+        float st, et;
+        const float di = ei[a] - si[a];
+        if (si[a] < ei[a]) {
+            if (si[a] > bmax[a] || ei[a] < bmin[a]) return false;
+            st = (si[a] < bmin[a]) ? (bmin[a] - si[a]) / di : 0.f;
+            et = (ei[a] > bmax[a]) ? (bmax[a] - si[a]) / di : 1.f;
+        } else {
+            if (ei[a] > bmax[a] || si[a] < bmin[a]) return false;
+            st = (si[a] > bmax[a]) ? (bmax[a] - si[a]) / di : 0.f;
+            et = (ei[a] < bmin[a]) ? (bmin[a] - si[a]) / di : 1.f;
+        }
+        fst = st > fst ? st : fst;
+        fet = et < fet ? et : fet;
+        if (fet < fst) return false;
+    }
+    ip = add(start, mul(sub(end, start), fst));
+    return true;
+}
+
+// WallGroupData::SplitWalls (WallGroupData.cu:108-206): every segment that
+// enters a cell (in bin_cell order) at a point more than EPSILON from both
+// ends is replaced by its two halves, appended to the list and split in turn.
+// Cells that cannot intersect (outside the segment's bounding box grown by one
+// cell) are skipped; the first intersecting cell in bin_cell order is
+// unchanged by that.
+static std::vector<Segment> split_walls(const std::vector<Segment>& in, const Grid& g) {
+    const V3 step = v3(g.ws[0] / float(g.wc[0]), g.ws[1] / float(g.wc[1]), g.ws[2] / float(g.wc[2]));
+    const float steps[3] = {step.x, step.y, step.z};
+    auto cell_lo = [&](unsigned ix, unsigned iy, unsigned iz) {
+        return v3(float(ix) * step.x - 0.5f * g.ws[0], float(iy) * step.y - 0.5f * g.ws[1],
+                  float(iz) * step.z - 0.5f * g.ws[2]);
+    };
+    auto axis_range = [&](float a, float b, int axis, unsigned& i0, unsigned& i1) {
+        const double lo = std::min(a, b), hi = std::max(a, b);
+        const double half = 0.5 * double(g.ws[axis]);
+        const double first = std::floor((lo + half) / steps[axis]) - 1.0;
+        const double last = std::floor((hi + half) / steps[axis]) + 1.0;
+        const double top = double(g.wc[axis]) - 1.0;
+        if (last < 0.0 || first > top) return false;
+        i0 = unsigned(first < 0.0 ? 0.0 : first);
+        i1 = unsigned(last > top ? top : last);
+        return true;
+    };
+    std::list<Segment> segs(in.begin(), in.end());
+    const float eps = 0.001f;
+    for (auto it = segs.begin(); it != segs.end();) {
+        const V3 s = it->s, e = it->e;
+        bool split = false;
+        unsigned x0, x1, y0, y1, z0, z1;
+        if (axis_range(s.x, e.x, 0, x0, x1) && axis_range(s.y, e.y, 1, y0, y1) &&
+            axis_range(s.z, e.z, 2, z0, z1)) {
+            for (unsigned iy = y0; iy <= y1 && !split; ++iy)
+                for (unsigned iz = z0; iz <= z1 && !split; ++iz)
+                    for (unsigned ix = x0; ix <= x1 && !split; ++ix) {
+                        const V3 lo = cell_lo(ix, iy, iz);
+                        V3 ip;
+                        if (!enters_box(s, e, lo, add(lo, step), ip)) continue;
+                        if (distance(s, ip) > eps && distance(ip, e) > eps) {
+                            segs.push_back(Segment{s, add(s, mul(sub(ip, s), 0.5f)), ip, it->n});
+                            segs.push_back(Segment{ip, add(ip, mul(sub(e, ip), 0.5f)), e, it->n});
+                            split = true;
+                        }
+                    }
+        }
+        if (split) it = segs.erase(it);
+        else ++it;
+    }
+    return std::vector<Segment>(segs.begin(), segs.end());
+}
+
+static gs_status make_walls(const std::vector<Segment>& raw, gs_bins bins, unsigned knw,
+                            gs_walls* out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "null output handle");
+    if (knw == 0 || knw > 8) return fail(GS_ERR_INVALID_ARG, "knw must be in 1..8");
+    std::vector<Segment> segs = bins ? split_walls(raw, bins->grid) : raw;
+    gs_walls w = new (std::nothrow) gs_walls_s();
+    if (!w) return fail(GS_ERR_OOM, "host allocation failed");
+    w->n = unsigned(segs.size());
+    w->knw = knw;
+    auto put = [](std::vector<float>& v, V3 a) {
+        v.push_back(a.x);
+        v.push_back(a.y);
+        v.push_back(a.z);
+        v.push_back(0.f);
+    };
+    for (const Segment& s : segs) {
+        put(w->h_start, s.s);
+        put(w->h_mid, s.m);
+        put(w->h_end, s.e);
+        put(w->h_normal, s.n);
+    }
+    gs_status st = GS_OK;
+    if (w->n > 0) {
+        st = dalloc(&w->start, w->n);
+        if (st == GS_OK) st = dalloc(&w->mid, w->n);
+        if (st == GS_OK) st = dalloc(&w->end, w->n);
+        if (st == GS_OK) st = dalloc(&w->normal, w->n);
+        if (st == GS_OK) {
+            const size_t bytes = size_t(w->n) * sizeof(float4);
+            cudaError_t e = cudaMemcpy(w->start, w->h_start.data(), bytes, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(w->mid, w->h_mid.data(), bytes, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(w->end, w->h_end.data(), bytes, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess)
+                e = cudaMemcpy(w->normal, w->h_normal.data(), bytes, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) st = cuda_fail(e, "wall upload");
+        }
+    }
+    if (st != GS_OK) {
+        gs_walls_destroy(w);
+        return st;
+    }
+    *out = w;
+    return GS_OK;
+}
+
+static gs_status walls_db(gs_walls w, const Grid& grid, unsigned C, cudaStream_t stream) {
+    const bool same = w->db.valid && w->db.cells == C &&
+                      std::memcmp(&w->db.grid, &grid, sizeof(Grid)) == 0;
+    if (same) return GS_OK;
+    GS_TRY(db_reserve(w->db, w->n, C));
+    GS_TRY(db_build(w->db, w->mid, w->n, grid, stream));
+    // later users may run on other streams
+    GS_CUDA(cudaStreamSynchronize(stream));
+    return GS_OK;
+}
+
+static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev& d) {
+    if (!p) return fail(GS_ERR_INVALID_ARG, "null step parameters");
+    if (p->knn_mode != GS_KNN_BINNED)
+        return fail(GS_ERR_UNSUPPORTED, "the fused step uses binned KNN");
+    if (p->k == 0 || p->k > 32) return fail(GS_ERR_INVALID_ARG, "fused step needs 1 <= k <= 32");
+    if (p->wrap_mode < 0 || p->wrap_mode > 2) return fail(GS_ERR_INVALID_ARG, "bad wrap mode");
+    if (p->n_order > 8) return fail(GS_ERR_INVALID_ARG, "at most 8 behaviours");
+    if (!std::isfinite(p->dt)) return fail(GS_ERR_NONFINITE, "dt is not finite");
+    std::memset(&d, 0, sizeof(d));
+    d.k = p->k;
+    d.knw = p->knw;
+    d.r = p->search_radius;
+    d.wrap_mode = p->wrap_mode;
+    d.clear_applied = p->clear_applied;
+    auto fl = [](float* out, float a, float b, float c, float w, unsigned m) {
+        out[0] = a;
+        out[1] = b;
+        out[2] = c;
+        out[3] = w;
+        std::memcpy(&out[4], &m, 4);
+    };
+    fl(d.sep, p->sep_min, p->sep_max, p->sep_cos, p->w_sep, p->mask_sep);
+    fl(d.ali, p->ali_min, p->ali_max, p->ali_cos, p->w_ali, p->mask_ali);
+    fl(d.coh, p->coh_min, p->coh_max, p->coh_cos, p->w_coh, p->mask_coh);
+    std::memcpy(d.seek_target, p->seek_target, sizeof(d.seek_target));
+    d.w_seek = p->w_seek;
+    d.mask_seek = p->mask_seek;
+    d.min_time_wall = p->min_time_to_wall;
+    d.w_walls = p->w_walls;
+    d.mask_walls = p->mask_walls;
+    d.min_time_col = p->min_time_to_collision;
+    d.min_sep = p->min_separation_distance;
+    d.avoid_close = p->avoid_close;
+    d.w_avoid = p->w_avoid;
+    d.mask_avoid = p->mask_avoid;
+    d.n_order = p->n_order;
+    d.dt = p->dt;
+    for (unsigned o = 0; o < p->n_order; ++o) {
+        const unsigned b = p->order[o];
+        d.order[o] = b;
+        switch (b) {
+            case GS_B_AVOID_WALLS:
+                if (o != 0)
+                    return fail(GS_ERR_UNSUPPORTED, "the fused step needs avoid-walls first");
+                d.need |= NEED_WALLS;
+                break;
+            case GS_B_AVOID_NEIGHBORS:
+                d.need |= NEED_AVOID | (p->avoid_close ? NEED_CLOSE : 0u);
+                break;
+            case GS_B_SEPARATION: d.need |= NEED_SEP; break;
+            case GS_B_ALIGNMENT: d.need |= NEED_ALI; break;
+            case GS_B_COHESION: d.need |= NEED_COH; break;
+            case GS_B_SEEK: break;
+            default: return fail(GS_ERR_INVALID_ARG, "unknown behaviour code");
+        }
+    }
+    if ((d.need & NEED_WALLS) && (p->knw == 0 || p->knw > 8))
+        return fail(GS_ERR_INVALID_ARG, "knw must be in 1..8");
+    (void)walls;
+    return GS_OK;
+}
+
+}  // namespace gs
+
+using namespace gs;
+
+extern "C" {
+
+const char* gs_status_string(gs_status s) {
+    switch (s) {
+        case GS_OK: return "ok";
+        case GS_ERR_INVALID_ARG: return "invalid argument";
+        case GS_ERR_OOM: return "out of memory";
+        case GS_ERR_CUDA: return "CUDA error";
+        case GS_ERR_TIMEOUT: return "timeout";
+        case GS_ERR_NONFINITE: return "non-finite value";
+        case GS_ERR_STATE: return "invalid state";
+        case GS_ERR_UNSUPPORTED: return "unsupported";
+        default: return "unknown status";
+    }
+}
+
+const char* gs_last_error(void) { return g_last_error.c_str(); }
+int gs_version(void) { return 1; }
+unsigned gs_max_k(void) { return kMaxK; }
+
+// ---- bins -----------------------------------------------------------------------
+gs_status gs_bins_create(const unsigned world_cells[3], const float world_size[3],
+                         unsigned search_radius, gs_bins* out) {
+    if (!out || !world_cells || !world_size) return fail(GS_ERR_INVALID_ARG, "null argument");
+    Grid g;
+    unsigned cells;
+    GS_TRY(check_grid(world_cells, world_size, g, cells));
+    gs_bins b = new (std::nothrow) gs_bins_s();
+    if (!b) return fail(GS_ERR_OOM, "host allocation failed");
+    b->grid = g;
+    b->radius = search_radius;
+    b->cells = cells;
+    *out = b;
+    return GS_OK;
+}
+
+gs_status gs_bins_destroy(gs_bins bins) {
+    delete bins;
+    return GS_OK;
+}
+
+gs_status gs_bins_num_cells(gs_bins bins, unsigned* out) {
+    if (!bins || !out) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *out = bins->cells;
+    return GS_OK;
+}
+
+gs_status gs_bins_get_cells(gs_bins bins, float* min3, float* max3, float* centre3, unsigned cap) {
+    if (!bins) return fail(GS_ERR_INVALID_ARG, "null bins");
+    if (cap < bins->cells) return fail(GS_ERR_INVALID_ARG, "output too small");
+    const Grid& g = bins->grid;
+    const float sx = g.ws[0] / float(g.wc[0]), sy = g.ws[1] / float(g.wc[1]),
+                sz = g.ws[2] / float(g.wc[2]);
+    unsigned i = 0;
+    for (unsigned iy = 0; iy < g.wc[1]; ++iy)
+        for (unsigned iz = 0; iz < g.wc[2]; ++iz)
+            for (unsigned ix = 0; ix < g.wc[0]; ++ix, ++i) {
+                const float lo[3] = {float(ix) * sx - 0.5f * g.ws[0], float(iy) * sy - 0.5f * g.ws[1],
+                                     float(iz) * sz - 0.5f * g.ws[2]};
+                const float st[3] = {sx, sy, sz};
+                for (int a = 0; a < 3; ++a) {
+                    if (min3) min3[3 * i + a] = lo[a];
+                    if (max3) max3[3 * i + a] = lo[a] + st[a];
+                    if (centre3) centre3[3 * i + a] = lo[a] + 0.5f * st[a];
+                }
+            }
+    return GS_OK;
+}
+
+// ---- groups -----------------------------------------------------------------------
+gs_status gs_group_destroy(gs_group g) {
+    if (!g) return GS_OK;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    dfree(g->position);
+    dfree(g->direction);
+    dfree(g->steering);
+    dfree(g->side);
+    dfree(g->up);
+    dfree(g->speed);
+    dfree(g->max_speed);
+    dfree(g->max_force);
+    dfree(g->radius);
+    dfree(g->mass);
+    dfree(g->applied);
+    db_release(g->db);
+    release_fused(g);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return GS_OK;
+}
+
+gs_status gs_group_create(unsigned k, unsigned capacity, void* stream, gs_group* out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "null output handle");
+    if (k == 0 || k > kMaxK) return fail(GS_ERR_INVALID_ARG, "k must be in 1..64");
+    if (capacity == 0 || capacity > (1u << 30)) return fail(GS_ERR_INVALID_ARG, "bad capacity");
+    gs_group g = new (std::nothrow) gs_group_s();
+    if (!g) return fail(GS_ERR_OOM, "host allocation failed");
+    std::memset(static_cast<void*>(g), 0, sizeof(*g));
+    new (&g->db) Database();
+    new (&g->fdb) Database();
+    g->k = k;
+    g->capacity = capacity;
+    gs_status s = GS_OK;
+    if (stream) {
+        g->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamCreate");
+        g->own_stream = true;
+    }
+    const size_t n = capacity;
+    if (s == GS_OK) s = dalloc(&g->position, n);
+    if (s == GS_OK) s = dalloc(&g->direction, n);
+    if (s == GS_OK) s = dalloc(&g->steering, n);
+    if (s == GS_OK) s = dalloc(&g->side, n);
+    if (s == GS_OK) s = dalloc(&g->up, n);
+    if (s == GS_OK) s = dalloc(&g->speed, n);
+    if (s == GS_OK) s = dalloc(&g->max_speed, n);
+    if (s == GS_OK) s = dalloc(&g->max_force, n);
+    if (s == GS_OK) s = dalloc(&g->radius, n);
+    if (s == GS_OK) s = dalloc(&g->mass, n);
+    if (s == GS_OK) s = dalloc(&g->applied, n);
+    if (s != GS_OK) {
+        const std::string msg = g_last_error;
+        gs_group_destroy(g);
+        set_error(msg);
+        return s;
+    }
+    *out = g;
+    return GS_OK;
+}
+
+gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
+    if (!g || !h) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (n > g->capacity) return fail(GS_ERR_INVALID_ARG, "more agents than the group's capacity");
+    if (!h->position || !h->direction || !h->steering || !h->side || !h->up || !h->speed ||
+        !h->max_speed || !h->max_force || !h->radius || !h->mass || !h->applied)
+        return fail(GS_ERR_INVALID_ARG, "upload needs every array");
+    cudaStream_t st = g->stream;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    const size_t f4b = size_t(n) * 16, f3b = size_t(n) * 12, f1b = size_t(n) * 4;
+    cudaError_t e = cp(g->position, h->position, f4b);
+    if (e == cudaSuccess) e = cp(g->direction, h->direction, f4b);
+    if (e == cudaSuccess) e = cp(g->steering, h->steering, f4b);
+    if (e == cudaSuccess) e = cp(g->side, h->side, f3b);
+    if (e == cudaSuccess) e = cp(g->up, h->up, f3b);
+    if (e == cudaSuccess) e = cp(g->speed, h->speed, f1b);
+    if (e == cudaSuccess) e = cp(g->max_speed, h->max_speed, f1b);
+    if (e == cudaSuccess) e = cp(g->max_force, h->max_force, f1b);
+    if (e == cudaSuccess) e = cp(g->radius, h->radius, f1b);
+    if (e == cudaSuccess) e = cp(g->mass, h->mass, f1b);
+    if (e == cudaSuccess) e = cp(g->applied, h->applied, f1b);
+    if (e != cudaSuccess) return cuda_fail(e, "upload");
+    g->n = n;
+    g->db.valid = false;
+    touched(g);
+    return GS_OK;
+}
+
+gs_status gs_group_download(gs_group g, const gs_agent_arrays* h) {
+    if (!g || !h) return fail(GS_ERR_INVALID_ARG, "null argument");
+    GS_TRY(ensure_reference(g));
+    cudaStream_t st = g->stream;
+    const unsigned n = g->n;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        if (!dst || bytes == 0) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+    };
+    const size_t f4b = size_t(n) * 16, f3b = size_t(n) * 12, f1b = size_t(n) * 4;
+    cudaError_t e = cp(h->position, g->position, f4b);
+    if (e == cudaSuccess) e = cp(h->direction, g->direction, f4b);
+    if (e == cudaSuccess) e = cp(h->steering, g->steering, f4b);
+    if (e == cudaSuccess) e = cp(h->side, g->side, f3b);
+    if (e == cudaSuccess) e = cp(h->up, g->up, f3b);
+    if (e == cudaSuccess) e = cp(h->speed, g->speed, f1b);
+    if (e == cudaSuccess) e = cp(h->max_speed, g->max_speed, f1b);
+    if (e == cudaSuccess) e = cp(h->max_force, g->max_force, f1b);
+    if (e == cudaSuccess) e = cp(h->radius, g->radius, f1b);
+    if (e == cudaSuccess) e = cp(h->mass, g->mass, f1b);
+    if (e == cudaSuccess) e = cp(h->applied, g->applied, f1b);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "download");
+    return GS_OK;
+}
+
+gs_status gs_group_size(gs_group g, unsigned* n) {
+    if (!g || !n) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *n = g->n;
+    return GS_OK;
+}
+
+gs_status gs_group_device_arrays(gs_group g, gs_agent_arrays* d) {
+    if (!g || !d) return fail(GS_ERR_INVALID_ARG, "null argument");
+    GS_TRY(ensure_reference(g));
+    d->position = reinterpret_cast<float*>(g->position);
+    d->direction = reinterpret_cast<float*>(g->direction);
+    d->steering = reinterpret_cast<float*>(g->steering);
+    d->side = reinterpret_cast<float*>(g->side);
+    d->up = reinterpret_cast<float*>(g->up);
+    d->speed = g->speed;
+    d->max_speed = g->max_speed;
+    d->max_force = g->max_force;
+    d->radius = g->radius;
+    d->mass = g->mass;
+    d->applied = g->applied;
+    // The caller may write through these pointers.
+    touched(g);
+    g->db.valid = false;
+    return GS_OK;
+}
+
+gs_status gs_group_stream(gs_group g, void** stream) {
+    if (!g || !stream) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *stream = g->stream;
+    return GS_OK;
+}
+
+gs_status gs_group_synchronize(gs_group g) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    GS_CUDA(cudaStreamSynchronize(g->stream));
+    return GS_OK;
+}
+
+// ---- KNN data -----------------------------------------------------------------------
+gs_status gs_knn_create(unsigned n, unsigned k, gs_knn* out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "null output handle");
+    if (k == 0 || k > kMaxK) return fail(GS_ERR_INVALID_ARG, "k must be in 1..64");
+    gs_knn kd = new (std::nothrow) gs_knn_s();
+    if (!kd) return fail(GS_ERR_OOM, "host allocation failed");
+    kd->n = n;
+    kd->k = k;
+    kd->idx = nullptr;
+    kd->dist = nullptr;
+    gs_status s = dalloc(&kd->idx, size_t(n) * k);
+    if (s == GS_OK) s = dalloc(&kd->dist, size_t(n) * k);
+    if (s != GS_OK) {
+        gs_knn_destroy(kd);
+        return s;
+    }
+    *out = kd;
+    return GS_OK;
+}
+
+gs_status gs_knn_destroy(gs_knn kd) {
+    if (!kd) return GS_OK;
+    dfree(kd->idx);
+    dfree(kd->dist);
+    delete kd;
+    return GS_OK;
+}
+
+gs_status gs_knn_download(gs_knn kd, gs_group g, unsigned* idx, float* dist) {
+    if (!kd) return fail(GS_ERR_INVALID_ARG, "null knn");
+    cudaStream_t st = g ? g->stream : nullptr;
+    const size_t cnt = size_t(kd->n) * kd->k;
+    if (idx) GS_CUDA(cudaMemcpyAsync(idx, kd->idx, cnt * 4, cudaMemcpyDeviceToHost, st));
+    if (dist) GS_CUDA(cudaMemcpyAsync(dist, kd->dist, cnt * 4, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    return GS_OK;
+}
+
+gs_status gs_knn_device_arrays(gs_knn kd, unsigned** idx, float** dist) {
+    if (!kd) return fail(GS_ERR_INVALID_ARG, "null knn");
+    if (idx) *idx = kd->idx;
+    if (dist) *dist = kd->dist;
+    return GS_OK;
+}
+
+// ---- walls -----------------------------------------------------------------------
+gs_status gs_walls_create(const float* start4, const float* end4, const float* normal4,
+                          unsigned n, gs_bins bins, unsigned knw, gs_walls* out) {
+    if (n > 0 && (!start4 || !end4 || !normal4)) return fail(GS_ERR_INVALID_ARG, "null arrays");
+    std::vector<Segment> raw(n);
+    for (unsigned i = 0; i < n; ++i) {
+        raw[i].s = v3(start4[4 * i], start4[4 * i + 1], start4[4 * i + 2]);
+        raw[i].e = v3(end4[4 * i], end4[4 * i + 1], end4[4 * i + 2]);
+        raw[i].n = v3(normal4[4 * i], normal4[4 * i + 1], normal4[4 * i + 2]);
+        // WallGroupData.cu:87-89
+        raw[i].m = v3(0.5f * (raw[i].s.x + raw[i].e.x), 0.5f * (raw[i].s.y + raw[i].e.y),
+                      0.5f * (raw[i].s.z + raw[i].e.z));
+    }
+    return make_walls(raw, bins, knw, out);
+}
+
+gs_status gs_walls_load(const char* path, gs_bins bins, unsigned knw, gs_walls* out) {
+    if (!path) return fail(GS_ERR_INVALID_ARG, "null path");
+    std::ifstream in(path);
+    if (!in.is_open()) return fail(GS_ERR_INVALID_ARG, std::string("cannot open ") + path);
+    std::vector<float> s4, e4, n4;
+    for (;;) {
+        float v[9];
+        for (float& x : v) in >> x;
+        if (!in.good()) break;
+        s4.insert(s4.end(), {v[0], v[1], v[2], 0.f});
+        e4.insert(e4.end(), {v[3], v[4], v[5], 0.f});
+        n4.insert(n4.end(), {v[6], v[7], v[8], 0.f});
+    }
+    return gs_walls_create(s4.data(), e4.data(), n4.data(), unsigned(s4.size() / 4), bins, knw,
+                           out);
+}
+
+gs_status gs_walls_destroy(gs_walls w) {
+    if (!w) return GS_OK;
+    dfree(w->start);
+    dfree(w->mid);
+    dfree(w->end);
+    dfree(w->normal);
+    db_release(w->db);
+    delete w;
+    return GS_OK;
+}
+
+gs_status gs_walls_size(gs_walls w, unsigned* n) {
+    if (!w || !n) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *n = w->n;
+    return GS_OK;
+}
+
+gs_status gs_walls_download(gs_walls w, float* start4, float* mid4, float* end4, float* normal4,
+                            unsigned cap) {
+    if (!w) return fail(GS_ERR_INVALID_ARG, "null walls");
+    if (cap < w->n) return fail(GS_ERR_INVALID_ARG, "output too small");
+    const size_t bytes = size_t(w->n) * 4 * sizeof(float);
+    if (start4) std::memcpy(start4, w->h_start.data(), bytes);
+    if (mid4) std::memcpy(mid4, w->h_mid.data(), bytes);
+    if (end4) std::memcpy(end4, w->h_end.data(), bytes);
+    if (normal4) std::memcpy(normal4, w->h_normal.data(), bytes);
+    return GS_OK;
+}
+
+// ---- GroupSteerLibrary ------------------------------------------------------------
+gs_status gs_wrap_world(gs_group g, const float world_size[3], int mode) {
+    if (!g || !world_size) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (mode < 0 || mode > 2) return fail(GS_ERR_INVALID_ARG, "bad wrap mode");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_wrap(g->position, g->n, world_size, mode, g->stream));
+    touched(g);
+    return GS_OK;
+}
+
+gs_status gs_update_knn_database(gs_group g, gs_bins bins) {
+    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(db_reserve(g->db, g->capacity, bins->cells));
+    GS_TRY(db_build(g->db, g->position, g->n, bins->grid, g->stream));
+    return GS_OK;
+}
+
+gs_status gs_walls_update_knn_database(gs_walls w, gs_bins bins) {
+    if (!w || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
+    return walls_db(w, bins->grid, bins->cells, nullptr);
+}
+
+gs_status gs_find_knn(gs_group g, gs_knn out, gs_bins bins, gs_group other,
+                      unsigned search_radius) {
+    (void)search_radius;  // the bins' radius applies, as in KNNBinningV2.cu:210-243
+    if (!g || !out || !bins || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (out->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    if (!g->db.valid || !other->db.valid || g->db.cells != bins->cells ||
+        other->db.cells != bins->cells)
+        return fail(GS_ERR_STATE, "call gs_update_knn_database on both groups first");
+    if (other != g) GS_CUDA(cudaStreamSynchronize(other->stream));
+    GS_TRY(launch_knn_binned(g->db, g->n, other->db, other == g, bins->radius, out->k, out->idx,
+                             out->dist, g->stream));
+    return GS_OK;
+}
+
+gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls,
+                            unsigned search_radius) {
+    (void)search_radius;
+    if (!g || !out || !bins || !walls) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (out->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    if (!g->db.valid || g->db.cells != bins->cells)
+        return fail(GS_ERR_STATE, "call gs_update_knn_database first");
+    GS_TRY(walls_db(walls, bins->grid, bins->cells, g->stream));
+    GS_TRY(launch_knn_binned(g->db, g->n, walls->db, false, bins->radius, out->k, out->idx,
+                             out->dist, g->stream));
+    return GS_OK;
+}
+
+gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
+    if (!g || !out || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (out->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    GS_TRY(ensure_reference(g));
+    if (other != g) {
+        GS_TRY(ensure_reference(other));
+        GS_CUDA(cudaStreamSynchronize(other->stream));
+    }
+    GS_TRY(launch_knn_brute(g->position, g->n, other->position, other->n, other == g, out->k,
+                            out->idx, out->dist, g->stream));
+    return GS_OK;
+}
+
+static gs_status flock_call(int kind, gs_group g, gs_knn knn, gs_group other, float a, float b,
+                            float c, float w, unsigned mask) {
+    if (!g || !knn || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knn->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    GS_TRY(ensure_reference(g));
+    if (other != g) {
+        GS_TRY(ensure_reference(other));
+        GS_CUDA(cudaStreamSynchronize(other->stream));
+    }
+    GS_TRY(launch_flock(kind, view(g), knn->idx, knn->k, other_view(other), a, b, c, w, mask,
+                        g->stream));
+    touched(g);
+    return GS_OK;
+}
+
+gs_status gs_steer_for_separation(gs_group g, gs_knn knn, gs_group other, float min_distance,
+                                  float max_distance, float cos_max_angle, float weight,
+                                  unsigned mask) {
+    return flock_call(0, g, knn, other, min_distance, max_distance, cos_max_angle, weight, mask);
+}
+gs_status gs_steer_for_alignment(gs_group g, gs_knn knn, gs_group other, float min_distance,
+                                 float max_distance, float cos_max_angle, float weight,
+                                 unsigned mask) {
+    return flock_call(1, g, knn, other, min_distance, max_distance, cos_max_angle, weight, mask);
+}
+gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float min_distance,
+                                float max_distance, float cos_max_angle, float weight,
+                                unsigned mask) {
+    return flock_call(2, g, knn, other, min_distance, max_distance, cos_max_angle, weight, mask);
+}
+
+gs_status gs_steer_for_seek(gs_group g, const float target[3], float weight, unsigned mask) {
+    if (!g || !target) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (!finite3(target)) return fail(GS_ERR_NONFINITE, "seek target is not finite");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_seek(view(g), target, weight, mask, g->stream));
+    touched(g);
+    return GS_OK;
+}
+
+gs_status gs_steer_to_avoid_neighbors(gs_group g, gs_knn knn, gs_group other,
+                                      float min_time_to_collision, float min_separation_distance,
+                                      int avoid_close, float weight, unsigned mask) {
+    if (!g || !knn || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knn->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    GS_TRY(ensure_reference(g));
+    if (other != g) {
+        GS_TRY(ensure_reference(other));
+        GS_CUDA(cudaStreamSynchronize(other->stream));
+    }
+    GS_TRY(launch_avoid_neighbors(view(g), knn->idx, knn->dist, knn->k, other_view(other),
+                                  min_time_to_collision, min_separation_distance,
+                                  avoid_close != 0, weight, mask, g->stream));
+    touched(g);
+    return GS_OK;
+}
+
+gs_status gs_steer_to_avoid_walls(gs_group g, gs_knn knw, gs_walls walls, float min_time,
+                                  float weight, unsigned mask) {
+    if (!g || !knw || !walls) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knw->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_avoid_walls(view(g), knw->idx, knw->k, walls->start, walls->end, walls->normal,
+                              walls->n, min_time, weight, mask, g->stream));
+    touched(g);
+    return GS_OK;
+}
+
+gs_status gs_update_group(gs_group g, float elapsed_time) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    if (!std::isfinite(elapsed_time)) return fail(GS_ERR_NONFINITE, "elapsed time is not finite");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_update(view(g), elapsed_time, g->stream));
+    g->fused_current = false;
+    g->accum_dirty = false;
+    return GS_OK;
+}
+
+gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, unsigned mask) {
+    if (!g || !knn || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knn->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    GS_TRY(ensure_reference(g));
+    if (other != g) {
+        GS_TRY(ensure_reference(other));
+        GS_CUDA(cudaStreamSynchronize(other->stream));
+    }
+    if (g->n == 0) return GS_OK;
+    // Scratch: the new positions and a snapshot of the other group's bits,
+    // from the fused-step buffers when they exist, else allocated here.
+    float4* pos_out = nullptr;
+    unsigned* snap = nullptr;
+    GS_TRY(dalloc(&pos_out, g->n));
+    gs_status s = dalloc(&snap, other->n ? other->n : 1);
+    if (s == GS_OK && other->n)
+        s = cudaMemcpyAsync(snap, other->applied, size_t(other->n) * 4, cudaMemcpyDeviceToDevice,
+                            g->stream) == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "snapshot");
+    if (s == GS_OK)
+        s = launch_antipenetration(view(g), knn->idx, knn->dist, knn->k, other_view(other), snap,
+                                   pos_out, mask, g->stream);
+    cudaStreamSynchronize(g->stream);
+    dfree(pos_out);
+    dfree(snap);
+    if (s == GS_OK) touched(g);
+    return s;
+}
+
+// ---- fused step ------------------------------------------------------------------
+static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k) {
+    if (!g->cellrank) {
+        const size_t n = g->capacity;
+        for (int j = 0; j < 6; ++j) {
+            GS_TRY(dalloc(&g->A.f[j], n));
+            GS_TRY(dalloc(&g->B.f[j], n));
+        }
+        GS_TRY(dalloc(&g->cellrank, n));
+        GS_TRY(dalloc(&g->d_scene, 1));
+    }
+    if (g->fdb.cells != C) GS_TRY(db_reserve(g->fdb, 0, C));
+    if (walls && (!g->w0 || g->fused_k_alloc < k)) {
+        const size_t n = g->capacity;
+        dfree(g->w0);
+        dfree(g->w1);
+        dfree(g->w2);
+        dfree(g->knn_slot);
+        dfree(g->knn_dist);
+        GS_TRY(dalloc(&g->w0, n));
+        GS_TRY(dalloc(&g->w1, n));
+        GS_TRY(dalloc(&g->w2, n));
+        GS_TRY(dalloc(&g->knn_slot, n * k));
+        GS_TRY(dalloc(&g->knn_dist, n * k));
+        g->fused_k_alloc = k;
+    }
+    return GS_OK;
+}
+
+gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
+                  unsigned steps) {
+    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
+    StepDev d;
+    GS_TRY(validate_step(p, walls, d));
+    Grid grid;
+    unsigned C;
+    GS_TRY(check_grid(p->world_cells, p->world_size, grid, C));
+    if (C != bins->cells || std::memcmp(&grid, &bins->grid, sizeof(Grid)) != 0)
+        return fail(GS_ERR_INVALID_ARG, "step grid differs from the bins");
+    const bool has_walls = d.need & NEED_WALLS;
+    if (has_walls && !walls) return fail(GS_ERR_INVALID_ARG, "avoid-walls needs a wall group");
+    if (steps == 0 || g->n == 0) return GS_OK;
+    cudaStream_t st = g->stream;
+    GS_TRY(reserve_fused(g, C, has_walls, d.k));
+    if (has_walls) GS_TRY(walls_db(walls, grid, C, st));
+
+    static_assert(sizeof(Scene) % 4 == 0, "scene layout");
+    Scene sc{};
+    sc.grid = grid;
+    sc.cell_offset = 0;
+    sc.agent_offset = 0;
+    sc.n_agents = g->n;
+    sc.n_walls = has_walls ? walls->n : 0;
+    // The scene table is tiny; a synchronous copy keeps the host struct's
+    // lifetime trivial.
+    GS_CUDA(cudaMemcpyAsync(g->d_scene, &sc, sizeof(Scene), cudaMemcpyHostToDevice, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+
+    bool dirty = false;
+    if (!g->fused_current) {
+        dirty = g->accum_dirty;
+        GS_TRY(fused_from_reference(view(g), nullptr, g->d_scene, g->A, g->cellrank, g->fdb.count,
+                                    d.wrap_mode, dirty, st));
+        g->fused_current = true;
+    } else if (g->fdb.grid.wc[0] != grid.wc[0] || g->fdb.grid.wc[1] != grid.wc[1] ||
+               g->fdb.grid.wc[2] != grid.wc[2] || g->fdb.grid.ws[0] != grid.ws[0] ||
+               g->fdb.grid.ws[1] != grid.ws[1] || g->fdb.grid.ws[2] != grid.ws[2] ||
+               g->fdb.valid == false || g->pending_wrap != d.wrap_mode) {
+        GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
+        GS_TRY(fused_recount(g->A, g->n, g->d_scene, g->cellrank, g->fdb.count, d.wrap_mode, st));
+    }
+    g->fdb.grid = grid;
+    g->fdb.valid = true;
+    g->pending_wrap = d.wrap_mode;
+
+    FusedLaunch L{};
+    L.A = g->A;
+    L.B = g->B;
+    L.cellrank = g->cellrank;
+    L.count = g->fdb.count;
+    L.start = g->fdb.start;
+    L.scenes = g->d_scene;
+    L.n = g->n;
+    if (has_walls) {
+        L.w_start = walls->start;
+        L.w_end = walls->end;
+        L.w_normal = walls->normal;
+        L.w_pos_id = walls->db.pos_id;
+        L.w_cell_start = walls->db.start;
+        L.w0 = g->w0;
+        L.w1 = g->w1;
+        L.w2 = g->w2;
+        L.knn_slot = g->knn_slot;
+        L.knn_dist = g->knn_dist;
+    }
+    for (unsigned step = 0; step < steps; ++step) {
+        d.dirty = dirty ? 1 : 0;
+        GS_TRY(scan_counts(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
+        GS_TRY(fused_permute(L, d.wrap_mode, dirty, st));
+        GS_TRY(fused_step(L, d, st));
+        dirty = false;
+    }
+    g->accum_dirty = false;
+    g->db.valid = false;
+    return GS_OK;
+}
+
+gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
+                       unsigned steps, const gs_agent_arrays* in, unsigned n,
+                       const gs_agent_arrays* out) {
+    GS_TRY(gs_group_upload(g, in, n));
+    GS_TRY(gs_step(g, bins, walls, p, steps));
+    return gs_group_download(g, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,142 @@
+// Internal structures of libgpusteer: handle layouts, launch helpers, error
+// reporting.  Not part of the ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gpusteer.h"
+#include "gs_math.cuh"
+
+namespace gs {
+
+constexpr unsigned kMaxK = 64;
+constexpr int kBlock = 256;
+
+// ---- errors -------------------------------------------------------------------
+void set_error(const std::string& msg);
+gs_status fail(gs_status s, const std::string& msg);
+gs_status cuda_fail(cudaError_t e, const char* what);
+
+#define GS_CUDA(call)                                             \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return ::gs::cuda_fail(e_, #call); \
+    } while (0)
+#define GS_LAUNCHED(what)                                         \
+    do {                                                          \
+        cudaError_t e_ = cudaGetLastError();                      \
+        if (e_ != cudaSuccess) return ::gs::cuda_fail(e_, what);  \
+    } while (0)
+#define GS_TRY(call)                       \
+    do {                                   \
+        gs_status s_ = (call);             \
+        if (s_ != GS_OK) return s_;        \
+    } while (0)
+
+inline unsigned blocks_for(unsigned n, unsigned b = kBlock) { return (n + b - 1) / b; }
+
+template <class T> gs_status dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return GS_OK;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(GS_ERR_OOM, "device allocation failed");
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    return GS_OK;
+}
+template <class T> void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// ---- scenes -------------------------------------------------------------------
+// One independent world.  A single group is one scene; the batched engine
+// concatenates many.  Cell labels of scene s occupy
+// [cell_offset, cell_offset + cells); its walls' cell table starts at
+// wall_cell_offset and its wall segments at wall_offset.
+struct Scene {
+    Grid grid;
+    unsigned cell_offset;
+    unsigned agent_offset;
+    unsigned n_agents;
+    unsigned wall_offset;
+    unsigned n_walls;
+    unsigned wall_cell_offset;
+};
+
+// Bucketed ("fused") state: six float4 streams per agent.
+//   f0 = position.xyz, agent index (bits)    f1 = direction.xyz, speed
+//   f2 = side.xyz, radius                    f3 = up.xyz, mass
+//   f4 = maxSpeed, maxForce, applied (bits), scene (bits)
+//   f5 = steering.xyz, 0  (read only while the steering may be non-zero)
+struct Fused {
+    float4* f[6];
+};
+
+// A group's bucketed binning database (KNNDatabase.cuh:30-38): cell of every
+// agent, the sorted agent indices and positions, and cell_start[C + 1]
+// (cell c holds slots cell_start[c] .. cell_start[c + 1]).
+struct Database {
+    unsigned cells = 0;         // C allocated for
+    unsigned* cell = nullptr;   // [n] cell label
+    unsigned* rank = nullptr;   // [n] rank within the cell (atomic order)
+    unsigned* sorted = nullptr; // [n] agent index of slot
+    float4* pos_id = nullptr;   // [n] (position.xyz, agent index bits) of slot
+    unsigned* start = nullptr;  // [C + 1]
+    unsigned* count = nullptr;  // [C] zero between uses
+    unsigned* tile = nullptr;   // scan scratch
+    bool valid = false;
+    Grid grid{};
+};
+
+}  // namespace gs
+
+struct gs_bins_s {
+    gs::Grid grid;
+    unsigned radius;
+    unsigned cells;
+};
+
+struct gs_knn_s {
+    unsigned n, k;
+    unsigned* idx;
+    float* dist;
+};
+
+struct gs_walls_s {
+    unsigned n, knw;
+    std::vector<float> h_start, h_mid, h_end, h_normal;  // float4 each
+    float4 *start = nullptr, *mid = nullptr, *end = nullptr, *normal = nullptr;
+    gs::Database db;  // agents vs wall midpoints
+    cudaStream_t stream = nullptr;
+};
+
+struct gs_group_s {
+    unsigned k, capacity, n;
+    cudaStream_t stream;
+    bool own_stream;
+    // reference-layout arrays
+    float4 *position, *direction, *steering;
+    float3 *side, *up;
+    float *speed, *max_speed, *max_force, *radius, *mass;
+    unsigned* applied;
+    // binning database for the per-function API
+    gs::Database db;
+    // fused-step state
+    gs::Fused A, B;
+    uint2* cellrank;       // next cell and rank per slot of A
+    float4 *w0, *w1, *w2;  // wall-phase outputs (corrected pos/dir, steering+applied)
+    unsigned* knn_slot;    // [k * n] neighbour slots (wall phase)
+    float* knn_dist;       // [k * n]
+    gs::Database fdb;      // counts / starts of the fused step
+    gs::Scene* d_scene;    // single-scene table
+    bool fused_current;    // true: A holds the state, reference arrays stale
+    bool accum_dirty;      // steering / applied may be non-zero
+    int pending_wrap;      // wrap mode the pending cell counts were taken with
+    unsigned fused_k_alloc;
+};

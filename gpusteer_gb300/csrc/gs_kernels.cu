@@ -1,0 +1,590 @@
+// Counting-sort binning and the per-function (drop-in) kernels.
+//
+// The bin rebuild replaces KNNBinningV2UpdateDBCUDA::run (KNNBinningV2.cu:87-162:
+// BuildDB, a host synchronisation, thrust::sort_by_key, a memset of every cell
+// and ReorderDB) with three passes that never leave the device: an atomic
+// count per cell (which also hands each agent its rank inside the cell), an
+// exclusive scan of the counts, and a scatter of (position, index) into
+// bucketed order.  The order inside a cell follows the atomics and is not
+// deterministic; nothing downstream depends on it because every KNN uses the
+// total order (distance, agent index).
+#include "gs_behaviours.cuh"
+#include "gs_knn.cuh"
+#include "gs_launch.h"
+
+namespace gs {
+
+// ---- exclusive scan -----------------------------------------------------------------
+constexpr unsigned kScanItems = 16;
+constexpr unsigned kScanTile = kBlock * kScanItems;
+
+unsigned scan_tile_count(unsigned C) { return (C + kScanTile - 1) / kScanTile; }
+
+__device__ __forceinline__ unsigned block_exclusive_sum(unsigned v, unsigned* warp_sums,
+                                                        unsigned& total) {
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= unsigned(o)) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < kBlock / 32 ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= unsigned(o)) w += y;
+        }
+        if (lane < kBlock / 32) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    total = warp_sums[kBlock / 32 - 1];
+    const unsigned before = warp ? warp_sums[warp - 1] : 0u;
+    __syncthreads();
+    return before + x - v;
+}
+
+// Loads tile t of count[] into shared memory (coalesced), returns this
+// thread's run of kScanItems consecutive items through `items`.
+__device__ __forceinline__ void load_tile(const unsigned* count, unsigned C, unsigned t,
+                                          unsigned* sh, unsigned items[kScanItems]) {
+    const unsigned base = t * kScanTile;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) {
+        const unsigned i = j * kBlock + threadIdx.x;
+        sh[i + i / 32] = (base + i < C) ? count[base + i] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) {
+        const unsigned i = threadIdx.x * kScanItems + j;
+        items[j] = sh[i + i / 32];
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_reduce(const unsigned* __restrict__ count,
+                                                        unsigned C, unsigned* __restrict__ tile) {
+    __shared__ unsigned sh[kScanTile + kScanTile / 32];
+    __shared__ unsigned ws[kBlock / 32];
+    unsigned items[kScanItems];
+    load_tile(count, C, blockIdx.x, sh, items);
+    unsigned s = 0;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) s += items[j];
+    unsigned total;
+    block_exclusive_sum(s, ws, total);
+    if (threadIdx.x == 0) tile[blockIdx.x] = total;
+}
+
+// One block scans the tile totals in place (exclusive) and writes start[C].
+__global__ void __launch_bounds__(1024) k_scan_tiles(unsigned* tile, unsigned T,
+                                                     unsigned* __restrict__ start, unsigned C) {
+    __shared__ unsigned ws[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (unsigned base = 0; base < T; base += 1024) {
+        const unsigned i = base + threadIdx.x;
+        const unsigned v = i < T ? tile[i] : 0u;
+        const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        unsigned x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= unsigned(o)) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = ws[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= unsigned(o)) w += y;
+            }
+            ws[lane] = w;
+        }
+        __syncthreads();
+        const unsigned before = (warp ? ws[warp - 1] : 0u) + carry;
+        if (i < T) tile[i] = before + x - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = before + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) start[C] = carry;
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_apply(unsigned* __restrict__ count, unsigned C,
+                                                       const unsigned* __restrict__ tile,
+                                                       unsigned* __restrict__ start) {
+    __shared__ unsigned sh[kScanTile + kScanTile / 32];
+    __shared__ unsigned ws[kBlock / 32];
+    unsigned items[kScanItems];
+    load_tile(count, C, blockIdx.x, sh, items);
+    unsigned s = 0;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) s += items[j];
+    unsigned total;
+    unsigned run = block_exclusive_sum(s, ws, total) + tile[blockIdx.x];
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) {
+        const unsigned i = threadIdx.x * kScanItems + j;
+        sh[i + i / 32] = run;
+        run += items[j];
+    }
+    __syncthreads();
+    const unsigned base = blockIdx.x * kScanTile;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) {
+        const unsigned i = j * kBlock + threadIdx.x;
+        if (base + i < C) {
+            start[base + i] = sh[i + i / 32];
+            count[base + i] = 0u;
+        }
+    }
+}
+
+gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
+                      cudaStream_t st) {
+    const unsigned T = scan_tile_count(C);
+    k_scan_reduce<<<T, kBlock, 0, st>>>(count, C, tile);
+    k_scan_tiles<<<1, 1024, 0, st>>>(tile, T, start, C);
+    k_scan_apply<<<T, kBlock, 0, st>>>(count, C, tile, start);
+    GS_LAUNCHED("scan");
+    return GS_OK;
+}
+
+// ---- database -----------------------------------------------------------------------
+gs_status db_reserve(Database& db, unsigned n, unsigned C) {
+    if (db.cells != C) {
+        dfree(db.start);
+        dfree(db.count);
+        dfree(db.tile);
+        GS_TRY(dalloc(&db.start, size_t(C) + 1));
+        GS_TRY(dalloc(&db.count, C));
+        GS_TRY(dalloc(&db.tile, scan_tile_count(C) + 1));
+        GS_CUDA(cudaMemset(db.count, 0, size_t(C) * sizeof(unsigned)));
+        // the counts are used next on a non-blocking stream
+        GS_CUDA(cudaDeviceSynchronize());
+        db.cells = C;
+    }
+    if (n > 0 && db.cell == nullptr) {
+        GS_TRY(dalloc(&db.cell, n));
+        GS_TRY(dalloc(&db.rank, n));
+        GS_TRY(dalloc(&db.sorted, n));
+        GS_TRY(dalloc(&db.pos_id, n));
+    }
+    db.valid = false;
+    return GS_OK;
+}
+
+void db_release(Database& db) {
+    dfree(db.cell);
+    dfree(db.rank);
+    dfree(db.sorted);
+    dfree(db.pos_id);
+    dfree(db.start);
+    dfree(db.count);
+    dfree(db.tile);
+    db.cells = 0;
+    db.valid = false;
+}
+
+__global__ void k_db_count(const float4* __restrict__ pos, unsigned n, Grid g,
+                           unsigned* __restrict__ cell, unsigned* __restrict__ rank,
+                           unsigned* __restrict__ count) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned c = cell_of(g, v3(pos[i]));
+    cell[i] = c;
+    rank[i] = atomicAdd(count + c, 1u);
+}
+
+__global__ void k_db_scatter(const float4* __restrict__ pos, unsigned n,
+                             const unsigned* __restrict__ cell, const unsigned* __restrict__ rank,
+                             const unsigned* __restrict__ start, unsigned* __restrict__ sorted,
+                             float4* __restrict__ pos_id) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned dst = start[cell[i]] + rank[i];
+    const float4 p = pos[i];
+    sorted[dst] = i;
+    pos_id[dst] = make_float4(p.x, p.y, p.z, __uint_as_float(i));
+}
+
+gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid,
+                   cudaStream_t st) {
+    const unsigned C = grid.wc[0] * grid.wc[1] * grid.wc[2];
+    if (db.cells != C || (n > 0 && db.cell == nullptr))
+        return fail(GS_ERR_STATE, "database not reserved for this grid");
+    if (n > 0) k_db_count<<<blocks_for(n), kBlock, 0, st>>>(pos, n, grid, db.cell, db.rank, db.count);
+    GS_TRY(scan_counts(db.count, db.start, C, db.tile, st));
+    if (n > 0)
+        k_db_scatter<<<blocks_for(n), kBlock, 0, st>>>(pos, n, db.cell, db.rank, db.start,
+                                                       db.sorted, db.pos_id);
+    GS_LAUNCHED("db_build");
+    db.grid = grid;
+    db.valid = true;
+    return GS_OK;
+}
+
+// ---- binned KNN, reference output layout (KNNBinningV2Kernel.cu:417-528) ----------
+// One thread per agent of A in bucketed order (neighbouring threads scan the
+// same cells); results go to idx/dist[a + i * nA].
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_knn_binned(
+    const unsigned* __restrict__ a_sorted, const float4* __restrict__ a_pos_id, unsigned nA,
+    const unsigned* __restrict__ b_start, const float4* __restrict__ b_pos_id, Grid g,
+    unsigned r, unsigned k, bool self, unsigned* __restrict__ idx, float* __restrict__ dist) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nA) return;
+    const unsigned a = a_sorted[s];
+    const V3 p = v3(a_pos_id[s]);
+    unsigned ix, iy, iz;
+    cell_coords(g, p, ix, iy, iz);
+    const Box box = cell_box(g, ix, iy, iz, r);
+    KList<KMAX> L;
+    L.init(int(k));
+    knn_scan_box<KMAX>(L, p, self ? a : UINT_MAX, g, box, 0u, b_start, b_pos_id);
+    L.for_each(int(k), [&](int r, unsigned long long key, unsigned) {
+        idx[a + size_t(r) * nA] = key_id(key);
+        dist[a + size_t(r) * nA] = key_dist(key);
+    });
+}
+
+gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
+                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
+    if (nA == 0) return GS_OK;
+    const unsigned nb = blocks_for(nA);
+    if (k <= 8)
+        k_knn_binned<8><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id, B.grid,
+                                              r, k, self, idx, dist);
+    else if (k <= 16)
+        k_knn_binned<16><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id,
+                                               B.grid, r, k, self, idx, dist);
+    else if (k <= 32)
+        k_knn_binned<32><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id,
+                                               B.grid, r, k, self, idx, dist);
+    else
+        k_knn_binned<64><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id,
+                                               B.grid, r, k, self, idx, dist);
+    GS_LAUNCHED("knn_binned");
+    return GS_OK;
+}
+
+// ---- brute-force KNN (KNNBruteForceCudaKernel.cu:207-283) ---------------------------
+// Candidates are staged through shared memory in tiles of kBlock positions.
+// A candidate needs its square root only when its squared distance is within
+// a rounded-up bound of the current k-th distance squared: a larger squared
+// distance has a correctly rounded square root strictly above the k-th
+// distance, so it can be skipped without changing the result.
+__device__ __forceinline__ float prefilter_bound(unsigned long long thr) {
+    const float td = key_dist(thr);
+    return __fmul_ru(__fmul_ru(td, td), 1.000004f);
+}
+
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_knn_brute(const float4* __restrict__ posA,
+                                                      unsigned nA,
+                                                      const float4* __restrict__ posB,
+                                                      unsigned nB, bool self, unsigned k,
+                                                      unsigned* __restrict__ idx,
+                                                      float* __restrict__ dist) {
+    __shared__ float4 tile[kBlock];
+    const unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = a < nA;
+    const V3 p = active ? v3(posA[a]) : v3(0.f, 0.f, 0.f);
+    KList<KMAX> L;
+    L.init(int(k));
+    float bound = prefilter_bound(L.key[KMAX - 1]);
+    for (unsigned base = 0; base < nB; base += kBlock) {
+        const unsigned j = base + threadIdx.x;
+        tile[threadIdx.x] = j < nB ? posB[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        const unsigned cnt = min(unsigned(kBlock), nB - base);
+        if (active) {
+            for (unsigned t = 0; t < cnt; ++t) {
+                const float4 q = tile[t];
+                const V3 o = sub(p, v3(q));
+                const float d2 = dot(o, o);
+                if (d2 <= bound) {
+                    const unsigned id = base + t;
+                    if (self && id == a) continue;
+                    L.insert(knn_key(sqrtf(d2), id), id);
+                    bound = prefilter_bound(L.key[KMAX - 1]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) return;
+    L.for_each(int(k), [&](int r, unsigned long long key, unsigned) {
+        idx[a + size_t(r) * nA] = key_id(key);
+        dist[a + size_t(r) * nA] = key_dist(key);
+    });
+}
+
+gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
+                           bool self, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
+    if (nA == 0) return GS_OK;
+    const unsigned nb = blocks_for(nA);
+    if (k <= 8)
+        k_knn_brute<8><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
+    else if (k <= 16)
+        k_knn_brute<16><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
+    else if (k <= 32)
+        k_knn_brute<32><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
+    else
+        k_knn_brute<64><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
+    GS_LAUNCHED("knn_brute");
+    return GS_OK;
+}
+
+// ---- WrapWorldCUDAKernel.cu:11-48 ---------------------------------------------------
+__global__ void k_wrap(float4* pos, unsigned n, float wx, float wy, float wz, int mode) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float ws[3] = {wx, wy, wz};
+    pos[i] = f4(wrap_world(v3(pos[i]), ws, mode), 0.f);
+}
+
+gs_status launch_wrap(float4* pos, unsigned n, const float ws[3], int mode, cudaStream_t st) {
+    if (n == 0) return GS_OK;
+    k_wrap<<<blocks_for(n), kBlock, 0, st>>>(pos, n, ws[0], ws[1], ws[2], mode);
+    GS_LAUNCHED("wrap_world");
+    return GS_OK;
+}
+
+// ---- one behaviour per launch ----------------------------------------------------------
+__device__ __forceinline__ Self load_self(const GroupView& g, unsigned i) {
+    Self s;
+    s.pos = v3(g.position[i]);
+    s.dir = v3(g.direction[i]);
+    const float3 sd = g.side[i], u = g.up[i];
+    s.side = v3(sd.x, sd.y, sd.z);
+    s.up = v3(u.x, u.y, u.z);
+    s.speed = g.speed[i];
+    s.radius = g.radius[i];
+    s.max_speed = g.max_speed[i];
+    s.max_force = g.max_force[i];
+    s.mass = g.mass[i];
+    return s;
+}
+
+__global__ void k_flock(int kind, GroupView g, const unsigned* __restrict__ knn, unsigned k,
+                        OtherView o, FlockParams fp) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    unsigned applied = g.applied[i];
+    if (applied & fp.mask) return;
+    const V3 pos = v3(g.position[i]), dir = v3(g.direction[i]);
+    FlockAcc acc;
+    flock_init(acc);
+    for (unsigned s = 0; s < k; ++s) {
+        const unsigned b = knn[i + size_t(s) * g.n];
+        if (b >= o.n) break;
+        const V3 bp = v3(o.position[b]);
+        const V3 offset = sub(bp, pos);
+        const float dsq = dot(offset, offset);
+        const float d = sqrtf(dsq);
+        if (kind == 0) separation_add(acc, fp, dir, offset, dsq, d);
+        else if (kind == 1) alignment_add(acc, fp, dir, offset, d, v3(o.direction[b]));
+        else cohesion_add(acc, fp, dir, offset, d, bp);
+    }
+    Self me;
+    me.pos = pos;
+    me.dir = dir;
+    V3 steer = v3(g.steering[i]);
+    flock_finish(kind, acc, fp, me, applied, steer);
+    g.steering[i] = f4(steer, 0.f);
+    g.applied[i] = applied;
+}
+
+gs_status launch_flock(int kind, GroupView g, const unsigned* knn, unsigned k, OtherView o,
+                       float min_d, float max_d, float cos_max, float w, unsigned mask,
+                       cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    const FlockParams fp{min_d, max_d, cos_max, w, mask};
+    k_flock<<<blocks_for(g.n), kBlock, 0, st>>>(kind, g, knn, k, o, fp);
+    GS_LAUNCHED("steer_flock");
+    return GS_OK;
+}
+
+__global__ void k_seek(GroupView g, float tx, float ty, float tz, float w, unsigned mask) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    unsigned applied = g.applied[i];
+    if (applied & mask) return;
+    Self me;
+    me.pos = v3(g.position[i]);
+    me.dir = v3(g.direction[i]);
+    V3 steer = v3(g.steering[i]);
+    seek_finish(v3(tx, ty, tz), w, mask, me, applied, steer);
+    g.steering[i] = f4(steer, 0.f);
+    g.applied[i] = applied;
+}
+
+gs_status launch_seek(GroupView g, const float target[3], float w, unsigned mask,
+                      cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_seek<<<blocks_for(g.n), kBlock, 0, st>>>(g, target[0], target[1], target[2], w, mask);
+    GS_LAUNCHED("steer_seek");
+    return GS_OK;
+}
+
+__global__ void k_avoid_close(GroupView g, const unsigned* __restrict__ knn,
+                              const float* __restrict__ knn_dist, unsigned k, OtherView o,
+                              float min_sep, float w, unsigned mask) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    unsigned applied = g.applied[i];
+    if (applied & mask) return;
+    const Self me = load_self(g, i);
+    CloseAcc acc;
+    close_init(acc);
+    for (unsigned s = 0; s < k; ++s) {
+        const unsigned b = knn[i + size_t(s) * g.n];
+        if (b >= o.n) break;
+        close_add(acc, me, min_sep, knn_dist[i + size_t(s) * g.n], v3(o.position[b]),
+                  o.radius[b]);
+        if (acc.found) break;
+    }
+    V3 steer = v3(g.steering[i]);
+    close_finish(acc, w, mask, applied, steer);
+    g.steering[i] = f4(steer, 0.f);
+    g.applied[i] = applied;
+}
+
+__global__ void k_avoid(GroupView g, const unsigned* __restrict__ knn, unsigned k, OtherView o,
+                        float min_time, float w, unsigned mask) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    unsigned applied = g.applied[i];
+    if (applied & (mask | AVOID_CLOSE_NEIGHBORS_BIT)) return;
+    const Self me = load_self(g, i);
+    AvoidAcc acc;
+    avoid_init(acc, min_time);
+    for (unsigned s = 0; s < k; ++s) {
+        const unsigned b = knn[i + size_t(s) * g.n];
+        if (b >= o.n) break;
+        avoid_add(acc, me, b, v3(o.position[b]), v3(o.direction[b]), o.speed[b], o.radius[b]);
+    }
+    if (acc.threat == UINT_MAX) return;
+    V3 steer = v3(g.steering[i]);
+    avoid_finish(acc, w, mask, me, applied, steer);
+    g.steering[i] = f4(steer, 0.f);
+    g.applied[i] = applied;
+}
+
+gs_status launch_avoid_neighbors(GroupView g, const unsigned* knn, const float* knn_dist,
+                                 unsigned k, OtherView o, float min_time, float min_sep,
+                                 bool avoid_close, float w, unsigned mask, cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    if (avoid_close)
+        k_avoid_close<<<blocks_for(g.n), kBlock, 0, st>>>(g, knn, knn_dist, k, o, min_sep, w,
+                                                          mask);
+    k_avoid<<<blocks_for(g.n), kBlock, 0, st>>>(g, knn, k, o, min_time, w, mask);
+    GS_LAUNCHED("steer_avoid_neighbors");
+    return GS_OK;
+}
+
+__global__ void k_avoid_walls(GroupView g, const unsigned* __restrict__ knw, unsigned kw,
+                              const float4* __restrict__ ls, const float4* __restrict__ le,
+                              const float4* __restrict__ ln, unsigned n_lines, float min_time,
+                              float w, unsigned mask) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    unsigned applied = g.applied[i];
+    if (applied & mask) return;
+    Self me = load_self(g, i);
+    WallAcc acc;
+    walls_init(acc, me, min_time);
+    for (unsigned s = 0; s < kw; ++s) {
+        const unsigned line = knw[i + size_t(s) * g.n];
+        if (line >= n_lines) break;
+        walls_add(acc, me, line, v3(ls[line]), v3(le[line]), v3(ln[line]));
+    }
+    V3 steer = v3(g.steering[i]);
+    walls_finish(acc, w, mask, me, applied, steer);
+    g.steering[i] = f4(steer, 0.f);
+    g.position[i] = f4(me.pos, 0.f);
+    g.direction[i] = f4(me.dir, 0.f);
+    g.applied[i] = applied;
+}
+
+gs_status launch_avoid_walls(GroupView g, const unsigned* knw, unsigned kw, const float4* start,
+                             const float4* end, const float4* normal, unsigned n_lines,
+                             float min_time, float w, unsigned mask, cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_avoid_walls<<<blocks_for(g.n), kBlock, 0, st>>>(g, knw, kw, start, end, normal, n_lines,
+                                                      min_time, w, mask);
+    GS_LAUNCHED("steer_avoid_walls");
+    return GS_OK;
+}
+
+__global__ void k_update(GroupView g, float dt) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    Self me = load_self(g, i);
+    integrate(me, v3(g.steering[i]), dt);
+    g.side[i] = make_float3(me.side.x, me.side.y, me.side.z);
+    g.up[i] = make_float3(me.up.x, me.up.y, me.up.z);
+    g.direction[i] = f4(me.dir, 0.f);
+    g.position[i] = f4(me.pos, 0.f);
+    g.steering[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    g.speed[i] = me.speed;
+    g.applied[i] = 0u;
+}
+
+gs_status launch_update(GroupView g, float dt, cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_update<<<blocks_for(g.n), kBlock, 0, st>>>(g, dt);
+    GS_LAUNCHED("update_group");
+    return GS_OK;
+}
+
+// AntiPenetrationAgentsCUDAKernel.cu:72-108.  Positions are read from the
+// group and written to pos_out (the reference's m_pdPositionNew); the other
+// group's applied bits are read from a snapshot taken before the launch (the
+// reference reads them while this kernel sets bit 13 on the same array).
+__global__ void k_antipen(GroupView g, const unsigned* __restrict__ knn,
+                          const float* __restrict__ knn_dist, OtherView o,
+                          const unsigned* __restrict__ applied_b, float4* __restrict__ out,
+                          unsigned mask) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    const float4 p4 = g.position[i];
+    out[i] = p4;
+    unsigned applied = g.applied[i];
+    if (applied & mask) return;
+    const unsigned b = knn[i];
+    if (b >= o.n) return;
+    const float sum_radii = g.radius[i] + o.radius[b];
+    const float overlap = sum_radii - knn_dist[i];
+    if (overlap < 0.f) return;
+    const V3 pos = v3(p4);
+    const V3 offset = sub(pos, v3(o.position[b]));
+    const V3 unit = normalize(offset);
+    const float move = (applied_b[b] & mask) ? overlap : 0.5f * overlap;
+    out[i] = f4(add(pos, mul(unit, move)), 0.f);
+    g.applied[i] = applied | ANTI_PENETRATION_AGENT;
+}
+
+gs_status launch_antipenetration(GroupView g, const unsigned* knn, const float* knn_dist,
+                                 unsigned k, OtherView o, const unsigned* applied_snapshot,
+                                 float4* pos_out, unsigned mask, cudaStream_t st) {
+    (void)k;
+    if (g.n == 0) return GS_OK;
+    k_antipen<<<blocks_for(g.n), kBlock, 0, st>>>(g, knn, knn_dist, o, applied_snapshot,
+                                                  pos_out, mask);
+    GS_LAUNCHED("anti_penetration_agents");
+    GS_CUDA(cudaMemcpyAsync(g.position, pos_out, size_t(g.n) * sizeof(float4),
+                            cudaMemcpyDeviceToDevice, st));
+    return GS_OK;
+}
+
+}  // namespace gs

@@ -1,0 +1,103 @@
+// Host-side launch wrappers shared by the C ABI implementation.
+#pragma once
+
+#include "gs_internal.cuh"
+
+namespace gs {
+
+// ---- counting-sort binning ---------------------------------------------------
+// Exclusive scan of count[0..C) into start[0..C]; zeroes count.
+gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
+                      cudaStream_t st);
+unsigned scan_tile_count(unsigned C);
+// Allocates db for C cells and n agents (keeps existing buffers when large enough).
+gs_status db_reserve(Database& db, unsigned n, unsigned C);
+void db_release(Database& db);
+// updateKNNDatabase: bucket n positions (float4, reference layout) by cell.
+gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid,
+                   cudaStream_t st);
+
+// ---- per-function (drop-in) kernels -----------------------------------------
+gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
+                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
+gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
+                           bool self, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
+gs_status launch_wrap(float4* pos, unsigned n, const float ws[3], int mode, cudaStream_t st);
+
+struct GroupView {
+    float4 *position, *direction, *steering;
+    float3 *side, *up;
+    float *speed, *max_speed, *max_force, *radius, *mass;
+    unsigned* applied;
+    unsigned n;
+};
+struct OtherView {
+    const float4 *position, *direction;
+    const float *speed, *radius;
+    const unsigned* applied;
+    unsigned n;
+};
+// kind: 0 separation, 1 alignment, 2 cohesion
+gs_status launch_flock(int kind, GroupView g, const unsigned* knn, unsigned k, OtherView o,
+                       float min_d, float max_d, float cos_max, float w, unsigned mask,
+                       cudaStream_t st);
+gs_status launch_seek(GroupView g, const float target[3], float w, unsigned mask,
+                      cudaStream_t st);
+gs_status launch_avoid_neighbors(GroupView g, const unsigned* knn, const float* knn_dist,
+                                 unsigned k, OtherView o, float min_time, float min_sep,
+                                 bool avoid_close, float w, unsigned mask, cudaStream_t st);
+gs_status launch_avoid_walls(GroupView g, const unsigned* knw, unsigned kw, const float4* start,
+                             const float4* end, const float4* normal, unsigned n_lines,
+                             float min_time, float w, unsigned mask, cudaStream_t st);
+gs_status launch_update(GroupView g, float dt, cudaStream_t st);
+gs_status launch_antipenetration(GroupView g, const unsigned* knn, const float* knn_dist,
+                                 unsigned k, OtherView o, const unsigned* applied_snapshot,
+                                 float4* pos_out, unsigned mask, cudaStream_t st);
+
+// ---- fused step ------------------------------------------------------------------
+struct StepDev {
+    unsigned k, knw, r;
+    int wrap_mode, clear_applied, dirty;
+    float sep[5], ali[5], coh[5];  // min, max, cos, weight, mask bits
+    float seek_target[3], w_seek;
+    unsigned mask_seek;
+    float min_time_wall, w_walls;
+    unsigned mask_walls;
+    float min_time_col, min_sep;
+    int avoid_close;
+    float w_avoid;
+    unsigned mask_avoid;
+    unsigned order[8];
+    unsigned n_order;
+    float dt;
+    unsigned need;  // NEED_* bits
+};
+constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
+                   NEED_WALLS = 32;
+
+struct FusedLaunch {
+    Fused A, B;
+    uint2* cellrank;
+    unsigned* count;
+    const unsigned* start;
+    const Scene* scenes;
+    unsigned n;
+    // walls (may be null)
+    const float4 *w_start, *w_end, *w_normal, *w_pos_id;
+    const unsigned* w_cell_start;
+    float4 *w0, *w1, *w2;
+    unsigned* knn_slot;
+    float* knn_dist;
+};
+
+gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
+                               Fused A, uint2* cellrank, unsigned* count, int wrap_mode,
+                               bool dirty, cudaStream_t st);
+gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
+                        unsigned* count, int wrap_mode, cudaStream_t st);
+gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st);
+gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st);
+gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView g,
+                             cudaStream_t st);
+
+}  // namespace gs

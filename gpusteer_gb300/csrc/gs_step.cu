@@ -1,0 +1,411 @@
+// The fused per-step engine.
+//
+// State lives in bucketed order in two ping-pong sets of six float4 streams
+// (Fused A and B, layout in gs_internal.cuh).  One step is
+//   scan      exclusive scan of the per-cell counts gathered by the previous
+//             step (or by fused_from_reference), zeroing the counts;
+//   permute   A -> B into bucketed order, applying the world wrap
+//             (WrapWorldCUDAKernel) on the way;
+//   fused     one thread per agent of B: binned KNN over B's own bucketed
+//             positions into a register k-list, one pass over the k
+//             neighbours feeding every enabled behaviour's accumulator, the
+//             behaviours finalised in the scenario's order with the
+//             reference's masks, UpdateCUDAKernel's integration, the new state
+//             written to A, and the next step's cell counted with an atomic.
+// With wall avoidance the fused kernel splits in two at the wall behaviour,
+// because avoid-walls moves agents (AvoidWallsCUDAKernel.cu:215-224) before
+// later behaviours read their neighbours: the first half writes the corrected
+// position/direction of every agent, the second half reads neighbours from
+// those.
+//
+// This replaces, per step, the reference's wrap, BuildDB, host sync, thrust
+// sort, memset, ReorderDB, KNN and one launch per behaviour plus update
+// (plugins/BoidsGroup.cpp:606-637, plugins/ChokePointNew.cpp:586-630).
+#include "gs_behaviours.cuh"
+#include "gs_knn.cuh"
+#include "gs_launch.h"
+
+namespace gs {
+
+__device__ __forceinline__ unsigned u(float x) { return __float_as_uint(x); }
+__device__ __forceinline__ float fb(unsigned x) { return __uint_as_float(x); }
+
+__device__ __forceinline__ unsigned count_next(const Scene& sc, V3 pos, int wrap_mode,
+                                               unsigned* count, unsigned& cell) {
+    const V3 wp = wrap_world(pos, sc.grid.ws, wrap_mode);
+    cell = sc.cell_offset + cell_of(sc.grid, wp);
+    return atomicAdd(count + cell, 1u);
+}
+
+// Reference layout -> A (identity order), counting the first step's cells.
+__global__ void k_from_reference(GroupView g, const unsigned* __restrict__ agent_scene,
+                                 const Scene* __restrict__ scenes, Fused A,
+                                 uint2* __restrict__ cellrank, unsigned* __restrict__ count,
+                                 int wrap_mode, int dirty) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    const unsigned si = agent_scene ? agent_scene[i] : 0u;
+    const Scene sc = scenes[si];
+    const unsigned id = i - sc.agent_offset;
+    const float4 p = g.position[i], d = g.direction[i];
+    const float3 sd = g.side[i], up = g.up[i];
+    A.f[0][i] = make_float4(p.x, p.y, p.z, fb(id));
+    A.f[1][i] = make_float4(d.x, d.y, d.z, g.speed[i]);
+    A.f[2][i] = make_float4(sd.x, sd.y, sd.z, g.radius[i]);
+    A.f[3][i] = make_float4(up.x, up.y, up.z, g.mass[i]);
+    A.f[4][i] = make_float4(g.max_speed[i], g.max_force[i], fb(g.applied[i]), fb(si));
+    if (dirty) A.f[5][i] = g.steering[i];
+    unsigned cell;
+    const unsigned rank = count_next(sc, v3(p), wrap_mode, count, cell);
+    cellrank[i] = make_uint2(cell, rank);
+}
+
+gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
+                               Fused A, uint2* cellrank, unsigned* count, int wrap_mode,
+                               bool dirty, cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_from_reference<<<blocks_for(g.n), kBlock, 0, st>>>(g, agent_scene, scenes, A, cellrank,
+                                                         count, wrap_mode, dirty ? 1 : 0);
+    GS_LAUNCHED("fused_from_reference");
+    return GS_OK;
+}
+
+__global__ void k_recount(Fused A, unsigned n, const Scene* __restrict__ scenes,
+                          uint2* __restrict__ cellrank, unsigned* __restrict__ count,
+                          int wrap_mode) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Scene sc = scenes[u(A.f[4][i].w)];
+    unsigned cell;
+    const unsigned rank = count_next(sc, v3(A.f[0][i]), wrap_mode, count, cell);
+    cellrank[i] = make_uint2(cell, rank);
+}
+
+gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
+                        unsigned* count, int wrap_mode, cudaStream_t st) {
+    if (n == 0) return GS_OK;
+    k_recount<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, cellrank, count, wrap_mode);
+    GS_LAUNCHED("fused_recount");
+    return GS_OK;
+}
+
+// A (slot i) -> B (slot start[cell] + rank), wrapping the position.
+__global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n,
+                                                    const uint2* __restrict__ cellrank,
+                                                    const unsigned* __restrict__ start,
+                                                    const Scene* __restrict__ scenes,
+                                                    int wrap_mode, int dirty) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 cr = cellrank[i];
+    const unsigned dst = start[cr.x] + cr.y;
+    const float4 f0 = A.f[0][i];
+    const float4 f4v = A.f[4][i];
+    const Scene sc = scenes[u(f4v.w)];
+    const V3 wp = wrap_world(v3(f0), sc.grid.ws, wrap_mode);
+    B.f[0][dst] = make_float4(wp.x, wp.y, wp.z, f0.w);
+    B.f[1][dst] = A.f[1][i];
+    B.f[2][dst] = A.f[2][i];
+    B.f[3][dst] = A.f[3][i];
+    B.f[4][dst] = f4v;
+    if (dirty) B.f[5][dst] = A.f[5][i];
+}
+
+gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st) {
+    if (L.n == 0) return GS_OK;
+    k_permute<<<blocks_for(L.n), kBlock, 0, st>>>(L.A, L.B, L.n, L.cellrank, L.start, L.scenes,
+                                                  wrap_mode, dirty ? 1 : 0);
+    GS_LAUNCHED("fused_permute");
+    return GS_OK;
+}
+
+__device__ __forceinline__ FlockParams flock_params(const float v[5]) {
+    return FlockParams{v[0], v[1], v[2], v[3], __float_as_uint(v[4])};
+}
+
+// Neighbour accumulators of every behaviour that reads the KNN list.
+struct Accs {
+    FlockAcc sep, ali, coh;
+    AvoidAcc avoid;
+    CloseAcc close;
+};
+
+__device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, const FlockParams& fs,
+                                           const FlockParams& fa, const FlockParams& fc,
+                                           const Self& me, unsigned bid, float knn_d, V3 bpos,
+                                           V3 bdir, float bspeed, float bradius) {
+    const V3 offset = sub(bpos, me.pos);
+    const float dsq = dot(offset, offset);
+    const float d = sqrtf(dsq);
+    if (p.need & NEED_SEP) separation_add(a.sep, fs, me.dir, offset, dsq, d);
+    if (p.need & NEED_ALI) alignment_add(a.ali, fa, me.dir, offset, d, bdir);
+    if (p.need & NEED_COH) cohesion_add(a.coh, fc, me.dir, offset, d, bpos);
+    if (p.need & NEED_AVOID) avoid_add(a.avoid, me, bid, bpos, bdir, bspeed, bradius);
+    if (p.need & NEED_CLOSE) close_add(a.close, me, p.min_sep, knn_d, bpos, bradius);
+}
+
+// Behaviours order[first..] in order, then nothing else.
+__device__ __forceinline__ void finish_all(const Accs& a, const StepDev& p, unsigned first,
+                                           const FlockParams& fs, const FlockParams& fa,
+                                           const FlockParams& fc, const Self& me,
+                                           unsigned& applied, V3& steer) {
+#pragma unroll
+    for (unsigned o = 0; o < 8; ++o) {
+        if (o < first || o >= p.n_order) continue;
+        switch (p.order[o]) {
+            case GS_B_SEPARATION: flock_finish(0, a.sep, fs, me, applied, steer); break;
+            case GS_B_ALIGNMENT: flock_finish(1, a.ali, fa, me, applied, steer); break;
+            case GS_B_COHESION: flock_finish(2, a.coh, fc, me, applied, steer); break;
+            case GS_B_SEEK:
+                seek_finish(v3(p.seek_target[0], p.seek_target[1], p.seek_target[2]), p.w_seek,
+                            p.mask_seek, me, applied, steer);
+                break;
+            case GS_B_AVOID_NEIGHBORS:
+                if (p.avoid_close) close_finish(a.close, p.w_avoid, p.mask_avoid, applied, steer);
+                avoid_finish(a.avoid, p.w_avoid, p.mask_avoid, me, applied, steer);
+                break;
+            default: break;
+        }
+    }
+}
+
+__device__ __forceinline__ void init_accs(Accs& a, const StepDev& p) {
+    flock_init(a.sep);
+    flock_init(a.ali);
+    flock_init(a.coh);
+    avoid_init(a.avoid, p.min_time_col);
+    close_init(a.close);
+}
+
+__device__ __forceinline__ void store_next(const FusedLaunch& L, unsigned s, const Self& me,
+                                           unsigned id, unsigned scene, const Scene& sc,
+                                           int wrap_mode) {
+    L.A.f[0][s] = make_float4(me.pos.x, me.pos.y, me.pos.z, fb(id));
+    L.A.f[1][s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
+    L.A.f[2][s] = make_float4(me.side.x, me.side.y, me.side.z, me.radius);
+    L.A.f[3][s] = make_float4(me.up.x, me.up.y, me.up.z, me.mass);
+    L.A.f[4][s] = make_float4(me.max_speed, me.max_force, fb(0u), fb(scene));
+    unsigned cell;
+    const unsigned rank = count_next(sc, me.pos, wrap_mode, L.count, cell);
+    L.cellrank[s] = make_uint2(cell, rank);
+}
+
+__device__ __forceinline__ Self load_fused(const Fused& B, unsigned s, float4& f0, float4& f4v) {
+    f0 = B.f[0][s];
+    const float4 f1 = B.f[1][s], f2 = B.f[2][s], f3 = B.f[3][s];
+    f4v = B.f[4][s];
+    Self me;
+    me.pos = v3(f0);
+    me.dir = v3(f1);
+    me.speed = f1.w;
+    me.side = v3(f2);
+    me.radius = f2.w;
+    me.up = v3(f3);
+    me.mass = f3.w;
+    me.max_speed = f4v.x;
+    me.max_force = f4v.y;
+    return me;
+}
+
+// ---- whole step without walls -------------------------------------------------------
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_fused(FusedLaunch L, StepDev p) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.n) return;
+    float4 f0, f4v;
+    Self me = load_fused(L.B, s, f0, f4v);
+    const unsigned id = u(f0.w), scene = u(f4v.w);
+    unsigned applied = p.clear_applied ? 0u : u(f4v.z);
+    V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
+    const Scene sc = L.scenes[scene];
+
+    // The k neighbours (slot, KNN distance) go to this thread's column of
+    // shared memory so the accumulation loop below can index them at run time.
+    extern __shared__ unsigned sh_list[];
+    const unsigned bd = blockDim.x, t = threadIdx.x;
+    {
+        KList<KMAX> list;
+        list.init(int(p.k));
+        unsigned ix, iy, iz;
+        cell_coords(sc.grid, me.pos, ix, iy, iz);
+        const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
+        knn_scan_box<KMAX>(list, me.pos, id, sc.grid, box, sc.cell_offset, L.start, L.B.f[0]);
+        list.for_each(int(p.k), [&](int r, unsigned long long key, unsigned slot) {
+            sh_list[r * bd + t] = key_id(key) == UINT_MAX ? UINT_MAX : slot;
+            sh_list[(p.k + r) * bd + t] = __float_as_uint(key_dist(key));
+        });
+    }
+    const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
+    Accs a;
+    init_accs(a, p);
+    const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
+    const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
+    for (unsigned r = 0; r < p.k; ++r) {
+        const unsigned bs = sh_list[r * bd + t];
+        if (bs == UINT_MAX) break;
+        const float4 b0 = L.B.f[0][bs];
+        const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float br = need_rad ? L.B.f[2][bs].w : 0.f;
+        accumulate(a, p, fs, fa, fc, me, u(b0.w), __uint_as_float(sh_list[(p.k + r) * bd + t]),
+                   v3(b0), v3(b1), b1.w, br);
+    }
+    finish_all(a, p, 0, fs, fa, fc, me, applied, steer);
+    integrate(me, steer, p.dt);
+    store_next(L, s, me, id, scene, sc, p.wrap_mode);
+}
+
+// ---- wall phase: KNN, wall KNN and avoid-walls ---------------------------------------
+template <int KMAX, int KW>
+__global__ void __launch_bounds__(kBlock) k_fused_walls(FusedLaunch L, StepDev p) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.n) return;
+    float4 f0, f4v;
+    Self me = load_fused(L.B, s, f0, f4v);
+    const unsigned id = u(f0.w), scene = u(f4v.w);
+    unsigned applied = p.clear_applied ? 0u : u(f4v.z);
+    V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
+    const Scene sc = L.scenes[scene];
+    unsigned ix, iy, iz;
+    cell_coords(sc.grid, me.pos, ix, iy, iz);
+    const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
+    {
+        KList<KMAX> list;
+        list.init(int(p.k));
+        knn_scan_box<KMAX>(list, me.pos, id, sc.grid, box, sc.cell_offset, L.start, L.B.f[0]);
+        list.for_each(int(p.k), [&](int r, unsigned long long key, unsigned slot) {
+            L.knn_slot[size_t(r) * L.n + s] = key_id(key) == UINT_MAX ? UINT_MAX : slot;
+            L.knn_dist[size_t(r) * L.n + s] = key_dist(key);
+        });
+    }
+    if (sc.n_walls > 0 && L.w_pos_id != nullptr) {
+        extern __shared__ unsigned sh_lines[];
+        const unsigned bd = blockDim.x, t = threadIdx.x;
+        {
+            KList<KW> wl;
+            wl.init(int(p.knw));
+            knn_scan_box<KW>(wl, me.pos, UINT_MAX, sc.grid, box, sc.wall_cell_offset,
+                             L.w_cell_start, L.w_pos_id + sc.wall_offset);
+            wl.for_each(int(p.knw), [&](int r, unsigned long long key, unsigned) {
+                sh_lines[r * bd + t] = key_id(key);
+            });
+        }
+        WallAcc wa;
+        walls_init(wa, me, p.min_time_wall);
+        for (unsigned r = 0; r < p.knw; ++r) {
+            const unsigned line = sh_lines[r * bd + t];
+            if (line >= sc.n_walls) break;
+            const unsigned g = sc.wall_offset + line;
+            walls_add(wa, me, line, v3(L.w_start[g]), v3(L.w_end[g]), v3(L.w_normal[g]));
+        }
+        walls_finish(wa, p.w_walls, p.mask_walls, me, applied, steer);
+    } else if (!(applied & p.mask_walls)) {
+        steer = add(mul(v3(0.f, 0.f, 0.f), p.w_walls), steer);
+    }
+    L.w0[s] = make_float4(me.pos.x, me.pos.y, me.pos.z, f0.w);
+    L.w1[s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
+    L.w2[s] = make_float4(steer.x, steer.y, steer.z, fb(applied));
+}
+
+// ---- rest of the step after the wall phase --------------------------------------------
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_fused_rest(FusedLaunch L, StepDev p) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= L.n) return;
+    const float4 w0 = L.w0[s], w1 = L.w1[s], w2 = L.w2[s];
+    const float4 f2 = L.B.f[2][s], f3 = L.B.f[3][s], f4v = L.B.f[4][s];
+    Self me;
+    me.pos = v3(w0);
+    me.dir = v3(w1);
+    me.speed = w1.w;
+    me.side = v3(f2);
+    me.radius = f2.w;
+    me.up = v3(f3);
+    me.mass = f3.w;
+    me.max_speed = f4v.x;
+    me.max_force = f4v.y;
+    const unsigned id = u(w0.w), scene = u(f4v.w);
+    unsigned applied = u(w2.w);
+    V3 steer = v3(w2);
+    const Scene sc = L.scenes[scene];
+    const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
+    Accs a;
+    init_accs(a, p);
+    const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
+    const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
+    for (unsigned i = 0; i < p.k; ++i) {
+        const unsigned bs = L.knn_slot[size_t(i) * L.n + s];
+        if (bs == UINT_MAX) break;
+        const float4 b0 = L.w0[bs];
+        const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float br = need_rad ? L.B.f[2][bs].w : 0.f;
+        accumulate(a, p, fs, fa, fc, me, u(b0.w), L.knn_dist[size_t(i) * L.n + s], v3(b0),
+                   v3(b1), b1.w, br);
+    }
+    finish_all(a, p, 1, fs, fa, fc, me, applied, steer);
+    integrate(me, steer, p.dt);
+    store_next(L, s, me, id, scene, sc, p.wrap_mode);
+}
+
+template <int KMAX>
+static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream_t st) {
+    const unsigned nb = blocks_for(L.n);
+    if (p.need & NEED_WALLS) {
+        const size_t smem = size_t(p.knw) * kBlock * sizeof(unsigned);
+        k_fused_walls<KMAX, 8><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused_rest<KMAX><<<nb, kBlock, 0, st>>>(L, p);
+    } else {
+        const size_t smem = size_t(2 * p.k) * kBlock * sizeof(unsigned);
+        if (smem > 48 * 1024) {
+            static bool opted = false;
+            if (!opted) {
+                GS_CUDA(cudaFuncSetAttribute(k_fused<KMAX>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(2 * KMAX * kBlock * sizeof(unsigned))));
+                opted = true;
+            }
+        }
+        k_fused<KMAX><<<nb, kBlock, smem, st>>>(L, p);
+    }
+    GS_LAUNCHED("fused_step");
+    return GS_OK;
+}
+
+gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st) {
+    if (L.n == 0) return GS_OK;
+    if ((p.need & NEED_WALLS) && p.knw > 8)
+        return fail(GS_ERR_UNSUPPORTED, "knw > 8 in the fused step");
+    if (p.k <= 8) return launch_fused<8>(L, p, st);
+    if (p.k <= 16) return launch_fused<16>(L, p, st);
+    return launch_fused<32>(L, p, st);
+}
+
+// A -> reference layout (scatter by agent index).
+__global__ void k_to_reference(Fused A, unsigned n, const Scene* __restrict__ scenes,
+                               GroupView g) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float4 f0 = A.f[0][s], f1 = A.f[1][s], f2 = A.f[2][s], f3 = A.f[3][s], f4v = A.f[4][s];
+    const Scene sc = scenes[u(f4v.w)];
+    const unsigned i = sc.agent_offset + u(f0.w);
+    g.position[i] = make_float4(f0.x, f0.y, f0.z, 0.f);
+    g.direction[i] = make_float4(f1.x, f1.y, f1.z, 0.f);
+    g.speed[i] = f1.w;
+    g.side[i] = make_float3(f2.x, f2.y, f2.z);
+    g.radius[i] = f2.w;
+    g.up[i] = make_float3(f3.x, f3.y, f3.z);
+    g.mass[i] = f3.w;
+    g.max_speed[i] = f4v.x;
+    g.max_force[i] = f4v.y;
+    g.applied[i] = u(f4v.z);
+    g.steering[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView g,
+                             cudaStream_t st) {
+    if (n == 0) return GS_OK;
+    k_to_reference<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, g);
+    GS_LAUNCHED("fused_to_reference");
+    return GS_OK;
+}
+
+}  // namespace gs

@@ -1,0 +1,317 @@
+"""Python mirror of the reference's group API over the C ABI.
+
+Classes follow the reference objects (AgentGroup, KNNData, KNNBinData,
+WallGroup) and the free functions keep the names and argument order of
+include/OpenSteer/CUDA/GroupSteerLibrary.cuh:43-223, so a plugin's update
+(e.g. plugins/BoidsGroup.cpp:606-637) reads the same here.  Failures raise
+GpuSteerError instead of aborting the process.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import AgentArrays, StepParams as _StepParamsC, call
+from .scenario import StepParams, WRAP_REFERENCE
+from .state import AgentState
+
+_fp = C.POINTER(C.c_float)
+_up = C.POINTER(C.c_uint)
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def _u3(v):
+    return (C.c_uint * 3)(*[int(x) for x in v])
+
+
+def _ptr(a: np.ndarray, t=C.c_float):
+    if not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous")
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def host_arrays(s: AgentState) -> AgentArrays:
+    """AgentArrays pointing at the numpy arrays of `s` (kept alive by the caller)."""
+    a = AgentArrays()
+    for k in AgentState.float_names():
+        arr = getattr(s, k)
+        if arr.dtype != np.float32:
+            raise TypeError(f"{k} must be float32")
+        setattr(a, k, _ptr(arr))
+    if s.applied.dtype != np.uint32:
+        raise TypeError("applied must be uint32")
+    a.applied = _ptr(s.applied, C.c_uint)
+    return a
+
+
+def step_params_c(p: StepParams) -> _StepParamsC:
+    s = _StepParamsC()
+    for name, _ in _StepParamsC._fields_:
+        if name in ("order", "n_order"):
+            continue
+        v = getattr(p, name)
+        if isinstance(v, (tuple, list)):
+            arr = getattr(s, name)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(s, name, v)
+    if len(p.order) > 8:
+        raise ValueError("at most 8 behaviours")
+    for i, b in enumerate(p.order):
+        s.order[i] = int(b)
+    s.n_order = len(p.order)
+    return s
+
+
+class KNNBinData:
+    """KNNBinDataV2(worldCells, worldSize, searchRadius), KNNBinDataV2.cu:30-42."""
+
+    def __init__(self, world_cells, world_size, search_radius: int = 1):
+        h = C.c_void_p()
+        call("gs_bins_create", _u3(world_cells), _f3(world_size), int(search_radius), C.byref(h))
+        self._h = h
+        self.world_cells = tuple(int(x) for x in world_cells)
+        self.world_size = tuple(float(x) for x in world_size)
+        self.search_radius = int(search_radius)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def num_cells(self) -> int:
+        n = C.c_uint()
+        call("gs_bins_num_cells", self._h, C.byref(n))
+        return n.value
+
+    def hv_cells(self):
+        """(min, max, centre) float3 per cell in bin_cell order."""
+        n = self.num_cells
+        lo, hi, c = (np.zeros((n, 3), np.float32) for _ in range(3))
+        call("gs_bins_get_cells", self._h, _ptr(lo), _ptr(hi), _ptr(c), n)
+        return lo, hi, c
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_bins_destroy(self._h)
+            self._h = None
+
+
+class AgentGroup:
+    """AgentGroup(worldCells, knn) (src/AgentGroup.cpp:8-11) with its device
+    arrays and binning database."""
+
+    def __init__(self, k: int, capacity: int, stream: int | None = None):
+        h = C.c_void_p()
+        call("gs_group_create", int(k), int(capacity), C.c_void_p(stream) if stream else None,
+             C.byref(h))
+        self._h = h
+        self.k = int(k)
+        self.capacity = int(capacity)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def upload(self, s: AgentState) -> None:
+        """Clear + AddAgent* + SyncDevice."""
+        a = host_arrays(s)
+        call("gs_group_upload", self._h, C.byref(a), s.n)
+        # the copies are asynchronous: keep the host arrays alive until done
+        call("gs_group_synchronize", self._h)
+
+    def download(self) -> AgentState:
+        """SyncHost: the whole state as host arrays."""
+        out = AgentState.zeros(self.size)
+        a = host_arrays(out)
+        call("gs_group_download", self._h, C.byref(a))
+        return out
+
+    @property
+    def size(self) -> int:
+        n = C.c_uint()
+        call("gs_group_size", self._h, C.byref(n))
+        return n.value
+
+    def device_arrays(self) -> dict:
+        """pdPosition()/pdDirection()/...: device addresses (ints)."""
+        a = AgentArrays()
+        call("gs_group_device_arrays", self._h, C.byref(a))
+        return {name: C.cast(getattr(a, name), C.c_void_p).value for name, _ in AgentArrays._fields_}
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        call("gs_group_stream", self._h, C.byref(s))
+        return s.value or 0
+
+    def synchronize(self) -> None:
+        call("gs_group_synchronize", self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_group_destroy(self._h)
+            self._h = None
+
+
+class KNNData:
+    """KNNData(nSize, nK): column-major k x n indices and distances."""
+
+    def __init__(self, n: int, k: int):
+        h = C.c_void_p()
+        call("gs_knn_create", int(n), int(k), C.byref(h))
+        self._h = h
+        self.n, self.k = int(n), int(k)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def download(self, group: AgentGroup | None = None):
+        idx = np.empty(self.k * self.n, np.uint32)
+        dist = np.empty(self.k * self.n, np.float32)
+        call("gs_knn_download", self._h, group.handle if group else None, _ptr(idx, C.c_uint),
+             _ptr(dist))
+        return idx, dist
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_knn_destroy(self._h)
+            self._h = None
+
+
+class WallGroup:
+    """WallGroup: LoadFromFile + SplitWalls + SyncDevice (ChokePointNew.cpp:107-119)."""
+
+    def __init__(self, rows: np.ndarray | None = None, bins: KNNBinData | None = None,
+                 knw: int = 3, path: str | None = None):
+        h = C.c_void_p()
+        if path is not None:
+            call("gs_walls_load", path.encode(), bins.handle if bins else None, int(knw),
+                 C.byref(h))
+        else:
+            rows = np.asarray(rows, np.float32).reshape(-1, 9)
+            n = rows.shape[0]
+            st = np.zeros((n, 4), np.float32)
+            en = np.zeros((n, 4), np.float32)
+            nm = np.zeros((n, 4), np.float32)
+            st[:, :3], en[:, :3], nm[:, :3] = rows[:, 0:3], rows[:, 3:6], rows[:, 6:9]
+            call("gs_walls_create", _ptr(st), _ptr(en), _ptr(nm), n,
+                 bins.handle if bins else None, int(knw), C.byref(h))
+        self._h = h
+        self.knw = int(knw)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def size(self) -> int:
+        n = C.c_uint()
+        call("gs_walls_size", self._h, C.byref(n))
+        return n.value
+
+    def download(self):
+        n = self.size
+        out = [np.zeros((n, 4), np.float32) for _ in range(4)]
+        call("gs_walls_download", self._h, *[_ptr(o) for o in out], n)
+        return tuple(out)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_walls_destroy(self._h)
+            self._h = None
+
+
+# ---- GroupSteerLibrary.cuh -----------------------------------------------------------
+
+def wrapWorld(group: AgentGroup, world_size, mode: int = WRAP_REFERENCE) -> None:
+    call("gs_wrap_world", group.handle, _f3(world_size), int(mode))
+
+
+def updateKNNDatabase(group, bins: KNNBinData) -> None:
+    if isinstance(group, WallGroup):
+        call("gs_walls_update_knn_database", group.handle, bins.handle)
+    else:
+        call("gs_update_knn_database", group.handle, bins.handle)
+
+
+def findKNearestNeighbors(group: AgentGroup, knn: KNNData, bins: KNNBinData, other,
+                          search_radius: int = 1) -> None:
+    if isinstance(other, WallGroup):
+        call("gs_find_knn_walls", group.handle, knn.handle, bins.handle, other.handle,
+             int(search_radius))
+    else:
+        call("gs_find_knn", group.handle, knn.handle, bins.handle, other.handle,
+             int(search_radius))
+
+
+def findKNearestNeighborsBruteForce(group: AgentGroup, knn: KNNData, other: AgentGroup) -> None:
+    call("gs_knn_bruteforce", group.handle, knn.handle, other.handle)
+
+
+def steerForSeparation(group, knn, other, min_distance, max_distance, cos_max_angle, weight,
+                       do_not_apply_with=0) -> None:
+    call("gs_steer_for_separation", group.handle, knn.handle, other.handle, min_distance,
+         max_distance, cos_max_angle, weight, int(do_not_apply_with))
+
+
+def steerForAlignment(group, knn, other, min_distance, max_distance, cos_max_angle, weight,
+                      do_not_apply_with=0) -> None:
+    call("gs_steer_for_alignment", group.handle, knn.handle, other.handle, min_distance,
+         max_distance, cos_max_angle, weight, int(do_not_apply_with))
+
+
+def steerForCohesion(group, knn, other, min_distance, max_distance, cos_max_angle, weight,
+                     do_not_apply_with=0) -> None:
+    call("gs_steer_for_cohesion", group.handle, knn.handle, other.handle, min_distance,
+         max_distance, cos_max_angle, weight, int(do_not_apply_with))
+
+
+def steerForSeek(group, target, weight, do_not_apply_with=0) -> None:
+    call("gs_steer_for_seek", group.handle, _f3(target), weight, int(do_not_apply_with))
+
+
+def steerToAvoidNeighbors(group, knn, other, min_time_to_collision, min_separation_distance,
+                          avoid_close_neighbors, weight, do_not_apply_with=0) -> None:
+    call("gs_steer_to_avoid_neighbors", group.handle, knn.handle, other.handle,
+         min_time_to_collision, min_separation_distance, int(bool(avoid_close_neighbors)),
+         weight, int(do_not_apply_with))
+
+
+def steerToAvoidWalls(group, knw, walls, min_time_to_collision, weight,
+                      do_not_apply_with=0) -> None:
+    call("gs_steer_to_avoid_walls", group.handle, knw.handle, walls.handle,
+         min_time_to_collision, weight, int(do_not_apply_with))
+
+
+def updateGroup(group, elapsed_time) -> None:
+    call("gs_update_group", group.handle, elapsed_time)
+
+
+def antiPenetrationAgents(group, knn, other, do_not_apply_with=0) -> None:
+    call("gs_anti_penetration_agents", group.handle, knn.handle, other.handle,
+         int(do_not_apply_with))
+
+
+def step(group: AgentGroup, bins: KNNBinData, walls: WallGroup | None, params: StepParams,
+         steps: int = 1) -> None:
+    """The fused whole step, `steps` times."""
+    p = step_params_c(params)
+    call("gs_step", group.handle, bins.handle, walls.handle if walls else None, C.byref(p),
+         int(steps))
+
+
+def step_host(group: AgentGroup, bins: KNNBinData, walls, params: StepParams, steps: int,
+              state_in: AgentState, state_out: AgentState) -> None:
+    """Upload from host arrays, `steps` fused steps, download into state_out."""
+    p = step_params_c(params)
+    a_in, a_out = host_arrays(state_in), host_arrays(state_out)
+    call("gs_step_host", group.handle, bins.handle, walls.handle if walls else None, C.byref(p),
+         int(steps), C.byref(a_in), state_in.n, C.byref(a_out))

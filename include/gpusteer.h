@@ -1,0 +1,228 @@
+/*
+ * gpusteer.h - C ABI of the GB300 (sm_103a) GPUSteer group library.
+ *
+ * This is the drop-in boundary for PsychoLogicAu/GPUSteer's group steering
+ * path.  The reference exposes it as C++ objects and `static` free functions
+ * (include/OpenSteer/CUDA/GroupSteerLibrary.cuh:43-223) over AgentGroup,
+ * KNNData, KNNBinData and WallGroup; every entry point below names the
+ * reference interface it replaces.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every function returns gs_status; GS_OK is 0.  gs_last_error() gives a
+ *    per-thread message for the last failure.  Nothing aborts the process
+ *    (the reference's CUDA_SAFE_CALL / cutilCheckMsg do).
+ *  - Host arrays use the reference layouts (AgentGroupData.cuh:30-46):
+ *    float4 position/direction/steering (w = 0), float3 side/up, float
+ *    speed/maxSpeed/maxForce/radius/mass, uint appliedKernels.  KNN results
+ *    are column-major idx[a + i*n] (KNNBinningV2Kernel.cu:524-525).
+ *  - Each group owns a CUDA stream (or uses the one passed in); calls on a
+ *    group are asynchronous on that stream unless they return host data.
+ *    Calls on one handle must not be made concurrently from several threads.
+ *  - Arithmetic is IEEE binary32 without FMA contraction; KNN ties break by
+ *    the lower agent index.
+ */
+#ifndef GPUSTEER_H
+#define GPUSTEER_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int gs_status;
+#define GS_OK 0
+#define GS_ERR_INVALID_ARG 1
+#define GS_ERR_OOM 2
+#define GS_ERR_CUDA 3
+#define GS_ERR_TIMEOUT 4
+#define GS_ERR_NONFINITE 5
+#define GS_ERR_STATE 6
+#define GS_ERR_UNSUPPORTED 7
+
+typedef struct gs_bins_s* gs_bins;     /* KNNBinDataV2 (KNNBinDataV2.cuh:18-63)        */
+typedef struct gs_group_s* gs_group;   /* AgentGroup + KNNDatabase (AgentGroup.h:12-56) */
+typedef struct gs_knn_s* gs_knn;       /* KNNData (KNNData.cuh:10-55)                   */
+typedef struct gs_walls_s* gs_walls;   /* WallGroup (WallGroup.h:12-37)                 */
+
+/* Pointers to one group's arrays (host or device, per the call). */
+typedef struct gs_agent_arrays {
+    float* position;  /* float4[n] */
+    float* direction; /* float4[n] */
+    float* steering;  /* float4[n] */
+    float* side;      /* float3[n] */
+    float* up;        /* float3[n] */
+    float* speed;
+    float* max_speed;
+    float* max_force;
+    float* radius;
+    float* mass;
+    unsigned* applied;
+} gs_agent_arrays;
+
+/* Wrap modes of gs_wrap_world and gs_step_params.wrap_mode. */
+#define GS_WRAP_REFERENCE 0 /* WrapWorldCUDAKernel.cu:27-43 (z < 0 -> halfZ + 100) */
+#define GS_WRAP_SYMMETRIC 1 /* z wrapped like x and y                              */
+#define GS_WRAP_NONE 2
+
+/* Behaviour codes of gs_step_params.order. */
+#define GS_B_AVOID_WALLS 1
+#define GS_B_AVOID_NEIGHBORS 2
+#define GS_B_SEPARATION 3
+#define GS_B_ALIGNMENT 4
+#define GS_B_COHESION 5
+#define GS_B_SEEK 6
+
+#define GS_KNN_BINNED 0
+#define GS_KNN_BRUTEFORCE 1
+
+/* One whole step (a plugin's XxxGroup::update, e.g. plugins/BoidsGroup.cpp:606-637,
+ * plugins/ChokePointNew.cpp:586-630): wrap, rebuild the bins, KNN (and wall
+ * KNN), the behaviours in `order`, then UpdateCUDAKernel. */
+typedef struct gs_step_params {
+    float world_size[3];
+    unsigned world_cells[3];
+    unsigned search_radius;
+    int wrap_mode;
+    int knn_mode;
+    unsigned k;
+    int clear_applied; /* zero appliedKernels at step start (ChokePointNew.cpp:595) */
+    unsigned knw;
+    float min_time_to_wall, w_walls;
+    unsigned mask_walls;
+    float min_time_to_collision, min_separation_distance;
+    int avoid_close;
+    float w_avoid;
+    unsigned mask_avoid;
+    float sep_min, sep_max, sep_cos, w_sep;
+    unsigned mask_sep;
+    float ali_min, ali_max, ali_cos, w_ali;
+    unsigned mask_ali;
+    float coh_min, coh_max, coh_cos, w_coh;
+    unsigned mask_coh;
+    float seek_target[3], w_seek;
+    unsigned mask_seek;
+    unsigned order[8];
+    unsigned n_order;
+    float dt;
+} gs_step_params;
+
+/* ---- library -------------------------------------------------------------- */
+const char* gs_status_string(gs_status s);
+const char* gs_last_error(void);
+int gs_version(void);
+/* Largest k the KNN kernels accept. */
+unsigned gs_max_k(void);
+
+/* ---- KNNBinData: KNNBinDataV2::KNNBinDataV2(worldCells, worldSize, searchRadius),
+ *      KNNBinDataV2.cu:30-42.  No device neighbour table is built: the
+ *      (2r+1)^d neighbour cells are computed arithmetically. */
+gs_status gs_bins_create(const unsigned world_cells[3], const float world_size[3],
+                         unsigned search_radius, gs_bins* out);
+gs_status gs_bins_destroy(gs_bins bins);
+gs_status gs_bins_num_cells(gs_bins bins, unsigned* out);
+/* KNNBinDataV2::hvCells(): float3 min bound, max bound and centre per cell in
+ * bin_cell order (KNNBinDataV2.cu:103-135). */
+gs_status gs_bins_get_cells(gs_bins bins, float* min3, float* max3, float* centre3, unsigned cap);
+
+/* ---- AgentGroup ------------------------------------------------------------- */
+/* AgentGroup(worldCells, knn) (src/AgentGroup.cpp:8-11).  `k` is the
+ * KNNDatabase's k; `capacity` bounds the agent count.  `stream` may be NULL
+ * (the group creates its own non-blocking stream). */
+gs_status gs_group_create(unsigned k, unsigned capacity, void* stream, gs_group* out);
+gs_status gs_group_destroy(gs_group g);
+/* Clear + AddAgent* + SyncDevice (src/AgentGroup.cpp:34-55,97-108,128-133):
+ * replaces the group's agents with n agents copied from host arrays. */
+gs_status gs_group_upload(gs_group g, const gs_agent_arrays* host, unsigned n);
+/* SyncHost (AgentGroupData.cuh:177-225): copies the device state to host arrays
+ * (any member may be NULL to skip it) and waits for the copy. */
+gs_status gs_group_download(gs_group g, const gs_agent_arrays* host);
+gs_status gs_group_size(gs_group g, unsigned* n);
+/* pdPosition()/pdDirection()/... accessors (AgentGroup.h:51-54,
+ * AgentGroupData.cuh:62-110): device pointers in the reference layout. */
+gs_status gs_group_device_arrays(gs_group g, gs_agent_arrays* dev);
+gs_status gs_group_stream(gs_group g, void** stream);
+gs_status gs_group_synchronize(gs_group g);
+
+/* ---- KNNData: KNNData(nSize, nK) (KNNData.cu) ---------------------------------- */
+gs_status gs_knn_create(unsigned n, unsigned k, gs_knn* out);
+gs_status gs_knn_destroy(gs_knn knn);
+/* KNNData::syncHost + hvKNNIndices/hvKNNDistances (column-major, k*n). */
+gs_status gs_knn_download(gs_knn knn, gs_group g, unsigned* idx, float* dist);
+gs_status gs_knn_device_arrays(gs_knn knn, unsigned** idx, float** dist);
+
+/* ---- WallGroup: WallGroup::LoadFromFile + SplitWalls + SyncDevice
+ *      (WallGroupData.cu:73-206, plugins/ChokePointNew.cpp:107-119) ------------- */
+/* Segments from host float4 arrays (start, end, normal; mid = (start+end)/2).
+ * When `bins` is given the walls are split at its cell boundaries.  `knw` is
+ * the wall database's k. */
+gs_status gs_walls_create(const float* start4, const float* end4, const float* normal4,
+                          unsigned n, gs_bins bins, unsigned knw, gs_walls* out);
+/* Reads a .map file: 9 floats per segment. */
+gs_status gs_walls_load(const char* path, gs_bins bins, unsigned knw, gs_walls* out);
+gs_status gs_walls_destroy(gs_walls w);
+gs_status gs_walls_size(gs_walls w, unsigned* n);
+gs_status gs_walls_download(gs_walls w, float* start4, float* mid4, float* end4, float* normal4,
+                            unsigned cap);
+
+/* ---- GroupSteerLibrary.cuh free functions ----------------------------------------- */
+/* wrapWorld (GroupSteerLibrary.cuh:43-50). */
+gs_status gs_wrap_world(gs_group g, const float world_size[3], int mode);
+/* updateKNNDatabase (GroupSteerLibrary.cuh:129-136): counting-sort rebuild. */
+gs_status gs_update_knn_database(gs_group g, gs_bins bins);
+gs_status gs_walls_update_knn_database(gs_walls w, gs_bins bins);
+/* findKNearestNeighbors (GroupSteerLibrary.cuh:138-157), binned.  `other` may
+ * equal `g` (self KNN).  k is the KNNData's k.  Both databases must be
+ * current (gs_update_knn_database). */
+gs_status gs_find_knn(gs_group g, gs_knn out, gs_bins bins, gs_group other,
+                      unsigned search_radius);
+/* findKNearestNeighbors against a WallGroup (plugins/ChokePointNew.cpp:600). */
+gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls,
+                            unsigned search_radius);
+/* KNNBruteForceCUDAV2 (KNNBruteForceCUDA.cu:163-187). */
+gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other);
+/* steerForSeparation / steerForAlignment / steerForCohesion
+ * (GroupSteerLibrary.cuh:161-186). */
+gs_status gs_steer_for_separation(gs_group g, gs_knn knn, gs_group other, float min_distance,
+                                  float max_distance, float cos_max_angle, float weight,
+                                  unsigned do_not_apply_with);
+gs_status gs_steer_for_alignment(gs_group g, gs_knn knn, gs_group other, float min_distance,
+                                 float max_distance, float cos_max_angle, float weight,
+                                 unsigned do_not_apply_with);
+gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float min_distance,
+                                float max_distance, float cos_max_angle, float weight,
+                                unsigned do_not_apply_with);
+/* steerForSeek (GroupSteerLibrary.cuh:52-59). */
+gs_status gs_steer_for_seek(gs_group g, const float target[3], float weight,
+                            unsigned do_not_apply_with);
+/* steerToAvoidNeighbors (GroupSteerLibrary.cuh:111-118). */
+gs_status gs_steer_to_avoid_neighbors(gs_group g, gs_knn knn, gs_group other,
+                                      float min_time_to_collision, float min_separation_distance,
+                                      int avoid_close_neighbors, float weight,
+                                      unsigned do_not_apply_with);
+/* steerToAvoidWalls (GroupSteerLibrary.cuh:120-127). */
+gs_status gs_steer_to_avoid_walls(gs_group g, gs_knn knw, gs_walls walls,
+                                  float min_time_to_collision, float weight,
+                                  unsigned do_not_apply_with);
+/* updateGroup (GroupSteerLibrary.cuh:189-196). */
+gs_status gs_update_group(gs_group g, float elapsed_time);
+/* antiPenetrationAgents (GroupSteerLibrary.cuh:216-223). */
+gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other,
+                                     unsigned do_not_apply_with);
+
+/* ---- fused step -------------------------------------------------------------- */
+/* Runs `steps` whole steps; the result equals the per-function sequence
+ * wrap -> rebuild -> KNN (+ wall KNN) -> behaviours in p->order -> update.
+ * Requires knn_mode GS_KNN_BINNED, and avoid-walls (if present) first in order.
+ * `walls` may be NULL when the order has no GS_B_AVOID_WALLS. */
+gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
+                  unsigned steps);
+/* As gs_step but the state comes from and goes back to host arrays, each copy
+ * on the group's stream (the reference's per-frame SyncDevice / SyncHost). */
+gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
+                       unsigned steps, const gs_agent_arrays* in, unsigned n,
+                       const gs_agent_arrays* out);
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,129 @@
+"""CPU-only checks of the C ABI library and the host-side logic."""
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import gpusteer_gb300 as gs
+from gpusteer_gb300 import _lib, scenario as sc
+from gpusteer_gb300.state import AgentState
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+def header_functions():
+    text = (REPO / "include" / "gpusteer.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gs_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_function():
+    lib = _lib.load()
+    names = header_functions()
+    assert len(names) > 30
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_bindings_cover_the_header():
+    assert set(header_functions()) == set(_lib.SIGNATURES)
+
+
+def test_status_strings_and_version():
+    lib = _lib.load()
+    assert lib.gs_version() >= 1
+    assert lib.gs_status_string(0) == b"ok"
+    assert lib.gs_status_string(1) == b"invalid argument"
+    assert lib.gs_max_k() == 64
+
+
+def test_bins_host_side_matches_reference_cell_layout():
+    b = gs.KNNBinData((8, 1, 4), (16.0, 10.0, 8.0), 1)
+    assert b.num_cells == 32
+    lo, hi, c = b.hv_cells()
+    # bin_cell order: width fastest, then depth, then height (KNNBinDataV2.cu:103-116)
+    np.testing.assert_allclose(lo[0], [-8.0, -5.0, -4.0])
+    np.testing.assert_allclose(lo[1], [-6.0, -5.0, -4.0])
+    np.testing.assert_allclose(lo[8], [-8.0, -5.0, -2.0])
+    np.testing.assert_allclose(hi[31], [8.0, 5.0, 4.0])
+    np.testing.assert_allclose(c[0], [-7.0, 0.0, -3.0])
+
+
+@pytest.mark.parametrize("cells,size", [((0, 1, 1), (1, 1, 1)), ((1, 1, 1), (0, 1, 1)),
+                                        ((1, 1, 1), (float("nan"), 1, 1))])
+def test_bins_reject_bad_grids(cells, size):
+    with pytest.raises(gs.GpuSteerError) as e:
+        gs.KNNBinData(cells, size, 1)
+    assert e.value.status == 1
+
+
+def test_splitmix_stream_is_fixed():
+    # first outputs of splitmix64 seeded with 0 (published test values)
+    v = sc.splitmix64(0, 3)
+    assert [hex(int(x)) for x in v] == ["0xe220a8397b1dcdaf", "0x6e789e6aa1b965f4",
+                                        "0x6c45d188009454f"]
+    u = sc.uniform01(7, 1000)
+    assert u.dtype == np.float32 and u.min() >= 0 and u.max() < 1
+
+
+def test_scenarios_are_deterministic_and_in_range():
+    a = sc.boids_sphere(500, seed=3)
+    b = sc.boids_sphere(500, seed=3)
+    for k in AgentState.names():
+        np.testing.assert_array_equal(getattr(a, k), getattr(b, k))
+    r = np.linalg.norm(a.position[:, :3], axis=1)
+    assert r.max() < 50 and np.allclose(np.linalg.norm(a.direction[:, :3], axis=1), 1, atol=1e-5)
+    c = sc.chokepoint_agents(300, seed=1)
+    assert (c.position[:, 1] == 0).all() and (c.speed == 0).all()
+    assert c.position[:, 2].min() >= 13.5 and c.position[:, 2].max() <= 113.5
+    q = sc.boids_cube(1000, size=512.0, seed=2)
+    assert np.abs(q.position[:, :3]).max() <= 256
+
+
+def test_params_reader_parses_reference_format():
+    text = """# comment
+    seed = 12345
+    knn = 6
+    cosMaxFlockingAngle = -0.5
+    maskAlignment = 272 # trailing comment
+    <world>
+        dimensions = 2048 10 2048
+        cells = 512 1 512
+        # mapFilename = none
+    </world>
+    <group>
+        numAgents = 10
+        <path>
+            point = 0 0 1
+            point = 0 0 -2
+            cyclic = 0
+        </path>
+    </group>
+    </simulation>"""
+    p = sc.load_params(text)
+    assert p.values["seed"] == 12345 and p.values["knn"] == 6
+    assert p.values["maskAlignment"] == 272
+    assert p.world["cells"] == (512, 1, 512)
+    assert p.groups[0]["numAgents"] == 10 and len(p.groups[0]["path"]) == 2
+    with pytest.raises(sc.ParamsError):
+        sc.load_params("bogusKey = 1\n</simulation>")
+
+
+def test_reference_params_files_parse():
+    data = Path("/root/reference/data")
+    if not data.exists():
+        pytest.skip("reference data not mounted")
+    for name in ("BoidsGroup.params", "ChokePoint.params", "MultiGroup.params"):
+        p = sc.load_params((data / name).read_text())
+        assert "knn" in p.values and p.groups
+    sp = sc.params_from_file(sc.load_params((data / "BoidsGroup.params").read_text()), 1 / 60)
+    assert sp.k == 6 and sp.mask_ali == 16 and sp.world_cells == (94, 94, 94)
+
+
+def test_step_params_struct_roundtrip():
+    p = sc.chokepoint_params()
+    c = gs.groups.step_params_c(p)
+    assert c.k == 16 and c.knw == 3 and c.n_order == 4
+    assert list(c.order)[:4] == [1, 2, 3, 6]
+    assert abs(c.dt - 1 / 30) < 1e-7 and c.mask_seek == 4480

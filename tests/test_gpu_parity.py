@@ -1,0 +1,415 @@
+"""sm_103a kernels against the CPU oracle and the reference's golden vectors,
+through the C ABI.  Bit-exact: every result is compared with
+np.testing.assert_array_equal (KNN indices and distances, forces, state)."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import gpusteer_gb300 as gs
+import oracle_lib as ol
+from gpusteer_gb300 import scenario as sc
+from gpusteer_gb300.state import AgentState
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def load(name):
+    z = np.load(GOLD / f"{name}.npz")
+    return z, json.loads(str(z["meta"]))
+
+
+def gstate(z, prefix):
+    return AgentState(**{k: np.array(z[prefix + k], copy=True) for k in AgentState.names()})
+
+
+def assert_state(got: AgentState, want: AgentState, skip_side=None, fields=None):
+    for k in fields or AgentState.names():
+        a, b = getattr(got, k), getattr(want, k)
+        if k == "side" and skip_side is not None:
+            a, b = a[~skip_side], b[~skip_side]
+        np.testing.assert_array_equal(a, b, err_msg=k)
+
+
+def group_of(s: AgentState, k=16):
+    g = gs.AgentGroup(k, max(1, s.n))
+    g.upload(s)
+    return g
+
+
+def pos_state(pos4):
+    s = AgentState.zeros(pos4.shape[0])
+    s.position[:] = pos4
+    return s
+
+
+# ---- KNN ----------------------------------------------------------------------------
+
+def gpu_knn_binned(posA, posB, self_, ws, wc, r, k):
+    bins = gs.KNNBinData(wc, ws, r)
+    A = group_of(pos_state(posA), k)
+    gs.updateKNNDatabase(A, bins)
+    if self_:
+        B = A
+    else:
+        B = group_of(pos_state(posB), k)
+        gs.updateKNNDatabase(B, bins)
+    knn = gs.KNNData(posA.shape[0], k)
+    gs.findKNearestNeighbors(A, knn, bins, B, r)
+    return knn.download(A)
+
+
+def test_knn_binned_matches_reference_golden_3d():
+    z, m = load("knn_binned_3d")
+    i, d = gpu_knn_binned(z["pos_self"], z["pos_self"], True, m["ws"], m["wc"], 1, m["k_self"])
+    np.testing.assert_array_equal(i, z["idx_self"])
+    np.testing.assert_array_equal(d, z["dist_self"])
+    i, d = gpu_knn_binned(z["pos_a"], z["pos_b"], False, m["ws"], m["wc"], 1, m["k_cross"])
+    np.testing.assert_array_equal(i, z["idx_cross"])
+    np.testing.assert_array_equal(d, z["dist_cross"])
+
+
+def test_knn_binned_matches_reference_golden_2d():
+    z, m = load("knn_binned_2d")
+    for r in (1, 2):
+        i, d = gpu_knn_binned(z["pos"], z["pos"], True, m["ws"], m["wc"], r, m["k"])
+        np.testing.assert_array_equal(i, z[f"idx_r{r}"])
+        np.testing.assert_array_equal(d, z[f"dist_r{r}"])
+
+
+@pytest.mark.parametrize("k", [1, 7, 16, 24, 33, 64])
+def test_knn_binned_matches_oracle_all_k(k):
+    p = sc.boids_sphere(3000, radius=20.0, seed=k).position
+    ws, wc = (64.0, 64.0, 64.0), (16, 16, 16)
+    i, d = gpu_knn_binned(p, p, True, ws, wc, 1, k)
+    oi, od = ol.knn_binned(p, p, True, ws, wc, 1, k)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+
+
+def test_knn_ties_break_by_lower_index():
+    # integer lattice with duplicated points: many exactly equal distances
+    g = np.stack(np.meshgrid(np.arange(6), np.arange(6), np.arange(6), indexing="ij"), -1)
+    g = g.reshape(-1, 3).astype(np.float32) - 3.0
+    pts = np.concatenate([g, g[::7]])  # duplicates at distance 0
+    p = np.zeros((pts.shape[0], 4), np.float32)
+    p[:, :3] = pts
+    ws, wc = (16.0, 16.0, 16.0), (8, 8, 8)
+    for k in (6, 16):
+        i, d = gpu_knn_binned(p, p, True, ws, wc, 1, k)
+        oi, od = ol.knn_binned(p, p, True, ws, wc, 1, k)
+        np.testing.assert_array_equal(i, oi)
+        np.testing.assert_array_equal(d, od)
+        bi, bd = ol.knn_brute(p, p, True, k)
+        # every agent has its 26-neighbourhood inside the 27-cell box here only
+        # for interior agents; compare those with brute force
+        n = p.shape[0]
+        sel = (np.abs(pts) <= 1).all(1)
+        for s in range(k):
+            np.testing.assert_array_equal(i[s * n:(s + 1) * n][sel], bi[s * n:(s + 1) * n][sel])
+
+
+def test_knn_edge_cases():
+    ws, wc = (32.0, 32.0, 32.0), (8, 8, 8)
+    # fewer candidates than k: padding is (UINT_MAX, FLT_MAX); agents outside
+    # the world clamp into the edge cells.
+    p = np.array([[0, 0, 0, 0], [1, 0, 0, 0], [100, 100, 100, 0], [-100, 5, 5, 0],
+                  [15.9, 15.9, 15.9, 0]], np.float32)
+    i, d = gpu_knn_binned(p, p, True, ws, wc, 1, 8)
+    oi, od = ol.knn_binned(p, p, True, ws, wc, 1, 8)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+    assert (i == 0xFFFFFFFF).sum() > 0 and (d[i == 0xFFFFFFFF] == np.finfo(np.float32).max).all()
+    # a single agent
+    i, d = gpu_knn_binned(p[:1], p[:1], True, ws, wc, 1, 4)
+    assert (i == 0xFFFFFFFF).all()
+
+
+def test_knn_bruteforce_matches_reference_golden():
+    z, m = load("knn_brute")
+    A = group_of(pos_state(z["pos"]))
+    knn = gs.KNNData(A.size, m["k_self"])
+    gs.findKNearestNeighborsBruteForce(A, knn, A)
+    i, d = knn.download(A)
+    np.testing.assert_array_equal(i, z["idx_self"])
+    np.testing.assert_array_equal(d, z["dist_self"])
+    A2 = group_of(pos_state(z["pos"][:500].copy()))
+    B2 = group_of(pos_state(z["pos_b"]))
+    knn2 = gs.KNNData(500, m["k_cross"])
+    gs.findKNearestNeighborsBruteForce(A2, knn2, B2)
+    i, d = knn2.download(A2)
+    np.testing.assert_array_equal(i, z["idx_cross"])
+    np.testing.assert_array_equal(d, z["dist_cross"])
+
+
+def test_knn_bruteforce_matches_oracle_larger():
+    p = sc.boids_cube(20000, size=128.0, seed=4).position
+    A = group_of(pos_state(p))
+    for k in (7, 16):
+        knn = gs.KNNData(A.size, k)
+        gs.findKNearestNeighborsBruteForce(A, knn, A)
+        i, d = knn.download(A)
+        oi, od = ol.knn_brute(p, p, True, k)
+        np.testing.assert_array_equal(i, oi)
+        np.testing.assert_array_equal(d, od)
+
+
+# ---- behaviours, one per launch -----------------------------------------------------
+
+def test_flocking_stages_match_reference_golden():
+    z, m = load("flock_stages")
+    s = gstate(z, "in_")
+    g = group_of(s, m["k"])
+    knn = gs.KNNData(s.n, m["k"])
+    # use the reference's own KNN result for the stage inputs
+    bins = gs.KNNBinData(m["wc"], m["ws"], 1)
+    gs.updateKNNDatabase(g, bins)
+    gs.findKNearestNeighbors(g, knn, bins, g, 1)
+    i, _ = knn.download(g)
+    np.testing.assert_array_equal(i, z["knn_idx"])
+    cos = -0.98480775301220805936674302458952
+    gs.steerForSeparation(g, knn, g, 0.5, 2.0, cos, 5.0, 0)
+    assert_state(g.download(), gstate(z, "sep_"))
+    gs.steerForCohesion(g, knn, g, 0.5, 7.0, cos, 4.0, 16)
+    assert_state(g.download(), gstate(z, "coh_"))
+    gs.steerForAlignment(g, knn, g, 0.5, 7.0, cos, 8.0, 16)
+    assert_state(g.download(), gstate(z, "ali_"))
+    gs.steerForSeek(g, m["seek_target"], 1.5, 64)
+    assert_state(g.download(), gstate(z, "seek_"))
+    gs.updateGroup(g, 1.0 / 60.0)
+    want = gstate(z, "upd_")
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+    w = AgentState.zeros(s.n)
+    w.position[:] = z["wrap_in"]
+    gw = group_of(w)
+    gs.wrapWorld(gw, (160.0, 160.0, 160.0), sc.WRAP_REFERENCE)
+    np.testing.assert_array_equal(gw.download().position, z["wrap_out"])
+
+
+def test_avoid_stages_match_oracle_on_golden_inputs():
+    z, m = load("avoid_stages")
+    s0 = gstate(z, "in_")
+    n, k, kw = s0.n, m["k"], m["knw"]
+    rows = np.concatenate([z["wall_start"][:, :3], z["wall_end"][:, :3],
+                           z["wall_normal"][:, :3]], 1)
+    walls = gs.WallGroup(rows, bins=None, knw=kw)  # already split
+    bins = gs.KNNBinData(m["wc"], m["ws"], 1)
+    g = group_of(s0, k)
+    gs.updateKNNDatabase(g, bins)
+    knw = gs.KNNData(n, kw)
+    gs.findKNearestNeighbors(g, knw, bins, walls, 1)
+    wi, wd = knw.download(g)
+    np.testing.assert_array_equal(wi, z["knw_idx"])
+    np.testing.assert_array_equal(wd, z["knw_dist"])
+    gs.steerToAvoidWalls(g, knw, walls, m["min_time_wall"], 1.0, 0)
+    assert_state(g.download(), gstate(z, "walls_"))
+    for close in (0, 1):
+        g = group_of(s0, k)
+        gs.updateKNNDatabase(g, bins)
+        knn = gs.KNNData(n, k)
+        gs.findKNearestNeighbors(g, knn, bins, g, 1)
+        gs.steerToAvoidNeighbors(g, knn, g, m["min_time"], m["min_sep"], close, 1.0, 0)
+        want = s0.copy()
+        ol.oracle().orc_steer_avoid_neighbors(
+            ol.C.byref(ol.group_struct(want)), ol.ptr(z["knn_idx"], ol.C.c_uint),
+            ol.ptr(z["knn_dist"]), k, ol.ptr(s0.position), ol.ptr(s0.direction),
+            ol.ptr(s0.speed), ol.ptr(s0.radius), n, ol.C.c_float(m["min_time"]),
+            ol.C.c_float(m["min_sep"]), close, ol.C.c_float(1.0), 0)
+        assert_state(g.download(), want)
+    # anti-penetration (the next ChokePoint stage)
+    g = group_of(s0, k)
+    st = s0.copy()
+    st.applied[:] = z["ap_in_applied"]
+    g.upload(st)
+    gs.updateKNNDatabase(g, bins)
+    knn = gs.KNNData(n, k)
+    gs.findKNearestNeighbors(g, knn, bins, g, 1)
+    gs.antiPenetrationAgents(g, knn, g, 4096)
+    out = g.download()
+    np.testing.assert_array_equal(out.position, z["ap_out_position"])
+    np.testing.assert_array_equal(out.applied, z["ap_out_applied"])
+
+
+def test_wall_split_matches_oracle():
+    for gap in (7.5, 10.0, 32.5):
+        for ws, wc in (((128.0, 10.0, 128.0), (64, 1, 64)), ((512.0, 10.0, 512.0), (256, 1, 256))):
+            bins = gs.KNNBinData(wc, ws, 1)
+            w = gs.WallGroup(sc.chokepoint_walls(gap), bins=bins, knw=3)
+            got = w.download()
+            want = ol.split_walls(*sc.walls_from_rows(sc.chokepoint_walls(gap)), ws, wc)
+            for a, b in zip(got, want):
+                np.testing.assert_array_equal(a, b)
+
+
+# ---- whole steps --------------------------------------------------------------------
+
+def dropin_flock_step(g, knn, bins, p: sc.StepParams):
+    gs.wrapWorld(g, p.world_size, p.wrap_mode)
+    gs.updateKNNDatabase(g, bins)
+    gs.findKNearestNeighbors(g, knn, bins, g, p.search_radius)
+    for b in p.order:
+        if b == sc.B_SEPARATION:
+            gs.steerForSeparation(g, knn, g, p.sep_min, p.sep_max, p.sep_cos, p.w_sep, p.mask_sep)
+        elif b == sc.B_COHESION:
+            gs.steerForCohesion(g, knn, g, p.coh_min, p.coh_max, p.coh_cos, p.w_coh, p.mask_coh)
+        elif b == sc.B_ALIGNMENT:
+            gs.steerForAlignment(g, knn, g, p.ali_min, p.ali_max, p.ali_cos, p.w_ali, p.mask_ali)
+    gs.updateGroup(g, p.dt)
+
+
+def test_flock_steps_match_reference_golden():
+    z, m = load("flock_steps")
+    s = gstate(z, "in_")
+    p = sc.boids_params(k=m["k"], world=m["world"], cell=m["cell"]).replace(wrap_mode=sc.WRAP_NONE)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    want = gstate(z, "out_")
+    # drop-in sequence
+    g = group_of(s, p.k)
+    knn = gs.KNNData(s.n, p.k)
+    for _ in range(m["steps"]):
+        dropin_flock_step(g, knn, bins, p)
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+    # fused
+    g2 = group_of(s, p.k)
+    gs.step(g2, bins, None, p, m["steps"])
+    assert_state(g2.download(), want, skip_side=want.speed == 0)
+
+
+def test_choke_steps_match_reference_golden():
+    z, m = load("choke_steps")
+    s = gstate(z, "in_")
+    p = sc.chokepoint_params(world=m["world"], cell=m["cell"]).replace(
+        order=(sc.B_AVOID_WALLS, sc.B_SEPARATION, sc.B_SEEK))
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    rows = np.concatenate([z["wall_start"][:, :3], z["wall_end"][:, :3],
+                           z["wall_normal"][:, :3]], 1)
+    walls = gs.WallGroup(rows, bins=None, knw=p.knw)
+    g = group_of(s, p.k)
+    gs.step(g, bins, walls, p, m["steps"])
+    want = gstate(z, "out_")
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+@pytest.mark.parametrize("masks", [False, True])
+def test_boids_config_fused_matches_oracle(masks):
+    """4,096 3D boids, k = 7, cell 4.0, 100 steps (bins), bit-exact."""
+    s = sc.boids_sphere(4096, seed=0)
+    p = sc.boids_params(k=7, masks=masks)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g = group_of(s, p.k)
+    gs.step(g, bins, None, p, 100)
+    want = s.copy()
+    ol.run(want, p, 100)
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+def test_boids_fused_equals_dropin_sequence():
+    s = sc.boids_sphere(2000, radius=15.0, seed=11)
+    p = sc.boids_params(k=16, world=64.0)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g1 = group_of(s, p.k)
+    knn = gs.KNNData(s.n, p.k)
+    for _ in range(10):
+        dropin_flock_step(g1, knn, bins, p)
+    g2 = group_of(s, p.k)
+    gs.step(g2, bins, None, p, 10)
+    assert_state(g2.download(), g1.download())
+
+
+def choke_walls(p):
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    walls = gs.WallGroup(sc.chokepoint_walls(10.0), bins=bins, knw=p.knw)
+    return bins, walls
+
+
+@pytest.mark.parametrize("avoid_close", [0, 1])
+def test_chokepoint_config_fused_matches_oracle(avoid_close):
+    """2D choke point: walls, neighbour avoidance, separation, seek; 10,000
+    agents, k = 16, cell 2.0, 60 steps, bit-exact."""
+    p = sc.chokepoint_params().replace(avoid_close=avoid_close)
+    s = sc.chokepoint_agents(10000, seed=0)
+    bins, walls = choke_walls(p)
+    g = group_of(s, p.k)
+    gs.step(g, bins, walls, p, 60)
+    want = s.copy()
+    ol.run(want, p, 60, walls=walls.download())
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+def test_fused_steps_resume_across_calls_and_downloads():
+    p = sc.chokepoint_params()
+    s = sc.chokepoint_agents(3000, seed=5)
+    bins, walls = choke_walls(p)
+    g = group_of(s, p.k)
+    gs.step(g, bins, walls, p, 7)
+    mid = g.download()
+    gs.step(g, bins, walls, p, 8)
+    want = s.copy()
+    ol.run(want, p, 7, walls=walls.download())
+    assert_state(mid, want, skip_side=want.speed == 0)
+    ol.run(want, p, 8, walls=walls.download())
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+def test_step_host_is_upload_step_download():
+    p = sc.boids_params(k=7)
+    s = sc.boids_sphere(3000, seed=2)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g = gs.AgentGroup(p.k, s.n)
+    out = AgentState.zeros(s.n)
+    gs.step_host(g, bins, None, p, 5, s, out)
+    want = s.copy()
+    ol.run(want, p, 5)
+    assert_state(out, want, skip_side=want.speed == 0)
+
+
+def test_large_flock_two_steps_match_oracle():
+    """The full 1,048,576-agent, k = 16 flock of the throughput benchmark,
+    two fused steps against the oracle."""
+    n = 1 << 20
+    s = sc.boids_cube(n, size=512.0, seed=0)
+    p = sc.boids_params(k=16, world=512.0, cell=4.0)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g = group_of(s, p.k)
+    gs.step(g, bins, None, p, 2)
+    want = s.copy()
+    ol.run(want, p, 2)
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+# ---- errors -----------------------------------------------------------------------
+
+def test_invalid_arguments_are_reported_not_fatal():
+    s = sc.boids_sphere(100, seed=1)
+    g = group_of(s, 7)
+    bins = gs.KNNBinData((8, 8, 8), (32.0, 32.0, 32.0), 1)
+    knn = gs.KNNData(50, 7)  # wrong size
+    gs.updateKNNDatabase(g, bins)
+    with pytest.raises(gs.GpuSteerError) as e:
+        gs.findKNearestNeighbors(g, knn, bins, g, 1)
+    assert e.value.status == 1
+    with pytest.raises(gs.GpuSteerError) as e:
+        gs.updateGroup(g, float("nan"))
+    assert e.value.status == 5
+    with pytest.raises(gs.GpuSteerError):
+        gs.AgentGroup(65, 10)
+    with pytest.raises(gs.GpuSteerError):
+        big = sc.boids_sphere(200, seed=1)
+        g.upload(big)  # over capacity
+    p = sc.boids_params(k=7).replace(order=(sc.B_SEPARATION, sc.B_AVOID_WALLS))
+    with pytest.raises(gs.GpuSteerError) as e:
+        gs.step(g, gs.KNNBinData(p.world_cells, p.world_size, 1), None, p, 1)
+    assert e.value.status == 7
+    # the group still works afterwards
+    gs.step(g, gs.KNNBinData((40, 40, 40), (160.0,) * 3, 1), None, sc.boids_params(k=7), 1)
+    assert g.download().n == 100
+
+
+def test_empty_group_steps():
+    g = gs.AgentGroup(7, 16)
+    g.upload(AgentState.zeros(0))
+    p = sc.boids_params(k=7)
+    gs.step(g, gs.KNNBinData(p.world_cells, p.world_size, 1), None, p, 3)
+    assert g.download().n == 0
