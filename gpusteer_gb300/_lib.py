@@ -60,6 +60,9 @@ SIGNATURES = {
     "gs_last_error": [],
     "gs_version": [],
     "gs_max_k": [],
+    "gs_set_device": [_i],
+    "gs_host_alloc": [C.c_size_t, C.POINTER(_vp)],
+    "gs_host_free": [_vp],
     "gs_bins_create": [_up, _fp, _u, C.POINTER(_vp)],
     "gs_bins_destroy": [_vp],
     "gs_bins_num_cells": [_vp, _up],
@@ -72,6 +75,8 @@ SIGNATURES = {
     "gs_group_device_arrays": [_vp, C.POINTER(AgentArrays)],
     "gs_group_stream": [_vp, C.POINTER(_vp)],
     "gs_group_synchronize": [_vp],
+    "gs_group_set_profiling": [_vp, _i],
+    "gs_group_phase_times": [_vp, _fp, _up, _u],
     "gs_knn_create": [_u, _u, C.POINTER(_vp)],
     "gs_knn_destroy": [_vp],
     "gs_knn_download": [_vp, _vp, _up, _fp],

@@ -45,6 +45,7 @@ static void release_fused(gs_group g) {
     dfree(g->knn_slot);
     dfree(g->knn_dist);
     dfree(g->d_scene);
+    dfree(g->d_err);
     db_release(g->fdb);
     g->fused_k_alloc = 0;
 }
@@ -283,6 +284,37 @@ static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev&
     return GS_OK;
 }
 
+// Records a (start, stop) event pair per phase launch on the group's stream
+// and folds finished pairs into the group's totals.
+struct Profiler final : PhaseHook {
+    gs_group g;
+    explicit Profiler(gs_group grp) : g(grp) {}
+    void mark(int phase, bool begin) override {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, g->stream);
+        g->prof_events->push_back(e);
+        if (begin) g->prof_phase->push_back(phase);
+    }
+};
+
+static void prof_collect(gs_group g) {
+    if (!g->prof_events) return;
+    auto& ev = *g->prof_events;
+    auto& ph = *g->prof_phase;
+    if (!ev.empty()) cudaEventSynchronize(ev.back());
+    for (size_t i = 0; i + 1 < ev.size() && i / 2 < ph.size(); i += 2) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ev[i], ev[i + 1]) == cudaSuccess) {
+            g->prof_ms[ph[i / 2]] += ms;
+            g->prof_launches[ph[i / 2]] += 1;
+        }
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    ev.clear();
+    ph.clear();
+}
+
 }  // namespace gs
 
 using namespace gs;
@@ -304,6 +336,51 @@ const char* gs_status_string(gs_status s) {
 }
 
 const char* gs_last_error(void) { return g_last_error.c_str(); }
+
+gs_status gs_set_device(int device) {
+    GS_CUDA(cudaSetDevice(device));
+    return GS_OK;
+}
+
+gs_status gs_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "null output");
+    *out = nullptr;
+    if (bytes == 0) return GS_OK;
+    cudaError_t e = cudaMallocHost(out, bytes);
+    if (e == cudaErrorMemoryAllocation) return fail(GS_ERR_OOM, "pinned allocation failed");
+    GS_CUDA(e);
+    return GS_OK;
+}
+
+gs_status gs_host_free(void* p) {
+    if (p) GS_CUDA(cudaFreeHost(p));
+    return GS_OK;
+}
+
+gs_status gs_group_set_profiling(gs_group g, int enable) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    if (!g->prof_events) {
+        g->prof_events = new std::vector<cudaEvent_t>();
+        g->prof_phase = new std::vector<int>();
+    }
+    prof_collect(g);
+    g->profiling = enable != 0;
+    for (int i = 0; i < 4; ++i) {
+        g->prof_ms[i] = 0.f;
+        g->prof_launches[i] = 0;
+    }
+    return GS_OK;
+}
+
+gs_status gs_group_phase_times(gs_group g, float* ms, unsigned* launches, unsigned cap) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    prof_collect(g);
+    for (unsigned i = 0; i < cap && i < 4; ++i) {
+        if (ms) ms[i] = g->prof_ms[i];
+        if (launches) launches[i] = g->prof_launches[i];
+    }
+    return GS_OK;
+}
 int gs_version(void) { return 1; }
 unsigned gs_max_k(void) { return kMaxK; }
 
@@ -373,6 +450,11 @@ gs_status gs_group_destroy(gs_group g) {
     dfree(g->applied);
     db_release(g->db);
     release_fused(g);
+    if (g->prof_events) {
+        prof_collect(g);
+        delete g->prof_events;
+        delete g->prof_phase;
+    }
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GS_OK;
@@ -448,6 +530,8 @@ gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
     return GS_OK;
 }
 
+static gs_status check_device_flags(gs_group g);
+
 gs_status gs_group_download(gs_group g, const gs_agent_arrays* h) {
     if (!g || !h) return fail(GS_ERR_INVALID_ARG, "null argument");
     GS_TRY(ensure_reference(g));
@@ -471,7 +555,7 @@ gs_status gs_group_download(gs_group g, const gs_agent_arrays* h) {
     if (e == cudaSuccess) e = cp(h->applied, g->applied, f1b);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "download");
-    return GS_OK;
+    return check_device_flags(g);
 }
 
 gs_status gs_group_size(gs_group g, unsigned* n) {
@@ -506,10 +590,24 @@ gs_status gs_group_stream(gs_group g, void** stream) {
     return GS_OK;
 }
 
+// Reads and clears the device error flags of the fused step.
+static gs_status check_device_flags(gs_group g) {
+    if (!g->d_err) return GS_OK;
+    unsigned flags = 0;
+    GS_CUDA(cudaMemcpyAsync(&flags, g->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            g->stream));
+    GS_CUDA(cudaStreamSynchronize(g->stream));
+    if (flags) {
+        GS_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned), g->stream));
+        return fail(GS_ERR_STATE, "fused step: inconsistent cell counts (state not updated)");
+    }
+    return GS_OK;
+}
+
 gs_status gs_group_synchronize(gs_group g) {
     if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
     GS_CUDA(cudaStreamSynchronize(g->stream));
-    return GS_OK;
+    return check_device_flags(g);
 }
 
 // ---- KNN data -----------------------------------------------------------------------
@@ -798,6 +896,9 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k) {
         }
         GS_TRY(dalloc(&g->cellrank, n));
         GS_TRY(dalloc(&g->d_scene, 1));
+        GS_TRY(dalloc(&g->d_err, 1));
+        GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
+        GS_CUDA(cudaDeviceSynchronize());
     }
     if (g->fdb.cells != C) GS_TRY(db_reserve(g->fdb, 0, C));
     if (walls && (!g->w0 || g->fused_k_alloc < k)) {
@@ -849,6 +950,8 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
     bool dirty = false;
     if (!g->fused_current) {
         dirty = g->accum_dirty;
+        // counts left pending by an earlier fused step no longer apply
+        GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
         GS_TRY(fused_from_reference(view(g), nullptr, g->d_scene, g->A, g->cellrank, g->fdb.count,
                                     d.wrap_mode, dirty, st));
         g->fused_current = true;
@@ -871,6 +974,7 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
     L.start = g->fdb.start;
     L.scenes = g->d_scene;
     L.n = g->n;
+    L.err = g->d_err;
     if (has_walls) {
         L.w_start = walls->start;
         L.w_end = walls->end;
@@ -883,11 +987,17 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
         L.knn_slot = g->knn_slot;
         L.knn_dist = g->knn_dist;
     }
+    Profiler prof(g);
+    PhaseHook* hook = g->profiling ? &prof : nullptr;
     for (unsigned step = 0; step < steps; ++step) {
         d.dirty = dirty ? 1 : 0;
+        if (hook) hook->mark(0, true);
         GS_TRY(scan_counts(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
+        if (hook) hook->mark(0, false);
+        if (hook) hook->mark(1, true);
         GS_TRY(fused_permute(L, d.wrap_mode, dirty, st));
-        GS_TRY(fused_step(L, d, st));
+        if (hook) hook->mark(1, false);
+        GS_TRY(fused_step(L, d, st, hook));
         dirty = false;
     }
     g->accum_dirty = false;

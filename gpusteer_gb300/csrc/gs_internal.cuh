@@ -135,8 +135,15 @@ struct gs_group_s {
     float* knn_dist;       // [k * n]
     gs::Database fdb;      // counts / starts of the fused step
     gs::Scene* d_scene;    // single-scene table
+    unsigned* d_err;       // device error flags (see FusedLaunch::err)
     bool fused_current;    // true: A holds the state, reference arrays stale
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with
     unsigned fused_k_alloc;
+    // phase profiling (gs_group_set_profiling)
+    bool profiling;
+    std::vector<cudaEvent_t>* prof_events;  // pairs of (start, stop) per recorded phase
+    std::vector<int>* prof_phase;
+    float prof_ms[4];
+    unsigned prof_launches[4];
 };

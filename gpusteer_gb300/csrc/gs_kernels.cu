@@ -211,6 +211,7 @@ __global__ void k_db_scatter(const float4* __restrict__ pos, unsigned n,
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const unsigned dst = start[cell[i]] + rank[i];
+    if (dst >= n) return;
     const float4 p = pos[i];
     sorted[dst] = i;
     pos_id[dst] = make_float4(p.x, p.y, p.z, __uint_as_float(i));

@@ -88,6 +88,7 @@ struct FusedLaunch {
     float4 *w0, *w1, *w2;
     unsigned* knn_slot;
     float* knn_dist;
+    unsigned* err;  // device flag: bit 0 = a bucketed slot fell outside [0, n)
 };
 
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
@@ -96,7 +97,13 @@ gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const S
 gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
                         unsigned* count, int wrap_mode, cudaStream_t st);
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st);
-gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st);
+// `phase` (may be null) brackets each launch: phase(i, true) before and
+// phase(i, false) after the launch of phase i.
+struct PhaseHook {
+    virtual void mark(int phase, bool begin) = 0;
+};
+gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
+                     PhaseHook* hook = nullptr);
 gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView g,
                              cudaStream_t st);
 

@@ -94,11 +94,16 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
                                                     const uint2* __restrict__ cellrank,
                                                     const unsigned* __restrict__ start,
                                                     const Scene* __restrict__ scenes,
-                                                    int wrap_mode, int dirty) {
+                                                    int wrap_mode, int dirty,
+                                                    unsigned* __restrict__ err) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint2 cr = cellrank[i];
     const unsigned dst = start[cr.x] + cr.y;
+    if (dst >= n) {  // inconsistent counts: record and write nothing
+        atomicOr(err, 1u);
+        return;
+    }
     const float4 f0 = A.f[0][i];
     const float4 f4v = A.f[4][i];
     const Scene sc = scenes[u(f4v.w)];
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st) {
     if (L.n == 0) return GS_OK;
     k_permute<<<blocks_for(L.n), kBlock, 0, st>>>(L.A, L.B, L.n, L.cellrank, L.start, L.scenes,
-                                                  wrap_mode, dirty ? 1 : 0);
+                                                  wrap_mode, dirty ? 1 : 0, L.err);
     GS_LAUNCHED("fused_permute");
     return GS_OK;
 }
@@ -347,12 +352,17 @@ __global__ void __launch_bounds__(kBlock) k_fused_rest(FusedLaunch L, StepDev p)
 }
 
 template <int KMAX>
-static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream_t st) {
+static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
+                              PhaseHook* hook) {
     const unsigned nb = blocks_for(L.n);
     if (p.need & NEED_WALLS) {
         const size_t smem = size_t(p.knw) * kBlock * sizeof(unsigned);
+        if (hook) hook->mark(2, true);
         k_fused_walls<KMAX, 8><<<nb, kBlock, smem, st>>>(L, p);
+        if (hook) hook->mark(2, false);
+        if (hook) hook->mark(3, true);
         k_fused_rest<KMAX><<<nb, kBlock, 0, st>>>(L, p);
+        if (hook) hook->mark(3, false);
     } else {
         const size_t smem = size_t(2 * p.k) * kBlock * sizeof(unsigned);
         if (smem > 48 * 1024) {
@@ -364,19 +374,21 @@ static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream
                 opted = true;
             }
         }
+        if (hook) hook->mark(2, true);
         k_fused<KMAX><<<nb, kBlock, smem, st>>>(L, p);
+        if (hook) hook->mark(2, false);
     }
     GS_LAUNCHED("fused_step");
     return GS_OK;
 }
 
-gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st) {
+gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st, PhaseHook* hook) {
     if (L.n == 0) return GS_OK;
     if ((p.need & NEED_WALLS) && p.knw > 8)
         return fail(GS_ERR_UNSUPPORTED, "knw > 8 in the fused step");
-    if (p.k <= 8) return launch_fused<8>(L, p, st);
-    if (p.k <= 16) return launch_fused<16>(L, p, st);
-    return launch_fused<32>(L, p, st);
+    if (p.k <= 8) return launch_fused<8>(L, p, st, hook);
+    if (p.k <= 16) return launch_fused<16>(L, p, st, hook);
+    return launch_fused<32>(L, p, st, hook);
 }
 
 // A -> reference layout (scatter by agent index).

@@ -113,6 +113,14 @@ const char* gs_last_error(void);
 int gs_version(void);
 /* Largest k the KNN kernels accept. */
 unsigned gs_max_k(void);
+/* Selects the CUDA device for the calling thread (cudaSetDevice); handles are
+ * bound to the device that was current when they were created.  The
+ * reference picks its device in the plugins (plugins/ChokePointNew.cpp:654-680). */
+gs_status gs_set_device(int device);
+/* Page-locked host buffers for the per-frame host copies (the reference's
+ * SyncDevice / SyncHost use pageable std::vector storage). */
+gs_status gs_host_alloc(size_t bytes, void** out);
+gs_status gs_host_free(void* p);
 
 /* ---- KNNBinData: KNNBinDataV2::KNNBinDataV2(worldCells, worldSize, searchRadius),
  *      KNNBinDataV2.cu:30-42.  No device neighbour table is built: the
@@ -143,6 +151,15 @@ gs_status gs_group_size(gs_group g, unsigned* n);
 gs_status gs_group_device_arrays(gs_group g, gs_agent_arrays* dev);
 gs_status gs_group_stream(gs_group g, void** stream);
 gs_status gs_group_synchronize(gs_group g);
+/* Phase timing of the fused step with CUDA events on the group's stream (the
+ * reference's optional TIMING instrumentation, KNNBinningV2.cu:106-161).
+ * While enabled, every phase launch is bracketed by events; the totals are
+ * read with gs_group_phase_times: ms[i] and launches[i] for phase i =
+ * 0 scan, 1 permute, 2 fused step (or its wall half), 3 second half after
+ * walls.  Enabling clears the totals. */
+#define GS_PHASES 4
+gs_status gs_group_set_profiling(gs_group g, int enable);
+gs_status gs_group_phase_times(gs_group g, float* ms, unsigned* launches, unsigned cap);
 
 /* ---- KNNData: KNNData(nSize, nK) (KNNData.cu) ---------------------------------- */
 gs_status gs_knn_create(unsigned n, unsigned k, gs_knn* out);
