@@ -46,6 +46,8 @@ static void release_fused(gs_group g) {
     dfree(g->knn_dist);
     dfree(g->d_scene);
     dfree(g->d_err);
+    dfree(g->retry);
+    dfree(g->retry_count);
     db_release(g->fdb);
     g->fused_k_alloc = 0;
 }
@@ -222,6 +224,17 @@ static gs_status walls_db(gs_walls w, const Grid& grid, unsigned C, cudaStream_t
     return GS_OK;
 }
 
+// Candidate capacity of the fast KNN scan: 32 when a uniform crowd of this
+// density puts the mean candidate count of the (2r+1)^d box at least four
+// standard deviations below 32, else 64.  Agents beyond it take the exact
+// redo path, so this only affects speed.
+static unsigned enum_capacity(unsigned n, unsigned C, const Grid& g, unsigned r) {
+    double box = 1.0;
+    for (int a = 0; a < 3; ++a) box *= double(std::min<unsigned>(2 * r + 1, g.wc[a]));
+    const double mean = double(n) / double(C) * box;
+    return (mean + 4.0 * std::sqrt(mean) + 1.0 <= 32.0) ? 32u : 64u;
+}
+
 static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev& d) {
     if (!p) return fail(GS_ERR_INVALID_ARG, "null step parameters");
     if (p->knn_mode != GS_KNN_BINNED)
@@ -369,6 +382,16 @@ gs_status gs_group_set_profiling(gs_group g, int enable) {
         g->prof_ms[i] = 0.f;
         g->prof_launches[i] = 0;
     }
+    return GS_OK;
+}
+
+gs_status gs_group_exact_redos(gs_group g, unsigned* count) {
+    if (!g || !count) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *count = 0;
+    if (!g->retry_count) return GS_OK;
+    GS_CUDA(cudaMemcpyAsync(count, g->retry_count, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            g->stream));
+    GS_CUDA(cudaStreamSynchronize(g->stream));
     return GS_OK;
 }
 
@@ -897,7 +920,10 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k) {
         GS_TRY(dalloc(&g->cellrank, n));
         GS_TRY(dalloc(&g->d_scene, 1));
         GS_TRY(dalloc(&g->d_err, 1));
+        GS_TRY(dalloc(&g->retry, n));
+        GS_TRY(dalloc(&g->retry_count, 1));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
+        GS_CUDA(cudaMemset(g->retry_count, 0, sizeof(unsigned)));
         GS_CUDA(cudaDeviceSynchronize());
     }
     if (g->fdb.cells != C) GS_TRY(db_reserve(g->fdb, 0, C));
@@ -975,6 +1001,9 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
     L.scenes = g->d_scene;
     L.n = g->n;
     L.err = g->d_err;
+    L.retry = g->retry;
+    L.retry_count = g->retry_count;
+    d.enum_cap = enum_capacity(g->n, C, grid, d.r);
     if (has_walls) {
         L.w_start = walls->start;
         L.w_end = walls->end;

@@ -136,6 +136,8 @@ struct gs_group_s {
     gs::Database fdb;      // counts / starts of the fused step
     gs::Scene* d_scene;    // single-scene table
     unsigned* d_err;       // device error flags (see FusedLaunch::err)
+    unsigned* retry;       // [capacity] exact-redo list and its counter
+    unsigned* retry_count;
     bool fused_current;    // true: A holds the state, reference arrays stale
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with

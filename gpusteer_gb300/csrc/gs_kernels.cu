@@ -248,33 +248,41 @@ __global__ void __launch_bounds__(kBlock) k_knn_binned(
     unsigned ix, iy, iz;
     cell_coords(g, p, ix, iy, iz);
     const Box box = cell_box(g, ix, iy, iz, r);
-    KList<KMAX> L;
-    L.init(int(k));
-    knn_scan_box<KMAX>(L, p, self ? a : UINT_MAX, g, box, 0u, b_start, b_pos_id);
-    L.for_each(int(k), [&](int r, unsigned long long key, unsigned) {
-        idx[a + size_t(r) * nA] = key_id(key);
-        dist[a + size_t(r) * nA] = key_dist(key);
-    });
+    extern __shared__ unsigned sh_col[];
+    unsigned* col = sh_col + threadIdx.x;
+    const unsigned bd = blockDim.x;
+    knn_neighbours<KMAX, 64>(int(k), p, self ? a : UINT_MAX, g, box, 0u, b_start, b_pos_id, col,
+                             bd);
+    for (unsigned r = 0; r < k; ++r) {
+        const unsigned bs = col[r * bd];
+        const float4 q = bs == UINT_MAX ? make_float4(0.f, 0.f, 0.f, 0.f) : b_pos_id[bs];
+        idx[a + size_t(r) * nA] = bs == UINT_MAX ? UINT_MAX : __float_as_uint(q.w);
+        dist[a + size_t(r) * nA] = bs == UINT_MAX ? FLT_MAX : distance(p, v3(q));
+    }
+}
+
+template <int KMAX>
+static gs_status knn_binned_k(const Database& A, unsigned nA, const Database& B, bool self,
+                              unsigned r, unsigned k, unsigned* idx, float* dist,
+                              cudaStream_t st) {
+    const size_t smem = size_t(2 * 64) * kBlock * sizeof(unsigned);
+    if (smem > 48 * 1024)
+        GS_CUDA(cudaFuncSetAttribute(k_knn_binned<KMAX>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    k_knn_binned<KMAX><<<blocks_for(nA), kBlock, smem, st>>>(A.sorted, A.pos_id, nA, B.start,
+                                                             B.pos_id, B.grid, r, k, self, idx,
+                                                             dist);
+    GS_LAUNCHED("knn_binned");
+    return GS_OK;
 }
 
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
                             unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
     if (nA == 0) return GS_OK;
-    const unsigned nb = blocks_for(nA);
-    if (k <= 8)
-        k_knn_binned<8><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id, B.grid,
-                                              r, k, self, idx, dist);
-    else if (k <= 16)
-        k_knn_binned<16><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id,
-                                               B.grid, r, k, self, idx, dist);
-    else if (k <= 32)
-        k_knn_binned<32><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id,
-                                               B.grid, r, k, self, idx, dist);
-    else
-        k_knn_binned<64><<<nb, kBlock, 0, st>>>(A.sorted, A.pos_id, nA, B.start, B.pos_id,
-                                               B.grid, r, k, self, idx, dist);
-    GS_LAUNCHED("knn_binned");
-    return GS_OK;
+    if (k <= 8) return knn_binned_k<8>(A, nA, B, self, r, k, idx, dist, st);
+    if (k <= 16) return knn_binned_k<16>(A, nA, B, self, r, k, idx, dist, st);
+    if (k <= 32) return knn_binned_k<32>(A, nA, B, self, r, k, idx, dist, st);
+    return knn_binned_k<64>(A, nA, B, self, r, k, idx, dist, st);
 }
 
 // ---- brute-force KNN (KNNBruteForceCudaKernel.cu:207-283) ---------------------------

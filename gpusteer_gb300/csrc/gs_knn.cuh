@@ -111,4 +111,185 @@ __device__ __forceinline__ void knn_scan_box(KList<KMAX>& L, V3 p, unsigned self
     }
 }
 
+// ---- fast scan: 32-bit keys ---------------------------------------------------------
+// key = distance bits with the low log2(ENUM) mantissa bits replaced by the
+// candidate's enumeration index e (slot and key kept in two per-thread
+// shared-memory tables at e).  Keys order candidates exactly like
+// (distance, index) whenever no two relevant candidates share the truncated
+// distance T = bits & ~(ENUM - 1): T(a) < T(b) implies d(a) < d(b).  The scan
+// records every way that assumption can fail - two list entries with equal T,
+// a candidate left out of a full list with T equal to the k-th entry's, more
+// than ENUM candidates - and then reports failure; the agent is then redone
+// with the exact 64-bit list (knn_scan_box).
+constexpr unsigned KEY32_EMPTY = 0xffffffffu;
+
+template <int KMAX>
+struct KList32 {
+    unsigned key[KMAX];
+    // Inserts c; returns the largest key, which leaves the list.
+    __device__ __forceinline__ unsigned insert(unsigned c) {
+#pragma unroll
+        for (int i = 0; i < KMAX; ++i) {
+            const unsigned lo = min(key[i], c);
+            c = max(key[i], c);
+            key[i] = lo;
+        }
+        return c;
+    }
+    // Ascending bitonic sort (compare-exchange = min + max).
+    __device__ __forceinline__ void sort() {
+#pragma unroll
+        for (int size = 2; size <= KMAX; size <<= 1) {
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+                for (int i = 0; i < KMAX; ++i) {
+                    const int j = i ^ stride;
+                    if (j > i) {
+                        const unsigned a = key[i], b = key[j];
+                        const bool up = (i & size) == 0;
+                        key[i] = up ? min(a, b) : max(a, b);
+                        key[j] = up ? max(a, b) : min(a, b);
+                    }
+                }
+            }
+        }
+    }
+};
+
+// Appends candidate slot s to the tables (self and non-finite distances
+// skip).  e counts past ENUM without storing; the caller checks it.  No early
+// exits: the warp's lanes reconverge after every candidate.
+template <unsigned ENUM>
+__device__ __forceinline__ void collect_one(unsigned s, V3 p, unsigned self_id,
+                                            const float4* __restrict__ pos_id, unsigned& e,
+                                            unsigned* slot_tab, unsigned* key_tab,
+                                            unsigned stride) {
+    const float4 q = __ldg(pos_id + s);
+    const unsigned bits = __float_as_uint(distance(p, v3(q)));
+    // never below FLT_MAX (inf, NaN): never listed
+    if (__float_as_uint(q.w) != self_id && bits < 0x7f7fffffu) {
+        if (e < ENUM) {
+            slot_tab[e * stride] = s;
+            key_tab[e * stride] = (bits & ~(ENUM - 1)) | e;
+        }
+        ++e;
+    }
+}
+
+// Collects every candidate of `box` into the tables; returns the count (which
+// exceeds ENUM when the tables overflowed).
+template <unsigned ENUM>
+__device__ __forceinline__ unsigned collect_box(V3 p, unsigned self_id, const Grid& g,
+                                                const Box& b, unsigned cell_offset,
+                                                const unsigned* __restrict__ cell_start,
+                                                const float4* __restrict__ pos_id,
+                                                unsigned* slot_tab, unsigned* key_tab,
+                                                unsigned stride) {
+    unsigned e = 0;
+    const unsigned span = b.x1 - b.x0 + 1;
+    if (b.y1 - b.y0 <= 2 && b.z1 - b.z0 <= 2) {
+        // at most 3 x 3 rows: load every row's range first, then walk them
+        unsigned rs[9], rn[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            const unsigned cy = b.y0 + unsigned(i / 3), cz = b.z0 + unsigned(i % 3);
+            const bool ok = cy <= b.y1 && cz <= b.z1;
+            const unsigned c0 = cell_offset + cell_label(g, b.x0, ok ? cy : b.y0, ok ? cz : b.z0);
+            const unsigned s0 = ok ? __ldg(cell_start + c0) : 0u;
+            const unsigned s1 = ok ? __ldg(cell_start + c0 + span) : 0u;
+            rs[i] = s0;
+            rn[i] = s1 - s0;
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i)
+            for (unsigned t = 0; t < rn[i]; ++t)
+                collect_one<ENUM>(rs[i] + t, p, self_id, pos_id, e, slot_tab, key_tab, stride);
+        return e;
+    }
+    for (unsigned cy = b.y0; cy <= b.y1; ++cy)
+        for (unsigned cz = b.z0; cz <= b.z1; ++cz) {
+            const unsigned c0 = cell_offset + cell_label(g, b.x0, cy, cz);
+            const unsigned s0 = __ldg(cell_start + c0), s1 = __ldg(cell_start + c0 + span);
+            for (unsigned s = s0; s < s1; ++s)
+                collect_one<ENUM>(s, p, self_id, pos_id, e, slot_tab, key_tab, stride);
+        }
+    return e;
+}
+
+// Fast path: the k nearest of `box` as slots in (distance, index) order at
+// key_tab[r * stride], UINT_MAX after the last neighbour.  Returns false when
+// the exact path must redo this agent.
+template <int KMAX, unsigned ENUM>
+__device__ __forceinline__ bool knn_neighbours_fast(int k, V3 p, unsigned self_id, const Grid& g,
+                                                    const Box& b, unsigned cell_offset,
+                                                    const unsigned* __restrict__ cell_start,
+                                                    const float4* __restrict__ pos_id,
+                                                    unsigned* slot_tab, unsigned* key_tab,
+                                                    unsigned stride) {
+    constexpr unsigned mask = ENUM - 1;
+    const unsigned n = collect_box<ENUM>(p, self_id, g, b, cell_offset, cell_start, pos_id,
+                                         slot_tab, key_tab, stride);
+    if (n > ENUM) return false;
+    // The first min(n, k) keys, KMAX - k sentinel zeros (sorted to the front)
+    // and empty keys: after sorting, entries KMAX-k .. KMAX-1 are the list.
+    KList32<KMAX> L;
+    const unsigned m = n < unsigned(k) ? n : unsigned(k);
+#pragma unroll
+    for (int i = 0; i < KMAX; ++i)
+        L.key[i] = unsigned(i) < m ? key_tab[i * stride] : (i < k ? KEY32_EMPTY : 0u);
+    L.sort();
+    unsigned out_min = KEY32_EMPTY;  // smallest key not (or no longer) in the list
+    for (unsigned e = m; e < n; ++e) {
+        const unsigned c = key_tab[e * stride];
+        out_min = min(out_min, c < L.key[KMAX - 1] ? L.insert(c) : c);
+    }
+    const unsigned last = L.key[KMAX - 1];
+    if (last != KEY32_EMPTY && (out_min & ~mask) == (last & ~mask)) return false;
+#pragma unroll
+    for (int i = KMAX - 1; i > 0; --i)
+        if (i > KMAX - k && L.key[i] != KEY32_EMPTY && (L.key[i] & ~mask) == (L.key[i - 1] & ~mask))
+            return false;
+#pragma unroll
+    for (int i = 0; i < KMAX; ++i)
+        if (i >= KMAX - k)
+            key_tab[(i - (KMAX - k)) * stride] =
+                L.key[i] != KEY32_EMPTY ? slot_tab[(L.key[i] & mask) * stride] : UINT_MAX;
+    return true;
+}
+
+// Exact path: the ordered slots go to col[r * stride].
+template <int KMAX>
+__device__ __forceinline__ void knn_neighbours_exact(int k, V3 p, unsigned self_id, const Grid& g,
+                                                     const Box& b, unsigned cell_offset,
+                                                     const unsigned* __restrict__ cell_start,
+                                                     const float4* __restrict__ pos_id,
+                                                     unsigned* col, unsigned stride) {
+    KList<KMAX> L;
+    L.init(k);
+    knn_scan_box<KMAX>(L, p, self_id, g, b, cell_offset, cell_start, pos_id);
+    L.for_each(k, [&](int r, unsigned long long key, unsigned slot) {
+        col[r * stride] = key_id(key) == UINT_MAX ? UINT_MAX : slot;
+    });
+}
+
+// The k nearest of `box` as slots in (distance, index) order at
+// col[r * stride] (UINT_MAX after the last neighbour): the fast scan, or the
+// exact list when the fast scan cannot vouch for its order.  col needs
+// ENUM + KMAX entries.
+template <int KMAX, unsigned ENUM>
+__device__ __forceinline__ void knn_neighbours(int k, V3 p, unsigned self_id, const Grid& g,
+                                               const Box& b, unsigned cell_offset,
+                                               const unsigned* __restrict__ cell_start,
+                                               const float4* __restrict__ pos_id,
+                                               unsigned* col, unsigned stride) {
+    // col holds the slot table (ENUM entries) then the key table / result
+    if (knn_neighbours_fast<KMAX, ENUM>(k, p, self_id, g, b, cell_offset, cell_start, pos_id, col,
+                                        col + ENUM * stride, stride)) {
+        for (int r = 0; r < k; ++r) col[r * stride] = col[(ENUM + r) * stride];
+        return;
+    }
+    knn_neighbours_exact<KMAX>(k, p, self_id, g, b, cell_offset, cell_start, pos_id, col, stride);
+}
+
 }  // namespace gs

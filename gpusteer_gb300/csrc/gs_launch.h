@@ -70,7 +70,8 @@ struct StepDev {
     unsigned order[8];
     unsigned n_order;
     float dt;
-    unsigned need;  // NEED_* bits
+    unsigned need;      // NEED_* bits
+    unsigned enum_cap;  // candidate capacity of the fast KNN scan (32 or 64)
 };
 constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
                    NEED_WALLS = 32;
@@ -89,6 +90,8 @@ struct FusedLaunch {
     unsigned* knn_slot;
     float* knn_dist;
     unsigned* err;  // device flag: bit 0 = a bucketed slot fell outside [0, n)
+    unsigned* retry;        // [n] slots the fast KNN handed to the exact redo
+    unsigned* retry_count;  // zeroed by the permute launch of each step
 };
 
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,

@@ -95,8 +95,10 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
                                                     const unsigned* __restrict__ start,
                                                     const Scene* __restrict__ scenes,
                                                     int wrap_mode, int dirty,
-                                                    unsigned* __restrict__ err) {
+                                                    unsigned* __restrict__ err,
+                                                    unsigned* __restrict__ retry_count) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *retry_count = 0u;  // the fused launch that follows refills it
     if (i >= n) return;
     const uint2 cr = cellrank[i];
     const unsigned dst = start[cr.x] + cr.y;
@@ -119,7 +121,7 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st) {
     if (L.n == 0) return GS_OK;
     k_permute<<<blocks_for(L.n), kBlock, 0, st>>>(L.A, L.B, L.n, L.cellrank, L.start, L.scenes,
-                                                  wrap_mode, dirty ? 1 : 0, L.err);
+                                                  wrap_mode, dirty ? 1 : 0, L.err, L.retry_count);
     GS_LAUNCHED("fused_permute");
     return GS_OK;
 }
@@ -142,11 +144,39 @@ __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, const Floc
     const V3 offset = sub(bpos, me.pos);
     const float dsq = dot(offset, offset);
     const float d = sqrtf(dsq);
-    if (p.need & NEED_SEP) separation_add(a.sep, fs, me.dir, offset, dsq, d);
-    if (p.need & NEED_ALI) alignment_add(a.ali, fa, me.dir, offset, d, bdir);
-    if (p.need & NEED_COH) cohesion_add(a.coh, fc, me.dir, offset, d, bpos);
+    if (p.need & (NEED_SEP | NEED_ALI | NEED_COH)) {
+        // inBoidNeighborhood (FlockingCommon.cuh:4-30) for the three flocking
+        // behaviours: the unit offset and its dot with the heading are the
+        // same operands for all three, so they are computed once.
+        const bool ang_s = (p.need & NEED_SEP) && !(d < fs.min_d) && !(d > fs.max_d);
+        const bool ang_a = (p.need & NEED_ALI) && !(d < fa.min_d) && !(d > fa.max_d);
+        const bool ang_c = (p.need & NEED_COH) && !(d < fc.min_d) && !(d > fc.max_d);
+        float fwd = 0.f;
+        if (ang_s || ang_a || ang_c) fwd = dot(me.dir, dvd(offset, d));
+        if (p.need & NEED_SEP) {
+            if ((d < fs.min_d) || (ang_s && fwd > fs.cos_max)) {
+                a.sep.sum = add(a.sep.sum, dvd(offset, -dsq));
+                a.sep.n++;
+            }
+        }
+        if (p.need & NEED_ALI) {
+            if ((d < fa.min_d) || (ang_a && fwd > fa.cos_max)) {
+                a.ali.sum = add(a.ali.sum, bdir);
+                a.ali.n++;
+            }
+        }
+        if (p.need & NEED_COH) {
+            if ((d < fc.min_d) || (ang_c && fwd > fc.cos_max)) {
+                a.coh.sum = add(a.coh.sum, bpos);
+                a.coh.n++;
+            }
+        }
+    }
     if (p.need & NEED_AVOID) avoid_add(a.avoid, me, bid, bpos, bdir, bspeed, bradius);
-    if (p.need & NEED_CLOSE) close_add(a.close, me, p.min_sep, knn_d, bpos, bradius);
+    // the KNN distance equals d unless the neighbour moved after the KNN
+    // (avoid-walls); the caller passes it then, else -1
+    if (p.need & NEED_CLOSE)
+        close_add(a.close, me, p.min_sep, knn_d < 0.f ? d : knn_d, bpos, bradius);
 }
 
 // Behaviours order[first..] in order, then nothing else.
@@ -212,103 +242,141 @@ __device__ __forceinline__ Self load_fused(const Fused& B, unsigned s, float4& f
     return me;
 }
 
-// ---- whole step without walls -------------------------------------------------------
-template <int KMAX>
-__global__ void __launch_bounds__(kBlock) k_fused(FusedLaunch L, StepDev p) {
-    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= L.n) return;
-    float4 f0, f4v;
-    Self me = load_fused(L.B, s, f0, f4v);
-    const unsigned id = u(f0.w), scene = u(f4v.w);
-    unsigned applied = p.clear_applied ? 0u : u(f4v.z);
-    V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
-    const Scene sc = L.scenes[scene];
+// ---- KNN of one agent (fast path, or exact redo) ----------------------------------
+// Writes the agent's neighbour slots in (distance, index) order to its shared
+// column: at col[(ENUM + r) * bd] on the fast path, col[r * bd] on the exact
+// path; returns the column offset of entry 0, or UINT_MAX when the fast path
+// gave up and the agent was appended to the retry list.
+template <int KMAX, unsigned ENUM, bool EXACT>
+__device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDev& p, unsigned s,
+                                              V3 pos, unsigned id, const Scene& sc,
+                                              const Box& box, unsigned* col, unsigned bd) {
+    if (EXACT) {
+        knn_neighbours_exact<KMAX>(int(p.k), pos, id, sc.grid, box, sc.cell_offset, L.start,
+                                   L.B.f[0], col, bd);
+        return 0;
+    }
+    if (knn_neighbours_fast<KMAX, ENUM>(int(p.k), pos, id, sc.grid, box, sc.cell_offset, L.start,
+                                        L.B.f[0], col, col + ENUM * bd, bd))
+        return ENUM;
+    L.retry[atomicAdd(L.retry_count, 1u)] = s;
+    return UINT_MAX;
+}
 
-    // The k neighbours (slot, KNN distance) go to this thread's column of
-    // shared memory so the accumulation loop below can index them at run time.
-    extern __shared__ unsigned sh_list[];
-    const unsigned bd = blockDim.x, t = threadIdx.x;
-    {
-        KList<KMAX> list;
-        list.init(int(p.k));
+// Agents handled by one thread: slot `it` of the launch (fast path), or the
+// it-th entry of the retry list (exact path, grid-stride).
+template <bool EXACT>
+__device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, unsigned& s) {
+    if (!EXACT) {
+        s = it;
+        return it < L.n;
+    }
+    if (it >= *L.retry_count) return false;
+    s = L.retry[it];
+    return true;
+}
+
+// ---- whole step without walls -------------------------------------------------------
+template <int KMAX, unsigned ENUM, bool EXACT>
+__global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
+    extern __shared__ unsigned sh_col[];
+    const unsigned bd = blockDim.x;
+    unsigned* col = sh_col + threadIdx.x;
+    const unsigned step = EXACT ? gridDim.x * blockDim.x : 0u;
+    for (unsigned it = blockIdx.x * blockDim.x + threadIdx.x;; it += step) {
+        unsigned s;
+        if (!next_agent<EXACT>(L, it, s)) return;
+        float4 f0, f4v;
+        Self me = load_fused(L.B, s, f0, f4v);
+        const unsigned id = u(f0.w), scene = u(f4v.w);
+        const Scene sc = L.scenes[scene];
         unsigned ix, iy, iz;
         cell_coords(sc.grid, me.pos, ix, iy, iz);
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
-        knn_scan_box<KMAX>(list, me.pos, id, sc.grid, box, sc.cell_offset, L.start, L.B.f[0]);
-        list.for_each(int(p.k), [&](int r, unsigned long long key, unsigned slot) {
-            sh_list[r * bd + t] = key_id(key) == UINT_MAX ? UINT_MAX : slot;
-            sh_list[(p.k + r) * bd + t] = __float_as_uint(key_dist(key));
-        });
+        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, me.pos, id, sc, box, col, bd);
+        if (base == UINT_MAX) {
+            if (EXACT) return;
+            return;
+        }
+        unsigned applied = p.clear_applied ? 0u : u(f4v.z);
+        V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
+        const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali),
+                          fc = flock_params(p.coh);
+        Accs a;
+        init_accs(a, p);
+        const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
+        const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
+        for (unsigned r = 0; r < p.k; ++r) {
+            const unsigned bs = col[(base + r) * bd];
+            if (bs == UINT_MAX) break;
+            const float4 b0 = L.B.f[0][bs];
+            const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float br = need_rad ? L.B.f[2][bs].w : 0.f;
+            accumulate(a, p, fs, fa, fc, me, u(b0.w), -1.f, v3(b0), v3(b1), b1.w, br);
+        }
+        finish_all(a, p, 0, fs, fa, fc, me, applied, steer);
+        integrate(me, steer, p.dt);
+        store_next(L, s, me, id, scene, sc, p.wrap_mode);
+        if (!EXACT) return;
     }
-    const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
-    Accs a;
-    init_accs(a, p);
-    const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
-    const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
-    for (unsigned r = 0; r < p.k; ++r) {
-        const unsigned bs = sh_list[r * bd + t];
-        if (bs == UINT_MAX) break;
-        const float4 b0 = L.B.f[0][bs];
-        const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float br = need_rad ? L.B.f[2][bs].w : 0.f;
-        accumulate(a, p, fs, fa, fc, me, u(b0.w), __uint_as_float(sh_list[(p.k + r) * bd + t]),
-                   v3(b0), v3(b1), b1.w, br);
-    }
-    finish_all(a, p, 0, fs, fa, fc, me, applied, steer);
-    integrate(me, steer, p.dt);
-    store_next(L, s, me, id, scene, sc, p.wrap_mode);
 }
 
 // ---- wall phase: KNN, wall KNN and avoid-walls ---------------------------------------
-template <int KMAX, int KW>
-__global__ void __launch_bounds__(kBlock) k_fused_walls(FusedLaunch L, StepDev p) {
-    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= L.n) return;
-    float4 f0, f4v;
-    Self me = load_fused(L.B, s, f0, f4v);
-    const unsigned id = u(f0.w), scene = u(f4v.w);
-    unsigned applied = p.clear_applied ? 0u : u(f4v.z);
-    V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
-    const Scene sc = L.scenes[scene];
-    unsigned ix, iy, iz;
-    cell_coords(sc.grid, me.pos, ix, iy, iz);
-    const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
-    {
-        KList<KMAX> list;
-        list.init(int(p.k));
-        knn_scan_box<KMAX>(list, me.pos, id, sc.grid, box, sc.cell_offset, L.start, L.B.f[0]);
-        list.for_each(int(p.k), [&](int r, unsigned long long key, unsigned slot) {
-            L.knn_slot[size_t(r) * L.n + s] = key_id(key) == UINT_MAX ? UINT_MAX : slot;
-            L.knn_dist[size_t(r) * L.n + s] = key_dist(key);
-        });
-    }
-    if (sc.n_walls > 0 && L.w_pos_id != nullptr) {
-        extern __shared__ unsigned sh_lines[];
-        const unsigned bd = blockDim.x, t = threadIdx.x;
-        {
-            KList<KW> wl;
-            wl.init(int(p.knw));
-            knn_scan_box<KW>(wl, me.pos, UINT_MAX, sc.grid, box, sc.wall_cell_offset,
-                             L.w_cell_start, L.w_pos_id + sc.wall_offset);
-            wl.for_each(int(p.knw), [&](int r, unsigned long long key, unsigned) {
-                sh_lines[r * bd + t] = key_id(key);
-            });
+template <int KMAX, int KW, unsigned ENUM, bool EXACT>
+__global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDev p) {
+    extern __shared__ unsigned sh_col[];
+    const unsigned bd = blockDim.x;
+    unsigned* col = sh_col + threadIdx.x;
+    const unsigned step = EXACT ? gridDim.x * blockDim.x : 0u;
+    for (unsigned it = blockIdx.x * blockDim.x + threadIdx.x;; it += step) {
+        unsigned s;
+        if (!next_agent<EXACT>(L, it, s)) return;
+        float4 f0, f4v;
+        Self me = load_fused(L.B, s, f0, f4v);
+        const unsigned id = u(f0.w), scene = u(f4v.w);
+        const Scene sc = L.scenes[scene];
+        unsigned ix, iy, iz;
+        cell_coords(sc.grid, me.pos, ix, iy, iz);
+        const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
+        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, me.pos, id, sc, box, col, bd);
+        if (base == UINT_MAX) return;
+        unsigned applied = p.clear_applied ? 0u : u(f4v.z);
+        V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
+        for (unsigned r = 0; r < p.k; ++r) {
+            const unsigned bs = col[(base + r) * bd];
+            L.knn_slot[size_t(r) * L.n + s] = bs;
+            // the KNN distance (before any wall correction moves agents)
+            L.knn_dist[size_t(r) * L.n + s] =
+                bs == UINT_MAX ? FLT_MAX : distance(me.pos, v3(L.B.f[0][bs]));
         }
-        WallAcc wa;
-        walls_init(wa, me, p.min_time_wall);
-        for (unsigned r = 0; r < p.knw; ++r) {
-            const unsigned line = sh_lines[r * bd + t];
-            if (line >= sc.n_walls) break;
-            const unsigned g = sc.wall_offset + line;
-            walls_add(wa, me, line, v3(L.w_start[g]), v3(L.w_end[g]), v3(L.w_normal[g]));
+        if (sc.n_walls > 0 && L.w_pos_id != nullptr) {
+            // wall lines staged in this thread's (now free) shared column
+            {
+                KList<KW> wl;
+                wl.init(int(p.knw));
+                knn_scan_box<KW>(wl, me.pos, UINT_MAX, sc.grid, box, sc.wall_cell_offset,
+                                 L.w_cell_start, L.w_pos_id + sc.wall_offset);
+                wl.for_each(int(p.knw), [&](int r, unsigned long long key, unsigned) {
+                    col[r * bd] = key_id(key);
+                });
+            }
+            WallAcc wa;
+            walls_init(wa, me, p.min_time_wall);
+            for (unsigned r = 0; r < p.knw; ++r) {
+                const unsigned line = col[r * bd];
+                if (line >= sc.n_walls) break;
+                const unsigned g = sc.wall_offset + line;
+                walls_add(wa, me, line, v3(L.w_start[g]), v3(L.w_end[g]), v3(L.w_normal[g]));
+            }
+            walls_finish(wa, p.w_walls, p.mask_walls, me, applied, steer);
+        } else if (!(applied & p.mask_walls)) {
+            steer = add(mul(v3(0.f, 0.f, 0.f), p.w_walls), steer);
         }
-        walls_finish(wa, p.w_walls, p.mask_walls, me, applied, steer);
-    } else if (!(applied & p.mask_walls)) {
-        steer = add(mul(v3(0.f, 0.f, 0.f), p.w_walls), steer);
+        L.w0[s] = make_float4(me.pos.x, me.pos.y, me.pos.z, f0.w);
+        L.w1[s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
+        L.w2[s] = make_float4(steer.x, steer.y, steer.z, fb(applied));
+        if (!EXACT) return;
     }
-    L.w0[s] = make_float4(me.pos.x, me.pos.y, me.pos.z, f0.w);
-    L.w1[s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
-    L.w2[s] = make_float4(steer.x, steer.y, steer.z, fb(applied));
 }
 
 // ---- rest of the step after the wall phase --------------------------------------------
@@ -351,35 +419,49 @@ __global__ void __launch_bounds__(kBlock) k_fused_rest(FusedLaunch L, StepDev p)
     store_next(L, s, me, id, scene, sc, p.wrap_mode);
 }
 
-template <int KMAX>
-static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
-                              PhaseHook* hook) {
+template <class K>
+static gs_status allow_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024)
+        GS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(bytes)));
+    return GS_OK;
+}
+
+// Redo launches over the retry list: a fixed grid that strides over however
+// many agents the fast launch appended (read on the device).
+constexpr unsigned kRetryBlocks = 152;
+
+template <int KMAX, unsigned ENUM>
+static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
+                                PhaseHook* hook) {
     const unsigned nb = blocks_for(L.n);
+    const size_t smem = size_t(2 * ENUM) * kBlock * sizeof(unsigned);
+    const size_t smem_x = size_t(KMAX > 8 ? KMAX : 8) * kBlock * sizeof(unsigned);
     if (p.need & NEED_WALLS) {
-        const size_t smem = size_t(p.knw) * kBlock * sizeof(unsigned);
+        GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
-        k_fused_walls<KMAX, 8><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused_walls<KMAX, 8, ENUM, false><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused_walls<KMAX, 8, ENUM, true><<<kRetryBlocks, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
         k_fused_rest<KMAX><<<nb, kBlock, 0, st>>>(L, p);
         if (hook) hook->mark(3, false);
     } else {
-        const size_t smem = size_t(2 * p.k) * kBlock * sizeof(unsigned);
-        if (smem > 48 * 1024) {
-            static bool opted = false;
-            if (!opted) {
-                GS_CUDA(cudaFuncSetAttribute(k_fused<KMAX>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(2 * KMAX * kBlock * sizeof(unsigned))));
-                opted = true;
-            }
-        }
+        GS_TRY(allow_smem(k_fused<KMAX, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
-        k_fused<KMAX><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused<KMAX, ENUM, false><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused<KMAX, ENUM, true><<<kRetryBlocks, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
     }
     GS_LAUNCHED("fused_step");
     return GS_OK;
+}
+
+template <int KMAX>
+static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
+                              PhaseHook* hook) {
+    if (p.enum_cap <= 32) return launch_fused_k<KMAX, 32>(L, p, st, hook);
+    return launch_fused_k<KMAX, 64>(L, p, st, hook);
 }
 
 gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st, PhaseHook* hook) {

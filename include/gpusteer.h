@@ -159,6 +159,10 @@ gs_status gs_group_synchronize(gs_group g);
  * walls.  Enabling clears the totals. */
 #define GS_PHASES 4
 gs_status gs_group_set_profiling(gs_group g, int enable);
+/* Agents of the last fused step whose neighbour order the fast 32-bit KNN
+ * scan could not vouch for (exact distance ties, crowded boxes) and that the
+ * exact path redid; waits for the group's stream. */
+gs_status gs_group_exact_redos(gs_group g, unsigned* count);
 gs_status gs_group_phase_times(gs_group g, float* ms, unsigned* launches, unsigned cap);
 
 /* ---- KNNData: KNNData(nSize, nK) (KNNData.cu) ---------------------------------- */

@@ -305,6 +305,25 @@ def test_boids_config_fused_matches_oracle(masks):
     assert_state(g.download(), want, skip_side=want.speed == 0)
 
 
+def test_fused_step_on_a_lattice_with_exact_ties():
+    """Agents on an integer lattice, some duplicated: many neighbours at
+    exactly equal distances, so the KNN order depends on the index
+    tie-break (the fused kernels' exact fallback path)."""
+    g3 = np.stack(np.meshgrid(np.arange(12), np.arange(12), np.arange(12), indexing="ij"), -1)
+    pts = g3.reshape(-1, 3).astype(np.float32) - 6.0
+    pts = np.concatenate([pts, pts[::5]])
+    s = sc.boids_sphere(pts.shape[0], seed=3)
+    s.position[:, :3] = pts
+    for k in (7, 16, 20):
+        p = sc.boids_params(k=k, world=64.0, cell=2.0)
+        bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+        g = group_of(s, p.k)
+        gs.step(g, bins, None, p, 3)
+        want = s.copy()
+        ol.run(want, p, 3)
+        assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
 def test_boids_fused_equals_dropin_sequence():
     s = sc.boids_sphere(2000, radius=15.0, seed=11)
     p = sc.boids_params(k=16, world=64.0)
