@@ -104,6 +104,7 @@ SIGNATURES = {
     "gs_step": [_vp, _vp, _vp, C.POINTER(StepParams), _u],
     "gs_step_host": [_vp, _vp, _vp, C.POINTER(StepParams), _u, C.POINTER(AgentArrays), _u,
                      C.POINTER(AgentArrays)],
+    "gs_knn_binned_noalloc": [_vp, _u, _up, _fp, _u, _u, _vp, _vp, _vp],
 }
 _RESTYPE = {"gs_status_string": C.c_char_p, "gs_last_error": C.c_char_p, "gs_version": _i,
             "gs_max_k": _u}

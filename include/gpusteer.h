@@ -243,6 +243,25 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
 gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
                        unsigned steps, const gs_agent_arrays* in, unsigned n,
                        const gs_agent_arrays* out);
+/* ---- KNN without device allocation ------------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot let a
+ * library allocate device memory (pre-sized memory pools, real-time loops
+ * that must not allocate, external allocation accounting).
+ * Binned self-KNN of n device positions (float4) into caller-provided device
+ * arrays idx_out / dist_out (k * n, column-major), with the same results as
+ * gs_update_knn_database + gs_find_knn on the same grid and radius.  Its work
+ * memory is a fixed 32 MiB array inside the library (reserved on every GPU
+ * that loads it, until exit): problems needing more than
+ * 8 * (cells + 1) + 4 * ceil(cells / 4096) + 28 * n bytes (plus alignment) of
+ * it return GS_ERR_INVALID_ARG.  Calls share that array: calls that overlap
+ * on the GPU race and must be serialised by the caller.  The first call on a
+ * device looks up the array's address (cudaGetSymbolAddress) with that device
+ * current; make it before any stream capture.  Asynchronous on `stream`. */
+gs_status gs_knn_binned_noalloc(const float* positions4, unsigned n,
+                                const unsigned world_cells[3], const float world_size[3],
+                                unsigned search_radius, unsigned k, unsigned* idx_out,
+                                float* dist_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
