@@ -37,6 +37,8 @@ WORKLOADS = {
     "large": "large plain flock: 1,048,576 3D boids in a 512^3 cube, k=16, cell 4.0",
     "chokepoint": "2D choke point: 10,000 agents, gap half-width 10, k=16, knw=3, cell 2.0",
     "boids": "plain 3D flock: 4,096 boids in a sphere of radius 50, k=7, cell 4.0",
+    "batched": "256 independent 2D choke-point scenes (gap half-widths 7.5..32.5, 1,000-20,000 "
+               "agents each), k=16, knw=3, 256x256 world, autotuned cell size and block shape",
 }
 
 
@@ -57,10 +59,19 @@ def make_workload(name):
 
 
 def fused_bytes_per_agent(p) -> int:
-    """Algorithmic DRAM bytes of the dominant fused kernel per agent: its own
+    """Algorithmic DRAM bytes of the dominant fused kernel(s) per agent: its own
     bucketed state read once (5 float4 = 80 B), the new state written once
     (80 B) and the next step's (cell, rank) pair (8 B).  Neighbour and
-    candidate reads hit the same bucketed arrays and are counted once."""
+    candidate reads hit the same bucketed arrays and are counted once.  With
+    avoid-walls the step is split in two launches that also write and read
+    the wall-phase state (3 float4) and the neighbour list (slot + distance
+    per neighbour)."""
+    from gpusteer_gb300 import scenario as sc
+
+    if sc.B_AVOID_WALLS in p.order:
+        walls_half = 80 + 48 + 8 * p.k
+        rest_half = 48 + 48 + 8 * p.k + 80 + 8
+        return walls_half + rest_half
     return 80 + 80 + 8
 
 

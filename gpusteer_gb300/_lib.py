@@ -104,6 +104,15 @@ SIGNATURES = {
     "gs_step": [_vp, _vp, _vp, C.POINTER(StepParams), _u],
     "gs_step_host": [_vp, _vp, _vp, C.POINTER(StepParams), _u, C.POINTER(AgentArrays), _u,
                      C.POINTER(AgentArrays)],
+    "gs_group_set_graphs": [_vp, _i],
+    "gs_group_set_block": [_vp, _u],
+    "gs_batch_create": [_u, _up, _u, _up, _fp, _u, _vp, C.POINTER(_vp)],
+    "gs_batch_destroy": [_vp],
+    "gs_batch_set_walls": [_vp, _u, _fp, _fp, _fp, _u],
+    "gs_batch_upload": [_vp, C.POINTER(AgentArrays)],
+    "gs_batch_download": [_vp, C.POINTER(AgentArrays)],
+    "gs_batch_group": [_vp, C.POINTER(_vp)],
+    "gs_batch_step": [_vp, C.POINTER(StepParams), _u],
     "gs_knn_binned_noalloc": [_vp, _u, _up, _fp, _u, _u, _vp, _vp, _vp],
 }
 _RESTYPE = {"gs_status_string": C.c_char_p, "gs_last_error": C.c_char_p, "gs_version": _i,

@@ -52,6 +52,11 @@ static void release_fused(gs_group g) {
     g->fused_k_alloc = 0;
 }
 
+static void drop_graph(gs_group g) {
+    if (g->graph_exec) cudaGraphExecDestroy(g->graph_exec);
+    g->graph_exec = nullptr;
+}
+
 // Brings the reference-layout arrays up to date after fused steps.
 static gs_status ensure_reference(gs_group g) {
     if (!g->fused_current) return GS_OK;
@@ -87,10 +92,6 @@ static gs_status check_grid(const unsigned wc[3], const float ws[3], Grid& g, un
 }
 
 // ---- walls: WallGroupData::LoadFromFile / SplitWalls --------------------------------
-struct Segment {
-    V3 s, m, e, n;
-};
-
 // WallGroupData::intersects (WallGroupData.cu:28-71): entry point of a
 // segment into an axis-aligned box, or false.
 static bool enters_box(V3 start, V3 end, V3 lo, V3 hi, V3& ip) {
@@ -478,6 +479,8 @@ gs_status gs_group_destroy(gs_group g) {
         delete g->prof_events;
         delete g->prof_phase;
     }
+    drop_graph(g);
+    delete g->h_scenes;
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     delete g;
     return GS_OK;
@@ -492,6 +495,8 @@ gs_status gs_group_create(unsigned k, unsigned capacity, void* stream, gs_group*
     std::memset(static_cast<void*>(g), 0, sizeof(*g));
     new (&g->db) Database();
     new (&g->fdb) Database();
+    g->use_graph = true;
+    g->block = kBlock;
     g->k = k;
     g->capacity = capacity;
     gs_status s = GS_OK;
@@ -910,7 +915,7 @@ gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, uns
 }
 
 // ---- fused step ------------------------------------------------------------------
-static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k) {
+static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, unsigned n_scenes) {
     if (!g->cellrank) {
         const size_t n = g->capacity;
         for (int j = 0; j < 6; ++j) {
@@ -918,13 +923,17 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k) {
             GS_TRY(dalloc(&g->B.f[j], n));
         }
         GS_TRY(dalloc(&g->cellrank, n));
-        GS_TRY(dalloc(&g->d_scene, 1));
         GS_TRY(dalloc(&g->d_err, 1));
         GS_TRY(dalloc(&g->retry, n));
         GS_TRY(dalloc(&g->retry_count, 1));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
         GS_CUDA(cudaMemset(g->retry_count, 0, sizeof(unsigned)));
         GS_CUDA(cudaDeviceSynchronize());
+    }
+    if (g->scene_alloc < n_scenes) {
+        dfree(g->d_scene);
+        GS_TRY(dalloc(&g->d_scene, n_scenes));
+        g->scene_alloc = n_scenes;
     }
     if (g->fdb.cells != C) GS_TRY(db_reserve(g->fdb, 0, C));
     if (walls && (!g->w0 || g->fused_k_alloc < k)) {
@@ -944,47 +953,53 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k) {
     return GS_OK;
 }
 
-gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
-                  unsigned steps) {
-    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
-    StepDev d;
-    GS_TRY(validate_step(p, walls, d));
-    Grid grid;
-    unsigned C;
-    GS_TRY(check_grid(p->world_cells, p->world_size, grid, C));
-    if (C != bins->cells || std::memcmp(&grid, &bins->grid, sizeof(Grid)) != 0)
-        return fail(GS_ERR_INVALID_ARG, "step grid differs from the bins");
-    const bool has_walls = d.need & NEED_WALLS;
-    if (has_walls && !walls) return fail(GS_ERR_INVALID_ARG, "avoid-walls needs a wall group");
-    if (steps == 0 || g->n == 0) return GS_OK;
+static_assert(sizeof(FusedLaunch) <= sizeof(FusedLaunchBytes), "graph key size");
+static_assert(sizeof(StepDev) <= sizeof(StepDevBytes), "graph key size");
+
+// Uploads the scene table when it differs from the one on the device.
+static gs_status put_scenes(gs_group g, const std::vector<Scene>& scenes) {
+    if (g->h_scenes && *g->h_scenes == scenes) return GS_OK;
+    if (!g->h_scenes) g->h_scenes = new std::vector<Scene>();
+    *g->h_scenes = scenes;
+    GS_CUDA(cudaMemcpyAsync(g->d_scene, g->h_scenes->data(), scenes.size() * sizeof(Scene),
+                            cudaMemcpyHostToDevice, g->stream));
+    return GS_OK;
+}
+
+struct WallsDev {
+    const float4 *start = nullptr, *end = nullptr, *normal = nullptr, *pos_id = nullptr;
+    const unsigned* cell_start = nullptr;
+};
+
+// One step's launches: scan, permute, fused (+ exact redo).
+static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, unsigned C,
+                           PhaseHook* hook) {
     cudaStream_t st = g->stream;
-    GS_TRY(reserve_fused(g, C, has_walls, d.k));
-    if (has_walls) GS_TRY(walls_db(walls, grid, C, st));
+    if (hook) hook->mark(0, true);
+    GS_TRY(scan_counts(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
+    if (hook) hook->mark(0, false);
+    if (hook) hook->mark(1, true);
+    GS_TRY(fused_permute(L, d.wrap_mode, d.dirty != 0, st));
+    if (hook) hook->mark(1, false);
+    GS_TRY(fused_step(L, d, st, hook));
+    return GS_OK;
+}
 
-    static_assert(sizeof(Scene) % 4 == 0, "scene layout");
-    Scene sc{};
-    sc.grid = grid;
-    sc.cell_offset = 0;
-    sc.agent_offset = 0;
-    sc.n_agents = g->n;
-    sc.n_walls = has_walls ? walls->n : 0;
-    // The scene table is tiny; a synchronous copy keeps the host struct's
-    // lifetime trivial.
-    GS_CUDA(cudaMemcpyAsync(g->d_scene, &sc, sizeof(Scene), cudaMemcpyHostToDevice, st));
-    GS_CUDA(cudaStreamSynchronize(st));
-
+// The fused engine for a group whose scene table is in g->h_scenes / d_scene
+// (one scene for a plain group, many for a batch).
+static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
+                           const unsigned* agent_scene, const WallsDev& w, unsigned steps) {
+    cudaStream_t st = g->stream;
     bool dirty = false;
     if (!g->fused_current) {
         dirty = g->accum_dirty;
         // counts left pending by an earlier fused step no longer apply
         GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
-        GS_TRY(fused_from_reference(view(g), nullptr, g->d_scene, g->A, g->cellrank, g->fdb.count,
-                                    d.wrap_mode, dirty, st));
+        GS_TRY(fused_from_reference(view(g), agent_scene, g->d_scene, g->A, g->cellrank,
+                                    g->fdb.count, d.wrap_mode, dirty, st));
         g->fused_current = true;
-    } else if (g->fdb.grid.wc[0] != grid.wc[0] || g->fdb.grid.wc[1] != grid.wc[1] ||
-               g->fdb.grid.wc[2] != grid.wc[2] || g->fdb.grid.ws[0] != grid.ws[0] ||
-               g->fdb.grid.ws[1] != grid.ws[1] || g->fdb.grid.ws[2] != grid.ws[2] ||
-               g->fdb.valid == false || g->pending_wrap != d.wrap_mode) {
+    } else if (std::memcmp(&g->fdb.grid, &grid, sizeof(Grid)) != 0 || !g->fdb.valid ||
+               g->pending_wrap != d.wrap_mode) {
         GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
         GS_TRY(fused_recount(g->A, g->n, g->d_scene, g->cellrank, g->fdb.count, d.wrap_mode, st));
     }
@@ -1003,13 +1018,12 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
     L.err = g->d_err;
     L.retry = g->retry;
     L.retry_count = g->retry_count;
-    d.enum_cap = enum_capacity(g->n, C, grid, d.r);
-    if (has_walls) {
-        L.w_start = walls->start;
-        L.w_end = walls->end;
-        L.w_normal = walls->normal;
-        L.w_pos_id = walls->db.pos_id;
-        L.w_cell_start = walls->db.start;
+    if (d.need & NEED_WALLS) {
+        L.w_start = w.start;
+        L.w_end = w.end;
+        L.w_normal = w.normal;
+        L.w_pos_id = w.pos_id;
+        L.w_cell_start = w.cell_start;
         L.w0 = g->w0;
         L.w1 = g->w1;
         L.w2 = g->w2;
@@ -1018,20 +1032,82 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
     }
     Profiler prof(g);
     PhaseHook* hook = g->profiling ? &prof : nullptr;
-    for (unsigned step = 0; step < steps; ++step) {
-        d.dirty = dirty ? 1 : 0;
-        if (hook) hook->mark(0, true);
-        GS_TRY(scan_counts(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
-        if (hook) hook->mark(0, false);
-        if (hook) hook->mark(1, true);
-        GS_TRY(fused_permute(L, d.wrap_mode, dirty, st));
-        if (hook) hook->mark(1, false);
-        GS_TRY(fused_step(L, d, st, hook));
-        dirty = false;
+    unsigned step = 0;
+    // A step with steering carried in from per-function calls runs eagerly;
+    // so do all steps while profiling, and the first step of a new launch
+    // configuration (which also performs one-time kernel set-up).
+    const bool cfg_same = g->graph_exec && std::memcmp(&g->graph_L, &L, sizeof(L)) == 0 &&
+                          std::memcmp(&g->graph_d, &d, sizeof(d)) == 0 && g->graph_C == C;
+    if (dirty || hook || !g->use_graph || !cfg_same) {
+        const unsigned eager = (hook || !g->use_graph) ? steps : 1u;
+        for (; step < eager && step < steps; ++step) {
+            d.dirty = dirty ? 1 : 0;
+            GS_TRY(step_body(g, L, d, C, hook));
+            dirty = false;
+        }
+    }
+    d.dirty = 0;
+    if (step < steps) {
+        if (!(g->graph_exec && std::memcmp(&g->graph_L, &L, sizeof(L)) == 0 &&
+              std::memcmp(&g->graph_d, &d, sizeof(d)) == 0 && g->graph_C == C)) {
+            drop_graph(g);
+            cudaGraph_t graph = nullptr;
+            GS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            const gs_status s = step_body(g, L, d, C, nullptr);
+            const cudaError_t e = cudaStreamEndCapture(st, &graph);
+            if (s != GS_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return s;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            const cudaError_t ei = cudaGraphInstantiate(&g->graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ei != cudaSuccess) {
+                g->graph_exec = nullptr;
+                return cuda_fail(ei, "cudaGraphInstantiate");
+            }
+            std::memcpy(&g->graph_L, &L, sizeof(L));
+            std::memcpy(&g->graph_d, &d, sizeof(d));
+            g->graph_C = C;
+        }
+        for (; step < steps; ++step) GS_CUDA(cudaGraphLaunch(g->graph_exec, st));
     }
     g->accum_dirty = false;
     g->db.valid = false;
     return GS_OK;
+}
+
+gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
+                  unsigned steps) {
+    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
+    StepDev d;
+    GS_TRY(validate_step(p, walls, d));
+    Grid grid;
+    unsigned C;
+    GS_TRY(check_grid(p->world_cells, p->world_size, grid, C));
+    if (C != bins->cells || std::memcmp(&grid, &bins->grid, sizeof(Grid)) != 0)
+        return fail(GS_ERR_INVALID_ARG, "step grid differs from the bins");
+    const bool has_walls = d.need & NEED_WALLS;
+    if (has_walls && !walls) return fail(GS_ERR_INVALID_ARG, "avoid-walls needs a wall group");
+    if (steps == 0 || g->n == 0) return GS_OK;
+    GS_TRY(reserve_fused(g, C, has_walls, d.k, 1));
+    if (has_walls) GS_TRY(walls_db(walls, grid, C, g->stream));
+    Scene sc{};
+    sc.grid = grid;
+    sc.n_agents = g->n;
+    sc.n_walls = has_walls ? walls->n : 0;
+    GS_TRY(put_scenes(g, std::vector<Scene>{sc}));
+    d.enum_cap = enum_capacity(g->n, C, grid, d.r);
+    d.block = g->block;
+    WallsDev w;
+    if (has_walls) {
+        w.start = walls->start;
+        w.end = walls->end;
+        w.normal = walls->normal;
+        w.pos_id = walls->db.pos_id;
+        w.cell_start = walls->db.start;
+    }
+    return fused_run(g, d, grid, C, nullptr, w, steps);
 }
 
 gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
@@ -1040,6 +1116,213 @@ gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_p
     GS_TRY(gs_group_upload(g, in, n));
     GS_TRY(gs_step(g, bins, walls, p, steps));
     return gs_group_download(g, out);
+}
+
+gs_status gs_group_set_graphs(gs_group g, int enable) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    g->use_graph = enable != 0;
+    if (!g->use_graph) drop_graph(g);
+    return GS_OK;
+}
+
+gs_status gs_group_set_block(gs_group g, unsigned threads) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    if (threads != 64 && threads != 128 && threads != 256)
+        return fail(GS_ERR_INVALID_ARG, "threads per block must be 64, 128 or 256");
+    g->block = threads;
+    return GS_OK;
+}
+
+// ---- batched scenes ---------------------------------------------------------------
+gs_status gs_batch_destroy(gs_batch b) {
+    if (!b) return GS_OK;
+    gs_group_destroy(b->g);
+    dfree(b->agent_scene);
+    dfree(b->w_start);
+    dfree(b->w_end);
+    dfree(b->w_normal);
+    dfree(b->w_pos_id);
+    dfree(b->w_cell_start);
+    delete b;
+    return GS_OK;
+}
+
+gs_status gs_batch_create(unsigned n_scenes, const unsigned* agents_per_scene, unsigned k,
+                          const unsigned world_cells[3], const float world_size[3],
+                          unsigned search_radius, void* stream, gs_batch* out) {
+    if (!out || !agents_per_scene || !world_cells || !world_size)
+        return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (n_scenes == 0) return fail(GS_ERR_INVALID_ARG, "no scenes");
+    Grid grid;
+    unsigned cells;
+    GS_TRY(check_grid(world_cells, world_size, grid, cells));
+    unsigned long long total = 0;
+    for (unsigned s = 0; s < n_scenes; ++s) total += agents_per_scene[s];
+    if (total == 0 || total > (1ull << 30)) return fail(GS_ERR_INVALID_ARG, "bad agent count");
+    if (static_cast<unsigned long long>(cells) * n_scenes > (1ull << 31))
+        return fail(GS_ERR_INVALID_ARG, "too many cells over all scenes");
+    gs_batch b = new (std::nothrow) gs_batch_s();
+    if (!b) return fail(GS_ERR_OOM, "host allocation failed");
+    b->grid = grid;
+    b->cells = cells;
+    b->radius = search_radius;
+    b->counts.assign(agents_per_scene, agents_per_scene + n_scenes);
+    b->walls.resize(n_scenes);
+    b->total = unsigned(total);
+    gs_status st = gs_group_create(k, b->total, stream, &b->g);
+    std::vector<unsigned> scene_of(b->total);
+    unsigned off = 0;
+    for (unsigned s = 0; s < n_scenes; ++s) {
+        Scene sc{};
+        sc.grid = grid;
+        sc.cell_offset = s * cells;
+        sc.agent_offset = off;
+        sc.n_agents = agents_per_scene[s];
+        sc.wall_cell_offset = s * cells;
+        b->scenes.push_back(sc);
+        for (unsigned i = 0; i < agents_per_scene[s]; ++i) scene_of[off + i] = s;
+        off += agents_per_scene[s];
+    }
+    if (st == GS_OK) st = dalloc(&b->agent_scene, b->total);
+    if (st == GS_OK &&
+        cudaMemcpy(b->agent_scene, scene_of.data(), size_t(b->total) * 4, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+        st = fail(GS_ERR_CUDA, "scene map upload");
+    if (st != GS_OK) {
+        const std::string msg = g_last_error;
+        gs_batch_destroy(b);
+        set_error(msg);
+        return st;
+    }
+    *out = b;
+    return GS_OK;
+}
+
+gs_status gs_batch_set_walls(gs_batch b, unsigned scene, const float* start4, const float* end4,
+                             const float* normal4, unsigned n) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
+    if (scene >= b->scenes.size()) return fail(GS_ERR_INVALID_ARG, "scene out of range");
+    if (n > 0 && (!start4 || !end4 || !normal4)) return fail(GS_ERR_INVALID_ARG, "null arrays");
+    std::vector<Segment> raw(n);
+    for (unsigned i = 0; i < n; ++i) {
+        raw[i].s = v3(start4[4 * i], start4[4 * i + 1], start4[4 * i + 2]);
+        raw[i].e = v3(end4[4 * i], end4[4 * i + 1], end4[4 * i + 2]);
+        raw[i].n = v3(normal4[4 * i], normal4[4 * i + 1], normal4[4 * i + 2]);
+        raw[i].m = v3(0.5f * (raw[i].s.x + raw[i].e.x), 0.5f * (raw[i].s.y + raw[i].e.y),
+                      0.5f * (raw[i].s.z + raw[i].e.z));
+    }
+    b->walls[scene] = split_walls(raw, b->grid);
+    b->walls_dirty = true;
+    return GS_OK;
+}
+
+// Concatenated wall arrays and the walls' bucketed database over all scenes'
+// cells (wall index = the scene-local index, as a per-scene run sees it).
+static gs_status batch_walls(gs_batch b) {
+    if (!b->walls_dirty) return GS_OK;
+    const unsigned S = unsigned(b->scenes.size());
+    const unsigned Ct = b->cells * S;
+    std::vector<float4> st, en, nm, mid;
+    std::vector<unsigned> label;
+    for (unsigned s = 0; s < S; ++s) {
+        b->scenes[s].wall_offset = unsigned(st.size());
+        b->scenes[s].n_walls = unsigned(b->walls[s].size());
+        for (unsigned j = 0; j < b->walls[s].size(); ++j) {
+            const Segment& w = b->walls[s][j];
+            st.push_back(f4(w.s, 0.f));
+            en.push_back(f4(w.e, 0.f));
+            nm.push_back(f4(w.n, 0.f));
+            float idbits;
+            std::memcpy(&idbits, &j, sizeof(float));
+            mid.push_back(f4(w.m, idbits));
+            label.push_back(b->scenes[s].cell_offset + cell_of(b->grid, w.m));
+        }
+    }
+    const unsigned W = unsigned(st.size());
+    std::vector<unsigned> start(size_t(Ct) + 1, 0u);
+    for (unsigned i = 0; i < W; ++i) start[label[i] + 1]++;
+    for (unsigned c = 0; c < Ct; ++c) start[c + 1] += start[c];
+    std::vector<float4> pos_id(W);
+    {
+        std::vector<unsigned> fill(start.begin(), start.end() - 1);
+        for (unsigned i = 0; i < W; ++i) pos_id[fill[label[i]]++] = mid[i];
+    }
+    dfree(b->w_start);
+    dfree(b->w_end);
+    dfree(b->w_normal);
+    dfree(b->w_pos_id);
+    dfree(b->w_cell_start);
+    GS_TRY(dalloc(&b->w_start, W));
+    GS_TRY(dalloc(&b->w_end, W));
+    GS_TRY(dalloc(&b->w_normal, W));
+    GS_TRY(dalloc(&b->w_pos_id, W));
+    GS_TRY(dalloc(&b->w_cell_start, size_t(Ct) + 1));
+    if (W) {
+        GS_CUDA(cudaMemcpy(b->w_start, st.data(), W * sizeof(float4), cudaMemcpyHostToDevice));
+        GS_CUDA(cudaMemcpy(b->w_end, en.data(), W * sizeof(float4), cudaMemcpyHostToDevice));
+        GS_CUDA(cudaMemcpy(b->w_normal, nm.data(), W * sizeof(float4), cudaMemcpyHostToDevice));
+        GS_CUDA(cudaMemcpy(b->w_pos_id, pos_id.data(), W * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    GS_CUDA(cudaMemcpy(b->w_cell_start, start.data(), (size_t(Ct) + 1) * 4,
+                       cudaMemcpyHostToDevice));
+    b->n_walls = W;
+    b->walls_dirty = false;
+    drop_graph(b->g);
+    return GS_OK;
+}
+
+gs_status gs_batch_upload(gs_batch b, const gs_agent_arrays* host) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
+    return gs_group_upload(b->g, host, b->total);
+}
+
+gs_status gs_batch_download(gs_batch b, const gs_agent_arrays* host) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
+    return gs_group_download(b->g, host);
+}
+
+gs_status gs_batch_group(gs_batch b, gs_group* g) {
+    if (!b || !g) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *g = b->g;
+    return GS_OK;
+}
+
+gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
+    StepDev d;
+    GS_TRY(validate_step(p, nullptr, d));
+    Grid grid;
+    unsigned C;
+    GS_TRY(check_grid(p->world_cells, p->world_size, grid, C));
+    if (std::memcmp(&grid, &b->grid, sizeof(Grid)) != 0)
+        return fail(GS_ERR_INVALID_ARG, "step grid differs from the batch grid");
+    if (d.r != b->radius) return fail(GS_ERR_INVALID_ARG, "search radius differs from the batch");
+    if (steps == 0) return GS_OK;
+    gs_group g = b->g;
+    const unsigned S = unsigned(b->scenes.size());
+    const unsigned Ct = b->cells * S;
+    const bool has_walls = d.need & NEED_WALLS;
+    GS_TRY(reserve_fused(g, Ct, has_walls, d.k, S));
+    if (has_walls) GS_TRY(batch_walls(b));
+    std::vector<Scene> scenes = b->scenes;
+    if (!has_walls)
+        for (Scene& sc : scenes) sc.n_walls = 0;
+    GS_TRY(put_scenes(g, scenes));
+    // the fast KNN's candidate capacity from the densest scene
+    unsigned cap = 32;
+    for (const Scene& sc : scenes)
+        cap = std::max(cap, enum_capacity(sc.n_agents, b->cells, grid, d.r));
+    d.enum_cap = cap;
+    d.block = g->block;
+    WallsDev w;
+    if (has_walls) {
+        w.start = b->w_start;
+        w.end = b->w_end;
+        w.normal = b->w_normal;
+        w.pos_id = b->w_pos_id;
+        w.cell_start = b->w_cell_start;
+    }
+    return fused_run(g, d, grid, Ct, b->agent_scene, w, steps);
 }
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -68,6 +69,9 @@ struct Scene {
     unsigned n_walls;
     unsigned wall_cell_offset;
 };
+inline bool operator==(const Scene& a, const Scene& b) {
+    return std::memcmp(&a, &b, sizeof(Scene)) == 0;
+}
 
 // Bucketed ("fused") state: six float4 streams per agent.
 //   f0 = position.xyz, agent index (bits)    f1 = direction.xyz, speed
@@ -76,6 +80,20 @@ struct Scene {
 //   f5 = steering.xyz, 0  (read only while the steering may be non-zero)
 struct Fused {
     float4* f[6];
+};
+
+// Wall segment (WallGroupData: start, mid, end, normal).
+struct Segment {
+    V3 s, m, e, n;
+};
+
+// Raw copies of a launch's parameter blocks (compared byte-wise to decide
+// whether a captured graph still applies).
+struct FusedLaunchBytes {
+    unsigned char b[256];
+};
+struct StepDevBytes {
+    unsigned char b[256];
 };
 
 // A group's bucketed binning database (KNNDatabase.cuh:30-38): cell of every
@@ -134,7 +152,9 @@ struct gs_group_s {
     unsigned* knn_slot;    // [k * n] neighbour slots (wall phase)
     float* knn_dist;       // [k * n]
     gs::Database fdb;      // counts / starts of the fused step
-    gs::Scene* d_scene;    // single-scene table
+    gs::Scene* d_scene;    // scene table (one entry for a plain group)
+    unsigned scene_alloc;
+    std::vector<gs::Scene>* h_scenes;  // host copy of the table on the device
     unsigned* d_err;       // device error flags (see FusedLaunch::err)
     unsigned* retry;       // [capacity] exact-redo list and its counter
     unsigned* retry_count;
@@ -148,4 +168,26 @@ struct gs_group_s {
     std::vector<int>* prof_phase;
     float prof_ms[4];
     unsigned prof_launches[4];
+    // CUDA graph of one fused step, replayed while the launch configuration
+    // (buffers, parameters, grid) stays the same
+    bool use_graph;
+    unsigned block;
+    cudaGraphExec_t graph_exec;
+    gs::FusedLaunchBytes graph_L;
+    gs::StepDevBytes graph_d;
+    unsigned graph_C;
+};
+
+struct gs_batch_s {
+    gs_group g = nullptr;  // all scenes' agents, concatenated
+    gs::Grid grid{};
+    unsigned cells = 0, radius = 1, total = 0;
+    std::vector<unsigned> counts;
+    std::vector<gs::Scene> scenes;
+    std::vector<std::vector<gs::Segment>> walls;  // per scene, split on the grid
+    bool walls_dirty = false;
+    unsigned n_walls = 0;
+    unsigned* agent_scene = nullptr;
+    float4 *w_start = nullptr, *w_end = nullptr, *w_normal = nullptr, *w_pos_id = nullptr;
+    unsigned* w_cell_start = nullptr;
 };

@@ -72,6 +72,7 @@ struct StepDev {
     float dt;
     unsigned need;      // NEED_* bits
     unsigned enum_cap;  // candidate capacity of the fast KNN scan (32 or 64)
+    unsigned block;     // threads per block of the fused launches (0: 256)
 };
 constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
                    NEED_WALLS = 32;

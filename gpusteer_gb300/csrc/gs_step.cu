@@ -23,6 +23,9 @@
 // (plugins/BoidsGroup.cpp:606-637, plugins/ChokePointNew.cpp:586-630).
 #include "gs_behaviours.cuh"
 #include "gs_knn.cuh"
+#include <map>
+#include <mutex>
+
 #include "gs_launch.h"
 
 namespace gs {
@@ -355,7 +358,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDe
                 KList<KW> wl;
                 wl.init(int(p.knw));
                 knn_scan_box<KW>(wl, me.pos, UINT_MAX, sc.grid, box, sc.wall_cell_offset,
-                                 L.w_cell_start, L.w_pos_id + sc.wall_offset);
+                                 L.w_cell_start, L.w_pos_id);
                 wl.for_each(int(p.knw), [&](int r, unsigned long long key, unsigned) {
                     col[r * bd] = key_id(key);
                 });
@@ -419,11 +422,20 @@ __global__ void __launch_bounds__(kBlock) k_fused_rest(FusedLaunch L, StepDev p)
     store_next(L, s, me, id, scene, sc, p.wrap_mode);
 }
 
+// Opts a kernel into more than 48 KiB of dynamic shared memory, once per
+// kernel (outside any stream capture: the first launch of a kernel is never
+// captured, see gs_capi.cu).
 template <class K>
 static gs_status allow_smem(K kernel, size_t bytes) {
-    if (bytes > 48 * 1024)
-        GS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     int(bytes)));
+    static std::mutex mu;
+    static std::map<const void*, size_t> done;
+    if (bytes <= 48 * 1024) return GS_OK;
+    std::lock_guard<std::mutex> lock(mu);
+    const void* key = reinterpret_cast<const void*>(kernel);
+    auto it = done.find(key);
+    if (it != done.end() && it->second >= bytes) return GS_OK;
+    GS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+    done[key] = bytes;
     return GS_OK;
 }
 
@@ -434,22 +446,23 @@ constexpr unsigned kRetryBlocks = 152;
 template <int KMAX, unsigned ENUM>
 static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
                                 PhaseHook* hook) {
-    const unsigned nb = blocks_for(L.n);
-    const size_t smem = size_t(2 * ENUM) * kBlock * sizeof(unsigned);
+    const unsigned bs = p.block ? p.block : kBlock;
+    const unsigned nb = blocks_for(L.n, bs);
+    const size_t smem = size_t(2 * ENUM) * bs * sizeof(unsigned);
     const size_t smem_x = size_t(KMAX > 8 ? KMAX : 8) * kBlock * sizeof(unsigned);
     if (p.need & NEED_WALLS) {
         GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
-        k_fused_walls<KMAX, 8, ENUM, false><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
         k_fused_walls<KMAX, 8, ENUM, true><<<kRetryBlocks, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
-        k_fused_rest<KMAX><<<nb, kBlock, 0, st>>>(L, p);
+        k_fused_rest<KMAX><<<nb, bs, 0, st>>>(L, p);
         if (hook) hook->mark(3, false);
     } else {
         GS_TRY(allow_smem(k_fused<KMAX, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
-        k_fused<KMAX, ENUM, false><<<nb, kBlock, smem, st>>>(L, p);
+        k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
         k_fused<KMAX, ENUM, true><<<kRetryBlocks, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
     }

@@ -229,6 +229,89 @@ class WallGroup:
             self._h = None
 
 
+class _GroupRef:
+    """A non-owning view of a group handle (e.g. a batch's underlying group)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        st = C.c_void_p()
+        call("gs_group_stream", self._h, C.byref(st))
+        return st.value or 0
+
+    def synchronize(self) -> None:
+        call("gs_group_synchronize", self._h)
+
+
+def set_graphs(group, enable: bool) -> None:
+    call("gs_group_set_graphs", group.handle, int(bool(enable)))
+
+
+def set_block(group, threads: int) -> None:
+    call("gs_group_set_block", group.handle, int(threads))
+
+
+class Batch:
+    """Many independent scenes advanced together (gs_batch_*): agents are
+    concatenated in scene order, each scene keeps scene-local indices, cells
+    and walls, and its result equals stepping it alone."""
+
+    def __init__(self, counts, k: int, world_cells, world_size, search_radius: int = 1,
+                 stream: int | None = None):
+        counts = np.ascontiguousarray(counts, np.uint32)
+        h = C.c_void_p()
+        call("gs_batch_create", len(counts), _ptr(counts, C.c_uint), int(k), _u3(world_cells),
+             _f3(world_size), int(search_radius), C.c_void_p(stream) if stream else None,
+             C.byref(h))
+        self._h = h
+        self.counts = counts
+        self.n = int(counts.sum())
+        g = C.c_void_p()
+        call("gs_batch_group", h, C.byref(g))
+        self.group = _GroupRef(g)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_walls(self, scene: int, rows: np.ndarray) -> None:
+        rows = np.asarray(rows, np.float32).reshape(-1, 9)
+        n = rows.shape[0]
+        st = np.zeros((n, 4), np.float32)
+        en = np.zeros((n, 4), np.float32)
+        nm = np.zeros((n, 4), np.float32)
+        st[:, :3], en[:, :3], nm[:, :3] = rows[:, 0:3], rows[:, 3:6], rows[:, 6:9]
+        call("gs_batch_set_walls", self._h, int(scene), _ptr(st), _ptr(en), _ptr(nm), n)
+
+    def upload(self, s: AgentState) -> None:
+        if s.n != self.n:
+            raise ValueError("state size differs from the batch")
+        a = host_arrays(s)
+        call("gs_batch_upload", self._h, C.byref(a))
+        self.group.synchronize()
+
+    def download(self) -> AgentState:
+        out = AgentState.zeros(self.n)
+        a = host_arrays(out)
+        call("gs_batch_download", self._h, C.byref(a))
+        return out
+
+    def step(self, params: StepParams, steps: int = 1) -> None:
+        p = step_params_c(params)
+        call("gs_batch_step", self._h, C.byref(p), int(steps))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_batch_destroy(self._h)
+            self._h = None
+
+
 # ---- GroupSteerLibrary.cuh -----------------------------------------------------------
 
 def wrapWorld(group: AgentGroup, world_size, mode: int = WRAP_REFERENCE) -> None:

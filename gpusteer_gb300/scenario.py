@@ -406,6 +406,23 @@ def params_from_file(sim: SimulationParams, dt: float) -> StepParams:
         dt=dt)
 
 
+CHOKEPOINT_GAPS = (7.5, 10.0, 12.5, 15.0, 17.5, 20.0, 22.5, 25.0, 27.5, 30.0, 32.5)
+
+
+def batched_chokepoint(n_scenes: int = 256, seed: int = 0, n_range=(1000, 20000),
+                       gaps=CHOKEPOINT_GAPS):
+    """Independent choke-point scenes: per scene s, a gap half-width drawn
+    uniformly from `gaps` (the data/ChokePoint{X}.map set) and an agent count
+    uniform in n_range, agents seeded with hash_seed(seed, s).
+    Returns (states, gaps_per_scene)."""
+    u = uniform01(seed ^ 0xB47C4, 2 * n_scenes).reshape(n_scenes, 2).astype(np.float64)
+    lo, hi = n_range
+    counts = (lo + np.floor(u[:, 0] * (hi - lo + 1))).astype(np.int64).clip(lo, hi)
+    picks = np.floor(u[:, 1] * len(gaps)).astype(np.int64).clip(0, len(gaps) - 1)
+    states = [chokepoint_agents(int(counts[s]), seed=hash_seed(seed, s)) for s in range(n_scenes)]
+    return states, [float(gaps[i]) for i in picks]
+
+
 def default_steps(name: str) -> int:
     return {"boids": 100, "chokepoint": 500, "large": 1000, "batched": 300, "adjoint": 64}[name]
 

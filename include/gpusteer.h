@@ -243,6 +243,34 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
 gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
                        unsigned steps, const gs_agent_arrays* in, unsigned n,
                        const gs_agent_arrays* out);
+/* Replays one captured CUDA graph per fused step while the launch
+ * configuration stays the same (default on).  Not part of the reference. */
+gs_status gs_group_set_graphs(gs_group g, int enable);
+/* Threads per block of the fused-step launches: 64, 128 or 256 (default).
+ * Results do not depend on it; the autotuner picks it. */
+gs_status gs_group_set_block(gs_group g, unsigned threads);
+
+/* ---- batched scenes -------------------------------------------------------------
+ * Many independent worlds (e.g. one ChokePoint plugin instance each) advanced
+ * together: every step of every scene is one CUDA graph launch, and each
+ * scene's result is bit-identical to stepping it alone with gs_step (scene-
+ * local agent and wall indices, scene-local cells).  All scenes share one
+ * grid; agents are uploaded concatenated in scene order.  No reference
+ * counterpart: the reference runs one group per plugin (plugins/ChokePointNew.cpp). */
+typedef struct gs_batch_s* gs_batch;
+gs_status gs_batch_create(unsigned n_scenes, const unsigned* agents_per_scene, unsigned k,
+                          const unsigned world_cells[3], const float world_size[3],
+                          unsigned search_radius, void* stream, gs_batch* out);
+gs_status gs_batch_destroy(gs_batch b);
+/* A scene's walls (split at the batch grid like gs_walls_create). */
+gs_status gs_batch_set_walls(gs_batch b, unsigned scene, const float* start4, const float* end4,
+                             const float* normal4, unsigned n);
+gs_status gs_batch_upload(gs_batch b, const gs_agent_arrays* host);
+gs_status gs_batch_download(gs_batch b, const gs_agent_arrays* host);
+/* The batch's underlying group (stream, profiling, graphs, block size). */
+gs_status gs_batch_group(gs_batch b, gs_group* g);
+gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps);
+
 /* ---- KNN without device allocation ------------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot let a
  * library allocate device memory (pre-sized memory pools, real-time loops

@@ -432,3 +432,66 @@ def test_empty_group_steps():
     p = sc.boids_params(k=7)
     gs.step(g, gs.KNNBinData(p.world_cells, p.world_size, 1), None, p, 3)
     assert g.download().n == 0
+
+
+# ---- batched scenes ---------------------------------------------------------------
+
+def batch_setup(states, gaps, p, graphs=True, block=256):
+    b = gs.Batch([s.n for s in states], p.k, p.world_cells, p.world_size, p.search_radius)
+    for i, g in enumerate(gaps):
+        b.set_walls(i, sc.chokepoint_walls(g))
+    b.upload(AgentState.concat(states))
+    gs.set_graphs(b.group, graphs)
+    gs.set_block(b.group, block)
+    return b
+
+
+def per_scene(states, gaps, p, steps):
+    outs = []
+    for s, g in zip(states, gaps):
+        bins = gs.KNNBinData(p.world_cells, p.world_size, p.search_radius)
+        walls = gs.WallGroup(sc.chokepoint_walls(g), bins=bins, knw=p.knw)
+        grp = group_of(s, p.k)
+        gs.step(grp, bins, walls, p, steps)
+        outs.append(grp.download())
+    return AgentState.concat(outs)
+
+
+def test_batched_scenes_equal_per_scene_runs():
+    states, gaps = sc.batched_chokepoint(7, seed=3, n_range=(300, 3000))
+    p = sc.chokepoint_params(world=256.0, cell=2.0)
+    want = per_scene(states, gaps, p, 15)
+    for graphs, block in ((True, 256), (False, 256), (True, 128)):
+        b = batch_setup(states, gaps, p, graphs=graphs, block=block)
+        b.step(p, 5)
+        b.step(p, 10)  # resumes across calls (graph replay)
+        assert_state(b.download(), want)
+
+
+def test_batched_scene_matches_oracle():
+    states, gaps = sc.batched_chokepoint(3, seed=9, n_range=(500, 2000))
+    p = sc.chokepoint_params(world=256.0, cell=2.0)
+    b = batch_setup(states, gaps, p)
+    b.step(p, 12)
+    got = b.download()
+    off = 0
+    for s, g in zip(states, gaps):
+        want = s.copy()
+        walls = ol.split_walls(*sc.walls_from_rows(sc.chokepoint_walls(g)), p.world_size,
+                               p.world_cells)
+        ol.run(want, p, 12, walls=walls)
+        assert_state(got.subset(slice(off, off + s.n)), want, skip_side=want.speed == 0)
+        off += s.n
+
+
+def test_graph_replay_equals_eager_single_group():
+    p = sc.boids_params(k=16, world=64.0)
+    s = sc.boids_sphere(5000, radius=20.0, seed=21)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g1 = group_of(s, p.k)
+    gs.set_graphs(g1, False)
+    gs.step(g1, bins, None, p, 12)
+    g2 = group_of(s, p.k)
+    gs.step(g2, bins, None, p, 4)
+    gs.step(g2, bins, None, p, 8)
+    assert_state(g2.download(), g1.download())
