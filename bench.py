@@ -1,18 +1,23 @@
-"""Throughput benchmark of the fused per-step agent update on GB300.
+"""Throughput benchmark of the per-step agent update on GB300.
 
-Default workload: the large plain flock - 1,048,576 3D boids uniform in a
-512^3 cube, k = 16, spatial bins of cell 4.0 (128^3 cells), FP32, symmetric
-world wrap.  A step is one whole update of every agent (wrap, bin rebuild,
-KNN, separation / cohesion / alignment, integration) through gs_step.
+Default workload (the headline): 256 independent 2D choke-point scenes
+advanced together, one CUDA-graph replay per step (gs_batch_step), against
+the same 256 scenes stepped one gs_step call per scene.  Gap half-widths are
+drawn from {7.5, 10, ..., 32.5}, agent counts uniformly from [1,000, 20,000];
+k = 16, walls k = 3, cell size and block shape from the autotuner, FP32.
+
+Other workloads: `large` (1,048,576 3D boids in a 512^3 cube, k = 16, cell
+4.0), `chokepoint` (one 10,000-agent scene), `boids` (4,096 boids, k = 7).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gs|reference]
-                  [--workload large|chokepoint|boids]
+                  [--workload batched|large|chokepoint|boids]
 
 Prints one JSON line (rank 0).  `value` is whole-job agent-steps/s with the
-state resident in HBM, timed with CUDA events on the group's stream; `e2e`
-is the same metric through gs_step_host with the state copied from and back
-to page-locked host memory every step.  Under torchrun every rank runs an
-independent replica on its own GPU (the flock is one world: replicas only).
+state resident in HBM, timed with CUDA events on the engine's stream; `e2e`
+is the same metric through the upload / step / download calls with the
+state copied from and back to page-locked host memory every step.  Under
+torchrun every rank runs an independent replica on its own GPU (scenes and
+flocks are not split across GPUs: replicas only).
 """
 from __future__ import annotations
 
@@ -38,7 +43,8 @@ WORKLOADS = {
     "chokepoint": "2D choke point: 10,000 agents, gap half-width 10, k=16, knw=3, cell 2.0",
     "boids": "plain 3D flock: 4,096 boids in a sphere of radius 50, k=7, cell 4.0",
     "batched": "256 independent 2D choke-point scenes (gap half-widths 7.5..32.5, 1,000-20,000 "
-               "agents each), k=16, knw=3, 256x256 world, autotuned cell size and block shape",
+               "agents each), k=16, knw=3, 512x512 world per scene, cell size (2.0 or larger), "
+               "block shape and KNN capacity from the autotuner",
 }
 
 
@@ -56,6 +62,14 @@ def make_workload(name):
     if name == "boids":
         return sc.boids_sphere(4096, seed=0), sc.boids_params(k=7), None
     raise SystemExit(f"unknown workload {name}")
+
+
+def make_batched(n_scenes=256, seed=0):
+    """(states, gaps, params, walls_rows(gap)) of the batched workload."""
+    from gpusteer_gb300 import scenario as sc
+
+    states, gaps = sc.batched_chokepoint(n_scenes, seed=seed)
+    return states, gaps, sc.chokepoint_params(), sc.chokepoint_walls
 
 
 def fused_bytes_per_agent(p) -> int:
@@ -195,12 +209,60 @@ def cpu_sample(state, p, walls_rows, seconds: float):
     return state.n * steps / el, steps, threads, state.n
 
 
+class BatchedOracle:
+    """The batched workload on the CPU oracle: every scene stepped in turn
+    (one scene at a time, all host threads per scene)."""
+
+    def __init__(self, states, gaps, p, walls_rows):
+        sys.path.insert(0, str(REPO / "tests"))
+        import oracle_lib as ol
+        from gpusteer_gb300 import scenario as sc
+
+        self.ol = ol
+        self.p = p
+        self.states = [s.copy() for s in states]
+        cache = {}
+        self.walls = []
+        for g in gaps:
+            if g not in cache:
+                cache[g] = ol.split_walls(*sc.walls_from_rows(walls_rows(g)), p.world_size,
+                                          p.world_cells)
+            self.walls.append(cache[g])
+        self.threads = ol.threads_available()
+        self.n = sum(s.n for s in states)
+
+    def step_scene(self, i):
+        self.ol.run(self.states[i], self.p, 1, walls=self.walls[i], threads=self.threads)
+        return self.states[i].n
+
+    def step(self):
+        for i in range(len(self.states)):
+            self.step_scene(i)
+
+
+def cpu_sample_batched(states, gaps, p, walls_rows, seconds: float):
+    """Oracle agent-steps/s over whole batched steps (scene after scene),
+    stopping after about `seconds`; returns (value, scene steps, threads)."""
+    bo = BatchedOracle(states, gaps, p, walls_rows)
+    bo.step_scene(0)  # warm-up
+    done, agents, t0 = 0, 0, time.perf_counter()
+    while True:
+        agents += bo.step_scene(done % len(states))
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return agents / el, done, bo.threads
+
+
 def run_reference(args, dist, rank):
     """--impl reference: the reference's CPU path.  The reference itself
     cannot run here (legacy CUDA texture references, Windows/cutil build),
     so this is the oracle's restatement of its kernels on the host cores."""
     if rank != 0:
         return
+    if args.workload == "batched":
+        return run_reference_batched(args)
     state, p, walls_rows = make_workload(args.workload)
     sys.path.insert(0, str(REPO / "tests"))
     import oracle_lib as ol
@@ -238,6 +300,37 @@ def run_reference(args, dist, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_batched(args):
+    states, gaps, p, walls_rows = make_batched()
+    bo = BatchedOracle(states, gaps, p, walls_rows)
+    t0 = time.perf_counter()
+    bo.step()  # one whole warm-up step of all scenes
+    per_step = time.perf_counter() - t0
+    # a bounded sample: at most about a minute of host time
+    steps = max(1, min(args.steps, int(60.0 / max(per_step, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        bo.step()
+    el = time.perf_counter() - t0
+    v = bo.n * steps / el
+    line = {
+        "impl": "reference", "metric": "agent-steps/s", "value": v, "unit": "agent-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS["batched"], "scenes": len(states), "agents": bo.n,
+                   "k": p.k},
+        "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": bo.threads,
+                         "kind": "port",
+                         "sample": f"{steps} whole steps of all {len(states)} scenes "
+                                   f"({bo.n} agents; CPU oracle restating the reference "
+                                   f"kernels, scene after scene, {bo.threads} threads)"},
+        "e2e": {"value": v, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---- GPU arm ------------------------------------------------------------------------
 
 def pinned_state(lib, n):
@@ -261,7 +354,195 @@ def pinned_state(lib, n):
     return AgentState(**arrays), ptrs
 
 
+def read_peaks():
+    pk_path = REPO / "MEASURED_PEAKS.json"
+    peaks = json.loads(pk_path.read_text()) if pk_path.exists() else {}
+    return peaks.get("hbm_gbs", 6800.0), ("measured" if "hbm_gbs" in peaks else "fallback")
+
+
+def read_traffic(workload):
+    tr_path = REPO / "profiles" / f"traffic_{workload}.json"
+    if tr_path.exists():
+        return json.loads(tr_path.read_text()).get("fused_bytes_per_launch")
+    return None
+
+
+def phase_times(lib, group, run, steps):
+    """Per-launch ms of the four step phases over `steps` profiled steps."""
+    from gpusteer_gb300._lib import check
+
+    check(lib.gs_group_set_profiling(group.handle, 1))
+    run(steps)
+    phase_ms = (C.c_float * 4)()
+    phase_n = (C.c_uint * 4)()
+    check(lib.gs_group_phase_times(group.handle, phase_ms, phase_n, 4))
+    check(lib.gs_group_set_profiling(group.handle, 0))
+    return {name: (phase_ms[i] / phase_n[i] if phase_n[i] else None)
+            for i, name in enumerate(["scan", "permute", "fused", "fused_rest"])}
+
+
+def run_gpu_batched(args, dist, rank, world, local_rank):
+    import torch
+
+    import gpusteer_gb300 as gs
+    from gpusteer_gb300 import autotune
+    from gpusteer_gb300._lib import check
+
+    lib = gs.load()
+    check(lib.gs_set_device(local_rank))
+    torch.cuda.set_device(local_rank)
+    states, gaps, base, walls_rows = make_batched()
+    n = sum(s.n for s in states)
+
+    # autotune cell size, block shape and KNN capacity on the scenes themselves
+    t0 = time.perf_counter()
+    tr = autotune.tune_batched(states, gaps, base, walls_rows)
+    tune_s = time.perf_counter() - t0
+    p = tr.params
+    b = autotune.batch_for(states, gaps, p, walls_rows)
+    gs.set_block(b.group, tr.block)
+    gs.set_knn_capacity(b.group, tr.capacity)
+    stream = torch.cuda.ExternalStream(b.group.stream)
+
+    # warm-up, then K timed steps (one graph replay each, state resident in HBM)
+    b.step(p, args.warmup)
+    b.group.synchronize()
+    barrier(dist)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            b.step(p, 1)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+    barrier(dist)
+    ms_max = allreduce_max(dist, ev0.elapsed_time(ev1))
+    value = n * args.steps * world / (ms_max / 1e3)
+    phases = phase_times(lib, b.group, lambda k: b.step(p, k), max(3, min(args.steps, 10)))
+    del b
+
+    # the same scenes, one gs_step call per scene per step (same grid, block,
+    # capacity; each scene's group has its own stream and CUDA graph)
+    per = []
+    for s, g in zip(states, gaps):
+        bins = gs.KNNBinData(p.world_cells, p.world_size, p.search_radius)
+        walls = gs.WallGroup(walls_rows(g), bins=bins, knw=p.knw)
+        grp = gs.AgentGroup(p.k, s.n)
+        grp.upload(s)
+        gs.set_block(grp, tr.block)
+        gs.set_knn_capacity(grp, tr.capacity)
+        per.append((grp, bins, walls))
+    for grp, bins, walls in per:
+        gs.step(grp, bins, walls, p, args.warmup)
+    for grp, _, _ in per:
+        grp.synchronize()
+    ps_steps = max(3, min(args.steps, 50))
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(ps_steps):
+        for grp, bins, walls in per:
+            gs.step(grp, bins, walls, p, 1)
+    for grp, _, _ in per:
+        grp.synchronize()
+    ps_s = allreduce_max(dist, time.perf_counter() - t0)
+    per_scene = n * ps_steps * world / ps_s
+
+    # identical results: a fresh batch stepped as often as the per-scene groups
+    total = args.warmup + ps_steps
+    b2 = autotune.batch_for(states, gaps, p, walls_rows)
+    gs.set_block(b2.group, tr.block)
+    gs.set_knn_capacity(b2.group, tr.capacity)
+    b2.step(p, total)
+    got = b2.download()
+    from gpusteer_gb300.state import AgentState
+
+    want = AgentState.concat([grp.download() for grp, _, _ in per])
+    identical = all(np.array_equal(getattr(got, k), getattr(want, k)) for k in got.names())
+    del per
+
+    # end to end: page-locked host state uploaded, stepped once and downloaded
+    # every step through the batch API
+    hio, keep = pinned_state(lib, n)
+    init = AgentState.concat(states)
+    for k in hio.names():
+        getattr(hio, k)[...] = getattr(init, k)
+    e2e_steps = max(3, min(args.steps, 20))
+    b2.upload(hio)
+    b2.step(p, 1)
+    b2.download(hio)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        b2.upload(hio)
+        b2.step(p, 1)
+        b2.download(hio)
+    e2e_s = allreduce_max(dist, time.perf_counter() - t0)
+    e2e = n * e2e_steps * world / e2e_s
+    bytes_state = n * (16 * 3 + 12 * 2 + 4 * 5 + 4)
+    for ptr in keep:
+        lib.gs_host_free(ptr)
+    del b2
+
+    if rank != 0:
+        return
+    peak, peak_src = read_peaks()
+    fused_ms = phases["fused"] + (phases["fused_rest"] or 0.0)
+    fbytes = fused_bytes_per_agent(p) * n
+    achieved = fbytes / (fused_ms / 1e3) / 1e9
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        v, done, threads = cpu_sample_batched(states, gaps, p, walls_rows, args.cpu_seconds)
+        cpu = {"value": v, "unit": "agent-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{done} scene-steps of the batched workload (scenes in order), "
+                         f"CPU oracle, {threads} threads"}
+    cells = int(np.prod(p.world_cells))
+    line = {
+        "metric": "agent-steps/s",
+        "value": value,
+        "unit": "agent-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS["batched"], "scenes": len(states),
+                   "agents_per_gpu": n, "k": p.k, "knw": p.knw,
+                   "cell": p.world_size[0] / p.world_cells[0], "cells_per_scene": cells,
+                   "block": tr.block, "knn_capacity": tr.capacity or "auto",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (about 270 MB of bucketed state per step)"},
+        "per_scene": {"value": per_scene, "unit": "agent-steps/s", "steps": ps_steps,
+                      "ms_per_step": 1e3 * ps_s / ps_steps,
+                      "timing": "host clock, every scene's stream synchronised on both sides",
+                      "batched_over_per_scene": value / per_scene},
+        "identical_to_per_scene": {"equal": bool(identical), "steps": total,
+                                   "compared": "every state array of every agent"},
+        "autotune": {"seconds": tune_s, "trials": tr.trials},
+        "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
+                "d2h_bytes_per_step": bytes_state},
+        "gpu_launches": 7 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": read_traffic("batched"),
+                     "kernel": "k_fused_walls+k_fused_rest",
+                     "algorithmic_bytes_per_launch": fbytes, "peak_source": peak_src},
+        "phases_ms": phases,
+        "step_model_gbs": step_model_bytes(n, p.k, cells * len(states)) /
+                          (ms_max / args.steps / 1e3) / 1e9,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, dist, rank, world, local_rank):
+    if args.workload == "batched":
+        return run_gpu_batched(args, dist, rank, world, local_rank)
     import torch
 
     import gpusteer_gb300 as gs
@@ -279,7 +560,7 @@ def run_gpu(args, dist, rank, world, local_rank):
     group.upload(state)
     stream = torch.cuda.ExternalStream(group.stream)
     has_walls = walls is not None
-    launches_per_step = 3 + 1 + (2 if has_walls else 1)
+    launches_per_step = 3 + 1 + (3 if has_walls else 2)  # scan, permute, fused (+ walls), redo
 
     # warm-up, then K timed steps (state resident in HBM)
     gs.step(group, bins, walls, p, args.warmup)
@@ -300,27 +581,13 @@ def run_gpu(args, dist, rank, world, local_rank):
     value = n * args.steps * world / (ms_max / 1e3)
 
     # dominant kernel: phase timing with CUDA events on the group's stream
-    check(lib.gs_group_set_profiling(group.handle, 1))
-    prof_steps = max(3, min(args.steps, 20))
-    gs.step(group, bins, walls, p, prof_steps)
-    phase_ms = (C.c_float * 4)()
-    phase_n = (C.c_uint * 4)()
-    check(lib.gs_group_phase_times(group.handle, phase_ms, phase_n, 4))
-    check(lib.gs_group_set_profiling(group.handle, 0))
-    phases = {name: (phase_ms[i] / phase_n[i] if phase_n[i] else None)
-              for i, name in enumerate(["scan", "permute", "fused", "fused_rest"])}
+    phases = phase_times(lib, group, lambda k: gs.step(group, bins, walls, p, k),
+                         max(3, min(args.steps, 20)))
     fused_ms = phases["fused"] + (phases["fused_rest"] or 0.0)
     fbytes = fused_bytes_per_agent(p) * n
-    peaks = {}
-    pk_path = REPO / "MEASURED_PEAKS.json"
-    if pk_path.exists():
-        peaks = json.loads(pk_path.read_text())
-    peak = peaks.get("hbm_gbs", 6800.0)
+    peak, peak_src = read_peaks()
     achieved = fbytes / (fused_ms / 1e3) / 1e9
-    traffic = None
-    tr_path = REPO / "profiles" / f"traffic_{args.workload}.json"
-    if tr_path.exists():
-        traffic = json.loads(tr_path.read_text()).get("fused_bytes_per_launch")
+    traffic = read_traffic(args.workload)
 
     # end to end: host state in page-locked memory, copied in and out every step
     hin, keep_in = pinned_state(lib, n)
@@ -370,8 +637,7 @@ def run_gpu(args, dist, rank, world, local_rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_fused" + ("_walls+k_fused_rest" if has_walls else ""),
-                     "algorithmic_bytes_per_launch": fbytes,
-                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+                     "algorithmic_bytes_per_launch": fbytes, "peak_source": peak_src},
         "phases_ms": phases,
         "step_model_gbs": step_model_bytes(n, p.k, cells) / (ms_max / args.steps / 1e3) / 1e9,
         "clocks": clocks.summary(),
@@ -383,13 +649,18 @@ def run_gpu(args, dist, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's own step count)")
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gs", choices=["gs", "reference"])
-    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        from gpusteer_gb300 import scenario as sc
+
+        args.steps = sc.default_steps(args.workload)
     if args.warmup < 3:
         args.warmup = 3
     dist, rank, world, local_rank = dist_setup()

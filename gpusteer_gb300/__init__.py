@@ -7,7 +7,7 @@ GroupSteerLibrary free functions), seeded scenarios and the build step.
 """
 from ._lib import GpuSteerError, load  # noqa: F401
 from .groups import (  # noqa: F401
-    AgentGroup, Batch, KNNBinData, KNNData, WallGroup, set_block, set_graphs, antiPenetrationAgents, findKNearestNeighbors,
+    AgentGroup, Batch, KNNBinData, KNNData, WallGroup, set_block, set_graphs, set_knn_capacity, antiPenetrationAgents, findKNearestNeighbors,
     findKNearestNeighborsBruteForce, step, step_host, steerForAlignment, steerForCohesion,
     steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, updateGroup,
     updateKNNDatabase, wrapWorld)

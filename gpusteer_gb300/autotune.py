@@ -1,32 +1,34 @@
-"""Autotuner for the batched choke-point engine.
+"""Autotuner for the batched engine.
 
-Picks the grid (cells per axis of the shared world) and the threads per block
-of the fused launches by timing a few batched steps of each candidate with
-CUDA events (per-phase profiling of the batch's group).  The block size never
-changes results; the grid does (it sets the reference's 3 x 3 neighbour-cell
-box), so whatever is picked is applied identically to the per-scene runs it
-is compared with.
+Picks the cell size of the shared per-scene grid, the threads per block of
+the fused launches and the candidate capacity of the fused KNN scan by
+timing a few batched steps of each candidate on the actual scenes.  Block
+size and capacity never change results.  The cell size does (it sets the
+reference's 3 x 3 neighbour-cell box), so the tuner only tries cells at
+least as large as the scenario's own, and whatever it picks is applied
+identically to any per-scene run that is compared with the batch.
 """
 from __future__ import annotations
 
-import ctypes as C
-from dataclasses import dataclass
+import time
+from dataclasses import dataclass, field
 
-from . import _lib
-from .groups import Batch, set_block
+from .groups import Batch, set_block, set_knn_capacity
 from .scenario import StepParams
 from .state import AgentState
 
 
 @dataclass
 class TuneResult:
-    cells: int
+    params: StepParams   # the scenario's parameters with the chosen grid
     block: int
+    capacity: int        # 0: chosen by the library from the crowd's density
     ms_per_step: float
-    trials: list
+    trials: list = field(default_factory=list)
 
 
 def batch_for(states, gaps, p: StepParams, walls_rows) -> Batch:
+    """A batch of the given scenes on p's grid, state uploaded."""
     b = Batch([s.n for s in states], p.k, p.world_cells, p.world_size, p.search_radius)
     for i, g in enumerate(gaps):
         b.set_walls(i, walls_rows(g))
@@ -34,35 +36,47 @@ def batch_for(states, gaps, p: StepParams, walls_rows) -> Batch:
     return b
 
 
-def step_ms(batch: Batch, p: StepParams, steps: int) -> float:
-    """Average ms per step over `steps` steps (sum of the phase timings)."""
-    _lib.call("gs_group_set_profiling", batch.group.handle, 1)
+def time_steps(batch: Batch, p: StepParams, steps: int) -> float:
+    """Host wall-clock ms per step over `steps` steps, stream synchronised on
+    both sides (graph replay after the first step of a configuration)."""
+    batch.group.synchronize()
+    t0 = time.perf_counter()
     batch.step(p, steps)
-    ms = (C.c_float * 4)()
-    n = (C.c_uint * 4)()
-    _lib.call("gs_group_phase_times", batch.group.handle, ms, n, 4)
-    _lib.call("gs_group_set_profiling", batch.group.handle, 0)
-    return sum(ms) / steps
+    batch.group.synchronize()
+    return (time.perf_counter() - t0) * 1e3 / steps
 
 
-def tune_batched(states, gaps, base: StepParams, walls_rows, cell_sizes=(2.0, 2.5, 3.0, 4.0),
-                 blocks=(128, 256), steps: int = 3, warmup: int = 2) -> TuneResult:
-    """Times every (cell size, block) pair on the batch; cell sizes are
-    rounded to a whole number of cells across the (square, 2D) world."""
-    world = base.world_size[0]
-    trials = []
-    best = None
-    for cs in cell_sizes:
-        cells = max(1, int(round(world / cs)))
-        p = base.replace(world_cells=(cells, 1, cells))
+def grid_for(base: StepParams, cell: float) -> StepParams:
+    """base with square 2D cells of side `cell` (rounded to whole cells)."""
+    wx, _, wz = base.world_size
+    cx = max(1, int(round(wx / cell)))
+    cz = max(1, int(round(wz / cell)))
+    return base.replace(world_cells=(cx, base.world_cells[1], cz))
+
+
+def tune_batched(states, gaps, base: StepParams, walls_rows, cell_scales=(1.0, 1.25, 1.5),
+                 blocks=(128, 256), capacities=(0, 256), steps: int = 4,
+                 warmup: int = 2) -> TuneResult:
+    """Times every (cell size, block, capacity) on the batch; cell sizes are
+    the scenario's cell times `cell_scales` (all >= 1)."""
+    cell0 = base.world_size[0] / base.world_cells[0]
+    trials, best = [], None
+    for scale in cell_scales:
+        if scale < 1.0:
+            raise ValueError("cells smaller than the scenario's change its neighbourhoods")
+        p = grid_for(base, cell0 * scale)
         b = batch_for(states, gaps, p, walls_rows)
         b.step(p, warmup)
         for blk in blocks:
-            set_block(b.group, blk)
-            b.step(p, 1)
-            ms = step_ms(b, p, steps)
-            trials.append({"cells": cells, "cell_size": world / cells, "block": blk, "ms": ms})
-            if best is None or ms < best[2]:
-                best = (cells, blk, ms)
+            for cap in capacities:
+                set_block(b.group, blk)
+                set_knn_capacity(b.group, cap)
+                b.step(p, 1)  # new configuration: eager step and graph capture
+                ms = time_steps(b, p, steps)
+                trials.append({"cell": cell0 * scale, "cells": list(p.world_cells), "block": blk,
+                               "capacity": cap, "ms": ms})
+                if best is None or ms < best.ms_per_step:
+                    best = TuneResult(params=p, block=blk, capacity=cap, ms_per_step=ms)
         del b
-    return TuneResult(cells=best[0], block=best[1], ms_per_step=best[2], trials=trials)
+    best.trials = trials
+    return best

@@ -30,6 +30,11 @@ struct FlockParams {
     unsigned mask;
 };
 
+// Packed (min, max, cos, weight, mask bits) as the fused step's parameters hold them.
+__device__ __forceinline__ FlockParams flock_params(const float v[5]) {
+    return FlockParams{v[0], v[1], v[2], v[3], __float_as_uint(v[4])};
+}
+
 GS_HD void flock_init(FlockAcc& a) {
     a.sum = v3(0.f, 0.f, 0.f);
     a.n = 0;

@@ -48,6 +48,7 @@ static void release_fused(gs_group g) {
     dfree(g->d_err);
     dfree(g->retry);
     dfree(g->retry_count);
+    dfree(g->d_stat);
     db_release(g->fdb);
     g->fused_k_alloc = 0;
 }
@@ -225,15 +226,28 @@ static gs_status walls_db(gs_walls w, const Grid& grid, unsigned C, cudaStream_t
     return GS_OK;
 }
 
-// Candidate capacity of the fast KNN scan: 32 when a uniform crowd of this
-// density puts the mean candidate count of the (2r+1)^d box at least four
-// standard deviations below 32, else 64.  Agents beyond it take the exact
-// redo path, so this only affects speed.
-static unsigned enum_capacity(unsigned n, unsigned C, const Grid& g, unsigned r) {
+// Candidate capacity of the fused KNN scan from the crowd's density.  The
+// crowd is taken as a Poisson scatter of lambda agents per cell over some
+// region of cells: then agents / occupied cells = lambda / (1 - exp(-lambda)),
+// solved for lambda by bisection, and an agent sees m = lambda * (2r+1)^d
+// candidates on average.  32 (collecting scan) when m is at least four
+// standard deviations below 32, else the streaming scan with 128 or 256
+// candidates.  Agents beyond the capacity take the exact redo path, so this
+// only affects speed.
+static unsigned knn_capacity(unsigned n, unsigned occupied, const Grid& g, unsigned r) {
     double box = 1.0;
     for (int a = 0; a < 3; ++a) box *= double(std::min<unsigned>(2 * r + 1, g.wc[a]));
-    const double mean = double(n) / double(C) * box;
-    return (mean + 4.0 * std::sqrt(mean) + 1.0 <= 32.0) ? 32u : 64u;
+    const double ratio = occupied ? double(n) / double(occupied) : 1.0;
+    double lo = 0.0, hi = std::max(ratio, 1e-9);
+    for (int it = 0; it < 60; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        const double f = mid > 1e-12 ? mid / (1.0 - std::exp(-mid)) : 1.0;
+        (f < ratio ? lo : hi) = mid;
+    }
+    const double m = 0.5 * (lo + hi) * box;
+    const double top = m + 4.0 * std::sqrt(m) + 1.0;
+    if (top <= 32.0) return 32u;
+    return top <= 128.0 ? 128u : 256u;
 }
 
 static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev& d) {
@@ -554,6 +568,7 @@ gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
     if (e != cudaSuccess) return cuda_fail(e, "upload");
     g->n = n;
     g->db.valid = false;
+    g->auto_cap_valid = false;
     touched(g);
     return GS_OK;
 }
@@ -926,6 +941,7 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         GS_TRY(dalloc(&g->d_err, 1));
         GS_TRY(dalloc(&g->retry, n));
         GS_TRY(dalloc(&g->retry_count, 1));
+        GS_TRY(dalloc(&g->d_stat, 1));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
         GS_CUDA(cudaMemset(g->retry_count, 0, sizeof(unsigned)));
         GS_CUDA(cudaDeviceSynchronize());
@@ -1006,6 +1022,21 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
     g->fdb.grid = grid;
     g->fdb.valid = true;
     g->pending_wrap = d.wrap_mode;
+    if (g->knn_cap) {
+        d.enum_cap = g->knn_cap;
+    } else {
+        if (!g->auto_cap_valid || g->auto_cap_r != d.r ||
+            std::memcmp(&g->auto_cap_grid, &grid, sizeof(Grid)) != 0) {
+            // one synchronising read per upload or grid change
+            unsigned occupied = 0;
+            GS_TRY(count_occupied(g->fdb.count, C, g->d_stat, &occupied, st));
+            g->auto_cap = knn_capacity(g->n, occupied, grid, d.r);
+            g->auto_cap_grid = grid;
+            g->auto_cap_r = d.r;
+            g->auto_cap_valid = true;
+        }
+        d.enum_cap = g->auto_cap;
+    }
 
     FusedLaunch L{};
     L.A = g->A;
@@ -1097,7 +1128,6 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
     sc.n_agents = g->n;
     sc.n_walls = has_walls ? walls->n : 0;
     GS_TRY(put_scenes(g, std::vector<Scene>{sc}));
-    d.enum_cap = enum_capacity(g->n, C, grid, d.r);
     d.block = g->block;
     WallsDev w;
     if (has_walls) {
@@ -1122,6 +1152,14 @@ gs_status gs_group_set_graphs(gs_group g, int enable) {
     if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
     g->use_graph = enable != 0;
     if (!g->use_graph) drop_graph(g);
+    return GS_OK;
+}
+
+gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    if (capacity != 0 && capacity != 32 && capacity != 64 && capacity != 128 && capacity != 256)
+        return fail(GS_ERR_INVALID_ARG, "KNN capacity must be 0 (auto), 32, 64, 128 or 256");
+    g->knn_cap = capacity;
     return GS_OK;
 }
 
@@ -1308,11 +1346,6 @@ gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
     if (!has_walls)
         for (Scene& sc : scenes) sc.n_walls = 0;
     GS_TRY(put_scenes(g, scenes));
-    // the fast KNN's candidate capacity from the densest scene
-    unsigned cap = 32;
-    for (const Scene& sc : scenes)
-        cap = std::max(cap, enum_capacity(sc.n_agents, b->cells, grid, d.r));
-    d.enum_cap = cap;
     d.block = g->block;
     WallsDev w;
     if (has_walls) {

@@ -158,6 +158,13 @@ struct gs_group_s {
     unsigned* d_err;       // device error flags (see FusedLaunch::err)
     unsigned* retry;       // [capacity] exact-redo list and its counter
     unsigned* retry_count;
+    unsigned* d_stat;      // one word of scratch for device-side statistics
+    // candidate capacity of the fused KNN scan: knn_cap fixed by the caller
+    // (gs_group_set_knn_capacity), else auto_cap, measured from the crowd's
+    // density when the state is uploaded or the grid changes
+    unsigned knn_cap, auto_cap, auto_cap_r;
+    bool auto_cap_valid;
+    gs::Grid auto_cap_grid;
     bool fused_current;    // true: A holds the state, reference arrays stale
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with

@@ -258,6 +258,77 @@ __device__ __forceinline__ bool knn_neighbours_fast(int k, V3 p, unsigned self_i
     return true;
 }
 
+// Streaming fast path for crowded boxes: the same 32-bit keys, but every
+// candidate goes straight into the register list (no per-candidate shared
+// memory), so the enumeration capacity is 2^EBITS whatever the block size.
+// e numbers every candidate of the box in row order, the agent itself
+// included, so a listed key's e is decoded back to its slot from the nine
+// row starts and the running row offsets alone.  Boxes of more than 3 x 3
+// rows (search radius above 1) are left to the exact path.  Writes the k
+// slots to out[r * stride]; returns false when the exact path must redo the
+// agent, on the same conditions as the collecting scan.
+template <int KMAX, unsigned EBITS>
+__device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self_id,
+                                                      const Grid& g, const Box& b,
+                                                      unsigned cell_offset,
+                                                      const unsigned* __restrict__ cell_start,
+                                                      const float4* __restrict__ pos_id,
+                                                      unsigned* out, unsigned stride) {
+    constexpr unsigned ENUM = 1u << EBITS, mask = ENUM - 1;
+    if (b.y1 - b.y0 > 2 || b.z1 - b.z0 > 2) return false;
+    const unsigned span = b.x1 - b.x0 + 1;
+    unsigned rs[9], pre[10];
+    pre[0] = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const unsigned cy = b.y0 + unsigned(i / 3), cz = b.z0 + unsigned(i % 3);
+        const bool ok = cy <= b.y1 && cz <= b.z1;
+        const unsigned c0 = cell_offset + cell_label(g, b.x0, ok ? cy : b.y0, ok ? cz : b.z0);
+        const unsigned s0 = ok ? __ldg(cell_start + c0) : 0u;
+        const unsigned s1 = ok ? __ldg(cell_start + c0 + span) : 0u;
+        rs[i] = s0;
+        pre[i + 1] = pre[i] + (s1 - s0);
+    }
+    if (pre[9] > ENUM) return false;
+    KList32<KMAX> L;
+#pragma unroll
+    for (int i = 0; i < KMAX; ++i) L.key[i] = i < KMAX - k ? 0u : KEY32_EMPTY;
+    unsigned out_min = KEY32_EMPTY;  // smallest key not (or no longer) in the list
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        const unsigned n_row = pre[i + 1] - pre[i];
+        for (unsigned t = 0; t < n_row; ++t) {
+            const float4 q = __ldg(pos_id + rs[i] + t);
+            const unsigned bits = __float_as_uint(distance(p, v3(q)));
+            if (__float_as_uint(q.w) != self_id && bits < 0x7f7fffffu) {
+                const unsigned c = (bits & ~mask) | (pre[i] + t);
+                out_min = min(out_min, c < L.key[KMAX - 1] ? L.insert(c) : c);
+            }
+        }
+    }
+    const unsigned last = L.key[KMAX - 1];
+    if (last != KEY32_EMPTY && (out_min & ~mask) == (last & ~mask)) return false;
+#pragma unroll
+    for (int i = KMAX - 1; i > 0; --i)
+        if (i > KMAX - k && L.key[i] != KEY32_EMPTY && (L.key[i] & ~mask) == (L.key[i - 1] & ~mask))
+            return false;
+#pragma unroll
+    for (int i = 0; i < KMAX; ++i) {
+        if (i < KMAX - k) continue;
+        const unsigned key = L.key[i];
+        unsigned slot = UINT_MAX;
+        if (key != KEY32_EMPTY) {
+            const unsigned e = key & mask;
+            slot = rs[0] + e;
+#pragma unroll
+            for (int j = 1; j < 9; ++j)
+                if (e >= pre[j]) slot = rs[j] + (e - pre[j]);
+        }
+        out[(i - (KMAX - k)) * stride] = slot;
+    }
+    return true;
+}
+
 // Exact path: the ordered slots go to col[r * stride].
 template <int KMAX>
 __device__ __forceinline__ void knn_neighbours_exact(int k, V3 p, unsigned self_id, const Grid& g,

@@ -71,7 +71,7 @@ struct StepDev {
     unsigned n_order;
     float dt;
     unsigned need;      // NEED_* bits
-    unsigned enum_cap;  // candidate capacity of the fast KNN scan (32 or 64)
+    unsigned enum_cap;  // candidate capacity of the fast KNN scan (32, 64: collecting; 128, 256: streaming)
     unsigned block;     // threads per block of the fused launches (0: 256)
 };
 constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
@@ -93,6 +93,11 @@ struct FusedLaunch {
     unsigned* err;  // device flag: bit 0 = a bucketed slot fell outside [0, n)
     unsigned* retry;        // [n] slots the fast KNN handed to the exact redo
     unsigned* retry_count;  // zeroed by the permute launch of each step
+    // optional record of the step's inputs by agent index (rollouts for the
+    // adjoint; walls-free steps only): null when not recording
+    float4* rec_pos;    // [n] position | speed before the step (after the wrap)
+    float4* rec_dir;    // [n] heading | 0
+    unsigned* rec_knn;  // [n * k] neighbour indices, row-major, UINT_MAX after the last
 };
 
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
@@ -110,5 +115,25 @@ gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
                      PhaseHook* hook = nullptr);
 gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView g,
                              cudaStream_t st);
+// ---- adjoint of the fused flocking step -------------------------------------------
+// Inputs recorded by a forward step (FusedLaunch::rec_*), the agents' constant
+// limits, and the adjoints of the step's outputs; accumulates the adjoints of
+// its inputs and the steering weights.
+struct AdjointLaunch {
+    const float4* pos;   // [n] recorded position | speed
+    const float4* dir;   // [n] recorded heading
+    const unsigned* knn; // [n * k] recorded neighbour indices
+    const float *max_speed, *max_force, *mass;
+    float4 *lp_in, *lv_in;    // d loss / d (position, velocity) after the step; zeroed
+    float4 *lp_out, *lv_out;  // d loss / d (position, velocity) before the step; += (atomic)
+    float* wpart;             // [blocks * 4] per-block sums: separation, alignment, cohesion
+    unsigned n, k;
+};
+unsigned adjoint_blocks(unsigned n);
+gs_status launch_flock_adjoint(const AdjointLaunch& A, const StepDev& p, cudaStream_t st);
+
+// Number of non-zero entries of count[0..C), read back to the host (syncs st).
+gs_status count_occupied(const unsigned* count, unsigned C, unsigned* d_tmp, unsigned* h_out,
+                         cudaStream_t st);
 
 }  // namespace gs

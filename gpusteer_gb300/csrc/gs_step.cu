@@ -23,6 +23,7 @@
 // (plugins/BoidsGroup.cpp:606-637, plugins/ChokePointNew.cpp:586-630).
 #include "gs_behaviours.cuh"
 #include "gs_knn.cuh"
+#include <algorithm>
 #include <map>
 #include <mutex>
 
@@ -127,10 +128,6 @@ gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStr
                                                   wrap_mode, dirty ? 1 : 0, L.err, L.retry_count);
     GS_LAUNCHED("fused_permute");
     return GS_OK;
-}
-
-__device__ __forceinline__ FlockParams flock_params(const float v[5]) {
-    return FlockParams{v[0], v[1], v[2], v[3], __float_as_uint(v[4])};
 }
 
 // Neighbour accumulators of every behaviour that reads the KNN list.
@@ -259,9 +256,16 @@ __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDe
                                    L.B.f[0], col, bd);
         return 0;
     }
-    if (knn_neighbours_fast<KMAX, ENUM>(int(p.k), pos, id, sc.grid, box, sc.cell_offset, L.start,
-                                        L.B.f[0], col, col + ENUM * bd, bd))
+    if constexpr (ENUM > 64) {
+        // crowded boxes: streaming scan, result at col[r * bd]
+        constexpr unsigned EBITS = ENUM >= 256 ? 8u : 7u;
+        if (knn_neighbours_stream<KMAX, EBITS>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
+                                               L.start, L.B.f[0], col, bd))
+            return 0;
+    } else if (knn_neighbours_fast<KMAX, ENUM>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
+                                               L.start, L.B.f[0], col, col + ENUM * bd, bd)) {
         return ENUM;
+    }
     L.retry[atomicAdd(L.retry_count, 1u)] = s;
     return UINT_MAX;
 }
@@ -309,13 +313,21 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
         init_accs(a, p);
         const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
         const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
-        for (unsigned r = 0; r < p.k; ++r) {
+        unsigned* rec_knn = L.rec_knn ? L.rec_knn + size_t(id) * p.k : nullptr;
+        unsigned r = 0;
+        for (; r < p.k; ++r) {
             const unsigned bs = col[(base + r) * bd];
             if (bs == UINT_MAX) break;
             const float4 b0 = L.B.f[0][bs];
             const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float br = need_rad ? L.B.f[2][bs].w : 0.f;
+            if (rec_knn) rec_knn[r] = u(b0.w);
             accumulate(a, p, fs, fa, fc, me, u(b0.w), -1.f, v3(b0), v3(b1), b1.w, br);
+        }
+        if (rec_knn) {
+            for (; r < p.k; ++r) rec_knn[r] = UINT_MAX;
+            L.rec_pos[id] = make_float4(me.pos.x, me.pos.y, me.pos.z, me.speed);
+            L.rec_dir[id] = make_float4(me.dir.x, me.dir.y, me.dir.z, 0.f);
         }
         finish_all(a, p, 0, fs, fa, fc, me, applied, steer);
         integrate(me, steer, p.dt);
@@ -439,22 +451,27 @@ static gs_status allow_smem(K kernel, size_t bytes) {
     return GS_OK;
 }
 
-// Redo launches over the retry list: a fixed grid that strides over however
-// many agents the fast launch appended (read on the device).
-constexpr unsigned kRetryBlocks = 152;
+// Redo launches over the retry list: a grid of up to four blocks per SM that
+// strides over however many agents the fast launch appended (read on the
+// device); agents that all overflowed still spread over the whole GPU.
+constexpr unsigned kRetryBlocksMax = 4 * 152;
 
 template <int KMAX, unsigned ENUM>
 static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
                                 PhaseHook* hook) {
     const unsigned bs = p.block ? p.block : kBlock;
     const unsigned nb = blocks_for(L.n, bs);
-    const size_t smem = size_t(2 * ENUM) * bs * sizeof(unsigned);
+    const unsigned nb_retry = std::min(blocks_for(L.n, kBlock), kRetryBlocksMax);
+    // collecting scan: slot and key tables of ENUM words per thread;
+    // streaming scan: the k result slots only
+    const size_t smem = ENUM > 64 ? size_t(KMAX > 8 ? KMAX : 8) * bs * sizeof(unsigned)
+                                  : size_t(2 * ENUM) * bs * sizeof(unsigned);
     const size_t smem_x = size_t(KMAX > 8 ? KMAX : 8) * kBlock * sizeof(unsigned);
     if (p.need & NEED_WALLS) {
         GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
         k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
-        k_fused_walls<KMAX, 8, ENUM, true><<<kRetryBlocks, kBlock, smem_x, st>>>(L, p);
+        k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
         k_fused_rest<KMAX><<<nb, bs, 0, st>>>(L, p);
@@ -463,7 +480,7 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
         GS_TRY(allow_smem(k_fused<KMAX, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
         k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
-        k_fused<KMAX, ENUM, true><<<kRetryBlocks, kBlock, smem_x, st>>>(L, p);
+        k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
     }
     GS_LAUNCHED("fused_step");
@@ -474,7 +491,9 @@ template <int KMAX>
 static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
                               PhaseHook* hook) {
     if (p.enum_cap <= 32) return launch_fused_k<KMAX, 32>(L, p, st, hook);
-    return launch_fused_k<KMAX, 64>(L, p, st, hook);
+    if (p.enum_cap <= 64) return launch_fused_k<KMAX, 64>(L, p, st, hook);
+    if (p.enum_cap <= 128) return launch_fused_k<KMAX, 128>(L, p, st, hook);
+    return launch_fused_k<KMAX, 256>(L, p, st, hook);
 }
 
 gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st, PhaseHook* hook) {
@@ -512,6 +531,33 @@ gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView
     if (n == 0) return GS_OK;
     k_to_reference<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, g);
     GS_LAUNCHED("fused_to_reference");
+    return GS_OK;
+}
+
+}  // namespace gs
+
+namespace gs {
+
+__global__ void k_count_occupied(const unsigned* __restrict__ count, unsigned C,
+                                 unsigned* __restrict__ out) {
+    unsigned local = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x)
+        local += count[i] != 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
+}
+
+gs_status count_occupied(const unsigned* count, unsigned C, unsigned* d_tmp, unsigned* h_out,
+                         cudaStream_t st) {
+    *h_out = 0;
+    if (C == 0) return GS_OK;
+    GS_CUDA(cudaMemsetAsync(d_tmp, 0, sizeof(unsigned), st));
+    const unsigned nb = std::min(blocks_for(C, kBlock), 8u * 152u);
+    k_count_occupied<<<nb, kBlock, 0, st>>>(count, C, d_tmp);
+    GS_LAUNCHED("count_occupied");
+    GS_CUDA(cudaMemcpyAsync(h_out, d_tmp, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
     return GS_OK;
 }
 

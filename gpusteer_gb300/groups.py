@@ -257,6 +257,11 @@ def set_block(group, threads: int) -> None:
     call("gs_group_set_block", group.handle, int(threads))
 
 
+def set_knn_capacity(group, capacity: int) -> None:
+    """0 = from the crowd's density; 32/64 collecting scan; 128/256 streaming."""
+    call("gs_group_set_knn_capacity", group.handle, int(capacity))
+
+
 class Batch:
     """Many independent scenes advanced together (gs_batch_*): agents are
     concatenated in scene order, each scene keeps scene-local indices, cells
@@ -296,8 +301,12 @@ class Batch:
         call("gs_batch_upload", self._h, C.byref(a))
         self.group.synchronize()
 
-    def download(self) -> AgentState:
-        out = AgentState.zeros(self.n)
+    def download(self, out: AgentState | None = None) -> AgentState:
+        """All scenes' agents in scene order (into `out` when given)."""
+        if out is None:
+            out = AgentState.zeros(self.n)
+        elif out.n != self.n:
+            raise ValueError("state size differs from the batch")
         a = host_arrays(out)
         call("gs_batch_download", self._h, C.byref(a))
         return out

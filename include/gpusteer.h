@@ -249,6 +249,12 @@ gs_status gs_group_set_graphs(gs_group g, int enable);
 /* Threads per block of the fused-step launches: 64, 128 or 256 (default).
  * Results do not depend on it; the autotuner picks it. */
 gs_status gs_group_set_block(gs_group g, unsigned threads);
+/* Candidate capacity of the fused step's KNN scan: 32 or 64 (collecting
+ * scan, for sparse crowds), 128 or 256 (streaming scan, for crowded cells),
+ * or 0 (default: chosen from the crowd's density, measured once after each
+ * upload).  Results do not depend on it: agents with more candidates are
+ * redone by the exact scan.  Not part of the reference. */
+gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity);
 
 /* ---- batched scenes -------------------------------------------------------------
  * Many independent worlds (e.g. one ChokePoint plugin instance each) advanced

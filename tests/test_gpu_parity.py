@@ -305,10 +305,12 @@ def test_boids_config_fused_matches_oracle(masks):
     assert_state(g.download(), want, skip_side=want.speed == 0)
 
 
-def test_fused_step_on_a_lattice_with_exact_ties():
+@pytest.mark.parametrize("capacity", [32, 64, 128, 256])
+def test_fused_step_on_a_lattice_with_exact_ties(capacity):
     """Agents on an integer lattice, some duplicated: many neighbours at
     exactly equal distances, so the KNN order depends on the index
-    tie-break (the fused kernels' exact fallback path)."""
+    tie-break (the fused kernels' exact fallback path), for the collecting
+    (32, 64) and streaming (128, 256) scans."""
     g3 = np.stack(np.meshgrid(np.arange(12), np.arange(12), np.arange(12), indexing="ij"), -1)
     pts = g3.reshape(-1, 3).astype(np.float32) - 6.0
     pts = np.concatenate([pts, pts[::5]])
@@ -318,10 +320,40 @@ def test_fused_step_on_a_lattice_with_exact_ties():
         p = sc.boids_params(k=k, world=64.0, cell=2.0)
         bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
         g = group_of(s, p.k)
+        gs.set_knn_capacity(g, capacity)
         gs.step(g, bins, None, p, 3)
         want = s.copy()
         ol.run(want, p, 3)
         assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+@pytest.mark.parametrize("capacity", [0, 32, 64, 128, 256])
+def test_knn_capacity_does_not_change_results(capacity):
+    """Dense 2D crowds (4 and 8 agents per cell, 36 and 72 candidates on
+    average) overflow the small capacities into the exact redo; every
+    capacity gives the oracle's result bit for bit."""
+    p = sc.chokepoint_params()
+    bins, walls = choke_walls(p)
+    for n in (10000, 20000):
+        s = sc.chokepoint_agents(n, seed=5)
+        g = group_of(s, p.k)
+        gs.set_knn_capacity(g, capacity)
+        gs.step(g, bins, walls, p, 20)
+        want = s.copy()
+        ol.run(want, p, 20, walls=walls.download())
+        assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+def test_streaming_scan_in_3d_matches_oracle():
+    s = sc.boids_sphere(20000, radius=25.0, seed=8)
+    p = sc.boids_params(k=16, world=64.0, cell=2.0)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g = group_of(s, p.k)
+    gs.set_knn_capacity(g, 128)
+    gs.step(g, bins, None, p, 5)
+    want = s.copy()
+    ol.run(want, p, 5)
+    assert_state(g.download(), want, skip_side=want.speed == 0)
 
 
 def test_boids_fused_equals_dropin_sequence():
