@@ -90,7 +90,7 @@ struct Segment {
 // Raw copies of a launch's parameter blocks (compared byte-wise to decide
 // whether a captured graph still applies).
 struct FusedLaunchBytes {
-    unsigned char b[256];
+    unsigned char b[384];
 };
 struct StepDevBytes {
     unsigned char b[256];
