@@ -381,6 +381,56 @@ def phase_times(lib, group, run, steps):
             for i, name in enumerate(["scan", "permute", "fused", "fused_rest"])}
 
 
+def adjoint_timing(reps: int = 5):
+    """Forward rollout vs adjoint pass of the differentiable fit's
+    configuration: 65,536 3D boids in a 200^3 cube, k = 16, 64 steps,
+    checkpoints every 8.  Host clock around each synchronised call, median
+    of `reps`; the plain fused step (gs_step, graph replay) alongside."""
+    import torch
+
+    import gpusteer_gb300 as gs
+    from gpusteer_gb300 import scenario as sc
+
+    n, steps, every = 65536, 64, 8
+    s = sc.boids_cube(n, size=200.0, seed=0)
+    p = sc.boids_params(k=16, world=256.0, cell=4.0)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g = gs.AgentGroup(p.k, n)
+    r = gs.Rollout(g, bins, steps, every)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    seed = torch.randn(n, 4, device="cuda", generator=gen) * 1e-3
+    gv = torch.zeros(n, 4, device="cuda")
+    gp = torch.zeros(n, 4, device="cuda")
+    fwd, bwd, plain = [], [], []
+    for it in range(reps + 1):
+        g.upload(s)
+        g.synchronize()
+        t0 = time.perf_counter()
+        r.forward(p)
+        g.synchronize()
+        t1 = time.perf_counter()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        r.backward(seed.data_ptr(), None, gp.data_ptr(), gv.data_ptr())
+        t3 = time.perf_counter()
+        g.upload(s)
+        gs.step(g, bins, None, p, 1)
+        g.synchronize()
+        t4 = time.perf_counter()
+        gs.step(g, bins, None, p, steps)
+        g.synchronize()
+        t5 = time.perf_counter()
+        if it > 0:
+            fwd.append((t1 - t0) * 1e3 / steps)
+            bwd.append((t3 - t2) * 1e3 / steps)
+            plain.append((t5 - t4) * 1e3 / steps)
+    f, b, pl = statistics.median(fwd), statistics.median(bwd), statistics.median(plain)
+    return {"config": "65,536 3D boids in a 200^3 cube, k=16, 64 steps, checkpoints every 8",
+            "fwd_ms_per_step": f, "bwd_ms_per_step": b, "bwd_over_fwd": b / f,
+            "plain_step_ms": pl, "bwd_over_plain_step": b / pl,
+            "timing": f"host clock around synchronised calls, median of {reps}"}
+
+
 def run_gpu_batched(args, dist, rank, world, local_rank):
     import torch
 
@@ -411,11 +461,13 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clocks:
         torch.cuda.synchronize()
+        torch.cuda.profiler.start()  # ncu --profile-from-start off sees the timed steps only
         ev0.record(stream)
         for _ in range(args.steps):
             b.step(p, 1)
         ev1.record(stream)
         ev1.synchronize()
+        torch.cuda.profiler.stop()
         torch.cuda.synchronize()
     barrier(dist)
     ms_max = allreduce_max(dist, ev0.elapsed_time(ev1))
@@ -485,6 +537,7 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         lib.gs_host_free(ptr)
     del b2
 
+    adjoint = adjoint_timing() if not args.no_adjoint else None
     if rank != 0:
         return
     peak, peak_src = read_peaks()
@@ -524,6 +577,7 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         "identical_to_per_scene": {"equal": bool(identical), "steps": total,
                                    "compared": "every state array of every agent"},
         "autotune": {"seconds": tune_s, "trials": tr.trials},
+        "adjoint": adjoint,
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state},
         "gpu_launches": 7 * args.steps,
@@ -569,11 +623,13 @@ def run_gpu(args, dist, rank, world, local_rank):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clocks:
         torch.cuda.synchronize()
+        torch.cuda.profiler.start()  # ncu --profile-from-start off sees the timed steps only
         ev0.record(stream)
         for _ in range(args.steps):
             gs.step(group, bins, walls, p, 1)
         ev1.record(stream)
         ev1.synchronize()
+        torch.cuda.profiler.stop()
         torch.cuda.synchronize()
     barrier(dist)
     ms = ev0.elapsed_time(ev1)
@@ -656,6 +712,8 @@ def main():
     ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the differentiable rollout's forward / backward timing")
     args = ap.parse_args()
     if args.steps is None:
         from gpusteer_gb300 import scenario as sc

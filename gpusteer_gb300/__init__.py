@@ -7,8 +7,9 @@ GroupSteerLibrary free functions), seeded scenarios and the build step.
 """
 from ._lib import GpuSteerError, load  # noqa: F401
 from .groups import (  # noqa: F401
-    AgentGroup, Batch, KNNBinData, KNNData, WallGroup, set_block, set_graphs, set_knn_capacity, antiPenetrationAgents, findKNearestNeighbors,
-    findKNearestNeighborsBruteForce, step, step_host, steerForAlignment, steerForCohesion,
+    AgentGroup, Batch, KNNBinData, KNNData, Rollout, WallGroup, antiPenetrationAgents,
+    findKNearestNeighbors, findKNearestNeighborsBruteForce, set_block, set_graphs,
+    set_knn_capacity, step, step_host, steerForAlignment, steerForCohesion,
     steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, updateGroup,
     updateKNNDatabase, wrapWorld)
 from .scenario import StepParams  # noqa: F401

@@ -115,6 +115,12 @@ SIGNATURES = {
     "gs_batch_group": [_vp, C.POINTER(_vp)],
     "gs_batch_step": [_vp, C.POINTER(StepParams), _u],
     "gs_knn_binned_noalloc": [_vp, _u, _up, _fp, _u, _u, _vp, _vp, _vp],
+    "gs_rollout_create": [_vp, _vp, _u, _u, C.POINTER(_vp)],
+    "gs_rollout_destroy": [_vp],
+    "gs_rollout_forward": [_vp, C.POINTER(StepParams)],
+    "gs_rollout_backward": [_vp, _vp, _vp, _vp, _vp, _fp],
+    "gs_flock_adjoint_step": [_vp, _vp, _vp, _u, _u, _vp, _vp, _vp, C.POINTER(StepParams), _vp,
+                              _vp, _vp, _vp, _vp, _u, _vp],
 }
 _RESTYPE = {"gs_status_string": C.c_char_p, "gs_last_error": C.c_char_p, "gs_version": _i,
             "gs_max_k": _u}

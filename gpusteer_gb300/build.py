@@ -18,7 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libgpusteer.so"
-SOURCES = ["gs_kernels.cu", "gs_step.cu", "gs_capi.cu", "gs_noalloc.cu"]
+SOURCES = ["gs_kernels.cu", "gs_step.cu", "gs_capi.cu", "gs_noalloc.cu", "gs_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
               "-prec-sqrt=true", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",

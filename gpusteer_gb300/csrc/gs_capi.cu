@@ -1001,12 +1001,15 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
     return GS_OK;
 }
 
-// The fused engine for a group whose scene table is in g->h_scenes / d_scene
-// (one scene for a plain group, many for a batch).
-static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
-                           const unsigned* agent_scene, const WallsDev& w, unsigned steps) {
+// Brings the fused engine's bucketed state and pending cell counts up to
+// date for steps on `grid` and fills the launch block L; picks the KNN
+// capacity into d.  dirty: the first step must add the steering and applied
+// bits left by per-function calls.
+static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned C,
+                             const unsigned* agent_scene, const WallsDev& w, FusedLaunch& L,
+                             bool& dirty) {
     cudaStream_t st = g->stream;
-    bool dirty = false;
+    dirty = false;
     if (!g->fused_current) {
         dirty = g->accum_dirty;
         // counts left pending by an earlier fused step no longer apply
@@ -1038,7 +1041,7 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
         d.enum_cap = g->auto_cap;
     }
 
-    FusedLaunch L{};
+    std::memset(static_cast<void*>(&L), 0, sizeof(L));  // byte-compared as a graph key
     L.A = g->A;
     L.B = g->B;
     L.cellrank = g->cellrank;
@@ -1061,6 +1064,17 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
         L.knn_slot = g->knn_slot;
         L.knn_dist = g->knn_dist;
     }
+    return GS_OK;
+}
+
+// The fused engine for a group whose scene table is in g->h_scenes / d_scene
+// (one scene for a plain group, many for a batch).
+static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
+                           const unsigned* agent_scene, const WallsDev& w, unsigned steps) {
+    cudaStream_t st = g->stream;
+    FusedLaunch L;
+    bool dirty = false;
+    GS_TRY(fused_setup(g, d, grid, C, agent_scene, w, L, dirty));
     Profiler prof(g);
     PhaseHook* hook = g->profiling ? &prof : nullptr;
     unsigned step = 0;
@@ -1359,3 +1373,300 @@ gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
 }
 
 }  // extern "C"
+
+// ---- differentiable rollouts: checkpointed forward, adjoint backward ----------------
+struct gs_rollout_s {
+    gs_group g = nullptr;
+    gs_bins bins = nullptr;
+    unsigned steps = 0, every = 0, n_seg = 0, cap = 0, k = 0;
+    unsigned n = 0;           // agents at the last forward pass
+    bool have_forward = false;
+    gs_step_params params{};  // of the last forward pass
+    // checkpoints [n_seg + 1][cap]: the state at the start of each segment, then the final state
+    float4 *ck_pos = nullptr, *ck_dir = nullptr;
+    float* ck_speed = nullptr;
+    float3 *ck_side = nullptr, *ck_up = nullptr;
+    // one segment's step records: [every][cap] and [every][cap * k]
+    float4 *rec_pos = nullptr, *rec_dir = nullptr;
+    unsigned* rec_knn = nullptr;
+    // adjoint state, ping-pong: d loss / d (position, velocity)
+    float4 *lp[2] = {nullptr, nullptr}, *lv[2] = {nullptr, nullptr};
+    float* wpart = nullptr;  // [adjoint_blocks(cap) * 4]
+};
+
+static void rollout_release(gs_rollout r) {
+    dfree(r->ck_pos);
+    dfree(r->ck_dir);
+    dfree(r->ck_speed);
+    dfree(r->ck_side);
+    dfree(r->ck_up);
+    dfree(r->rec_pos);
+    dfree(r->rec_dir);
+    dfree(r->rec_knn);
+    for (int i = 0; i < 2; ++i) {
+        dfree(r->lp[i]);
+        dfree(r->lv[i]);
+    }
+    dfree(r->wpart);
+}
+
+gs_status gs_rollout_create(gs_group g, gs_bins bins, unsigned steps, unsigned checkpoint_every,
+                            gs_rollout* out) {
+    if (!g || !bins || !out) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (steps == 0 || checkpoint_every == 0)
+        return fail(GS_ERR_INVALID_ARG, "steps and checkpoint interval must be positive");
+    if (g->k > 32) return fail(GS_ERR_INVALID_ARG, "rollouts need k <= 32");
+    gs_rollout r = new (std::nothrow) gs_rollout_s();
+    if (!r) return fail(GS_ERR_OOM, "host allocation failed");
+    r->g = g;
+    r->bins = bins;
+    r->steps = steps;
+    r->every = std::min(checkpoint_every, steps);
+    r->n_seg = (steps + r->every - 1) / r->every;
+    r->cap = g->capacity;
+    r->k = g->k;
+    const size_t cap = r->cap, nck = size_t(r->n_seg) + 1;
+    gs_status s = dalloc(&r->ck_pos, nck * cap);
+    if (s == GS_OK) s = dalloc(&r->ck_dir, nck * cap);
+    if (s == GS_OK) s = dalloc(&r->ck_speed, nck * cap);
+    if (s == GS_OK) s = dalloc(&r->ck_side, nck * cap);
+    if (s == GS_OK) s = dalloc(&r->ck_up, nck * cap);
+    if (s == GS_OK) s = dalloc(&r->rec_pos, size_t(r->every) * cap);
+    if (s == GS_OK) s = dalloc(&r->rec_dir, size_t(r->every) * cap);
+    if (s == GS_OK) s = dalloc(&r->rec_knn, size_t(r->every) * cap * r->k);
+    for (int i = 0; i < 2 && s == GS_OK; ++i) {
+        s = dalloc(&r->lp[i], cap);
+        if (s == GS_OK) s = dalloc(&r->lv[i], cap);
+    }
+    if (s == GS_OK) s = dalloc(&r->wpart, size_t(adjoint_blocks(r->cap)) * 4);
+    if (s != GS_OK) {
+        rollout_release(r);
+        delete r;
+        return s;
+    }
+    *out = r;
+    return GS_OK;
+}
+
+gs_status gs_rollout_destroy(gs_rollout r) {
+    if (!r) return GS_OK;
+    if (r->g) cudaStreamSynchronize(r->g->stream);
+    rollout_release(r);
+    delete r;
+    return GS_OK;
+}
+
+// Checks that p is a walls-free flock the adjoint covers and fills d, grid, C.
+static gs_status rollout_params(gs_rollout r, const gs_step_params* p, StepDev& d, Grid& grid,
+                                unsigned& C) {
+    GS_TRY(validate_step(p, nullptr, d));
+    if (d.need & ~(NEED_SEP | NEED_ALI | NEED_COH))
+        return fail(GS_ERR_UNSUPPORTED,
+                    "differentiable rollouts cover separation, alignment and cohesion");
+    for (unsigned o = 0; o < p->n_order; ++o)
+        if (p->order[o] == GS_B_SEEK)
+            return fail(GS_ERR_UNSUPPORTED,
+                        "differentiable rollouts cover separation, alignment and cohesion");
+    if (p->k != r->k) return fail(GS_ERR_INVALID_ARG, "k differs from the group's");
+    GS_TRY(check_grid(p->world_cells, p->world_size, grid, C));
+    if (C != r->bins->cells || std::memcmp(&grid, &r->bins->grid, sizeof(Grid)) != 0)
+        return fail(GS_ERR_INVALID_ARG, "step grid differs from the bins");
+    return GS_OK;
+}
+
+// Copies the group's time-varying state (reference layout) to checkpoint c.
+static gs_status rollout_save(gs_rollout r, unsigned c) {
+    gs_group g = r->g;
+    const size_t n = r->n, off = size_t(c) * r->cap;
+    cudaStream_t st = g->stream;
+    GS_TRY(ensure_reference(g));
+    GS_CUDA(cudaMemcpyAsync(r->ck_pos + off, g->position, n * 16, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(r->ck_dir + off, g->direction, n * 16, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(r->ck_speed + off, g->speed, n * 4, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(r->ck_side + off, g->side, n * 12, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(r->ck_up + off, g->up, n * 12, cudaMemcpyDeviceToDevice, st));
+    return GS_OK;
+}
+
+// Puts checkpoint c back into the group, with steering and applied bits cleared.
+static gs_status rollout_restore(gs_rollout r, unsigned c) {
+    gs_group g = r->g;
+    const size_t n = r->n, off = size_t(c) * r->cap;
+    cudaStream_t st = g->stream;
+    GS_CUDA(cudaMemcpyAsync(g->position, r->ck_pos + off, n * 16, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(g->direction, r->ck_dir + off, n * 16, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(g->speed, r->ck_speed + off, n * 4, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(g->side, r->ck_side + off, n * 12, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(g->up, r->ck_up + off, n * 12, cudaMemcpyDeviceToDevice, st));
+    GS_CUDA(cudaMemsetAsync(g->steering, 0, n * 16, st));
+    GS_CUDA(cudaMemsetAsync(g->applied, 0, n * 4, st));
+    g->fused_current = false;
+    g->accum_dirty = false;
+    g->db.valid = false;
+    return GS_OK;
+}
+
+gs_status gs_rollout_forward(gs_rollout r, const gs_step_params* p) {
+    if (!r) return fail(GS_ERR_INVALID_ARG, "null rollout");
+    gs_group g = r->g;
+    StepDev d;
+    Grid grid;
+    unsigned C;
+    GS_TRY(rollout_params(r, p, d, grid, C));
+    r->have_forward = false;
+    r->n = g->n;
+    r->params = *p;
+    if (g->n == 0) {
+        r->have_forward = true;
+        return GS_OK;
+    }
+    // the rollout starts from zero steering and applied bits
+    GS_TRY(ensure_reference(g));
+    GS_CUDA(cudaMemsetAsync(g->steering, 0, size_t(g->n) * 16, g->stream));
+    GS_CUDA(cudaMemsetAsync(g->applied, 0, size_t(g->n) * 4, g->stream));
+    g->fused_current = false;
+    g->accum_dirty = false;
+    GS_TRY(rollout_save(r, 0));
+    for (unsigned c = 0; c < r->n_seg; ++c) {
+        const unsigned len = std::min(r->every, r->steps - c * r->every);
+        GS_TRY(gs_step(g, r->bins, nullptr, p, len));
+        GS_TRY(rollout_save(r, c + 1));
+    }
+    r->have_forward = true;
+    return GS_OK;
+}
+
+// Re-runs segment c from its checkpoint, recording every step's inputs.
+static gs_status rollout_record(gs_rollout r, unsigned c, StepDev d, const Grid& grid,
+                                unsigned C, unsigned len) {
+    gs_group g = r->g;
+    GS_TRY(rollout_restore(r, c));
+    GS_TRY(reserve_fused(g, C, false, d.k, 1));
+    Scene sc{};
+    sc.grid = grid;
+    sc.n_agents = g->n;
+    GS_TRY(put_scenes(g, std::vector<Scene>{sc}));
+    d.block = g->block;
+    FusedLaunch L;
+    bool dirty = false;
+    GS_TRY(fused_setup(g, d, grid, C, nullptr, WallsDev{}, L, dirty));
+    d.dirty = 0;
+    for (unsigned j = 0; j < len; ++j) {
+        FusedLaunch Lj = L;
+        Lj.rec_pos = r->rec_pos + size_t(j) * r->cap;
+        Lj.rec_dir = r->rec_dir + size_t(j) * r->cap;
+        Lj.rec_knn = r->rec_knn + size_t(j) * r->cap * r->k;
+        GS_TRY(step_body(g, Lj, d, C, nullptr));
+    }
+    g->db.valid = false;
+    return GS_OK;
+}
+
+gs_status gs_rollout_backward(gs_rollout r, const float* adj_position, const float* adj_velocity,
+                              float* grad_position0, float* grad_velocity0,
+                              float grad_weights[3]) {
+    if (!r) return fail(GS_ERR_INVALID_ARG, "null rollout");
+    if (!r->have_forward) return fail(GS_ERR_INVALID_ARG, "backward needs a forward pass first");
+    gs_group g = r->g;
+    if (g->n != r->n) return fail(GS_ERR_INVALID_ARG, "the group changed size since forward");
+    StepDev d;
+    Grid grid;
+    unsigned C;
+    GS_TRY(rollout_params(r, &r->params, d, grid, C));
+    cudaStream_t st = g->stream;
+    const size_t n = r->n;
+    const unsigned nb = adjoint_blocks(r->cap);
+    if (n == 0) {
+        if (grad_weights) grad_weights[0] = grad_weights[1] = grad_weights[2] = 0.f;
+        return GS_OK;
+    }
+    if (adj_position)
+        GS_CUDA(cudaMemcpyAsync(r->lp[0], adj_position, n * 16, cudaMemcpyDeviceToDevice, st));
+    else
+        GS_CUDA(cudaMemsetAsync(r->lp[0], 0, n * 16, st));
+    if (adj_velocity)
+        GS_CUDA(cudaMemcpyAsync(r->lv[0], adj_velocity, n * 16, cudaMemcpyDeviceToDevice, st));
+    else
+        GS_CUDA(cudaMemsetAsync(r->lv[0], 0, n * 16, st));
+    GS_CUDA(cudaMemsetAsync(r->lp[1], 0, n * 16, st));
+    GS_CUDA(cudaMemsetAsync(r->lv[1], 0, n * 16, st));
+    GS_CUDA(cudaMemsetAsync(r->wpart, 0, size_t(nb) * 16, st));
+    int cur = 0;
+    for (unsigned c = r->n_seg; c-- > 0;) {
+        const unsigned len = std::min(r->every, r->steps - c * r->every);
+        GS_TRY(rollout_record(r, c, d, grid, C, len));
+        for (unsigned j = len; j-- > 0;) {
+            AdjointLaunch A;
+            A.pos = r->rec_pos + size_t(j) * r->cap;
+            A.dir = r->rec_dir + size_t(j) * r->cap;
+            A.knn = r->rec_knn + size_t(j) * r->cap * r->k;
+            A.max_speed = g->max_speed;
+            A.max_force = g->max_force;
+            A.mass = g->mass;
+            A.lp_in = r->lp[cur];
+            A.lv_in = r->lv[cur];
+            A.lp_out = r->lp[1 - cur];
+            A.lv_out = r->lv[1 - cur];
+            A.wpart = r->wpart;
+            A.n = r->n;
+            A.k = r->k;
+            GS_TRY(launch_flock_adjoint(A, d, st));
+            cur = 1 - cur;
+        }
+    }
+    if (grad_position0)
+        GS_CUDA(cudaMemcpyAsync(grad_position0, r->lp[cur], n * 16, cudaMemcpyDeviceToDevice, st));
+    if (grad_velocity0)
+        GS_CUDA(cudaMemcpyAsync(grad_velocity0, r->lv[cur], n * 16, cudaMemcpyDeviceToDevice, st));
+    std::vector<float> part(size_t(nb) * 4);
+    GS_CUDA(cudaMemcpyAsync(part.data(), r->wpart, part.size() * 4, cudaMemcpyDeviceToHost, st));
+    // leave the group at the rollout's final state
+    GS_TRY(rollout_restore(r, r->n_seg));
+    GS_CUDA(cudaStreamSynchronize(st));
+    GS_TRY(check_device_flags(g));
+    if (grad_weights) {
+        for (int b = 0; b < 3; ++b) {
+            double sum = 0.0;  // host-side sum of the per-block partials
+            for (unsigned i = 0; i < nb; ++i) sum += part[size_t(i) * 4 + b];
+            grad_weights[b] = float(sum);
+        }
+    }
+    return GS_OK;
+}
+
+gs_status gs_flock_adjoint_step(const float* position_speed, const float* heading,
+                                const unsigned* knn, unsigned n, unsigned k,
+                                const float* max_speed, const float* max_force, const float* mass,
+                                const gs_step_params* p, float* adj_position_out,
+                                float* adj_velocity_out, float* adj_position_in,
+                                float* adj_velocity_in, float* weight_partials,
+                                unsigned partials_cap, void* stream) {
+    StepDev d;
+    GS_TRY(validate_step(p, nullptr, d));
+    if (d.need & ~(NEED_SEP | NEED_ALI | NEED_COH))
+        return fail(GS_ERR_UNSUPPORTED, "the adjoint covers separation, alignment and cohesion");
+    if (k != p->k) return fail(GS_ERR_INVALID_ARG, "k differs from the parameters'");
+    if (n == 0) return GS_OK;
+    if (!position_speed || !heading || !knn || !max_speed || !max_force || !mass ||
+        !adj_position_out || !adj_velocity_out || !adj_position_in || !adj_velocity_in ||
+        !weight_partials)
+        return fail(GS_ERR_INVALID_ARG, "null device array");
+    if (partials_cap < adjoint_blocks(n) * 4)
+        return fail(GS_ERR_INVALID_ARG, "weight partials need 4 * ceil(n / 256) floats");
+    AdjointLaunch A;
+    A.pos = reinterpret_cast<const float4*>(position_speed);
+    A.dir = reinterpret_cast<const float4*>(heading);
+    A.knn = knn;
+    A.max_speed = max_speed;
+    A.max_force = max_force;
+    A.mass = mass;
+    A.lp_in = reinterpret_cast<float4*>(adj_position_out);
+    A.lv_in = reinterpret_cast<float4*>(adj_velocity_out);
+    A.lp_out = reinterpret_cast<float4*>(adj_position_in);
+    A.lv_out = reinterpret_cast<float4*>(adj_velocity_in);
+    A.wpart = weight_partials;
+    A.n = n;
+    A.k = k;
+    return launch_flock_adjoint(A, d, static_cast<cudaStream_t>(stream));
+}

@@ -321,6 +321,40 @@ class Batch:
             self._h = None
 
 
+class Rollout:
+    """Checkpointed differentiable rollout of a plain flock (gs_rollout_*):
+    `steps` fused steps from the group's state, then the adjoint backwards
+    with KNN lists and memberships frozen.  Device arrays are passed as raw
+    pointers (float4 per agent, agent order)."""
+
+    def __init__(self, group: AgentGroup, bins: KNNBinData, steps: int,
+                 checkpoint_every: int = 8):
+        h = C.c_void_p()
+        call("gs_rollout_create", group.handle, bins.handle, int(steps), int(checkpoint_every),
+             C.byref(h))
+        self._h = h
+        self.group = group
+        self.steps = steps
+
+    def forward(self, params: StepParams) -> None:
+        p = step_params_c(params)
+        call("gs_rollout_forward", self._h, C.byref(p))
+
+    def backward(self, adj_position: int | None, adj_velocity: int | None = None,
+                 grad_position0: int | None = None, grad_velocity0: int | None = None):
+        """Returns d loss / d (w_separation, w_alignment, w_cohesion)."""
+        gw = np.zeros(3, np.float32)
+        vp = lambda x: C.c_void_p(x) if x else None  # noqa: E731
+        call("gs_rollout_backward", self._h, vp(adj_position), vp(adj_velocity),
+             vp(grad_position0), vp(grad_velocity0), _ptr(gw))
+        return gw
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_rollout_destroy(self._h)
+            self._h = None
+
+
 # ---- GroupSteerLibrary.cuh -----------------------------------------------------------
 
 def wrapWorld(group: AgentGroup, world_size, mode: int = WRAP_REFERENCE) -> None:

@@ -277,6 +277,48 @@ gs_status gs_batch_download(gs_batch b, const gs_agent_arrays* host);
 gs_status gs_batch_group(gs_batch b, gs_group* g);
 gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps);
 
+/* ---- differentiable rollouts --------------------------------------------------------
+ * No counterpart in the reference.  A rollout runs `steps` fused steps of a
+ * plain flock (separation, alignment, cohesion; no walls, seek or neighbour
+ * avoidance) from the group's current state, keeping the time-varying state
+ * every `checkpoint_every` steps, and then runs the hand-written adjoint of
+ * the fused steering-plus-integrate step backwards through it: each segment
+ * between checkpoints is re-run once with its steps' inputs and KNN lists
+ * recorded, so memory grows with steps / checkpoint_every + checkpoint_every
+ * states.  KNN lists and neighbourhood memberships are frozen at the
+ * forward pass's values (piecewise constant); the derivative of the world
+ * wrap is the identity.  Velocities are heading * speed. */
+typedef struct gs_rollout_s* gs_rollout;
+gs_status gs_rollout_create(gs_group g, gs_bins bins, unsigned steps, unsigned checkpoint_every,
+                            gs_rollout* out);
+gs_status gs_rollout_destroy(gs_rollout r);
+/* Runs the rollout with parameters p (steering and applied bits start at zero);
+ * the group is left at the final state. */
+gs_status gs_rollout_forward(gs_rollout r, const gs_step_params* p);
+/* Given device arrays (float4 per agent, agent order, .w ignored) of
+ * d loss / d final position and velocity (either may be null: zero), writes
+ * d loss / d initial position and velocity (device, float4 per agent; either
+ * may be null) and d loss / d (w_separation, w_alignment, w_cohesion) to the
+ * host array grad_weights.  Synchronous; the group is left at the final state. */
+gs_status gs_rollout_backward(gs_rollout r, const float* adj_position, const float* adj_velocity,
+                              float* grad_position0, float* grad_velocity0,
+                              float grad_weights[3]);
+/* The adjoint kernel of one step on caller-provided device arrays: the step's
+ * recorded inputs (position | speed and heading as float4 per agent, KNN as
+ * n x k row-major agent indices, UINT_MAX after the last), the constant
+ * per-agent limits, and the adjoints of its outputs (adj_*_out, float4 per
+ * agent; zeroed on return).  Adds the adjoints of its inputs to adj_*_in
+ * (float4 per agent) and per-block sums of d loss / d weights to
+ * weight_partials (4 floats per block of 256 agents: separation, alignment,
+ * cohesion, unused).  Asynchronous on `stream`. */
+gs_status gs_flock_adjoint_step(const float* position_speed, const float* heading,
+                                const unsigned* knn, unsigned n, unsigned k,
+                                const float* max_speed, const float* max_force, const float* mass,
+                                const gs_step_params* p, float* adj_position_out,
+                                float* adj_velocity_out, float* adj_position_in,
+                                float* adj_velocity_in, float* weight_partials,
+                                unsigned partials_cap, void* stream);
+
 /* ---- KNN without device allocation ------------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot let a
  * library allocate device memory (pre-sized memory pools, real-time loops
