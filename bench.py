@@ -476,30 +476,40 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     del b
 
     # the same scenes, one gs_step call per scene per step (same grid, block,
-    # capacity; each scene's group has its own stream and CUDA graph)
-    per = []
-    for s, g in zip(states, gaps):
-        bins = gs.KNNBinData(p.world_cells, p.world_size, p.search_radius)
-        walls = gs.WallGroup(walls_rows(g), bins=bins, knw=p.knw)
-        grp = gs.AgentGroup(p.k, s.n)
-        grp.upload(s)
-        gs.set_block(grp, tr.block)
-        gs.set_knn_capacity(grp, tr.capacity)
-        per.append((grp, bins, walls))
-    for grp, bins, walls in per:
-        gs.step(grp, bins, walls, p, args.warmup)
-    for grp, _, _ in per:
-        grp.synchronize()
+    # capacity; each scene's group keeps its CUDA graph).  "sequential": all
+    # scenes' groups on one stream, one scene's step after another, as the
+    # reference's plugins run on the default stream; "concurrent": each
+    # group on its own stream, so the GPU may overlap scenes.
     ps_steps = max(3, min(args.steps, 50))
-    barrier(dist)
-    t0 = time.perf_counter()
-    for _ in range(ps_steps):
-        for grp, bins, walls in per:
-            gs.step(grp, bins, walls, p, 1)
-    for grp, _, _ in per:
-        grp.synchronize()
-    ps_s = allreduce_max(dist, time.perf_counter() - t0)
-    per_scene = n * ps_steps * world / ps_s
+
+    def per_scene_run(shared: bool):
+        groups, first = [], None
+        for s, g in zip(states, gaps):
+            bins = gs.KNNBinData(p.world_cells, p.world_size, p.search_radius)
+            walls = gs.WallGroup(walls_rows(g), bins=bins, knw=p.knw)
+            grp = gs.AgentGroup(p.k, s.n, stream=first.stream if (shared and first) else None)
+            first = first or grp
+            grp.upload(s)
+            gs.set_block(grp, tr.block)
+            gs.set_knn_capacity(grp, tr.capacity)
+            groups.append((grp, bins, walls))
+        for grp, bins, walls in groups:
+            gs.step(grp, bins, walls, p, args.warmup)
+        for grp, _, _ in groups:
+            grp.synchronize()
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(ps_steps):
+            for grp, bins, walls in groups:
+                gs.step(grp, bins, walls, p, 1)
+        for grp, _, _ in groups:
+            grp.synchronize()
+        el = allreduce_max(dist, time.perf_counter() - t0)
+        return n * ps_steps * world / el, 1e3 * el / ps_steps, groups
+
+    per_seq, per_seq_ms, groups = per_scene_run(shared=True)
+    del groups
+    per_conc, per_conc_ms, per = per_scene_run(shared=False)
 
     # identical results: a fresh batch stepped as often as the per-scene groups
     total = args.warmup + ps_steps
@@ -570,10 +580,15 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
                    "block": tr.block, "knn_capacity": tr.capacity or "auto",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (about 270 MB of bucketed state per step)"},
-        "per_scene": {"value": per_scene, "unit": "agent-steps/s", "steps": ps_steps,
-                      "ms_per_step": 1e3 * ps_s / ps_steps,
-                      "timing": "host clock, every scene's stream synchronised on both sides",
-                      "batched_over_per_scene": value / per_scene},
+        "per_scene": {"value": per_seq, "unit": "agent-steps/s", "steps": ps_steps,
+                      "ms_per_step": per_seq_ms,
+                      "launch": "one gs_step per scene per step, all scenes on one stream",
+                      "timing": "host clock, streams synchronised on both sides",
+                      "batched_over_per_scene": value / per_seq,
+                      "concurrent": {"value": per_conc, "ms_per_step": per_conc_ms,
+                                     "launch": "one gs_step per scene per step, each scene "
+                                               "on its own stream",
+                                     "batched_over": value / per_conc}},
         "identical_to_per_scene": {"equal": bool(identical), "steps": total,
                                    "compared": "every state array of every agent"},
         "autotune": {"seconds": tune_s, "trials": tr.trials},

@@ -272,6 +272,15 @@ __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDe
 
 // Agents handled by one thread: slot `it` of the launch (fast path), or the
 // it-th entry of the retry list (exact path, grid-stride).
+// The exact launch numbers its threads block-fastest (thread t of block b is
+// it = t * gridDim.x + b), so the few hundred agents of a typical retry list
+// land one or two per block across every SM instead of filling the first
+// blocks: the redo then takes one agent's latency, not a queue of them.
+template <bool EXACT>
+__device__ __forceinline__ unsigned first_agent() {
+    return EXACT ? threadIdx.x * gridDim.x + blockIdx.x : blockIdx.x * blockDim.x + threadIdx.x;
+}
+
 template <bool EXACT>
 __device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, unsigned& s) {
     if (!EXACT) {
@@ -290,7 +299,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
     const unsigned bd = blockDim.x;
     unsigned* col = sh_col + threadIdx.x;
     const unsigned step = EXACT ? gridDim.x * blockDim.x : 0u;
-    for (unsigned it = blockIdx.x * blockDim.x + threadIdx.x;; it += step) {
+    for (unsigned it = first_agent<EXACT>();; it += step) {
         unsigned s;
         if (!next_agent<EXACT>(L, it, s)) return;
         float4 f0, f4v;
@@ -343,7 +352,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDe
     const unsigned bd = blockDim.x;
     unsigned* col = sh_col + threadIdx.x;
     const unsigned step = EXACT ? gridDim.x * blockDim.x : 0u;
-    for (unsigned it = blockIdx.x * blockDim.x + threadIdx.x;; it += step) {
+    for (unsigned it = first_agent<EXACT>();; it += step) {
         unsigned s;
         if (!next_agent<EXACT>(L, it, s)) return;
         float4 f0, f4v;
@@ -360,9 +369,11 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDe
         for (unsigned r = 0; r < p.k; ++r) {
             const unsigned bs = col[(base + r) * bd];
             L.knn_slot[size_t(r) * L.n + s] = bs;
-            // the KNN distance (before any wall correction moves agents)
-            L.knn_dist[size_t(r) * L.n + s] =
-                bs == UINT_MAX ? FLT_MAX : distance(me.pos, v3(L.B.f[0][bs]));
+            // the KNN distance (before any wall correction moves agents),
+            // read by avoid-close-neighbours only
+            if (p.need & NEED_CLOSE)
+                L.knn_dist[size_t(r) * L.n + s] =
+                    bs == UINT_MAX ? FLT_MAX : distance(me.pos, v3(L.B.f[0][bs]));
         }
         if (sc.n_walls > 0 && L.w_pos_id != nullptr) {
             // wall lines staged in this thread's (now free) shared column
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDe
 
 // ---- rest of the step after the wall phase --------------------------------------------
 template <int KMAX>
-__global__ void __launch_bounds__(kBlock) k_fused_rest(FusedLaunch L, StepDev p) {
+__global__ void __launch_bounds__(kBlock, 3) k_fused_rest(FusedLaunch L, StepDev p) {
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.n) return;
     const float4 w0 = L.w0[s], w1 = L.w1[s], w2 = L.w2[s];
@@ -426,8 +437,8 @@ __global__ void __launch_bounds__(kBlock) k_fused_rest(FusedLaunch L, StepDev p)
         const float4 b0 = L.w0[bs];
         const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float br = need_rad ? L.B.f[2][bs].w : 0.f;
-        accumulate(a, p, fs, fa, fc, me, u(b0.w), L.knn_dist[size_t(i) * L.n + s], v3(b0),
-                   v3(b1), b1.w, br);
+        const float kd = (p.need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
+        accumulate(a, p, fs, fa, fc, me, u(b0.w), kd, v3(b0), v3(b1), b1.w, br);
     }
     finish_all(a, p, 1, fs, fa, fc, me, applied, steer);
     integrate(me, steer, p.dt);
