@@ -301,7 +301,7 @@ def run_reference(args, dist, rank):
 
 
 def run_reference_batched(args):
-    states, gaps, p, walls_rows = make_batched()
+    states, gaps, p, walls_rows = make_batched(args.scenes)
     bo = BatchedOracle(states, gaps, p, walls_rows)
     t0 = time.perf_counter()
     bo.step()  # one whole warm-up step of all scenes
@@ -318,7 +318,9 @@ def run_reference_batched(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS["batched"], "scenes": len(states), "agents": bo.n,
+        "config": {"workload": WORKLOADS["batched"] if args.scenes == 256 else
+                   WORKLOADS["batched"].replace("256", str(args.scenes), 1),
+                   "scenes": len(states), "agents": bo.n,
                    "k": p.k},
         "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": bo.threads,
                          "kind": "port",
@@ -441,12 +443,15 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     lib = gs.load()
     check(lib.gs_set_device(local_rank))
     torch.cuda.set_device(local_rank)
-    states, gaps, base, walls_rows = make_batched()
+    states, gaps, base, walls_rows = make_batched(args.scenes)
     n = sum(s.n for s in states)
 
     # autotune cell size, block shape and KNN capacity on the scenes themselves
     t0 = time.perf_counter()
-    tr = autotune.tune_batched(states, gaps, base, walls_rows)
+    if args.fixed_config:
+        tr = autotune.TuneResult(params=base, block=256, capacity=0, ms_per_step=0.0)
+    else:
+        tr = autotune.tune_batched(states, gaps, base, walls_rows)
     tune_s = time.perf_counter() - t0
     p = tr.params
     b = autotune.batch_for(states, gaps, p, walls_rows)
@@ -507,22 +512,33 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         el = allreduce_max(dist, time.perf_counter() - t0)
         return n * ps_steps * world / el, 1e3 * el / ps_steps, groups
 
-    per_seq, per_seq_ms, groups = per_scene_run(shared=True)
-    del groups
-    per_conc, per_conc_ms, per = per_scene_run(shared=False)
+    from gpusteer_gb300.state import AgentState
 
-    # identical results: a fresh batch stepped as often as the per-scene groups
     total = args.warmup + ps_steps
     b2 = autotune.batch_for(states, gaps, p, walls_rows)
     gs.set_block(b2.group, tr.block)
     gs.set_knn_capacity(b2.group, tr.capacity)
-    b2.step(p, total)
-    got = b2.download()
-    from gpusteer_gb300.state import AgentState
-
-    want = AgentState.concat([grp.download() for grp, _, _ in per])
-    identical = all(np.array_equal(getattr(got, k), getattr(want, k)) for k in got.names())
-    del per
+    per_scene, identical = None, None
+    if not args.no_per_scene:
+        per_seq, per_seq_ms, groups = per_scene_run(shared=True)
+        del groups
+        per_conc, per_conc_ms, per = per_scene_run(shared=False)
+        # identical results: a fresh batch stepped as often as the per-scene groups
+        b2.step(p, total)
+        got = b2.download()
+        want = AgentState.concat([grp.download() for grp, _, _ in per])
+        identical = all(np.array_equal(getattr(got, k), getattr(want, k)) for k in got.names())
+        del per
+        per_scene = {
+            "value": per_seq, "unit": "agent-steps/s", "steps": ps_steps,
+            "ms_per_step": per_seq_ms,
+            "launch": "one gs_step per scene per step, all scenes on one stream",
+            "timing": "host clock, streams synchronised on both sides",
+            "batched_over_per_scene": value / per_seq,
+            "concurrent": {"value": per_conc, "ms_per_step": per_conc_ms,
+                           "launch": "one gs_step per scene per step, each scene on its own "
+                                     "stream",
+                           "batched_over": value / per_conc}}
 
     # end to end: page-locked host state uploaded, stepped once and downloaded
     # every step through the batch API
@@ -574,23 +590,18 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOADS["batched"], "scenes": len(states),
+        "config": {"workload": WORKLOADS["batched"] if args.scenes == 256 else
+                   WORKLOADS["batched"].replace("256", str(args.scenes), 1),
+                   "scenes": len(states),
                    "agents_per_gpu": n, "k": p.k, "knw": p.knw,
                    "cell": p.world_size[0] / p.world_cells[0], "cells_per_scene": cells,
                    "block": tr.block, "knn_capacity": tr.capacity or "auto",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (about 270 MB of bucketed state per step)"},
-        "per_scene": {"value": per_seq, "unit": "agent-steps/s", "steps": ps_steps,
-                      "ms_per_step": per_seq_ms,
-                      "launch": "one gs_step per scene per step, all scenes on one stream",
-                      "timing": "host clock, streams synchronised on both sides",
-                      "batched_over_per_scene": value / per_seq,
-                      "concurrent": {"value": per_conc, "ms_per_step": per_conc_ms,
-                                     "launch": "one gs_step per scene per step, each scene "
-                                               "on its own stream",
-                                     "batched_over": value / per_conc}},
-        "identical_to_per_scene": {"equal": bool(identical), "steps": total,
-                                   "compared": "every state array of every agent"},
+        "per_scene": per_scene,
+        "identical_to_per_scene": None if identical is None else {
+            "equal": bool(identical), "steps": total,
+            "compared": "every state array of every agent"},
         "autotune": {"seconds": tune_s, "trials": tr.trials},
         "adjoint": adjoint,
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
@@ -729,6 +740,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the differentiable rollout's forward / backward timing")
+    ap.add_argument("--scenes", type=int, default=256, help="batched workload: scene count")
+    ap.add_argument("--fixed-config", action="store_true",
+                    help="batched workload: the scenario's grid, 256 threads, KNN capacity "
+                         "from the density (no autotuning)")
+    ap.add_argument("--no-per-scene", action="store_true",
+                    help="batched workload: skip the per-scene baselines")
     args = ap.parse_args()
     if args.steps is None:
         from gpusteer_gb300 import scenario as sc
