@@ -78,13 +78,14 @@ def fused_bytes_per_agent(p) -> int:
     (80 B) and the next step's (cell, rank) pair (8 B).  Neighbour and
     candidate reads hit the same bucketed arrays and are counted once.  With
     avoid-walls the step is split in two launches that also write and read
-    the wall-phase state (3 float4) and the neighbour list (slot + distance
-    per neighbour)."""
+    the wall-phase state (3 float4) and the neighbour slots (4 B each; plus
+    the KNN distances, 4 B each, when avoid-close-neighbours needs them)."""
     from gpusteer_gb300 import scenario as sc
 
     if sc.B_AVOID_WALLS in p.order:
-        walls_half = 80 + 48 + 8 * p.k
-        rest_half = 48 + 48 + 8 * p.k + 80 + 8
+        lists = 4 * p.k * (2 if (sc.B_AVOID_NEIGHBORS in p.order and p.avoid_close) else 1)
+        walls_half = 80 + lists + 48
+        rest_half = 48 + 48 + lists + 80 + 8
         return walls_half + rest_half
     return 80 + 80 + 8
 
