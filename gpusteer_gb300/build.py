@@ -58,13 +58,39 @@ def build(verbose: bool = False, force: bool = False) -> Path:
                 sys.stderr.write(r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed: {' '.join(cmd)}")
+    relinked = False
     if force or jobs or _stale(LIB, objs):
         cmd = [nvcc(), *ARCH, "-shared", "--cudart", "static", "-o", str(LIB), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed")
+        relinked = True
+    build_headless(force or relinked, verbose)
     return LIB
+
+
+HEADLESS_SRC = PKG / "plugins" / "headless.cpp"
+HEADLESS = BUILD / "gs_headless"
+
+
+def build_headless(force: bool = False, verbose: bool = False) -> Path:
+    """The headless plugin driver: C++ plugins on include/GroupSteerLibrary.h,
+    linked against libgpusteer.so (found next to it at run time)."""
+    inc = PKG.parent / "include"
+    deps = [HEADLESS_SRC, LIB, inc / "GroupSteerLibrary.h", inc / "PlugIn.h", inc / "gpusteer.h"]
+    if not force and not _stale(HEADLESS, deps):
+        return HEADLESS
+    cuda_inc = Path(nvcc()).resolve().parent.parent / "include"
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-ffp-contract=off",
+           "-I", str(inc), "-I", str(cuda_inc), str(HEADLESS_SRC), "-o", str(HEADLESS),
+           "-L", str(BUILD), "-lgpusteer", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if verbose or r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+    if r.returncode != 0:
+        raise RuntimeError("headless driver build failed")
+    return HEADLESS
 
 
 if __name__ == "__main__":

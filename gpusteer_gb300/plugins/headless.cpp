@@ -1,0 +1,297 @@
+// Headless driver for plugins written against the reference's group API.
+//
+// Two plugins re-state the reference's per-frame updates through the C++
+// drop-in (include/GroupSteerLibrary.h), call for call:
+//   Boids       BoidsGroup::update (plugins/BoidsGroup.cpp:606-637):
+//               wrapWorld, updateKNNDatabase, findKNearestNeighbors,
+//               separation, cohesion, alignment, updateGroup
+//   ChokePoint  CtfGroup::update (plugins/ChokePointNew.cpp:586-630) with the
+//               behaviours of the choke-point configuration: wrapWorld,
+//               updateKNNDatabase, KNN of agents and of walls,
+//               steerToAvoidWalls, steerToAvoidNeighbors, separation, seek,
+//               updateGroup
+// The world (KNNBinData, WallGroup loaded from a .map file and split on the
+// bins) is built in open() as CtfWorld does (ChokePointNew.cpp:103-120).
+//
+//   gs_headless <Boids|ChokePoint> <state_in> <state_out> <frames> [key=value ...]
+//
+// State files: uint32 n, then position (4n f32), direction (4n), steering
+// (4n), side (3n), up (3n), speed, max_speed, max_force, radius, mass (n
+// f32 each), applied (n u32).  The final state is written by redraw() after
+// the last frame.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <vector_functions.h>
+
+#include "GroupSteerLibrary.h"
+#include "PlugIn.h"
+
+using namespace OpenSteer;
+
+namespace {
+
+typedef std::map<std::string, std::string> Params;
+
+float fparam(const Params& p, const char* k, float def) {
+    auto it = p.find(k);
+    return it == p.end() ? def : std::strtof(it->second.c_str(), nullptr);
+}
+uint uparam(const Params& p, const char* k, uint def) {
+    auto it = p.find(k);
+    return it == p.end() ? def : uint(std::strtoul(it->second.c_str(), nullptr, 10));
+}
+float3 f3param(const Params& p, const char* k, float3 def) {
+    auto it = p.find(k);
+    if (it == p.end()) return def;
+    std::istringstream in(it->second);
+    char c;
+    in >> def.x >> c >> def.y >> c >> def.z;
+    return def;
+}
+uint3 u3param(const Params& p, const char* k, uint3 def) {
+    auto it = p.find(k);
+    if (it == p.end()) return def;
+    std::istringstream in(it->second);
+    char c;
+    in >> def.x >> c >> def.y >> c >> def.z;
+    return def;
+}
+
+// ---- state files ---------------------------------------------------------------------
+std::vector<AgentData> read_state(const char* path) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) throw std::runtime_error(std::string("cannot open ") + path);
+    uint32_t n = 0;
+    if (std::fread(&n, 4, 1, f) != 1) throw std::runtime_error("short state file");
+    std::vector<float> pos(4 * n), dir(4 * n), st(4 * n), side(3 * n), up(3 * n), sp(n), ms(n),
+        mf(n), rad(n), mass(n);
+    std::vector<uint32_t> ap(n);
+    auto rd = [&](void* d, size_t bytes) {
+        if (bytes && std::fread(d, 1, bytes, f) != bytes) throw std::runtime_error("short state file");
+    };
+    rd(pos.data(), pos.size() * 4);
+    rd(dir.data(), dir.size() * 4);
+    rd(st.data(), st.size() * 4);
+    rd(side.data(), side.size() * 4);
+    rd(up.data(), up.size() * 4);
+    rd(sp.data(), n * 4);
+    rd(ms.data(), n * 4);
+    rd(mf.data(), n * 4);
+    rd(rad.data(), n * 4);
+    rd(mass.data(), n * 4);
+    rd(ap.data(), n * 4);
+    std::fclose(f);
+    std::vector<AgentData> out(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        AgentData& a = out[i];
+        a.id = i;
+        a.position = make_float4(pos[4 * i], pos[4 * i + 1], pos[4 * i + 2], pos[4 * i + 3]);
+        a.direction = make_float4(dir[4 * i], dir[4 * i + 1], dir[4 * i + 2], dir[4 * i + 3]);
+        a.steering = make_float4(st[4 * i], st[4 * i + 1], st[4 * i + 2], st[4 * i + 3]);
+        a.side = make_float3(side[3 * i], side[3 * i + 1], side[3 * i + 2]);
+        a.up = make_float3(up[3 * i], up[3 * i + 1], up[3 * i + 2]);
+        a.speed = sp[i];
+        a.maxSpeed = ms[i];
+        a.maxForce = mf[i];
+        a.radius = rad[i];
+        a.mass = mass[i];
+        a.appliedKernels = ap[i];
+    }
+    return out;
+}
+
+void write_state(const char* path, AgentGroup& g) {
+    const uint32_t n = g.Size();
+    std::vector<float> pos, dir, st, side, up, sp, ms, mf, rad, mass;
+    std::vector<uint32_t> ap;
+    for (uint32_t i = 0; i < n; ++i) {
+        AgentData a;
+        if (!g.GetDataForAgent(i, a)) throw std::runtime_error("missing agent");
+        pos.insert(pos.end(), {a.position.x, a.position.y, a.position.z, a.position.w});
+        dir.insert(dir.end(), {a.direction.x, a.direction.y, a.direction.z, a.direction.w});
+        st.insert(st.end(), {a.steering.x, a.steering.y, a.steering.z, a.steering.w});
+        side.insert(side.end(), {a.side.x, a.side.y, a.side.z});
+        up.insert(up.end(), {a.up.x, a.up.y, a.up.z});
+        sp.push_back(a.speed);
+        ms.push_back(a.maxSpeed);
+        mf.push_back(a.maxForce);
+        rad.push_back(a.radius);
+        mass.push_back(a.mass);
+        ap.push_back(a.appliedKernels);
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) throw std::runtime_error(std::string("cannot write ") + path);
+    std::fwrite(&n, 4, 1, f);
+    for (auto* v : {&pos, &dir, &st, &side, &up, &sp, &ms, &mf, &rad, &mass})
+        std::fwrite(v->data(), 4, v->size(), f);
+    std::fwrite(ap.data(), 4, ap.size(), f);
+    std::fclose(f);
+}
+
+// ---- plugins -------------------------------------------------------------------------
+class HeadlessPlugIn : public PlugIn {
+public:
+    Params params;
+    std::string in_path, out_path;
+};
+
+class BoidsPlugIn : public HeadlessPlugIn {
+public:
+    const char* name() { return "Boids"; }
+    void open() {
+        const Params& p = params;
+        m_worldSize = f3param(p, "world", make_float3(160.f, 160.f, 160.f));
+        m_worldCells = u3param(p, "cells", make_uint3(40, 40, 40));
+        m_k = uparam(p, "k", 7);
+        m_radius = uparam(p, "radius", 1);
+        m_bins.reset(new KNNBinData(m_worldCells, m_worldSize, m_radius));
+        m_group.reset(new AgentGroup(m_worldCells, m_k));
+        for (const AgentData& a : read_state(in_path.c_str())) m_group->AddAgent(a);
+        m_group->SyncDevice();
+        m_knn.reset(new KNNData(m_group->Size(), m_k));
+    }
+    // BoidsGroup::update (plugins/BoidsGroup.cpp:606-637)
+    void update(const float, const float elapsedTime) {
+        const Params& p = params;
+        AgentGroup* g = m_group.get();
+        wrapWorld(g, m_worldSize);
+        updateKNNDatabase(g, m_bins.get());
+        findKNearestNeighbors(g, m_knn.get(), m_bins.get(), g, m_radius);
+        steerForSeparation(g, m_knn.get(), g, fparam(p, "sep_min", 0.5f), fparam(p, "sep_max", 2.f),
+                           fparam(p, "sep_cos", -0.9848077f), fparam(p, "w_sep", 5.f),
+                           uparam(p, "mask_sep", 0));
+        steerForCohesion(g, m_knn.get(), g, fparam(p, "coh_min", 0.5f), fparam(p, "coh_max", 7.f),
+                         fparam(p, "coh_cos", -0.9848077f), fparam(p, "w_coh", 4.f),
+                         uparam(p, "mask_coh", 0));
+        steerForAlignment(g, m_knn.get(), g, fparam(p, "ali_min", 0.5f), fparam(p, "ali_max", 7.f),
+                          fparam(p, "ali_cos", -0.9848077f), fparam(p, "w_ali", 8.f),
+                          uparam(p, "mask_ali", 0));
+        updateGroup(g, elapsedTime);
+    }
+    void redraw(const float, const float) { write_state(out_path.c_str(), *m_group); }
+    void close() {
+        m_knn.reset();
+        m_group.reset();
+        m_bins.reset();
+    }
+
+private:
+    float3 m_worldSize;
+    uint3 m_worldCells;
+    uint m_k = 7, m_radius = 1;
+    std::unique_ptr<KNNBinData> m_bins;
+    std::unique_ptr<AgentGroup> m_group;
+    std::unique_ptr<KNNData> m_knn;
+};
+
+class ChokePointPlugIn : public HeadlessPlugIn {
+public:
+    const char* name() { return "ChokePoint"; }
+    // CtfWorld (ChokePointNew.cpp:103-120) and CtfGroup set-up
+    void open() {
+        const Params& p = params;
+        m_worldSize = f3param(p, "world", make_float3(512.f, 10.f, 512.f));
+        m_worldCells = u3param(p, "cells", make_uint3(256, 1, 256));
+        m_k = uparam(p, "k", 16);
+        m_knw = uparam(p, "knw", 3);
+        m_radius = uparam(p, "radius", 1);
+        m_bins.reset(new KNNBinData(m_worldCells, m_worldSize, m_radius));
+        m_walls.reset(new WallGroup(m_worldCells, m_knw));
+        auto it = p.find("map");
+        if (it == p.end() || !m_walls->LoadFromFile(it->second.c_str()))
+            throw std::runtime_error("ChokePoint needs map=<file.map>");
+        m_walls->SplitWalls(m_bins->hvCells());
+        m_walls->SyncDevice();
+        updateKNNDatabase(m_walls.get(), m_bins.get());
+        m_group.reset(new AgentGroup(m_worldCells, m_k));
+        for (const AgentData& a : read_state(in_path.c_str())) m_group->AddAgent(a);
+        m_group->SyncDevice();
+        m_knnSelf.reset(new KNNData(m_group->Size(), m_k));
+        m_knnWalls.reset(new KNNData(m_group->Size(), m_knw));
+    }
+    // CtfGroup::update (ChokePointNew.cpp:586-630), choke-point behaviours.
+    // The reference clears the applied bits with a cudaMemset before the KNN;
+    // updateGroup leaves them cleared after every frame, and the agents are
+    // added with none set, so that call has nothing to clear here.
+    void update(const float, const float elapsedTime) {
+        const Params& p = params;
+        AgentGroup* g = m_group.get();
+        wrapWorld(g, m_worldSize);
+        updateKNNDatabase(g, m_bins.get());
+        findKNearestNeighbors(g, m_knnSelf.get(), m_bins.get(), g, m_radius);
+        findKNearestNeighbors(g, m_knnWalls.get(), m_bins.get(), m_walls.get(), m_radius);
+        steerToAvoidWalls(g, m_knnWalls.get(), m_walls.get(), fparam(p, "min_time_wall", 10.f),
+                          fparam(p, "w_walls", 1.f), uparam(p, "mask_walls", 0));
+        steerToAvoidNeighbors(g, m_knnSelf.get(), g, fparam(p, "min_time_col", 2.f),
+                              fparam(p, "min_sep", 0.5f), uparam(p, "avoid_close", 0) != 0,
+                              fparam(p, "w_avoid", 1.f), uparam(p, "mask_avoid", 0));
+        steerForSeparation(g, m_knnSelf.get(), g, fparam(p, "sep_min", 0.5f),
+                           fparam(p, "sep_max", 1.2f), fparam(p, "sep_cos", -0.8660254f),
+                           fparam(p, "w_sep", 10.f), uparam(p, "mask_sep", KERNEL_ANTI_PENETRATION_WALL));
+        steerForSeek(g, f3param(p, "seek", make_float3(0.f, 0.f, -93.5f)), fparam(p, "w_seek", 1.5f),
+                     uparam(p, "mask_seek", 4480));
+        updateGroup(g, elapsedTime);
+    }
+    void redraw(const float, const float) { write_state(out_path.c_str(), *m_group); }
+    void close() {
+        m_knnSelf.reset();
+        m_knnWalls.reset();
+        m_group.reset();
+        m_walls.reset();
+        m_bins.reset();
+    }
+
+private:
+    float3 m_worldSize;
+    uint3 m_worldCells;
+    uint m_k = 16, m_knw = 3, m_radius = 1;
+    std::unique_ptr<KNNBinData> m_bins;
+    std::unique_ptr<WallGroup> m_walls;
+    std::unique_ptr<AgentGroup> m_group;
+    std::unique_ptr<KNNData> m_knnSelf, m_knnWalls;
+};
+
+BoidsPlugIn gBoidsPlugIn;
+ChokePointPlugIn gChokePointPlugIn;
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 5) {
+        std::fprintf(stderr,
+                     "usage: %s <Boids|ChokePoint> <state_in> <state_out> <frames> [key=value ...]\n",
+                     argv[0]);
+        return 2;
+    }
+    HeadlessPlugIn* plugin = static_cast<HeadlessPlugIn*>(PlugIn::findByName(argv[1]));
+    if (!plugin) {
+        std::fprintf(stderr, "unknown plugin %s\n", argv[1]);
+        return 2;
+    }
+    plugin->in_path = argv[2];
+    plugin->out_path = argv[3];
+    const unsigned frames = unsigned(std::strtoul(argv[4], nullptr, 10));
+    for (int i = 5; i < argc; ++i) {
+        const char* eq = std::strchr(argv[i], '=');
+        if (!eq) {
+            std::fprintf(stderr, "bad parameter %s\n", argv[i]);
+            return 2;
+        }
+        plugin->params[std::string(argv[i], size_t(eq - argv[i]))] = eq + 1;
+    }
+    try {
+        const float dt = fparam(plugin->params, "dt", 1.f / 60.f);
+        runHeadless(*plugin, frames, dt, frames ? frames : 1);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "%s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

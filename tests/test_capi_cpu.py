@@ -127,3 +127,58 @@ def test_step_params_struct_roundtrip():
     assert c.k == 16 and c.knw == 3 and c.n_order == 4
     assert list(c.order)[:4] == [1, 2, 3, 6]
     assert abs(c.dt - 1 / 30) < 1e-7 and c.mask_seek == 4480
+
+
+def test_cpp_facade_has_the_reference_signatures(tmp_path):
+    """include/GroupSteerLibrary.h declares the reference's free functions
+    with their parameter lists (GroupSteerLibrary.cuh:43-223); a plugin's
+    calls bind to them as written."""
+    import shutil
+    import subprocess
+
+    from gpusteer_gb300 import build as gb
+
+    src = tmp_path / "sig.cpp"
+    src.write_text(r'''
+#include "GroupSteerLibrary.h"
+using namespace OpenSteer;
+void (*a)(AgentGroup*, float3 const&) = wrapWorld;
+void (*b)(AgentGroup*, float3 const&, float const, uint const) = steerForSeek;
+void (*c)(AgentGroup*, KNNData*, AgentGroup*, const float, float const, bool const, float const,
+          uint const) = steerToAvoidNeighbors;
+void (*d)(AgentGroup*, KNNData*, WallGroup*, float const, float const, uint const) = steerToAvoidWalls;
+void (*e)(BaseGroup*, KNNBinData*) = updateKNNDatabase;
+void (*f)(AgentGroup*, KNNData*, KNNBinData*, BaseGroup*, uint const) = findKNearestNeighbors;
+void (*g1)(AgentGroup*, KNNData*, AgentGroup*, float const, float const, float const, float const,
+           uint const) = steerForSeparation;
+void (*g2)(AgentGroup*, KNNData*, AgentGroup*, float const, float const, float const, float const,
+           uint const) = steerForAlignment;
+void (*g3)(AgentGroup*, KNNData*, AgentGroup*, float const, float const, float const, float const,
+           uint const) = steerForCohesion;
+void (*h)(AgentGroup*, const float) = updateGroup;
+void (*i)(AgentGroup*, KNNData*, AgentGroup*, uint const) = antiPenetrationAgents;
+int main() {
+    AgentGroup* grp = nullptr;
+    (void)grp;
+    AgentData ad;
+    ad.id = 0;
+    ad.appliedKernels = KERNEL_SEPARATION_BIT | KERNEL_ANTI_PENETRATION_WALL;
+    return int(ad.appliedKernels & 1u);
+}
+''')
+    cuda_inc = Path(gb.nvcc()).resolve().parent.parent / "include"
+    cxx = shutil.which("g++")
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-fsyntax-only",
+                        "-I", str(REPO / "include"), "-I", str(cuda_inc), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_headless_driver_builds_and_links():
+    import subprocess
+
+    from gpusteer_gb300 import build as gb
+
+    gb.build()
+    r = subprocess.run([str(gb.HEADLESS)], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr

@@ -527,3 +527,71 @@ def test_graph_replay_equals_eager_single_group():
     gs.step(g2, bins, None, p, 4)
     gs.step(g2, bins, None, p, 8)
     assert_state(g2.download(), g1.download())
+
+
+# ---- MultiGroup: cross-group KNN and steering (plugins/MultiGroup.cpp:545-610) ------
+
+def test_multigroup_cross_group_steps_match_oracle():
+    """Two groups in one world, stepped as MultiGroupSimulation::update does:
+    every group wraps and rebuilds its database first (Group::preUpdate),
+    then each group in turn runs KNN against every group, avoids the other
+    group, separates from every group, aligns and coheres with itself and
+    integrates.  A later group's KNN reads an earlier group's database built
+    before that group moved, while the steering reads its current state."""
+    p = sc.boids_params(k=8, world=96.0, cell=4.0)
+    min_time, min_sep, w_avoid = 2.0, 0.5, 1.0
+    states = [sc.boids_sphere(3000, radius=18.0, seed=31), sc.boids_sphere(2000, radius=18.0, seed=32)]
+    G = len(states)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    groups = [group_of(s, p.k) for s in states]
+    knns = [[gs.KNNData(states[i].n, p.k) for _ in range(G)] for i in range(G)]
+    want = [s.copy() for s in states]
+    o = ol.oracle()
+    f = ol.C.c_float
+    for _ in range(6):
+        for g in groups:
+            gs.wrapWorld(g, p.world_size, sc.WRAP_REFERENCE)
+            gs.updateKNNDatabase(g, bins)
+        for s in want:
+            o.orc_wrap_world(ol.C.byref(ol.group_struct(s)), ol.f3(p.world_size), sc.WRAP_REFERENCE)
+        snap = [s.position.copy() for s in want]  # the databases' positions
+        for i, g in enumerate(groups):
+            for j, other in enumerate(groups):
+                gs.findKNearestNeighbors(g, knns[i][j], bins, other, 1)
+            lists = [ol.knn_binned(snap[i], snap[j], i == j, p.world_size, p.world_cells, 1, p.k)
+                     for j in range(G)]
+            for j in range(G):
+                gi, gd = knns[i][j].download(g)
+                np.testing.assert_array_equal(gi, lists[j][0])
+                np.testing.assert_array_equal(gd, lists[j][1])
+            me = ol.group_struct(want[i])
+            for j, other in enumerate(groups):
+                if j == i:
+                    continue
+                gs.steerToAvoidNeighbors(g, knns[i][j], other, min_time, min_sep, 1, w_avoid, 0)
+                ob = want[j]
+                o.orc_steer_avoid_neighbors(
+                    ol.C.byref(me), ol.ptr(lists[j][0], ol.C.c_uint), ol.ptr(lists[j][1]), p.k,
+                    ol.ptr(ob.position), ol.ptr(ob.direction), ol.ptr(ob.speed), ol.ptr(ob.radius),
+                    ob.n, f(min_time), f(min_sep), 1, f(w_avoid), 0)
+            for j, other in enumerate(groups):
+                gs.steerForSeparation(g, knns[i][j], other, p.sep_min, p.sep_max, p.sep_cos,
+                                      p.w_sep, p.mask_sep)
+                ob = want[j]
+                o.orc_steer_separation(ol.C.byref(me), ol.ptr(lists[j][0], ol.C.c_uint), p.k,
+                                       ol.ptr(ob.position), ob.n, f(p.sep_min), f(p.sep_max),
+                                       f(p.sep_cos), f(p.w_sep), p.mask_sep)
+            gs.steerForAlignment(g, knns[i][i], g, p.ali_min, p.ali_max, p.ali_cos, p.w_ali,
+                                 p.mask_ali)
+            o.orc_steer_alignment(ol.C.byref(me), ol.ptr(lists[i][0], ol.C.c_uint), p.k,
+                                  ol.ptr(want[i].position), ol.ptr(want[i].direction), want[i].n,
+                                  f(p.ali_min), f(p.ali_max), f(p.ali_cos), f(p.w_ali), p.mask_ali)
+            gs.steerForCohesion(g, knns[i][i], g, p.coh_min, p.coh_max, p.coh_cos, p.w_coh,
+                                p.mask_coh)
+            o.orc_steer_cohesion(ol.C.byref(me), ol.ptr(lists[i][0], ol.C.c_uint), p.k,
+                                 ol.ptr(want[i].position), want[i].n, f(p.coh_min), f(p.coh_max),
+                                 f(p.coh_cos), f(p.w_coh), p.mask_coh)
+            gs.updateGroup(g, p.dt)
+            o.orc_update(ol.C.byref(me), f(p.dt))
+    for g, s in zip(groups, want):
+        assert_state(g.download(), s, skip_side=s.speed == 0)
