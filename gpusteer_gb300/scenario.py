@@ -188,6 +188,7 @@ def walls_from_rows(rows: np.ndarray):
 # ---- step parameters -----------------------------------------------------------
 
 B_AVOID_WALLS, B_AVOID_NEIGHBORS, B_SEPARATION, B_ALIGNMENT, B_COHESION, B_SEEK = 1, 2, 3, 4, 5, 6
+B_FOLLOW_PATH = 7
 WRAP_REFERENCE, WRAP_SYMMETRIC, WRAP_NONE = 0, 1, 2
 KNN_BINNED, KNN_BRUTEFORCE = 0, 1
 
@@ -233,6 +234,11 @@ class StepParams:
     mask_seek: int = 0
     order: tuple = (B_SEPARATION, B_COHESION, B_ALIGNMENT)
     dt: float = 1.0 / 60.0
+    # path following (ChokePoint.params: pathPredictionTime, weightFollowPath,
+    # maskFollowPath); the path itself is passed beside the parameters
+    path_prediction_time: float = 3.0
+    w_path: float = 1.0
+    mask_path: int = 0
 
     def replace(self, **kw) -> "StepParams":
         d = dict(self.__dict__)
@@ -424,7 +430,8 @@ def batched_chokepoint(n_scenes: int = 256, seed: int = 0, n_range=(1000, 20000)
 
 
 def default_steps(name: str) -> int:
-    return {"boids": 100, "chokepoint": 500, "large": 1000, "batched": 300, "adjoint": 64}[name]
+    return {"boids": 100, "chokepoint": 500, "large": 1000, "batched": 300, "adjoint": 64,
+            "brute": 20}[name]
 
 
 def isqrt_cells(world: float, cell: float) -> int:

@@ -93,6 +93,7 @@ constexpr unsigned AVOID_WALLS_BIT = 1u << 8;
 constexpr unsigned AVOID_NEIGHBORS_BIT = 1u << 9;
 constexpr unsigned AVOID_CLOSE_NEIGHBORS_BIT = 1u << 10;
 constexpr unsigned ANTI_PENETRATION_WALL = 1u << 12;
+constexpr unsigned FOLLOW_PATH_BIT = 1u << 11;
 
 inline int nthreads(int t) {
 #ifdef _OPENMP
@@ -310,6 +311,129 @@ template <class T> void seek(Group<T> g, V3<T> target, T w, unsigned mask, int t
         V3<T> steering = sub(desired, ld4<T>(g.direction, i));
         steering = mul(normalize(steering), w);
         if (!is_zero(steering)) g.applied[i] |= SEEK_BIT;
+        add_steering(g.steering, i, steering);
+    }
+}
+
+// ---- path following: SteerToFollowPathCUDAKernel.cu:35-287 ------------------
+template <class T> struct PathView {
+    const float* points;   // float3[n]
+    const float* lengths;  // [n]
+    const float* normals;  // float3[n]
+    unsigned n;
+    T radius;
+    bool cyclic;
+    T total;
+};
+// pointToSegmentDistance (:35-70): distance to the segment ep0-ep1, its
+// projection and the nearest point
+template <class T>
+inline T point_to_segment(V3<T> point, V3<T> ep0, V3<T> ep1, V3<T> normal, T seg_len, T& proj,
+                          V3<T>& chosen) {
+    const V3<T> local = sub(point, ep0);
+    proj = dot(normal, local);
+    if (proj < T(0)) {
+        chosen = ep0;
+        proj = 0;
+        return distance(point, ep0);
+    }
+    if (proj > seg_len) {
+        chosen = ep1;
+        proj = seg_len;
+        return distance(point, ep1);
+    }
+    chosen = add(ep0, mul(normal, proj));
+    return distance(point, chosen);
+}
+// mapPointToPathDistance (:72-100)
+template <class T> inline T map_point_to_path_distance(V3<T> point, const PathView<T>& P) {
+    T min_d = std::numeric_limits<T>::max(), total = 0, path_d = 0;
+    V3<T> chosen{0, 0, 0};
+    for (unsigned i = 1; i < P.n; ++i) {
+        const T seg_len = T(P.lengths[i]);
+        T proj;
+        const T d = point_to_segment(point, ld3<T>(P.points, i - 1), ld3<T>(P.points, i),
+                                     ld3<T>(P.normals, i), seg_len, proj, chosen);
+        if (d < min_d) {
+            min_d = d;
+            path_d = total + proj;
+        }
+        total += seg_len;
+    }
+    return path_d;
+}
+// mapPointToPath (:102-141): nearest point on the path, its segment's
+// direction, and how far outside the tube the point is
+template <class T>
+inline V3<T> map_point_to_path(V3<T> point, const PathView<T>& P, V3<T>& tangent, T& outside) {
+    T min_d = std::numeric_limits<T>::max();
+    V3<T> on_path{0, 0, 0}, chosen{0, 0, 0};
+    for (unsigned i = 1; i < P.n; ++i) {
+        T proj;
+        const T d = point_to_segment(point, ld3<T>(P.points, i - 1), ld3<T>(P.points, i),
+                                     ld3<T>(P.normals, i), T(P.lengths[i]), proj, chosen);
+        if (d < min_d) {
+            min_d = d;
+            on_path = chosen;
+            tangent = ld3<T>(P.normals, i);
+        }
+    }
+    outside = distance(on_path, point) - P.radius;
+    return on_path;
+}
+// mapPathDistanceToPoint (:143-181).  Decision (viii): when the segment walk
+// runs past the last segment (rounding), the path's last point is returned;
+// the reference returns an uninitialised value there.
+template <class T> inline V3<T> map_path_distance_to_point(T path_d, const PathView<T>& P) {
+    T remaining = path_d;
+    if (P.cyclic) {
+        remaining = std::fmod(path_d, P.total);
+    } else {
+        if (path_d < T(0)) return ld3<T>(P.points, 0);
+        if (path_d >= P.total) return ld3<T>(P.points, P.n - 1);
+    }
+    for (unsigned i = 1; i < P.n; ++i) {
+        const T seg_len = T(P.lengths[i]);
+        if (seg_len < remaining) {
+            remaining -= seg_len;
+        } else {
+            const T ratio = remaining / seg_len;
+            const V3<T> a = ld3<T>(P.points, i - 1), b = ld3<T>(P.points, i);
+            return add(a, mul(sub(b, a), ratio));  // interpolate (VectorUtils.cuh:292-295)
+        }
+    }
+    return ld3<T>(P.points, P.n - 1);
+}
+template <class T> PathView<T> path_view(const orc_path* p) {
+    return PathView<T>{p->points, p->lengths, p->normals, p->n, T(p->radius), p->cyclic != 0,
+                       T(p->total_length)};
+}
+
+// FollowPathCUDAKernel (:183-287)
+template <class T>
+void follow_path(Group<T> g, const PathView<T>& P, T prediction_time, T w, unsigned mask,
+                 int threads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (long long ii = 0; ii < (long long)g.n; ++ii) {
+        const size_t i = size_t(ii);
+        if (g.applied[i] & mask) continue;
+        const V3<T> pos = ld4<T>(g.position, i), dir = ld4<T>(g.direction, i);
+        const T speed = g.speed[i];
+        const T offset = prediction_time * speed;
+        const V3<T> future = add(pos, mul(mul(dir, speed), prediction_time));
+        const T now_d = map_point_to_path_distance(pos, P);
+        const T future_d = map_point_to_path_distance(future, P);
+        const bool rightway = (offset > T(0)) ? (now_d < future_d) : (now_d > future_d);
+        V3<T> tangent{0, 0, 0};
+        T outside;
+        map_point_to_path(future, P, tangent, outside);
+        V3<T> steering{0, 0, 0};
+        if (!((outside < T(0)) && rightway)) {
+            const V3<T> target = map_path_distance_to_point(now_d + offset, P);
+            steering = sub(sub(target, pos), dir);
+        }
+        steering = mul(normalize(steering), w);
+        if (!is_zero(steering)) g.applied[i] |= FOLLOW_PATH_BIT;
         add_steering(g.steering, i, steering);
     }
 }
@@ -606,6 +730,11 @@ int run_steps(Group<T> g, const orc_walls* walls, const orc_step_params* p, unsi
                     flock<T, T>(g, 2, idx.data(), k, g.position, g.direction, n, T(p->coh_min),
                                 T(p->coh_max), T(p->coh_cos), T(p->w_coh), p->mask_coh, threads);
                     break;
+                case ORC_B_FOLLOW_PATH:
+                    if (!p->path || p->path->n < 2) return -3;
+                    follow_path(g, path_view<T>(p->path), T(p->path_prediction_time),
+                                T(p->w_path), p->mask_path, threads);
+                    break;
                 case ORC_B_SEEK:
                     seek(g, V3<T>{T(p->seek_target[0]), T(p->seek_target[1]), T(p->seek_target[2])},
                          T(p->w_seek), p->mask_seek, threads);
@@ -739,6 +868,35 @@ void orc_steer_avoid_walls(orc_group* g, const unsigned* knw_idx, unsigned knw,
 }
 
 void orc_update(orc_group* g, float dt) { update(view<float>(g), dt, 0); }
+
+// PolylinePathwayCUDA::Initialize (PolylinePathwayCUDA.cu:17-56): binary32
+// host arithmetic, in the reference's order.
+int orc_path_init(const float* points3, unsigned n_in, int cyclic, float* points_out3,
+                  float* lengths_out, float* normals_out3, float* total_out) {
+    const unsigned n = n_in + (cyclic ? 1u : 0u);
+    float total = 0.f;
+    for (unsigned i = 0; i < n; ++i) {
+        const bool close_cycle = cyclic && i == n - 1;
+        const unsigned j = close_cycle ? 0 : i;
+        st3(points_out3, i, ld3<float>(points3, j));
+        if (i > 0) {
+            const V3<float> seg = sub(ld3<float>(points_out3, i), ld3<float>(points_out3, i - 1));
+            lengths_out[i] = length(seg);
+            st3(normals_out3, i, normalize(seg));
+            total += lengths_out[i];
+        } else {
+            lengths_out[0] = 0.f;
+            st3(normals_out3, 0, V3<float>{0.f, 0.f, 0.f});
+        }
+    }
+    *total_out = total;
+    return int(n);
+}
+
+void orc_steer_follow_path(orc_group* g, const orc_path* path, float prediction_time, float w,
+                           unsigned mask) {
+    follow_path(view<float>(g), path_view<float>(path), prediction_time, w, mask, 0);
+}
 
 // WallGroupData::LoadFromFile, WallGroupData.cu:73-106.
 int orc_walls_load(const char* path, float* start4, float* mid4, float* end4, float* normal4,

@@ -77,8 +77,22 @@ enum {
     ORC_B_SEPARATION      = 3,
     ORC_B_ALIGNMENT       = 4,
     ORC_B_COHESION        = 5,
-    ORC_B_SEEK            = 6
+    ORC_B_SEEK            = 6,
+    ORC_B_FOLLOW_PATH     = 7
 };
+
+/* A polyline pathway as PolylinePathwayCUDA holds it (PolylinePathwayCUDA.cu:17-56):
+ * n points (a cyclic path repeats the first point at the end), lengths[i] and
+ * unit normals[i] of the segment from point i-1 to point i (index 0 unused). */
+typedef struct orc_path {
+    const float* points;   /* float3[n] */
+    const float* lengths;  /* [n] */
+    const float* normals;  /* float3[n] */
+    unsigned     n;
+    float        radius;
+    int          cyclic;
+    float        total_length;
+} orc_path;
 
 /* Wrap modes. */
 enum {
@@ -121,6 +135,10 @@ typedef struct orc_step_params {
     unsigned order[8];
     unsigned n_order;
     float    dt;
+    /* path following (ChokePointNew.cpp:620) */
+    const orc_path* path;
+    float    path_prediction_time, w_path;
+    unsigned mask_path;
 } orc_step_params;
 
 /* ---- cells and KNN --------------------------------------------------- */
@@ -158,6 +176,15 @@ void orc_steer_avoid_walls(orc_group* g, const unsigned* knw_idx, unsigned knw,
                            const orc_walls* walls, float min_time, float w,
                            unsigned mask);
 void orc_update(orc_group* g, float dt);
+
+/* PolylinePathwayCUDA::Initialize: from n_in float3 points, writes the path's
+ * points, lengths and normals (n_in + cyclic entries, caller capacity n_in + 1)
+ * and its total length; returns the number of points. */
+int orc_path_init(const float* points3, unsigned n_in, int cyclic, float* points_out3,
+                  float* lengths_out, float* normals_out3, float* total_out);
+/* FollowPathCUDAKernel (SteerToFollowPathCUDAKernel.cu:183-287). */
+void orc_steer_follow_path(orc_group* g, const orc_path* path, float prediction_time, float w,
+                           unsigned mask);
 
 /* ---- walls (WallGroupData.cu:73-206) ---------------------------------- */
 /* Parse a .map file: 9 floats per segment (start, end, normal).

@@ -135,6 +135,7 @@ inline T tex3D(const texture<T, D, M>& t, float x, float y, float z) {
 #define OPENSTEER_STEERFORALIGNMENTCUDE_CUH
 #define OPENSTEER_ANTIPENETRATIONAGENTSCUDA_CUH
 #define UPDATECUDA_H
+#define OPENSTEER_STEERTOFOLLOWPATHCUDA_CUH     /* host wrapper class (AbstractCUDAKernel) */
 #define KNN_THREADSPERBLOCK 128                /* KNNBinDataV2.cuh:13 */
 
 #include <OpenSteer/CUDA/CUDAUtils.cuh>          /* OpenSteer::swap */

@@ -118,6 +118,9 @@ namespace ref_wrap { GSREF_DYNAMIC_SHARED
 namespace ref_antipen { GSREF_DYNAMIC_SHARED
 #include "AntiPenetrationAgentsCUDAKernel.cu"
 }
+namespace ref_path { GSREF_DYNAMIC_SHARED
+#include "SteerToFollowPathCUDAKernel.cu"
+}
 
 namespace {
 constexpr unsigned TPB = THREADSPERBLOCK;  // AbstractCUDAKernel.cuh:46-54
@@ -290,6 +293,20 @@ void gsref_seek(float* pos4, float* dir4, float* steer4, unsigned* applied, unsi
     const float3 t = make_float3(target[0], target[1], target[2]);
     launch(blocks(n, TPB), TPB, [&] {
         ref_seek::SteerForSeekCUDAKernel(f4(steer4), f4(pos4), f4(dir4), t, n, w, applied, mask);
+    });
+}
+
+// SteerToFollowPathCUDA::run, SteerToFollowPathCUDA.cu:45-81.  The path
+// arrays are the PolylinePathwayCUDA members (points/normals float3[n],
+// lengths[n]).
+void gsref_follow_path(float* pos4, float* dir4, float* speed, float* steer4, unsigned* applied,
+                       unsigned n, const float* points3, const float* lengths,
+                       const float* normals3, unsigned n_points, float radius, int cyclic,
+                       float total_length, float prediction_time, float w, unsigned mask) {
+    launch(blocks(n, TPB), TPB, [&] {
+        ref_path::FollowPathCUDAKernel(f4(pos4), f4(dir4), speed, f4(steer4), f3(points3), lengths,
+                                       f3(normals3), n_points, radius, cyclic != 0, total_length,
+                                       prediction_time, n, w, applied, mask);
     });
 }
 

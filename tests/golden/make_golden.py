@@ -248,6 +248,42 @@ def choke_steps(ref):
          wall_mid=walls[1], wall_end=walls[2], wall_normal=walls[3])
 
 
+PATH_CASES = [
+    # name, points, radius, cyclic, prediction time, weight, mask
+    ("line", [(0.0, 0.0, 13.5), (0.0, 0.0, -1650.0)], 20.0, 0, 5.0, 1.0, 16),  # ChokePoint.params
+    ("loop", [(-40.0, 0.0, -40.0), (40.0, 0.0, -40.0), (40.0, 0.0, 40.0), (-40.0, 0.0, 40.0)],
+     6.0, 1, 2.0, 1.5, 0),
+    ("bend", [(0.0, 0.0, 100.0), (0.0, 0.0, 0.0), (60.0, 0.0, -30.0), (60.0, 0.0, -200.0)],
+     4.0, 0, -1.0, 1.0, 0),
+]
+
+
+def path_case(ref):
+    """FollowPathCUDAKernel on 2D crowds around three paths: the choke
+    point's straight path, a cyclic square and a bent path followed with a
+    negative prediction time; some agents masked, some at speed 0."""
+    for ci, (name, pts, radius, cyclic, pt, w, mask) in enumerate(PATH_CASES):
+        s = sc.chokepoint_agents(1500, x_range=(-70.0, 70.0), z_range=(-120.0, 140.0),
+                                 seed=40 + ci)
+        u = sc.uniform01(50 + ci, 3 * s.n).reshape(3, s.n)
+        s.speed[:] = np.where(u[0] < 0.05, 0.0, 3.0 * u[1]).astype(np.float32)
+        s.steering[:, :3] = (sc.uniform01(60 + ci, 3 * s.n).reshape(s.n, 3) - 0.5).astype(np.float32)
+        s.applied[:] = np.where(u[2] < 0.25, 16, 0).astype(np.uint32)
+        P = ol.path_init(pts, radius, cyclic)
+        po, ln, nm, tot = P.arrays
+        po, ln, nm = np.ascontiguousarray(po), np.ascontiguousarray(ln), np.ascontiguousarray(nm)
+        out = s.copy()
+        ref.gsref_follow_path(fp(out.position), fp(out.direction), fp(out.speed), fp(out.steering),
+                              up(out.applied), out.n, fp(po), fp(ln), fp(nm), int(P.n),
+                              C.c_float(radius), int(cyclic), C.c_float(tot), C.c_float(pt),
+                              C.c_float(w), mask)
+        save(f"path_{name}", {"points": pts, "radius": radius, "cyclic": cyclic,
+                              "prediction_time": pt, "weight": w, "mask": mask},
+             path_points=po, path_lengths=ln, path_normals=nm,
+             path_total=np.array([tot], np.float32), **state_arrays("in_", s),
+             out_steering=out.steering, out_applied=out.applied)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -260,6 +296,7 @@ def main():
     avoid_case(ref)
     flock_steps(ref)
     choke_steps(ref)
+    path_case(ref)
 
 
 if __name__ == "__main__":

@@ -59,13 +59,39 @@ class OrcStepParams(C.Structure):
         ("w_coh", C.c_float), ("mask_coh", C.c_uint),
         ("seek_target", C.c_float * 3), ("w_seek", C.c_float), ("mask_seek", C.c_uint),
         ("order", C.c_uint * 8), ("n_order", C.c_uint), ("dt", C.c_float),
+        ("path", C.c_void_p), ("path_prediction_time", C.c_float), ("w_path", C.c_float),
+        ("mask_path", C.c_uint),
     ]
 
 
-def step_params_struct(p: StepParams) -> OrcStepParams:
+class OrcPath(C.Structure):
+    _fields_ = [("points", _fp), ("lengths", _fp), ("normals", _fp), ("n", C.c_uint),
+                ("radius", C.c_float), ("cyclic", C.c_int), ("total_length", C.c_float)]
+
+
+def path_init(points, radius, cyclic):
+    """PolylinePathwayCUDA::Initialize through the oracle: an OrcPath (with its
+    arrays kept alive on it) for float32 points (m, 3)."""
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    m = pts.shape[0]
+    po = np.zeros((m + 1, 3), np.float32)
+    ln = np.zeros(m + 1, np.float32)
+    nm = np.zeros((m + 1, 3), np.float32)
+    tot = C.c_float()
+    n = oracle().orc_path_init(ptr(pts), m, int(bool(cyclic)), ptr(po), ptr(ln), ptr(nm),
+                               C.byref(tot))
+    P = OrcPath()
+    P.points, P.lengths, P.normals = ptr(po), ptr(ln), ptr(nm)
+    P.n, P.radius, P.cyclic, P.total_length = n, float(radius), int(bool(cyclic)), tot.value
+    P._keep = (po, ln, nm)
+    P.arrays = (po[:n], ln[:n], nm[:n], tot.value)
+    return P
+
+
+def step_params_struct(p: StepParams, path=None) -> OrcStepParams:
     s = OrcStepParams()
     for name, _ in OrcStepParams._fields_:
-        if name in ("order", "n_order"):
+        if name in ("order", "n_order", "path"):
             continue
         v = getattr(p, name)
         if isinstance(v, (tuple, list)):
@@ -77,6 +103,9 @@ def step_params_struct(p: StepParams) -> OrcStepParams:
     for i, b in enumerate(p.order):
         s.order[i] = b
     s.n_order = len(p.order)
+    if path is not None:
+        s.path = C.cast(C.pointer(path), C.c_void_p)
+        s._keep_path = path
     return s
 
 
@@ -172,25 +201,26 @@ def knn_brute(posA, posB, self_, k, threads=0):
     return idx, dist
 
 
-def run(state: AgentState, p: StepParams, steps: int, walls=None, threads=0, want_knn=False):
-    """Advance `state` in place by `steps` oracle steps."""
+def run(state: AgentState, p: StepParams, steps: int, walls=None, threads=0, want_knn=False,
+        path=None):
+    """Advance `state` in place by `steps` oracle steps (path: an OrcPath)."""
     g = group_struct(state)
     w = walls_struct(*walls) if walls is not None else None
     idx = np.empty(p.k * state.n, np.uint32) if want_knn else None
     dist = np.empty(p.k * state.n, np.float32) if want_knn else None
     rc = oracle().orc_run(C.byref(g), C.byref(w) if w is not None else None,
-                          C.byref(step_params_struct(p)), steps,
+                          C.byref(step_params_struct(p, path)), steps,
                           ptr(idx, C.c_uint) if want_knn else None,
                           ptr(dist) if want_knn else None, threads)
     assert rc == 0, rc
     return (idx, dist) if want_knn else None
 
 
-def run_d(state64: AgentState, p: StepParams, steps: int, walls=None, threads=0):
+def run_d(state64: AgentState, p: StepParams, steps: int, walls=None, threads=0, path=None):
     g = group_struct_d(state64)
     w = walls_struct(*walls) if walls is not None else None
     rc = oracle().orc_run_d(C.byref(g), C.byref(w) if w is not None else None,
-                            C.byref(step_params_struct(p)), steps, threads)
+                            C.byref(step_params_struct(p, path)), steps, threads)
     assert rc == 0, rc
 
 

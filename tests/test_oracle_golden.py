@@ -182,3 +182,51 @@ def test_chokepoint_map_generator_matches_reference_files(gap):
     if not path.exists():
         pytest.skip("reference data not mounted")
     np.testing.assert_array_equal(sc.read_map(str(path)), sc.chokepoint_walls(float(gap)))
+
+
+# ---- path following (SteerToFollowPathCUDAKernel.cu, PolylinePathwayCUDA.cu) ----------
+
+def fixture_path(z, m):
+    P = ol.OrcPath()
+    po = np.ascontiguousarray(z["path_points"])
+    ln = np.ascontiguousarray(z["path_lengths"])
+    nm = np.ascontiguousarray(z["path_normals"])
+    P.points, P.lengths, P.normals = ol.ptr(po), ol.ptr(ln), ol.ptr(nm)
+    P.n, P.radius, P.cyclic = po.shape[0], m["radius"], m["cyclic"]
+    P.total_length = float(z["path_total"][0])
+    P._keep = (po, ln, nm)
+    return P
+
+
+@pytest.mark.parametrize("name", ["line", "loop", "bend"])
+def test_follow_path_matches_reference(name):
+    z, m = load(f"path_{name}")
+    s = state(z, "in_")
+    ol.oracle().orc_steer_follow_path(C.byref(ol.group_struct(s)), C.byref(fixture_path(z, m)),
+                                      C.c_float(m["prediction_time"]), C.c_float(m["weight"]),
+                                      m["mask"])
+    np.testing.assert_array_equal(s.steering, z["out_steering"])
+    np.testing.assert_array_equal(s.applied, z["out_applied"])
+    assert (s.applied & (1 << 11)).any(), "no agent steered"
+
+
+@pytest.mark.parametrize("name", ["line", "loop", "bend"])
+def test_path_initialize_restates_the_pathway(name):
+    """PolylinePathwayCUDA::Initialize: segment vectors, their lengths
+    (sqrt of the dot product) and unit normals, in binary32."""
+    z, m = load(f"path_{name}")
+    P = ol.path_init(m["points"], m["radius"], m["cyclic"])
+    po, ln, nm, tot = P.arrays
+    pts = np.array(m["points"], np.float32)
+    if m["cyclic"]:
+        pts = np.concatenate([pts, pts[:1]])
+    np.testing.assert_array_equal(po, pts)
+    seg = (pts[1:] - pts[:-1]).astype(np.float32)
+    lens = np.sqrt((seg[:, 0] * seg[:, 0] + seg[:, 1] * seg[:, 1]) + seg[:, 2] * seg[:, 2])
+    np.testing.assert_array_equal(ln[1:], lens)
+    np.testing.assert_array_equal(nm[1:], seg / lens[:, None])
+    total = np.float32(0)
+    for v in lens:
+        total = np.float32(total + v)
+    assert np.float32(tot) == total
+    np.testing.assert_array_equal(po, z["path_points"])
