@@ -42,6 +42,8 @@ WORKLOADS = {
     "large": "large plain flock: 1,048,576 3D boids in a 512^3 cube, k=16, cell 4.0",
     "chokepoint": "2D choke point: 10,000 agents, gap half-width 10, k=16, knw=3, cell 2.0",
     "boids": "plain 3D flock: 4,096 boids in a sphere of radius 50, k=7, cell 4.0",
+    "brute": "brute-force KNN: 65,536 agents uniform in a 512^3 cube, k=16, FP32 (one query "
+             "per agent against all agents)",
     "batched": "256 independent 2D choke-point scenes (gap half-widths 7.5..32.5, 1,000-20,000 "
                "agents each), k=16, knw=3, 512x512 world per scene, cell size (2.0 or larger), "
                "block shape and KNN capacity from the autotuner",
@@ -264,6 +266,8 @@ def run_reference(args, dist, rank):
         return
     if args.workload == "batched":
         return run_reference_batched(args)
+    if args.workload == "brute":
+        return run_reference_brute(args)
     state, p, walls_rows = make_workload(args.workload)
     sys.path.insert(0, str(REPO / "tests"))
     import oracle_lib as ol
@@ -296,6 +300,40 @@ def run_reference(args, dist, rank):
                          "sample": f"{steps} whole steps of the {state.n}-agent workload "
                                    f"(CPU oracle restating the reference kernels)"},
         "e2e": {"value": v, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_brute(args):
+    """The oracle's brute-force KNN on the host cores: a bounded sample of the
+    65,536 queries per step (about 10 s of work in all)."""
+    sys.path.insert(0, str(REPO / "tests"))
+    import oracle_lib as ol
+    from gpusteer_gb300 import scenario as sc
+
+    n, k = 65536, 16
+    pos = sc.boids_cube(n, size=512.0, seed=0).position
+    threads = ol.threads_available()
+    t0 = time.perf_counter()
+    ol.knn_brute(pos[:1024], pos, False, k, threads=threads)
+    per_query = (time.perf_counter() - t0) / 1024
+    m = int(max(256, min(n, 10.0 / max(1, args.steps) / max(per_query, 1e-9))))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ol.knn_brute(pos[:m], pos, False, k, threads=threads)
+    el = time.perf_counter() - t0
+    v = m * args.steps / el
+    line = {
+        "impl": "reference", "metric": "agent-queries/s", "value": v, "unit": "agent-queries/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps * n / m, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS["brute"], "agents": n, "k": k},
+        "cpu_baseline": {"value": v, "unit": "agent-queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{m} of the {n} queries per step against all {n} agents "
+                                   f"(CPU oracle restating KNNBruteForceCUDAV2, {threads} threads)"},
+        "e2e": {"value": v, "unit": "agent-queries/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -621,9 +659,119 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def fp32_peak_tflops():
+    """Measured FP32 peak: cuBLAS SGEMM with TF32 off (FP32 FMA pipe),
+    8192^3, best of 5, CUDA events."""
+    import torch
+
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        torch.matmul(a, b)
+        best = None
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def run_gpu_brute(args, dist, rank, world, local_rank):
+    """gs_knn_bruteforce (KNNBruteForceCUDAV2) over 65,536 agents, k = 16."""
+    import torch
+
+    import gpusteer_gb300 as gs
+    from gpusteer_gb300 import scenario as sc
+    from gpusteer_gb300._lib import check
+
+    lib = gs.load()
+    check(lib.gs_set_device(local_rank))
+    torch.cuda.set_device(local_rank)
+    n, k = 65536, 16
+    s = sc.boids_cube(n, size=512.0, seed=0)
+    g = gs.AgentGroup(k, n)
+    g.upload(s)
+    knn = gs.KNNData(n, k)
+    stream = torch.cuda.ExternalStream(g.stream)
+    for _ in range(args.warmup):
+        gs.findKNearestNeighborsBruteForce(g, knn, g)
+    g.synchronize()
+    barrier(dist)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            gs.findKNearestNeighborsBruteForce(g, knn, g)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.profiler.stop()
+    barrier(dist)
+    ms_max = allreduce_max(dist, ev0.elapsed_time(ev1))
+    per = ms_max / args.steps
+    pairs = float(n) * (n - 1)
+    tflops = 8.0 * pairs / (per / 1e3) / 1e12
+    peak = fp32_peak_tflops()
+    # end to end: positions up, lists down, every query
+    hp = s.copy()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, min(args.steps, 20))
+    for _ in range(e2e_steps):
+        g.upload(hp)
+        gs.findKNearestNeighborsBruteForce(g, knn, g)
+        knn.download(g)
+    e2e_s = allreduce_max(dist, time.perf_counter() - t0)
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        sys.path.insert(0, str(REPO / "tests"))
+        import oracle_lib as ol
+
+        threads = ol.threads_available()
+        sub = s.position[:4096]
+        t0 = time.perf_counter()
+        ol.knn_brute(sub, s.position, False, k, threads=threads)
+        el = time.perf_counter() - t0
+        cpu = {"value": 4096 / el, "unit": "agent-queries/s", "cores": threads, "kind": "port",
+               "sample": f"4,096 of the 65,536 queries against all 65,536 agents, CPU oracle, "
+                         f"{threads} threads"}
+    line = {
+        "metric": "agent-queries/s", "value": n * world / (per / 1e3), "unit": "agent-queries/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOADS["brute"], "agents": n, "k": k,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "1 MB of positions, L2-resident by design (compute-bound)"},
+        "e2e": {"value": n * e2e_steps * world / e2e_s, "unit": "agent-queries/s",
+                "h2d_bytes_per_step": n * 96, "d2h_bytes_per_step": n * k * 8},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp32", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": tflops / peak, "traffic": None, "kernel": "k_knn_brute3",
+                     "algorithmic_flops_per_launch": 8.0 * pairs,
+                     "peak_source": "measured here: cuBLAS SGEMM 8192^3 with TF32 off"},
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_gpu(args, dist, rank, world, local_rank):
     if args.workload == "batched":
         return run_gpu_batched(args, dist, rank, world, local_rank)
+    if args.workload == "brute":
+        return run_gpu_brute(args, dist, rank, world, local_rank)
     import torch
 
     import gpusteer_gb300 as gs

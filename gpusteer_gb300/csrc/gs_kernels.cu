@@ -10,6 +10,7 @@
 // total order (distance, agent index).
 #include "gs_behaviours.cuh"
 #include "gs_knn.cuh"
+
 #include "gs_launch.h"
 
 namespace gs {
@@ -337,18 +338,151 @@ __global__ void __launch_bounds__(kBlock) k_knn_brute(const float4* __restrict__
     });
 }
 
+// ---- brute force, FP32-pipe form (k <= 32) ----------------------------------------------
+// One warp serves kBruteQW queries and keeps each query's exact (distance,
+// index) top-k list spread over its lanes: lane r holds entry r, so the
+// list is sorted across the warp and its k-th key is one shuffle away.  The
+// block stages kBruteTile candidates in shared memory as x / y / z arrays;
+// each lane takes two neighbouring candidates per step and computes their
+// squared distances to every query of its warp with packed f32x2 subtract,
+// multiply and fused multiply-add.  Those squared distances only filter:
+// the warp votes on "within the rounded-up bound of a list's k-th distance"
+// and, when any lane says yes, every lane recomputes the candidate's distance
+// with the reference's unfused binary32 operations (KNNBruteForceCudaKernel.cu
+// :245-271) and the list takes it with one shuffle-and-select insertion.  The
+// packed d^2 differs from the unfused one by a few units in the last place,
+// far inside the bound's 4e-6 relative margin, so no candidate that belongs
+// in a list is filtered out; insertion is by the exact key, so the lists are
+// the reference's (distance, lower index) order.  After the first few
+// hundred candidates almost no step has a vote, so the warp runs the packed
+// arithmetic without divergence.
+constexpr unsigned kBruteWarps = 8;
+constexpr unsigned kBruteQW = 4;      // queries per warp
+constexpr unsigned kBruteTile = 2048; // candidates staged per block step
+
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// Inserts candidate (x, y, z, id) into the lane-distributed list `entry`
+// (lane r holds rank r < k) if its exact key is below the k-th; updates the
+// filter bound.  Every lane runs it with the same candidate.
+__device__ __forceinline__ void warp_list_insert(unsigned long long& entry, float& bound, V3 q,
+                                                 float x, float y, float z, unsigned id,
+                                                 unsigned k, unsigned lane) {
+    const unsigned long long key = knn_key(distance(q, v3(x, y, z)), id);
+    const unsigned long long kth = __shfl_sync(0xffffffffu, entry, int(k) - 1);
+    if (!(key < kth)) return;  // warp-uniform
+    const unsigned long long left = __shfl_up_sync(0xffffffffu, entry, 1);
+    if (lane < k && key < entry) entry = (lane == 0 || key > left) ? key : left;
+    bound = prefilter_bound(__shfl_sync(0xffffffffu, entry, int(k) - 1));
+}
+
+__global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
+    const float4* __restrict__ posA, unsigned nA, const float4* __restrict__ posB, unsigned nB,
+    bool self, unsigned k, unsigned* __restrict__ idx, float* __restrict__ dist) {
+    __shared__ __align__(16) float sx[kBruteTile], sy[kBruteTile], sz[kBruteTile];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned q0 = (blockIdx.x * kBruteWarps + warp) * kBruteQW;
+    V3 q[kBruteQW];
+    unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW], entry[kBruteQW];
+    float bound[kBruteQW];
+#pragma unroll
+    for (unsigned j = 0; j < kBruteQW; ++j) {
+        const bool act = q0 + j < nA;
+        q[j] = act ? v3(posA[q0 + j]) : v3(0.f, 0.f, 0.f);
+        px[j] = pack2(q[j].x, q[j].x);
+        py[j] = pack2(q[j].y, q[j].y);
+        pz[j] = pack2(q[j].z, q[j].z);
+        entry[j] = KEY_EMPTY;
+        bound[j] = act ? prefilter_bound(KEY_EMPTY) : -1.f;
+    }
+    const float inf = __int_as_float(0x7f800000);
+    for (unsigned base = 0; base < nB; base += kBruteTile) {
+        __syncthreads();
+        for (unsigned c = threadIdx.x; c < kBruteTile; c += blockDim.x) {
+            const float4 v = base + c < nB ? posB[base + c] : make_float4(inf, inf, inf, 0.f);
+            sx[c] = v.x;
+            sy[c] = v.y;
+            sz[c] = v.z;
+        }
+        __syncthreads();
+        const unsigned cnt = min(kBruteTile, nB - base);
+        for (unsigned t0 = 0; t0 < cnt; t0 += 64) {
+            const unsigned t = t0 + 2 * lane;
+            const unsigned long long x2 = *reinterpret_cast<const unsigned long long*>(sx + t);
+            const unsigned long long y2 = *reinterpret_cast<const unsigned long long*>(sy + t);
+            const unsigned long long z2 = *reinterpret_cast<const unsigned long long*>(sz + t);
+            bool hit[kBruteQW];
+            bool any = false;
+#pragma unroll
+            for (unsigned j = 0; j < kBruteQW; ++j) {
+                const unsigned long long dx = sub2(px[j], x2), dy = sub2(py[j], y2),
+                                         dz = sub2(pz[j], z2);
+                float e0, e1;
+                unpack2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))), e0, e1);
+                hit[j] = (e0 <= bound[j]) | (e1 <= bound[j]);
+                any |= hit[j];
+            }
+            if (!__any_sync(0xffffffffu, any)) continue;
+#pragma unroll
+            for (unsigned j = 0; j < kBruteQW; ++j) {
+                unsigned m = __ballot_sync(0xffffffffu, hit[j]);
+                while (m) {
+                    const unsigned src = unsigned(__ffs(m)) - 1u;
+                    m &= m - 1u;
+                    for (unsigned h = 0; h < 2; ++h) {
+                        const unsigned c = t0 + 2 * src + h;
+                        const unsigned id = base + c;
+                        if (c >= cnt || (self && id == q0 + j)) continue;
+                        warp_list_insert(entry[j], bound[j], q[j], sx[c], sy[c], sz[c], id, k,
+                                         lane);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (unsigned j = 0; j < kBruteQW; ++j) {
+        const unsigned qq = q0 + j;
+        if (qq < nA && lane < k) {
+            idx[qq + size_t(lane) * nA] = key_id(entry[j]);
+            dist[qq + size_t(lane) * nA] = key_dist(entry[j]);
+        }
+    }
+}
+
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
                            bool self, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
     if (nA == 0) return GS_OK;
-    const unsigned nb = blocks_for(nA);
-    if (k <= 8)
-        k_knn_brute<8><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
-    else if (k <= 16)
-        k_knn_brute<16><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
-    else if (k <= 32)
-        k_knn_brute<32><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
-    else
-        k_knn_brute<64><<<nb, kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
+    if (k <= 32) {
+        const unsigned per_block = kBruteWarps * kBruteQW;
+        k_knn_brute3<<<(nA + per_block - 1) / per_block, kBruteWarps * 32, 0, st>>>(
+            posA, nA, posB, nB, self, k, idx, dist);
+    } else {
+        k_knn_brute<64><<<blocks_for(nA), kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
+    }
     GS_LAUNCHED("knn_brute");
     return GS_OK;
 }
@@ -442,6 +576,30 @@ gs_status launch_seek(GroupView g, const float target[3], float w, unsigned mask
     if (g.n == 0) return GS_OK;
     k_seek<<<blocks_for(g.n), kBlock, 0, st>>>(g, target[0], target[1], target[2], w, mask);
     GS_LAUNCHED("steer_seek");
+    return GS_OK;
+}
+
+__global__ void k_follow_path(GroupView g, PathDev path, float prediction_time, float w,
+                              unsigned mask) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    unsigned applied = g.applied[i];
+    if (applied & mask) return;
+    Self me;
+    me.pos = v3(g.position[i]);
+    me.dir = v3(g.direction[i]);
+    me.speed = g.speed[i];
+    V3 steer = v3(g.steering[i]);
+    follow_path_finish(path, prediction_time, w, mask, me, applied, steer);
+    g.steering[i] = f4(steer, 0.f);
+    g.applied[i] = applied;
+}
+
+gs_status launch_follow_path(GroupView g, const PathDev& path, float prediction_time, float w,
+                             unsigned mask, cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_follow_path<<<blocks_for(g.n), kBlock, 0, st>>>(g, path, prediction_time, w, mask);
+    GS_LAUNCHED("steer_follow_path");
     return GS_OK;
 }
 

@@ -156,6 +156,43 @@ def test_knn_bruteforce_matches_oracle_larger():
         np.testing.assert_array_equal(d, od)
 
 
+@pytest.mark.parametrize("k", [1, 8, 16, 24, 32, 40])
+def test_knn_bruteforce_sizes_ties_and_cross_groups(k):
+    """Group sizes that are not multiples of the 64-query block or of the
+    eight candidate slices, an integer lattice with duplicated points (exact
+    distance ties, broken by the lower index), and a cross-group search."""
+    rng = np.random.default_rng(k)
+    g3 = np.stack(np.meshgrid(np.arange(9), np.arange(9), np.arange(9), indexing="ij"), -1)
+    lat = g3.reshape(-1, 3).astype(np.float32) - 4.0
+    lat = np.concatenate([lat, lat[::3]])                 # 972 points, duplicates
+    pa = np.zeros((lat.shape[0], 4), np.float32)
+    pa[:, :3] = lat
+    pb = np.zeros((1999, 4), np.float32)
+    pb[:, :3] = rng.uniform(-6, 6, (1999, 3)).astype(np.float32)
+    A, B = group_of(pos_state(pa)), group_of(pos_state(pb))
+    for (G, O, P, Q, self_) in ((A, A, pa, pa, True), (A, B, pa, pb, False), (B, A, pb, pa, False)):
+        knn = gs.KNNData(G.size, k)
+        gs.findKNearestNeighborsBruteForce(G, knn, O)
+        i, d = knn.download(G)
+        oi, od = ol.knn_brute(P, Q, self_, k)
+        np.testing.assert_array_equal(i, oi)
+        np.testing.assert_array_equal(d, od)
+
+
+def test_knn_bruteforce_fewer_candidates_than_k():
+    pa = np.zeros((70, 4), np.float32)
+    pa[:, 0] = np.arange(70, dtype=np.float32)
+    pb = pa[:5].copy()
+    A, B = group_of(pos_state(pa)), group_of(pos_state(pb))
+    knn = gs.KNNData(70, 16)
+    gs.findKNearestNeighborsBruteForce(A, knn, B)
+    i, d = knn.download(A)
+    oi, od = ol.knn_brute(pa, pb, False, 16)
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(d, od)
+    assert (i.reshape(16, 70)[5:] == 0xFFFFFFFF).all()
+
+
 # ---- behaviours, one per launch -----------------------------------------------------
 
 def test_flocking_stages_match_reference_golden():
@@ -595,3 +632,67 @@ def test_multigroup_cross_group_steps_match_oracle():
             o.orc_update(ol.C.byref(me), f(p.dt))
     for g, s in zip(groups, want):
         assert_state(g.download(), s, skip_side=s.speed == 0)
+
+
+# ---- path following (SteerToFollowPathCUDAKernel.cu, PolylinePathwayCUDA.cu) ----------
+
+@pytest.mark.parametrize("name", ["line", "loop", "bend"])
+def test_follow_path_matches_reference_golden(name):
+    z, m = load(f"path_{name}")
+    path = gs.Path(m["points"], m["radius"], m["cyclic"])
+    po, ln, nm, tot = path.arrays()
+    np.testing.assert_array_equal(po, z["path_points"])
+    np.testing.assert_array_equal(ln, z["path_lengths"])
+    np.testing.assert_array_equal(nm, z["path_normals"])
+    assert np.float32(tot) == z["path_total"][0]
+    s = gstate(z, "in_")
+    g = group_of(s)
+    gs.steerToFollowPath(g, path, m["prediction_time"], m["weight"], m["mask"])
+    out = g.download()
+    np.testing.assert_array_equal(out.steering, z["out_steering"])
+    np.testing.assert_array_equal(out.applied, z["out_applied"])
+
+
+def chokepoint_with_path():
+    """CtfGroup::update's behaviours (ChokePointNew.cpp:603-624): walls,
+    separation, alignment, cohesion, follow path, seek the path's second
+    point, update; path and weights of data/ChokePoint.params."""
+    pts = [(0.0, 0.0, 13.5), (0.0, 0.0, -1650.0)]
+    p = sc.chokepoint_params().replace(
+        order=(sc.B_AVOID_WALLS, sc.B_SEPARATION, sc.B_ALIGNMENT, sc.B_COHESION,
+               sc.B_FOLLOW_PATH, sc.B_SEEK),
+        ali_min=0.5, ali_max=7.0, w_ali=2.0, coh_min=0.5, coh_max=7.0, w_coh=1.0,
+        seek_target=pts[1], path_prediction_time=5.0, w_path=1.0, mask_path=16)
+    return p, pts, 20.0
+
+
+def test_fused_step_with_path_matches_dropin_and_oracle():
+    p, pts, radius = chokepoint_with_path()
+    s = sc.chokepoint_agents(8000, seed=13)
+    s.speed[:] = np.float32(1.0)
+    bins, walls = choke_walls(p)
+    path = gs.Path(pts, radius)
+    g = group_of(s, p.k)
+    gs.step(g, bins, walls, p, 25, path=path)
+    fused = g.download()
+    # the same frames through the per-function API
+    g2 = group_of(s, p.k)
+    knn = gs.KNNData(s.n, p.k)
+    knw = gs.KNNData(s.n, p.knw)
+    for _ in range(25):
+        gs.wrapWorld(g2, p.world_size, p.wrap_mode)
+        gs.updateKNNDatabase(g2, bins)
+        gs.findKNearestNeighbors(g2, knn, bins, g2, 1)
+        gs.findKNearestNeighbors(g2, knw, bins, walls, 1)
+        gs.steerToAvoidWalls(g2, knw, walls, p.min_time_to_wall, p.w_walls, p.mask_walls)
+        gs.steerForSeparation(g2, knn, g2, p.sep_min, p.sep_max, p.sep_cos, p.w_sep, p.mask_sep)
+        gs.steerForAlignment(g2, knn, g2, p.ali_min, p.ali_max, p.ali_cos, p.w_ali, p.mask_ali)
+        gs.steerForCohesion(g2, knn, g2, p.coh_min, p.coh_max, p.coh_cos, p.w_coh, p.mask_coh)
+        gs.steerToFollowPath(g2, path, p.path_prediction_time, p.w_path, p.mask_path)
+        gs.steerForSeek(g2, p.seek_target, p.w_seek, p.mask_seek)
+        gs.updateGroup(g2, p.dt)
+    assert_state(fused, g2.download())
+    want = s.copy()
+    ol.run(want, p, 25, walls=walls.download(), path=ol.path_init(pts, radius, False))
+    assert_state(fused, want)
+    assert (fused.position[:, 2] < s.position[:, 2]).mean() > 0.5  # heading down the path
