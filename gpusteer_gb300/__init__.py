@@ -7,10 +7,11 @@ GroupSteerLibrary free functions), seeded scenarios and the build step.
 """
 from ._lib import GpuSteerError, load  # noqa: F401
 from .groups import (  # noqa: F401
-    AgentGroup, Batch, KNNBinData, KNNData, Rollout, WallGroup, antiPenetrationAgents,
+    AgentGroup, Batch, KNNBinData, KNNData, Path, Rollout, WallGroup, antiPenetrationAgents,
     findKNearestNeighbors, findKNearestNeighborsBruteForce, set_block, set_graphs,
     set_knn_capacity, step, step_host, steerForAlignment, steerForCohesion,
-    steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, updateGroup,
+    steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, steerToFollowPath,
+    updateGroup,
     updateKNNDatabase, wrapWorld)
 from .scenario import StepParams  # noqa: F401
 from .state import AgentState  # noqa: F401

@@ -51,6 +51,7 @@ class StepParams(C.Structure):
         ("coh_min", _f), ("coh_max", _f), ("coh_cos", _f), ("w_coh", _f), ("mask_coh", _u),
         ("seek_target", _f * 3), ("w_seek", _f), ("mask_seek", _u),
         ("order", _u * 8), ("n_order", _u), ("dt", _f),
+        ("path", _vp), ("path_prediction_time", _f), ("w_path", _f), ("mask_path", _u),
     ]
 
 
@@ -115,6 +116,10 @@ SIGNATURES = {
     "gs_batch_group": [_vp, C.POINTER(_vp)],
     "gs_batch_step": [_vp, C.POINTER(StepParams), _u],
     "gs_knn_binned_noalloc": [_vp, _u, _up, _fp, _u, _u, _vp, _vp, _vp],
+    "gs_path_create": [_fp, _u, _f, _i, C.POINTER(_vp)],
+    "gs_path_destroy": [_vp],
+    "gs_path_get": [_vp, _fp, _fp, _fp, _u, _up, _fp],
+    "gs_steer_to_follow_path": [_vp, _vp, _f, _f, _u],
     "gs_rollout_create": [_vp, _vp, _u, _u, C.POINTER(_vp)],
     "gs_rollout_destroy": [_vp],
     "gs_rollout_forward": [_vp, C.POINTER(StepParams)],

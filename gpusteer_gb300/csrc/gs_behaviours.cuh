@@ -89,6 +89,117 @@ GS_HD void seek_finish(V3 target, float w, unsigned mask, const Self& s, unsigne
     steer = add(r, steer);
 }
 
+// ---- FollowPathCUDAKernel (SteerToFollowPathCUDAKernel.cu:35-287) -------------------
+// A polyline pathway on the device: points, segment lengths and unit segment
+// directions (index i describes the segment from point i-1 to point i).
+struct PathDev {
+    const float3* points;
+    const float* lengths;
+    const float3* normals;
+    unsigned n;
+    float radius;
+    int cyclic;
+    float total;
+};
+
+GS_HD V3 path_point(const PathDev& P, unsigned i) {
+    const float3 v = P.points[i];
+    return v3(v.x, v.y, v.z);
+}
+GS_HD V3 path_normal(const PathDev& P, unsigned i) {
+    const float3 v = P.normals[i];
+    return v3(v.x, v.y, v.z);
+}
+// Distance from `point` to segment i (1 <= i < n), its clamped projection
+// along the segment and the nearest point (:35-70).
+GS_HD float segment_distance(const PathDev& P, unsigned i, V3 point, float& proj, V3& nearest) {
+    const V3 a = path_point(P, i - 1), nrm = path_normal(P, i);
+    const float len = P.lengths[i];
+    proj = dot(nrm, sub(point, a));
+    if (proj < 0.f) {
+        proj = 0.f;
+        nearest = a;
+    } else if (proj > len) {
+        proj = len;
+        nearest = path_point(P, i);
+    } else {
+        nearest = add(a, mul(nrm, proj));
+    }
+    return distance(point, nearest);
+}
+// Path distance of the point's nearest path point, first nearest segment (:72-100).
+GS_HD float path_distance_of(const PathDev& P, V3 point) {
+    float best = FLT_MAX, walked = 0.f, along = 0.f;
+    for (unsigned i = 1; i < P.n; ++i) {
+        float proj;
+        V3 nearest;
+        const float d = segment_distance(P, i, point, proj, nearest);
+        if (d < best) {
+            best = d;
+            along = walked + proj;
+        }
+        walked += P.lengths[i];
+    }
+    return along;
+}
+// Nearest path point and how far `point` is outside the tube (:102-141).
+GS_HD V3 nearest_on_path(const PathDev& P, V3 point, float& outside) {
+    float best = FLT_MAX;
+    V3 on = v3(0.f, 0.f, 0.f);
+    for (unsigned i = 1; i < P.n; ++i) {
+        float proj;
+        V3 nearest;
+        const float d = segment_distance(P, i, point, proj, nearest);
+        if (d < best) {
+            best = d;
+            on = nearest;
+        }
+    }
+    outside = distance(on, point) - P.radius;
+    return on;
+}
+// The point at a path distance (:143-181); past the last segment (only by
+// rounding) it is the last point, where the reference leaves a value unset.
+GS_HD V3 point_at_path_distance(const PathDev& P, float along) {
+    float rest = along;
+    if (P.cyclic) {
+        rest = fmodf(along, P.total);
+    } else {
+        if (along < 0.f) return path_point(P, 0);
+        if (along >= P.total) return path_point(P, P.n - 1);
+    }
+    for (unsigned i = 1; i < P.n; ++i) {
+        const float len = P.lengths[i];
+        if (len < rest) {
+            rest -= len;
+            continue;
+        }
+        const V3 a = path_point(P, i - 1), b = path_point(P, i);
+        return add(a, mul(sub(b, a), rest / len));
+    }
+    return path_point(P, P.n - 1);
+}
+// The behaviour for one agent (:183-287): seek a point `prediction_time *
+// speed` further along the path unless the predicted position is inside the
+// tube and moving the right way.
+GS_HD void follow_path_finish(const PathDev& P, float prediction_time, float w, unsigned mask,
+                              const Self& s, unsigned& applied, V3& steer) {
+    if (applied & mask) return;
+    const float ahead = prediction_time * s.speed;
+    const V3 future = add(s.pos, mul(mul(s.dir, s.speed), prediction_time));
+    const float now_d = path_distance_of(P, s.pos);
+    const float future_d = path_distance_of(P, future);
+    const bool rightway = (ahead > 0.f) ? (now_d < future_d) : (now_d > future_d);
+    float outside;
+    nearest_on_path(P, future, outside);
+    V3 r = v3(0.f, 0.f, 0.f);
+    if (!((outside < 0.f) && rightway))
+        r = sub(sub(point_at_path_distance(P, now_d + ahead), s.pos), s.dir);
+    r = mul(normalize(r), w);
+    if (!is_zero(r)) applied |= FOLLOW_PATH_BIT;
+    steer = add(r, steer);
+}
+
 // ---- SteerToAvoidCloseNeighborsCUDAKernel (SteerToAvoidNeighborsCUDAKernel.cu:93-187)
 struct CloseAcc {
     bool found;

@@ -303,6 +303,17 @@ static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev&
             case GS_B_ALIGNMENT: d.need |= NEED_ALI; break;
             case GS_B_COHESION: d.need |= NEED_COH; break;
             case GS_B_SEEK: break;
+            case GS_B_FOLLOW_PATH: {
+                const gs_path P = p->path;
+                if (!P || P->n < 2)
+                    return fail(GS_ERR_INVALID_ARG, "follow-path needs a path of 2+ points");
+                d.path = PathDev{P->d_points, P->d_lengths, P->d_normals, P->n, P->radius,
+                                 P->cyclic, P->total};
+                d.path_time = p->path_prediction_time;
+                d.w_path = p->w_path;
+                d.mask_path = p->mask_path;
+                break;
+            }
             default: return fail(GS_ERR_INVALID_ARG, "unknown behaviour code");
         }
     }
@@ -852,6 +863,98 @@ gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float mi
                                 float max_distance, float cos_max_angle, float weight,
                                 unsigned mask) {
     return flock_call(2, g, knn, other, min_distance, max_distance, cos_max_angle, weight, mask);
+}
+
+// ---- PolylinePathwayCUDA ------------------------------------------------------------
+gs_status gs_path_create(const float* points3, unsigned n_in, float radius, int cyclic,
+                         gs_path* out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "null output handle");
+    *out = nullptr;
+    if (!points3 || n_in == 0) return fail(GS_ERR_INVALID_ARG, "a path needs points");
+    if (!std::isfinite(radius)) return fail(GS_ERR_NONFINITE, "radius is not finite");
+    for (unsigned i = 0; i < 3 * n_in; ++i)
+        if (!std::isfinite(points3[i])) return fail(GS_ERR_NONFINITE, "path point not finite");
+    gs_path P = new (std::nothrow) gs_path_s();
+    if (!P) return fail(GS_ERR_OOM, "host allocation failed");
+    // PolylinePathwayCUDA::Initialize: binary32, the reference's operation order
+    const unsigned n = n_in + (cyclic ? 1u : 0u);
+    P->n = n;
+    P->radius = radius;
+    P->cyclic = cyclic ? 1 : 0;
+    P->h_points.assign(3 * size_t(n), 0.f);
+    P->h_lengths.assign(n, 0.f);
+    P->h_normals.assign(3 * size_t(n), 0.f);
+    float total = 0.f;
+    for (unsigned i = 0; i < n; ++i) {
+        const unsigned j = (cyclic && i == n - 1) ? 0u : i;
+        for (int c = 0; c < 3; ++c) P->h_points[3 * i + c] = points3[3 * j + c];
+        if (i == 0) continue;
+        const float sx = P->h_points[3 * i] - P->h_points[3 * i - 3];
+        const float sy = P->h_points[3 * i + 1] - P->h_points[3 * i - 2];
+        const float sz = P->h_points[3 * i + 2] - P->h_points[3 * i - 1];
+        const float len = std::sqrt(((sx * sx) + (sy * sy)) + (sz * sz));
+        P->h_lengths[i] = len;
+        const bool nz = len > 0.f;
+        P->h_normals[3 * i] = nz ? sx / len : sx;
+        P->h_normals[3 * i + 1] = nz ? sy / len : sy;
+        P->h_normals[3 * i + 2] = nz ? sz / len : sz;
+        total += len;
+    }
+    P->total = total;
+    gs_status s = dalloc(&P->d_points, n);
+    if (s == GS_OK) s = dalloc(&P->d_lengths, n);
+    if (s == GS_OK) s = dalloc(&P->d_normals, n);
+    if (s == GS_OK &&
+        (cudaMemcpy(P->d_points, P->h_points.data(), size_t(n) * 12, cudaMemcpyHostToDevice) !=
+             cudaSuccess ||
+         cudaMemcpy(P->d_lengths, P->h_lengths.data(), size_t(n) * 4, cudaMemcpyHostToDevice) !=
+             cudaSuccess ||
+         cudaMemcpy(P->d_normals, P->h_normals.data(), size_t(n) * 12, cudaMemcpyHostToDevice) !=
+             cudaSuccess))
+        s = fail(GS_ERR_CUDA, "path upload");
+    if (s != GS_OK) {
+        gs_path_destroy(P);
+        return s;
+    }
+    *out = P;
+    return GS_OK;
+}
+
+gs_status gs_path_destroy(gs_path P) {
+    if (!P) return GS_OK;
+    dfree(P->d_points);
+    dfree(P->d_lengths);
+    dfree(P->d_normals);
+    delete P;
+    return GS_OK;
+}
+
+gs_status gs_path_get(gs_path P, float* points3, float* lengths, float* normals3, unsigned cap,
+                      unsigned* n, float* total_length) {
+    if (!P) return fail(GS_ERR_INVALID_ARG, "null path");
+    if (n) *n = P->n;
+    if (total_length) *total_length = P->total;
+    if ((points3 || lengths || normals3) && cap < P->n)
+        return fail(GS_ERR_INVALID_ARG, "path arrays too small");
+    if (points3) std::memcpy(points3, P->h_points.data(), size_t(P->n) * 12);
+    if (lengths) std::memcpy(lengths, P->h_lengths.data(), size_t(P->n) * 4);
+    if (normals3) std::memcpy(normals3, P->h_normals.data(), size_t(P->n) * 12);
+    return GS_OK;
+}
+
+gs_status gs_steer_to_follow_path(gs_group g, gs_path P, float prediction_time, float weight,
+                                  unsigned mask) {
+    if (!g || !P) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (P->n < 2) return fail(GS_ERR_INVALID_ARG, "follow-path needs a path of 2+ points");
+    if (!std::isfinite(prediction_time) || !std::isfinite(weight))
+        return fail(GS_ERR_NONFINITE, "non-finite parameter");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_follow_path(view(g),
+                              PathDev{P->d_points, P->d_lengths, P->d_normals, P->n, P->radius,
+                                      P->cyclic, P->total},
+                              prediction_time, weight, mask, g->stream));
+    touched(g);
+    return GS_OK;
 }
 
 gs_status gs_steer_for_seek(gs_group g, const float target[3], float weight, unsigned mask) {

@@ -93,7 +93,7 @@ struct FusedLaunchBytes {
     unsigned char b[384];
 };
 struct StepDevBytes {
-    unsigned char b[256];
+    unsigned char b[384];
 };
 
 // A group's bucketed binning database (KNNDatabase.cuh:30-38): cell of every
@@ -183,6 +183,18 @@ struct gs_group_s {
     gs::FusedLaunchBytes graph_L;
     gs::StepDevBytes graph_d;
     unsigned graph_C;
+};
+
+// PolylinePathwayCUDA: host arrays (binary32, PolylinePathwayCUDA.cu:17-56)
+// and their device copies.
+struct gs_path_s {
+    std::vector<float> h_points, h_lengths, h_normals;  // float3[n], [n], float3[n]
+    float3* d_points = nullptr;
+    float* d_lengths = nullptr;
+    float3* d_normals = nullptr;
+    unsigned n = 0;
+    float radius = 0.f, total = 0.f;
+    int cyclic = 0;
 };
 
 struct gs_batch_s {

@@ -1,6 +1,7 @@
 // Host-side launch wrappers shared by the C ABI implementation.
 #pragma once
 
+#include "gs_behaviours.cuh"
 #include "gs_internal.cuh"
 
 namespace gs {
@@ -50,6 +51,8 @@ gs_status launch_avoid_walls(GroupView g, const unsigned* knw, unsigned kw, cons
                              const float4* end, const float4* normal, unsigned n_lines,
                              float min_time, float w, unsigned mask, cudaStream_t st);
 gs_status launch_update(GroupView g, float dt, cudaStream_t st);
+gs_status launch_follow_path(GroupView g, const PathDev& path, float prediction_time, float w,
+                             unsigned mask, cudaStream_t st);
 gs_status launch_antipenetration(GroupView g, const unsigned* knn, const float* knn_dist,
                                  unsigned k, OtherView o, const unsigned* applied_snapshot,
                                  float4* pos_out, unsigned mask, cudaStream_t st);
@@ -73,6 +76,9 @@ struct StepDev {
     unsigned need;      // NEED_* bits
     unsigned enum_cap;  // candidate capacity of the fast KNN scan (32, 64: collecting; 128, 256: streaming)
     unsigned block;     // threads per block of the fused launches (0: 256)
+    PathDev path;       // path following (GS_B_FOLLOW_PATH)
+    float path_time, w_path;
+    unsigned mask_path;
 };
 constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
                    NEED_WALLS = 32;

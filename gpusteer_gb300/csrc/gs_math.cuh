@@ -57,6 +57,7 @@ constexpr unsigned COHESION_BIT = 1u << 6;
 constexpr unsigned AVOID_WALLS_BIT = 1u << 8;
 constexpr unsigned AVOID_NEIGHBORS_BIT = 1u << 9;
 constexpr unsigned AVOID_CLOSE_NEIGHBORS_BIT = 1u << 10;
+constexpr unsigned FOLLOW_PATH_BIT = 1u << 11;
 constexpr unsigned ANTI_PENETRATION_WALL = 1u << 12;
 constexpr unsigned ANTI_PENETRATION_AGENT = 1u << 13;
 

@@ -199,6 +199,9 @@ __device__ __forceinline__ void finish_all(const Accs& a, const StepDev& p, unsi
                 if (p.avoid_close) close_finish(a.close, p.w_avoid, p.mask_avoid, applied, steer);
                 avoid_finish(a.avoid, p.w_avoid, p.mask_avoid, me, applied, steer);
                 break;
+            case GS_B_FOLLOW_PATH:
+                follow_path_finish(p.path, p.path_time, p.w_path, p.mask_path, me, applied, steer);
+                break;
             default: break;
         }
     }

@@ -49,10 +49,11 @@ def host_arrays(s: AgentState) -> AgentArrays:
     return a
 
 
-def step_params_c(p: StepParams) -> _StepParamsC:
+def step_params_c(p: StepParams, path=None) -> _StepParamsC:
+    """The C parameter block; `path` (a Path) serves GS_B_FOLLOW_PATH."""
     s = _StepParamsC()
     for name, _ in _StepParamsC._fields_:
-        if name in ("order", "n_order"):
+        if name in ("order", "n_order", "path"):
             continue
         v = getattr(p, name)
         if isinstance(v, (tuple, list)):
@@ -66,7 +67,44 @@ def step_params_c(p: StepParams) -> _StepParamsC:
     for i, b in enumerate(p.order):
         s.order[i] = int(b)
     s.n_order = len(p.order)
+    if path is not None:
+        s.path = path.handle.value
     return s
+
+
+class Path:
+    """PolylinePathwayCUDA(points, radius, cyclic) (PolylinePathwayCUDA.cu:7-56)."""
+
+    def __init__(self, points, radius: float, cyclic: bool = False):
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        h = C.c_void_p()
+        call("gs_path_create", _ptr(pts), pts.shape[0], float(radius), int(bool(cyclic)),
+             C.byref(h))
+        self._h = h
+        self.radius = float(radius)
+        self.cyclic = bool(cyclic)
+        self.points_in = pts
+
+    @property
+    def handle(self):
+        return self._h
+
+    def arrays(self):
+        """(points (n, 3), lengths (n,), normals (n, 3), total length)."""
+        n = C.c_uint()
+        call("gs_path_get", self._h, None, None, None, 0, C.byref(n), None)
+        po = np.zeros((n.value, 3), np.float32)
+        ln = np.zeros(n.value, np.float32)
+        nm = np.zeros((n.value, 3), np.float32)
+        tot = np.zeros(1, np.float32)
+        call("gs_path_get", self._h, _ptr(po), _ptr(ln), _ptr(nm), n.value, C.byref(n),
+             _ptr(tot))
+        return po, ln, nm, float(tot[0])
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib._lib is not None:
+            _lib._lib.gs_path_destroy(self._h)
+            self._h = None
 
 
 class KNNBinData:
@@ -426,18 +464,23 @@ def antiPenetrationAgents(group, knn, other, do_not_apply_with=0) -> None:
          int(do_not_apply_with))
 
 
+def steerToFollowPath(group, path: Path, prediction_time, weight, do_not_apply_with=0) -> None:
+    call("gs_steer_to_follow_path", group.handle, path.handle, prediction_time, weight,
+         int(do_not_apply_with))
+
+
 def step(group: AgentGroup, bins: KNNBinData, walls: WallGroup | None, params: StepParams,
-         steps: int = 1) -> None:
-    """The fused whole step, `steps` times."""
-    p = step_params_c(params)
+         steps: int = 1, path: Path | None = None) -> None:
+    """The fused whole step, `steps` times (path: for GS_B_FOLLOW_PATH)."""
+    p = step_params_c(params, path)
     call("gs_step", group.handle, bins.handle, walls.handle if walls else None, C.byref(p),
          int(steps))
 
 
 def step_host(group: AgentGroup, bins: KNNBinData, walls, params: StepParams, steps: int,
-              state_in: AgentState, state_out: AgentState) -> None:
+              state_in: AgentState, state_out: AgentState, path: Path | None = None) -> None:
     """Upload from host arrays, `steps` fused steps, download into state_out."""
-    p = step_params_c(params)
+    p = step_params_c(params, path)
     a_in, a_out = host_arrays(state_in), host_arrays(state_out)
     call("gs_step_host", group.handle, bins.handle, walls.handle if walls else None, C.byref(p),
          int(steps), C.byref(a_in), state_in.n, C.byref(a_out))

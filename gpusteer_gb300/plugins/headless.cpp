@@ -13,7 +13,10 @@
 // The world (KNNBinData, WallGroup loaded from a .map file and split on the
 // bins) is built in open() as CtfWorld does (ChokePointNew.cpp:103-120).
 //
-//   gs_headless <Boids|ChokePoint> <state_in> <state_out> <frames> [key=value ...]
+//   ChokePointNew  CtfGroup::update as ChokePointNew.cpp:586-630 has it, with
+//               path following and anti-penetration (below)
+//
+//   gs_headless <Boids|ChokePoint|ChokePointNew> <state_in> <state_out> <frames> [key=value ...]
 //
 // State files: uint32 n, then position (4n f32), direction (4n), steering
 // (4n), side (3n), up (3n), speed, max_speed, max_force, radius, mass (n
@@ -258,15 +261,106 @@ private:
     std::unique_ptr<KNNData> m_knnSelf, m_knnWalls;
 };
 
+// CtfGroup::update as plugins/ChokePointNew.cpp:586-630 has it: walls,
+// separation, alignment, cohesion, path following, seek the path's second
+// point, update, anti-penetration between agents.  The path comes from the
+// parameters: path=x,y,z;x,y,z;...  path_radius=  path_cyclic=
+class ChokePointNewPlugIn : public HeadlessPlugIn {
+public:
+    const char* name() { return "ChokePointNew"; }
+    void open() {
+        const Params& p = params;
+        m_worldSize = f3param(p, "world", make_float3(512.f, 10.f, 512.f));
+        m_worldCells = u3param(p, "cells", make_uint3(256, 1, 256));
+        m_k = uparam(p, "k", 16);
+        m_knw = uparam(p, "knw", 3);
+        m_radius = uparam(p, "radius", 1);
+        m_bins.reset(new KNNBinData(m_worldCells, m_worldSize, m_radius));
+        m_walls.reset(new WallGroup(m_worldCells, m_knw));
+        auto it = p.find("map");
+        if (it == p.end() || !m_walls->LoadFromFile(it->second.c_str()))
+            throw std::runtime_error("ChokePointNew needs map=<file.map>");
+        m_walls->SplitWalls(m_bins->hvCells());
+        m_walls->SyncDevice();
+        updateKNNDatabase(m_walls.get(), m_bins.get());
+        std::vector<float3> pts;
+        auto pp = p.find("path");
+        if (pp == p.end()) throw std::runtime_error("ChokePointNew needs path=x,y,z;x,y,z...");
+        std::istringstream in(pp->second);
+        std::string item;
+        while (std::getline(in, item, ';')) {
+            std::istringstream v(item);
+            float3 q;
+            char c;
+            v >> q.x >> c >> q.y >> c >> q.z;
+            pts.push_back(q);
+        }
+        m_path.reset(new PolylinePathwayCUDA(pts, fparam(p, "path_radius", 20.f),
+                                             uparam(p, "path_cyclic", 0) != 0));
+        m_group.reset(new AgentGroup(m_worldCells, m_k));
+        for (const AgentData& a : read_state(in_path.c_str())) m_group->AddAgent(a);
+        m_group->SyncDevice();
+        m_knnSelf.reset(new KNNData(m_group->Size(), m_k));
+        m_knnWalls.reset(new KNNData(m_group->Size(), m_knw));
+    }
+    void update(const float, const float elapsedTime) {
+        const Params& p = params;
+        AgentGroup* g = m_group.get();
+        wrapWorld(g, m_worldSize);
+        updateKNNDatabase(g, m_bins.get());
+        findKNearestNeighbors(g, m_knnSelf.get(), m_bins.get(), g, m_radius);
+        findKNearestNeighbors(g, m_knnWalls.get(), m_bins.get(), m_walls.get(), m_radius);
+        steerToAvoidWalls(g, m_knnWalls.get(), m_walls.get(), fparam(p, "min_time_wall", 10.f),
+                          fparam(p, "w_walls", 1.f), uparam(p, "mask_walls", 0));
+        steerForSeparation(g, m_knnSelf.get(), g, fparam(p, "sep_min", 0.5f),
+                           fparam(p, "sep_max", 1.2f), fparam(p, "sep_cos", -0.8660254f),
+                           fparam(p, "w_sep", 10.f), KERNEL_ANTI_PENETRATION_WALL);
+        steerForAlignment(g, m_knnSelf.get(), g, fparam(p, "ali_min", 0.5f),
+                          fparam(p, "ali_max", 7.f), fparam(p, "ali_cos", -0.8660254f),
+                          fparam(p, "w_ali", 2.f), uparam(p, "mask_ali", 0));
+        steerForCohesion(g, m_knnSelf.get(), g, fparam(p, "coh_min", 0.5f),
+                         fparam(p, "coh_max", 7.f), fparam(p, "coh_cos", -0.8660254f),
+                         fparam(p, "w_coh", 1.f), uparam(p, "mask_coh", 0));
+        steerToFollowPath(g, m_path.get(), fparam(p, "path_time", 5.f), fparam(p, "w_path", 1.f),
+                          uparam(p, "mask_path", 16));
+        steerForSeek(g, m_path->hvPoints()[1], fparam(p, "w_seek", 1.5f),
+                     uparam(p, "mask_seek", 4480));
+        updateGroup(g, elapsedTime);
+        if (uparam(p, "antipen", 1))
+            antiPenetrationAgents(g, m_knnSelf.get(), g, uparam(p, "mask_antipen", 0));
+    }
+    void redraw(const float, const float) { write_state(out_path.c_str(), *m_group); }
+    void close() {
+        m_knnSelf.reset();
+        m_knnWalls.reset();
+        m_group.reset();
+        m_path.reset();
+        m_walls.reset();
+        m_bins.reset();
+    }
+
+private:
+    float3 m_worldSize;
+    uint3 m_worldCells;
+    uint m_k = 16, m_knw = 3, m_radius = 1;
+    std::unique_ptr<KNNBinData> m_bins;
+    std::unique_ptr<WallGroup> m_walls;
+    std::unique_ptr<PolylinePathwayCUDA> m_path;
+    std::unique_ptr<AgentGroup> m_group;
+    std::unique_ptr<KNNData> m_knnSelf, m_knnWalls;
+};
+
 BoidsPlugIn gBoidsPlugIn;
 ChokePointPlugIn gChokePointPlugIn;
+ChokePointNewPlugIn gChokePointNewPlugIn;
 
 }  // namespace
 
 int main(int argc, char** argv) {
     if (argc < 5) {
         std::fprintf(stderr,
-                     "usage: %s <Boids|ChokePoint> <state_in> <state_out> <frames> [key=value ...]\n",
+                     "usage: %s <Boids|ChokePoint|ChokePointNew> <state_in> <state_out> <frames> "
+                     "[key=value ...]\n",
                      argv[0]);
         return 2;
     }

@@ -9,9 +9,9 @@
  * namespace OpenSteer.  Differences:
  *   - errors throw OpenSteer::GpuSteerError (the reference aborts through
  *     CUDA_SAFE_CALL);
- *   - the behaviours outside the GB300 path (flee, pursuit, evade, path
- *     following, obstacle and wall anti-penetration) are not declared, so a
- *     plugin that calls them fails to compile rather than at run time;
+ *   - the behaviours outside the GB300 path (flee, pursuit, evade, stay-on-
+ *     path, obstacles, wall anti-penetration) are not declared, so a plugin
+ *     that calls them fails to compile rather than at run time;
  *   - WallGroup::SplitWalls takes the cell list of a KNNBinData made by this
  *     header (the split runs in the library, on that grid).
  * Results are bit-identical to the reference kernels' restatement (oracle/). */
@@ -512,6 +512,37 @@ private:
     std::vector<float> m_start, m_end, m_normal;
 };
 
+/* ---- PolylinePathwayCUDA (PolylinePathwayCUDA.cuh) ---------------------------------- */
+class PolylinePathwayCUDA {
+public:
+    PolylinePathwayCUDA(std::vector<float3> const& points, float const radius, bool const cyclic)
+        : m_points(points), m_radius(radius), m_cyclic(cyclic) {
+        std::vector<float> p3(points.size() * 3);
+        for (size_t i = 0; i < points.size(); ++i) {
+            p3[3 * i] = points[i].x;
+            p3[3 * i + 1] = points[i].y;
+            p3[3 * i + 2] = points[i].z;
+        }
+        gsCheck(gs_path_create(p3.data(), unsigned(points.size()), radius, cyclic ? 1 : 0,
+                               &m_path));
+    }
+    ~PolylinePathwayCUDA() { gs_path_destroy(m_path); }
+    PolylinePathwayCUDA(PolylinePathwayCUDA const&) = delete;
+    PolylinePathwayCUDA& operator=(PolylinePathwayCUDA const&) = delete;
+
+    /* The points as given (a cyclic path's closing point is not repeated). */
+    std::vector<float3> const& hvPoints() const { return m_points; }
+    float radius() const { return m_radius; }
+    bool cyclic() const { return m_cyclic; }
+    gs_path handle() const { return m_path; }
+
+private:
+    std::vector<float3> m_points;
+    float m_radius;
+    bool m_cyclic;
+    gs_path m_path = nullptr;
+};
+
 /* ---- the free functions (GroupSteerLibrary.cuh:43-223) ------------------------------ */
 namespace detail {
 inline gs_group group(AgentGroup* g) {
@@ -538,6 +569,13 @@ inline void steerForSeek(AgentGroup* pAgentGroup, float3 const& target, float co
     float t[3];
     detail::f3(target, t);
     gsCheck(gs_steer_for_seek(detail::group(pAgentGroup), t, fWeight, doNotApplyWith));
+}
+/* :88 */
+inline void steerToFollowPath(AgentGroup* pAgentGroup, PolylinePathwayCUDA* pPath,
+                              float const predictionTime, float const fWeight,
+                              uint const doNotApplyWith) {
+    gsCheck(gs_steer_to_follow_path(detail::group(pAgentGroup), pPath->handle(), predictionTime,
+                                    fWeight, doNotApplyWith));
 }
 /* :111 */
 inline void steerToAvoidNeighbors(AgentGroup* pAgentGroup, KNNData* pKNNData,

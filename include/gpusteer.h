@@ -44,6 +44,7 @@ typedef struct gs_bins_s* gs_bins;     /* KNNBinDataV2 (KNNBinDataV2.cuh:18-63) 
 typedef struct gs_group_s* gs_group;   /* AgentGroup + KNNDatabase (AgentGroup.h:12-56) */
 typedef struct gs_knn_s* gs_knn;       /* KNNData (KNNData.cuh:10-55)                   */
 typedef struct gs_walls_s* gs_walls;   /* WallGroup (WallGroup.h:12-37)                 */
+typedef struct gs_path_s* gs_path;     /* PolylinePathwayCUDA (PolylinePathwayCUDA.cuh)  */
 
 /* Pointers to one group's arrays (host or device, per the call). */
 typedef struct gs_agent_arrays {
@@ -72,6 +73,7 @@ typedef struct gs_agent_arrays {
 #define GS_B_ALIGNMENT 4
 #define GS_B_COHESION 5
 #define GS_B_SEEK 6
+#define GS_B_FOLLOW_PATH 7 /* needs gs_step_params.path */
 
 #define GS_KNN_BINNED 0
 #define GS_KNN_BRUTEFORCE 1
@@ -105,6 +107,11 @@ typedef struct gs_step_params {
     unsigned order[8];
     unsigned n_order;
     float dt;
+    /* path following (ChokePointNew.cpp:620: pathPredictionTime, weightFollowPath,
+     * maskFollowPath); path may be NULL when GS_B_FOLLOW_PATH is not in order */
+    gs_path path;
+    float path_prediction_time, w_path;
+    unsigned mask_path;
 } gs_step_params;
 
 /* ---- library -------------------------------------------------------------- */
@@ -214,6 +221,18 @@ gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float mi
                                 float max_distance, float cos_max_angle, float weight,
                                 unsigned do_not_apply_with);
 /* steerForSeek (GroupSteerLibrary.cuh:52-59). */
+/* ---- PolylinePathwayCUDA (PolylinePathwayCUDA.cu:7-56): n float3 points, tube
+ * radius, cyclic closes the loop.  Segment lengths, unit directions and the
+ * total length are computed on the host in binary32, as the reference does. */
+gs_status gs_path_create(const float* points3, unsigned n, float radius, int cyclic,
+                         gs_path* out);
+gs_status gs_path_destroy(gs_path path);
+/* The path's arrays (n + cyclic points; lengths[0] and normals[0] unused). */
+gs_status gs_path_get(gs_path path, float* points3, float* lengths, float* normals3,
+                      unsigned cap, unsigned* n, float* total_length);
+/* steerToFollowPath (GroupSteerLibrary.cuh:88, SteerToFollowPathCUDAKernel.cu:183-287). */
+gs_status gs_steer_to_follow_path(gs_group g, gs_path path, float prediction_time, float weight,
+                                  unsigned do_not_apply_with);
 gs_status gs_steer_for_seek(gs_group g, const float target[3], float weight,
                             unsigned do_not_apply_with);
 /* steerToAvoidNeighbors (GroupSteerLibrary.cuh:111-118). */

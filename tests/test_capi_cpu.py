@@ -157,6 +157,8 @@ void (*g3)(AgentGroup*, KNNData*, AgentGroup*, float const, float const, float c
            uint const) = steerForCohesion;
 void (*h)(AgentGroup*, const float) = updateGroup;
 void (*i)(AgentGroup*, KNNData*, AgentGroup*, uint const) = antiPenetrationAgents;
+void (*j)(AgentGroup*, PolylinePathwayCUDA*, float const, float const, uint const) =
+    steerToFollowPath;
 int main() {
     AgentGroup* grp = nullptr;
     (void)grp;

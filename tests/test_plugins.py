@@ -112,3 +112,60 @@ def test_chokepoint_plugin_equals_fused_step_and_oracle(tmp_path):
     for k in FIELDS:
         np.testing.assert_array_equal(getattr(got, k), getattr(fused, k), err_msg=k)
         np.testing.assert_array_equal(getattr(got, k), getattr(want, k), err_msg=k)
+
+
+def test_chokepoint_new_plugin_with_path_and_antipenetration(tmp_path):
+    """CtfGroup::update as ChokePointNew.cpp:586-630 runs it (path following,
+    seek to the path's second point, anti-penetration after the update):
+    without anti-penetration it equals the fused step and the oracle, with it
+    the per-function sequence through the Python binding."""
+    import test_gpu_parity as tp
+
+    p, pts, radius = tp.chokepoint_with_path()
+    s = sc.chokepoint_agents(6000, seed=17)
+    s.speed[:] = np.float32(1.0)
+    rows = sc.chokepoint_walls(10.0)
+    mp = tmp_path / "ChokePoint10.map"
+    mp.write_text("\n".join(" ".join(f32(x) for x in r) for r in rows) + "\n")
+    args = flock_args(p)
+    args.update({"knw": p.knw, "map": str(mp), "min_time_wall": f32(p.min_time_to_wall),
+                 "w_walls": f32(p.w_walls), "mask_walls": p.mask_walls,
+                 "path": ";".join(v3(q) for q in pts), "path_radius": f32(radius),
+                 "path_time": f32(p.path_prediction_time), "w_path": f32(p.w_path),
+                 "mask_path": p.mask_path, "w_seek": f32(p.w_seek), "mask_seek": p.mask_seek})
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    walls = gs.WallGroup(rows, bins=bins, knw=p.knw)
+    path = gs.Path(pts, radius)
+    # without anti-penetration: the fused step and the oracle
+    got = run_driver(tmp_path, "ChokePointNew", s, 20, dict(args, antipen=0))
+    g = gs.AgentGroup(p.k, s.n)
+    g.upload(s)
+    gs.step(g, bins, walls, p, 20, path=path)
+    fused = g.download()
+    want = s.copy()
+    ol.run(want, p, 20, walls=walls.download(), path=ol.path_init(pts, radius, False))
+    for k in FIELDS:
+        np.testing.assert_array_equal(getattr(got, k), getattr(fused, k), err_msg=k)
+        np.testing.assert_array_equal(getattr(got, k), getattr(want, k), err_msg=k)
+    # with anti-penetration: the per-function sequence
+    got = run_driver(tmp_path, "ChokePointNew", s, 20, dict(args, antipen=1))
+    g2 = gs.AgentGroup(p.k, s.n)
+    g2.upload(s)
+    knn = gs.KNNData(s.n, p.k)
+    knw = gs.KNNData(s.n, p.knw)
+    for _ in range(20):
+        gs.wrapWorld(g2, p.world_size, p.wrap_mode)
+        gs.updateKNNDatabase(g2, bins)
+        gs.findKNearestNeighbors(g2, knn, bins, g2, 1)
+        gs.findKNearestNeighbors(g2, knw, bins, walls, 1)
+        gs.steerToAvoidWalls(g2, knw, walls, p.min_time_to_wall, p.w_walls, p.mask_walls)
+        gs.steerForSeparation(g2, knn, g2, p.sep_min, p.sep_max, p.sep_cos, p.w_sep, p.mask_sep)
+        gs.steerForAlignment(g2, knn, g2, p.ali_min, p.ali_max, p.ali_cos, p.w_ali, p.mask_ali)
+        gs.steerForCohesion(g2, knn, g2, p.coh_min, p.coh_max, p.coh_cos, p.w_coh, p.mask_coh)
+        gs.steerToFollowPath(g2, path, p.path_prediction_time, p.w_path, p.mask_path)
+        gs.steerForSeek(g2, p.seek_target, p.w_seek, p.mask_seek)
+        gs.updateGroup(g2, p.dt)
+        gs.antiPenetrationAgents(g2, knn, g2, 0)
+    dropin = g2.download()
+    for k in FIELDS:
+        np.testing.assert_array_equal(getattr(got, k), getattr(dropin, k), err_msg=k)
