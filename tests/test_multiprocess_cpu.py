@@ -1,0 +1,63 @@
+"""The N > 1 path of bench.py on CPU: gloo ranks for the barrier and the
+max-over-ranks timing, and the reference arm under torchrun (rank 0 alone
+prints its line, the other ranks exit 0 without work).  No GPU."""
+import json
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+import torch.multiprocessing as mp
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+def free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    os.environ.update({"RANK": str(rank), "LOCAL_RANK": str(rank), "WORLD_SIZE": str(world),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, str(REPO))
+    import bench
+
+    dist, r, ws, lr = bench.dist_setup()
+    assert (r, ws, lr) == (rank, world, rank)
+    bench.barrier(dist)
+    m = bench.allreduce_max(dist, 1.5 + rank)
+    out.put((rank, m))
+    dist.destroy_process_group()
+
+
+def test_bench_ranks_agree_on_the_max_time():
+    world, port = 2, free_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(world))
+    assert got == [(0, 2.5), (1, 2.5)]
+
+
+def test_reference_arm_under_torchrun_prints_one_line():
+    port = free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), str(REPO / "bench.py"),
+           "--impl", "reference", "--workload", "boids", "--gpus", "2", "--steps", "1",
+           "--warmup", "3"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port"
