@@ -865,6 +865,45 @@ gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float mi
     return flock_call(2, g, knn, other, min_distance, max_distance, cos_max_angle, weight, mask);
 }
 
+// ---- ExtractData diagnostics ----------------------------------------------------------
+static gs_status diag_check(gs_group g, gs_bins bins) {
+    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (!g->db.valid || g->db.cells != bins->cells ||
+        std::memcmp(&g->db.grid, &bins->grid, sizeof(Grid)) != 0)
+        return fail(GS_ERR_STATE, "call gs_update_knn_database on this grid first");
+    return GS_OK;
+}
+
+gs_status gs_cell_density(gs_group g, gs_bins bins, unsigned* counts) {
+    GS_TRY(diag_check(g, bins));
+    if (!counts) return fail(GS_ERR_INVALID_ARG, "null output");
+    unsigned* d = nullptr;
+    GS_TRY(dalloc(&d, g->db.cells));
+    gs_status s = launch_cell_density(g->db, d, g->stream);
+    if (s == GS_OK && cudaMemcpyAsync(counts, d, size_t(g->db.cells) * 4, cudaMemcpyDeviceToHost,
+                                      g->stream) != cudaSuccess)
+        s = fail(GS_ERR_CUDA, "cell density copy");
+    if (cudaStreamSynchronize(g->stream) != cudaSuccess && s == GS_OK)
+        s = fail(GS_ERR_CUDA, "cell density");
+    dfree(d);
+    return s;
+}
+
+gs_status gs_cell_avg_velocity(gs_group g, gs_bins bins, float* avg3) {
+    GS_TRY(diag_check(g, bins));
+    if (!avg3) return fail(GS_ERR_INVALID_ARG, "null output");
+    float3* d = nullptr;
+    GS_TRY(dalloc(&d, g->db.cells));
+    gs_status s = launch_cell_avg_velocity(g->db, g->direction, g->speed, d, g->stream);
+    if (s == GS_OK && cudaMemcpyAsync(avg3, d, size_t(g->db.cells) * 12, cudaMemcpyDeviceToHost,
+                                      g->stream) != cudaSuccess)
+        s = fail(GS_ERR_CUDA, "cell velocity copy");
+    if (cudaStreamSynchronize(g->stream) != cudaSuccess && s == GS_OK)
+        s = fail(GS_ERR_CUDA, "cell velocity");
+    dfree(d);
+    return s;
+}
+
 // ---- PolylinePathwayCUDA ------------------------------------------------------------
 gs_status gs_path_create(const float* points3, unsigned n_in, float radius, int cyclic,
                          gs_path* out) {

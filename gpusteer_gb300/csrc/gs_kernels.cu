@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
             const unsigned long long x2 = *reinterpret_cast<const unsigned long long*>(sx + t);
             const unsigned long long y2 = *reinterpret_cast<const unsigned long long*>(sy + t);
             const unsigned long long z2 = *reinterpret_cast<const unsigned long long*>(sz + t);
-            bool hit[kBruteQW];
+            bool hit0[kBruteQW], hit1[kBruteQW];
             bool any = false;
 #pragma unroll
             for (unsigned j = 0; j < kBruteQW; ++j) {
@@ -442,17 +442,21 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
                                          dz = sub2(pz[j], z2);
                 float e0, e1;
                 unpack2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))), e0, e1);
-                hit[j] = (e0 <= bound[j]) | (e1 <= bound[j]);
-                any |= hit[j];
+                hit0[j] = e0 <= bound[j];
+                hit1[j] = e1 <= bound[j];
+                any |= hit0[j] | hit1[j];
             }
             if (!__any_sync(0xffffffffu, any)) continue;
+            // only the candidates that passed: the lane's first (h = 0) and
+            // second (h = 1) candidate have separate votes
 #pragma unroll
             for (unsigned j = 0; j < kBruteQW; ++j) {
-                unsigned m = __ballot_sync(0xffffffffu, hit[j]);
-                while (m) {
-                    const unsigned src = unsigned(__ffs(m)) - 1u;
-                    m &= m - 1u;
-                    for (unsigned h = 0; h < 2; ++h) {
+#pragma unroll
+                for (unsigned h = 0; h < 2; ++h) {
+                    unsigned m = __ballot_sync(0xffffffffu, h ? hit1[j] : hit0[j]);
+                    while (m) {
+                        const unsigned src = unsigned(__ffs(m)) - 1u;
+                        m &= m - 1u;
                         const unsigned c = t0 + 2 * src + h;
                         const unsigned id = base + c;
                         if (c >= cnt || (self && id == q0 + j)) continue;
@@ -484,6 +488,55 @@ gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, 
         k_knn_brute<64><<<blocks_for(nA), kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
     }
     GS_LAUNCHED("knn_brute");
+    return GS_OK;
+}
+
+// ---- ExtractData diagnostics (ProcessData.cu:132-237) -------------------------------------
+__global__ void k_cell_density(const unsigned* __restrict__ start, unsigned C,
+                               unsigned* __restrict__ out) {
+    const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < C) out[c] = start[c + 1] - start[c];
+}
+
+// A cell's agents are added in ascending index, the order the reference's
+// stable sort leaves them in; this database's counting sort orders a cell's
+// slots arbitrarily, so the cell's thread picks its agents by increasing
+// index (quadratic in the cell's count: a diagnostic, not a step kernel).
+__global__ void k_cell_avg_velocity(const unsigned* __restrict__ start,
+                                    const unsigned* __restrict__ sorted, unsigned C,
+                                    const float4* __restrict__ dir,
+                                    const float* __restrict__ speed, float3* __restrict__ out) {
+    const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const unsigned s0 = start[c], s1 = start[c + 1];
+    V3 sum = v3(0.f, 0.f, 0.f);
+    unsigned last = 0;
+    for (unsigned t = 0; t < s1 - s0; ++t) {
+        unsigned next = UINT_MAX;
+        for (unsigned s = s0; s < s1; ++s) {
+            const unsigned id = sorted[s];
+            if ((t == 0 || id > last) && id < next) next = id;
+        }
+        last = next;
+        sum = add(sum, mul(v3(dir[next]), speed[next]));
+    }
+    const V3 avg = s1 > s0 ? dvd(sum, float(s1 - s0)) : v3(0.f, 0.f, 0.f);
+    out[c] = make_float3(avg.x, avg.y, avg.z);
+}
+
+gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st) {
+    if (db.cells == 0) return GS_OK;
+    k_cell_density<<<blocks_for(db.cells), kBlock, 0, st>>>(db.start, db.cells, out);
+    GS_LAUNCHED("cell_density");
+    return GS_OK;
+}
+
+gs_status launch_cell_avg_velocity(const Database& db, const float4* dir, const float* speed,
+                                   float3* out, cudaStream_t st) {
+    if (db.cells == 0) return GS_OK;
+    k_cell_avg_velocity<<<blocks_for(db.cells), kBlock, 0, st>>>(db.start, db.sorted, db.cells,
+                                                                  dir, speed, out);
+    GS_LAUNCHED("cell_avg_velocity");
     return GS_OK;
 }
 

@@ -24,6 +24,9 @@ gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, b
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
                            bool self, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
 gs_status launch_wrap(float4* pos, unsigned n, const float ws[3], int mode, cudaStream_t st);
+gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st);
+gs_status launch_cell_avg_velocity(const Database& db, const float4* dir, const float* speed,
+                                   float3* out, cudaStream_t st);
 
 struct GroupView {
     float4 *position, *direction, *steering;

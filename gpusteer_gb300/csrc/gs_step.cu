@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
 
 // ---- wall phase: KNN, wall KNN and avoid-walls ---------------------------------------
 template <int KMAX, int KW, unsigned ENUM, bool EXACT>
-__global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDev p) {
+__global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDev p) {
     extern __shared__ unsigned sh_col[];
     const unsigned bd = blockDim.x;
     unsigned* col = sh_col + threadIdx.x;
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused_walls(FusedLaunch L, StepDe
 
 // ---- rest of the step after the wall phase --------------------------------------------
 template <int KMAX>
-__global__ void __launch_bounds__(kBlock, 3) k_fused_rest(FusedLaunch L, StepDev p) {
+__global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev p) {
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.n) return;
     const float4 w0 = L.w0[s], w1 = L.w1[s], w2 = L.w2[s];

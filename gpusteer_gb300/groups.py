@@ -464,6 +464,25 @@ def antiPenetrationAgents(group, knn, other, do_not_apply_with=0) -> None:
          int(do_not_apply_with))
 
 
+def cell_density(group: AgentGroup, bins: KNNBinData) -> np.ndarray:
+    """ComputeCellDensity (ProcessData.cu:74-101): agents per cell of the
+    group's database (updateKNNDatabase first)."""
+    n = C.c_uint()
+    call("gs_bins_num_cells", bins.handle, C.byref(n))
+    out = np.zeros(n.value, np.uint32)
+    call("gs_cell_density", group.handle, bins.handle, _ptr(out, C.c_uint))
+    return out
+
+
+def cell_avg_velocity(group: AgentGroup, bins: KNNBinData) -> np.ndarray:
+    """ComputeAvgCellVelocity (ProcessData.cu:103-134): mean velocity per cell."""
+    n = C.c_uint()
+    call("gs_bins_num_cells", bins.handle, C.byref(n))
+    out = np.zeros((n.value, 3), np.float32)
+    call("gs_cell_avg_velocity", group.handle, bins.handle, _ptr(out))
+    return out
+
+
 def steerToFollowPath(group, path: Path, prediction_time, weight, do_not_apply_with=0) -> None:
     call("gs_steer_to_follow_path", group.handle, path.handle, prediction_time, weight,
          int(do_not_apply_with))

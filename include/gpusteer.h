@@ -221,6 +221,15 @@ gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float mi
                                 float max_distance, float cos_max_angle, float weight,
                                 unsigned do_not_apply_with);
 /* steerForSeek (GroupSteerLibrary.cuh:52-59). */
+/* ---- ExtractData diagnostics: ComputeCellDensity / ComputeAvgCellVelocity
+ *      (ProcessData.cu:74-237, used by src/ExtractData.cpp).  On the group's KNN
+ *      database (gs_update_knn_database with these bins first): agents per cell,
+ *      and each cell's mean velocity (direction * speed summed in ascending agent
+ *      index, divided by the count; zero when empty).  Host outputs: one unsigned
+ *      / one float3 per cell.  Synchronous. */
+gs_status gs_cell_density(gs_group g, gs_bins bins, unsigned* counts);
+gs_status gs_cell_avg_velocity(gs_group g, gs_bins bins, float* avg3);
+
 /* ---- PolylinePathwayCUDA (PolylinePathwayCUDA.cu:7-56): n float3 points, tube
  * radius, cyclic closes the loop.  Segment lengths, unit directions and the
  * total length are computed on the host in binary32, as the reference does. */

@@ -794,6 +794,37 @@ void orc_cell_index(const float* pos4, unsigned n, const float ws[3], const unsi
     }
 }
 
+// ComputeCellDensityKernel (ProcessData.cu:132-160).
+void orc_cell_density(const float* pos4, unsigned n, const float ws[3], const unsigned wc[3],
+                      unsigned* counts_out) {
+    const size_t C = size_t(wc[0]) * wc[1] * wc[2];
+    std::fill(counts_out, counts_out + C, 0u);
+    for (unsigned i = 0; i < n; ++i) {
+        unsigned ix, iy, iz;
+        cell_coords(ld4<float>(pos4, i), ws, wc, ix, iy, iz);
+        counts_out[cell_label(ix, iy, iz, wc)]++;
+    }
+}
+
+// ComputeAvgCellVelocityKernel (ProcessData.cu:194-237): the database holds
+// each cell's agents in the stable sort's order, i.e. ascending index, so
+// visiting agents in index order and adding into their cell is that order.
+void orc_cell_avg_velocity(const float* pos4, const float* dir4, const float* speed, unsigned n,
+                           const float ws[3], const unsigned wc[3], float* avg3_out) {
+    const size_t C = size_t(wc[0]) * wc[1] * wc[2];
+    std::vector<V3<float>> sum(C, V3<float>{0.f, 0.f, 0.f});
+    std::vector<unsigned> cnt(C, 0u);
+    for (unsigned i = 0; i < n; ++i) {
+        unsigned ix, iy, iz;
+        cell_coords(ld4<float>(pos4, i), ws, wc, ix, iy, iz);
+        const unsigned c = cell_label(ix, iy, iz, wc);
+        sum[c] = add(sum[c], mul(ld4<float>(dir4, i), speed[i]));
+        cnt[c]++;
+    }
+    for (size_t c = 0; c < C; ++c)
+        st3(avg3_out, c, cnt[c] ? dvd(sum[c], float(cnt[c])) : V3<float>{0.f, 0.f, 0.f});
+}
+
 int orc_knn_binned(const float* posA4, unsigned nA, const float* posB4, unsigned nB,
                    int group_with_self, const float ws[3], const unsigned wc[3],
                    unsigned search_radius, unsigned k, unsigned* idx_out, float* dist_out,

@@ -154,6 +154,17 @@ int orc_knn_bruteforce(const float* posA4, unsigned nA, const float* posB4, unsi
                        int group_with_self, unsigned k, unsigned* idx_out,
                        float* dist_out, int threads);
 
+/* ---- ExtractData diagnostics (ProcessData.cu:132-237) ----------------- */
+/* Agents per cell of the binned database (cellEnd - cellStart, 0 when empty). */
+void orc_cell_density(const float* pos4, unsigned n, const float world_size[3],
+                      const unsigned world_cells[3], unsigned* counts_out);
+/* Each cell's mean velocity: direction * speed of its agents summed in the
+ * stable sort's order (ascending agent index), divided by the count; zero
+ * for an empty cell.  avg3_out holds a float3 per cell. */
+void orc_cell_avg_velocity(const float* pos4, const float* dir4, const float* speed, unsigned n,
+                           const float world_size[3], const unsigned world_cells[3],
+                           float* avg3_out);
+
 /* ---- behaviours (one reference kernel each) -------------------------- */
 void orc_wrap_world(orc_group* g, const float world_size[3], int mode);
 

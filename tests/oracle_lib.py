@@ -191,6 +191,25 @@ def knn_binned(posA, posB, self_, ws, wc, r, k, threads=0):
     return idx, dist
 
 
+def cell_index(pos, ws, wc):
+    out = np.empty(pos.shape[0], np.uint32)
+    oracle().orc_cell_index(ptr(pos), pos.shape[0], f3(ws), u3(wc), ptr(out, C.c_uint))
+    return out
+
+
+def cell_density(pos, ws, wc):
+    out = np.empty(int(np.prod(wc)), np.uint32)
+    oracle().orc_cell_density(ptr(pos), pos.shape[0], f3(ws), u3(wc), ptr(out, C.c_uint))
+    return out
+
+
+def cell_avg_velocity(pos, direction, speed, ws, wc):
+    out = np.empty((int(np.prod(wc)), 3), np.float32)
+    oracle().orc_cell_avg_velocity(ptr(pos), ptr(direction), ptr(speed), pos.shape[0], f3(ws),
+                                   u3(wc), ptr(out))
+    return out
+
+
 def knn_brute(posA, posB, self_, k, threads=0):
     nA, nB = posA.shape[0], posB.shape[0]
     idx = np.empty(k * nA, np.uint32)

@@ -696,3 +696,24 @@ def test_fused_step_with_path_matches_dropin_and_oracle():
     ol.run(want, p, 25, walls=walls.download(), path=ol.path_init(pts, radius, False))
     assert_state(fused, want)
     assert (fused.position[:, 2] < s.position[:, 2]).mean() > 0.5  # heading down the path
+
+
+# ---- ExtractData diagnostics ----------------------------------------------------------
+
+@pytest.mark.parametrize("case", ["crowd2d", "flock3d"])
+def test_cell_diagnostics_match_oracle(case):
+    if case == "crowd2d":
+        s = sc.chokepoint_agents(20000, seed=23)
+        s.speed[:] = (sc.uniform01(6, s.n) * 3.0).astype(np.float32)
+        ws, wc = (512.0, 10.0, 512.0), (256, 1, 256)
+    else:
+        s = sc.boids_sphere(30000, radius=40.0, seed=24)
+        ws, wc = (160.0, 160.0, 160.0), (40, 40, 40)
+    bins = gs.KNNBinData(wc, ws, 1)
+    g = group_of(s)
+    gs.updateKNNDatabase(g, bins)
+    from gpusteer_gb300.groups import cell_avg_velocity, cell_density
+
+    np.testing.assert_array_equal(cell_density(g, bins), ol.cell_density(s.position, ws, wc))
+    np.testing.assert_array_equal(cell_avg_velocity(g, bins),
+                                  ol.cell_avg_velocity(s.position, s.direction, s.speed, ws, wc))

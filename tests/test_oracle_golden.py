@@ -230,3 +230,25 @@ def test_path_initialize_restates_the_pathway(name):
         total = np.float32(total + v)
     assert np.float32(tot) == total
     np.testing.assert_array_equal(po, z["path_points"])
+
+
+# ---- ExtractData diagnostics (ProcessData.cu:132-237) ---------------------------------
+
+def test_cell_diagnostics_restate_processdata():
+    """Agents per cell and the mean cell velocity, summed in ascending agent
+    index (the stable sort's order) in binary32, against a plain loop."""
+    s = sc.chokepoint_agents(3000, seed=21)
+    s.speed[:] = (sc.uniform01(5, s.n) * 3.0).astype(np.float32)
+    ws, wc = (128.0, 10.0, 128.0), (64, 1, 64)
+    cells = ol.cell_index(s.position, ws, wc)
+    dens = ol.cell_density(s.position, ws, wc)
+    np.testing.assert_array_equal(dens, np.bincount(cells, minlength=64 * 64))
+    avg = ol.cell_avg_velocity(s.position, s.direction, s.speed, ws, wc)
+    acc = np.zeros((64 * 64, 3), np.float32)
+    for i in range(s.n):
+        acc[cells[i]] = (acc[cells[i]] + s.direction[i, :3] * s.speed[i]).astype(np.float32)
+    want = np.zeros_like(acc)
+    nz = dens > 0
+    want[nz] = acc[nz] / dens[nz].astype(np.float32)[:, None]
+    np.testing.assert_array_equal(avg, want)
+    assert dens.max() >= 5
