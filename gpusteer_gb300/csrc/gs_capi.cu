@@ -498,6 +498,9 @@ gs_status gs_group_destroy(gs_group g) {
     dfree(g->mass);
     dfree(g->applied);
     db_release(g->db);
+    db_release(g->bf_a);
+    db_release(g->bf_b);
+    dfree(g->bf_tmp);
     release_fused(g);
     if (g->prof_events) {
         prof_collect(g);
@@ -821,6 +824,37 @@ gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls
     return GS_OK;
 }
 
+// A grid centred on the origin that covers every position of the other
+// group (largest |coordinate| per axis).  Its cell count per axis with extent
+// depends on n alone (about two agents per cell for an even spread), so a
+// moving crowd keeps the same database; only the cell size follows the
+// extent.  False when the extent is not finite.
+static bool brute_seed_grid(const float ext[3], unsigned n, Grid& grid, unsigned& C) {
+    double w[3], wmax = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(ext[a])) return false;
+        w[a] = 2.0 * double(ext[a]) * 1.001 + 1e-6;
+        wmax = std::max(wmax, w[a]);
+    }
+    bool active[3];
+    int dims = 0;
+    for (int a = 0; a < 3; ++a) {
+        active[a] = w[a] > 1e-3 * wmax;
+        dims += active[a];
+    }
+    const double per_axis =
+        std::floor(std::pow(std::max(1.0, double(n) / 2.0), 1.0 / std::max(1, dims)));
+    unsigned long long cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        grid.wc[a] = active[a] ? unsigned(std::min(std::max(per_axis, 1.0), 1024.0)) : 1u;
+        grid.ws[a] = float(w[a]);
+        cells *= grid.wc[a];
+    }
+    if (cells > (1ull << 22)) return false;
+    C = unsigned(cells);
+    return true;
+}
+
 gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
     if (!g || !out || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
     if (out->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
@@ -829,8 +863,36 @@ gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
         GS_TRY(ensure_reference(other));
         GS_CUDA(cudaStreamSynchronize(other->stream));
     }
+    cudaStream_t st = g->stream;
+    const float* seed = nullptr;
+    // Seed every query's filter with the k-th distance among the candidates
+    // of its 3 x 3 x 3 cells on an automatic grid: the k-th distance among a
+    // subset of the candidates bounds the true one from above, so the full
+    // scan still sees every pair and gives the same lists.
+    if (out->k <= 32 && g->n >= 4096 && other->n > out->k) {
+        if (!g->bf_tmp) GS_TRY(dalloc(&g->bf_tmp, 4));
+        float ext[3];
+        GS_TRY(abs_extent(other->position, other->n, g->bf_tmp, ext, st));
+        Grid grid;
+        unsigned C = 0;
+        if (brute_seed_grid(ext, other->n, grid, C)) {
+            Database& A = g->bf_a;
+            Database& B = other == g ? g->bf_a : g->bf_b;
+            GS_TRY(db_reserve(A, g->capacity, C));
+            GS_TRY(db_build(A, g->position, g->n, grid, st));
+            if (other != g) {
+                // sized for the other group's capacity (it may differ per call)
+                if (B.cell != nullptr && B.agent_cap < other->capacity) db_release(B);
+                GS_TRY(db_reserve(B, other->capacity, C));
+                B.agent_cap = other->capacity;
+                GS_TRY(db_build(B, other->position, other->n, grid, st));
+            }
+            GS_TRY(launch_knn_binned(A, g->n, B, other == g, 1, out->k, out->idx, out->dist, st));
+            seed = out->dist + size_t(out->k - 1) * g->n;  // the k-th distance column
+        }
+    }
     GS_TRY(launch_knn_brute(g->position, g->n, other->position, other->n, other == g, out->k,
-                            out->idx, out->dist, g->stream));
+                            seed, out->idx, out->dist, st));
     return GS_OK;
 }
 

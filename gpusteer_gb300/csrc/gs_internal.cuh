@@ -108,6 +108,7 @@ struct Database {
     unsigned* start = nullptr;  // [C + 1]
     unsigned* count = nullptr;  // [C] zero between uses
     unsigned* tile = nullptr;   // scan scratch
+    unsigned agent_cap = 0;     // agents the per-agent arrays hold, where tracked
     bool valid = false;
     Grid grid{};
 };
@@ -152,6 +153,10 @@ struct gs_group_s {
     unsigned* knn_slot;    // [k * n] neighbour slots (wall phase)
     float* knn_dist;       // [k * n]
     gs::Database fdb;      // counts / starts of the fused step
+    // brute-force KNN's seed search: databases of the queries and of the
+    // other group on an automatic grid, and three words of scratch
+    gs::Database bf_a, bf_b;
+    unsigned* bf_tmp;
     gs::Scene* d_scene;    // scene table (one entry for a plain group)
     unsigned scene_alloc;
     std::vector<gs::Scene>* h_scenes;  // host copy of the table on the device

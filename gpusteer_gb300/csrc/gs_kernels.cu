@@ -8,6 +8,9 @@
 // bucketed order.  The order inside a cell follows the atomics and is not
 // deterministic; nothing downstream depends on it because every KNN uses the
 // total order (distance, agent index).
+#include <algorithm>
+#include <cstring>
+
 #include "gs_behaviours.cuh"
 #include "gs_knn.cuh"
 
@@ -192,6 +195,7 @@ void db_release(Database& db) {
     dfree(db.count);
     dfree(db.tile);
     db.cells = 0;
+    db.agent_cap = 0;
     db.valid = false;
 }
 
@@ -388,26 +392,37 @@ __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigne
 // Inserts candidate (x, y, z, id) into the lane-distributed list `entry`
 // (lane r holds rank r < k) if its exact key is below the k-th; updates the
 // filter bound.  Every lane runs it with the same candidate.
-__device__ __forceinline__ void warp_list_insert(unsigned long long& entry, float& bound, V3 q,
-                                                 float x, float y, float z, unsigned id,
-                                                 unsigned k, unsigned lane) {
+__device__ __forceinline__ void warp_list_insert(unsigned long long& entry, float& bound,
+                                                 float seed_bound, V3 q, float x, float y,
+                                                 float z, unsigned id, unsigned k,
+                                                 unsigned lane) {
     const unsigned long long key = knn_key(distance(q, v3(x, y, z)), id);
     const unsigned long long kth = __shfl_sync(0xffffffffu, entry, int(k) - 1);
     if (!(key < kth)) return;  // warp-uniform
     const unsigned long long left = __shfl_up_sync(0xffffffffu, entry, 1);
     if (lane < k && key < entry) entry = (lane == 0 || key > left) ? key : left;
-    bound = prefilter_bound(__shfl_sync(0xffffffffu, entry, int(k) - 1));
+    bound = fminf(seed_bound, prefilter_bound(__shfl_sync(0xffffffffu, entry, int(k) - 1)));
 }
 
+// Rounded-up filter bound for a known upper bound d of the k-th distance.
+__device__ __forceinline__ float seed_prefilter(float d) {
+    return __fmul_ru(__fmul_ru(d, d), 1.000004f);
+}
+
+// seed (may be null): per query an upper bound of its k-th distance (the
+// k-th distance among any subset of the candidates is one); the filter then
+// starts at that bound instead of infinity, so a query's list takes little
+// more than its k final entries.
 __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
     const float4* __restrict__ posA, unsigned nA, const float4* __restrict__ posB, unsigned nB,
-    bool self, unsigned k, unsigned* __restrict__ idx, float* __restrict__ dist) {
+    bool self, unsigned k, const float* __restrict__ seed, unsigned* __restrict__ idx,
+    float* __restrict__ dist) {
     __shared__ __align__(16) float sx[kBruteTile], sy[kBruteTile], sz[kBruteTile];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned q0 = (blockIdx.x * kBruteWarps + warp) * kBruteQW;
     V3 q[kBruteQW];
     unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW], entry[kBruteQW];
-    float bound[kBruteQW];
+    float bound[kBruteQW], seed_bound[kBruteQW];
 #pragma unroll
     for (unsigned j = 0; j < kBruteQW; ++j) {
         const bool act = q0 + j < nA;
@@ -416,7 +431,8 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
         py[j] = pack2(q[j].y, q[j].y);
         pz[j] = pack2(q[j].z, q[j].z);
         entry[j] = KEY_EMPTY;
-        bound[j] = act ? prefilter_bound(KEY_EMPTY) : -1.f;
+        seed_bound[j] = (act && seed) ? seed_prefilter(seed[q0 + j]) : prefilter_bound(KEY_EMPTY);
+        bound[j] = act ? seed_bound[j] : -1.f;
     }
     const float inf = __int_as_float(0x7f800000);
     for (unsigned base = 0; base < nB; base += kBruteTile) {
@@ -460,8 +476,8 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
                         const unsigned c = t0 + 2 * src + h;
                         const unsigned id = base + c;
                         if (c >= cnt || (self && id == q0 + j)) continue;
-                        warp_list_insert(entry[j], bound[j], q[j], sx[c], sy[c], sz[c], id, k,
-                                         lane);
+                        warp_list_insert(entry[j], bound[j], seed_bound[j], q[j], sx[c], sy[c],
+                                         sz[c], id, k, lane);
                     }
                 }
             }
@@ -477,13 +493,46 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
     }
 }
 
+// Largest |coordinate| per axis of n positions, as float bits (non-negative
+// floats order like their bits), into out[0..2] (zeroed by the caller).
+__global__ void k_abs_extent(const float4* __restrict__ pos, unsigned n, unsigned* out) {
+    unsigned m[3] = {0u, 0u, 0u};
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        m[0] = max(m[0], __float_as_uint(fabsf(p.x)));
+        m[1] = max(m[1], __float_as_uint(fabsf(p.y)));
+        m[2] = max(m[2], __float_as_uint(fabsf(p.z)));
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m[a] = max(m[a], __shfl_down_sync(0xffffffffu, m[a], o));
+        if ((threadIdx.x & 31) == 0) atomicMax(out + a, m[a]);
+    }
+}
+
+gs_status abs_extent(const float4* pos, unsigned n, unsigned* d_tmp3, float out[3],
+                     cudaStream_t st) {
+    unsigned h[3] = {0u, 0u, 0u};
+    GS_CUDA(cudaMemsetAsync(d_tmp3, 0, 3 * sizeof(unsigned), st));
+    if (n > 0) {
+        k_abs_extent<<<std::min(blocks_for(n), 4u * 152u), kBlock, 0, st>>>(pos, n, d_tmp3);
+        GS_LAUNCHED("abs_extent");
+    }
+    GS_CUDA(cudaMemcpyAsync(h, d_tmp3, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    for (int a = 0; a < 3; ++a) std::memcpy(&out[a], &h[a], 4);
+    return GS_OK;
+}
+
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
-                           bool self, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
+                           bool self, unsigned k, const float* seed, unsigned* idx, float* dist,
+                           cudaStream_t st) {
     if (nA == 0) return GS_OK;
     if (k <= 32) {
         const unsigned per_block = kBruteWarps * kBruteQW;
         k_knn_brute3<<<(nA + per_block - 1) / per_block, kBruteWarps * 32, 0, st>>>(
-            posA, nA, posB, nB, self, k, idx, dist);
+            posA, nA, posB, nB, self, k, seed, idx, dist);
     } else {
         k_knn_brute<64><<<blocks_for(nA), kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
     }

@@ -21,8 +21,13 @@ gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid
 // ---- per-function (drop-in) kernels -----------------------------------------
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
                             unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
+// seed (may be null, k <= 32 only): per query of A an upper bound of its k-th distance.
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
-                           bool self, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
+                           bool self, unsigned k, const float* seed, unsigned* idx, float* dist,
+                           cudaStream_t st);
+// Largest |coordinate| per axis of n positions (synchronises st); d_tmp3: 3 words.
+gs_status abs_extent(const float4* pos, unsigned n, unsigned* d_tmp3, float out[3],
+                     cudaStream_t st);
 gs_status launch_wrap(float4* pos, unsigned n, const float ws[3], int mode, cudaStream_t st);
 gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st);
 gs_status launch_cell_avg_velocity(const Database& db, const float4* dir, const float* speed,

@@ -179,6 +179,37 @@ def test_knn_bruteforce_sizes_ties_and_cross_groups(k):
         np.testing.assert_array_equal(d, od)
 
 
+@pytest.mark.parametrize("k", [8, 16, 32])
+def test_knn_bruteforce_seeded_large_groups(k):
+    """Groups of 4,096 and more take the seeded filter (k-th distance of a
+    binned search on an automatic grid): a lattice with duplicates (ties), a
+    flat 2D crowd, and a cross-group search with queries outside the other
+    group's extent all give the oracle's lists."""
+    g3 = np.stack(np.meshgrid(np.arange(17), np.arange(17), np.arange(17), indexing="ij"), -1)
+    lat = g3.reshape(-1, 3).astype(np.float32) - 8.0
+    lat = np.concatenate([lat, lat[::7]])
+    pa = np.zeros((lat.shape[0], 4), np.float32)
+    pa[:, :3] = lat
+    crowd = sc.chokepoint_agents(6000, seed=k).position.copy()
+    rng = np.random.default_rng(k)
+    pb = np.zeros((5000, 4), np.float32)
+    pb[:, :3] = rng.uniform(-30, 30, (5000, 3)).astype(np.float32)
+    pb[:2000, 0] += 100.0
+    for P, Q, self_ in ((pa, pa, True), (crowd, crowd, True), (pb, pa, False), (pa, pb, False)):
+        A = group_of(pos_state(P))
+        B = A if self_ else group_of(pos_state(Q))
+        knn = gs.KNNData(A.size, k)
+        gs.findKNearestNeighborsBruteForce(A, knn, B)
+        i, d = knn.download(A)
+        oi, od = ol.knn_brute(P, Q, self_, k)
+        np.testing.assert_array_equal(i, oi)
+        np.testing.assert_array_equal(d, od)
+        # a second call reuses the seed databases
+        gs.findKNearestNeighborsBruteForce(A, knn, B)
+        i2, d2 = knn.download(A)
+        np.testing.assert_array_equal(i2, oi)
+
+
 def test_knn_bruteforce_fewer_candidates_than_k():
     pa = np.zeros((70, 4), np.float32)
     pa[:, 0] = np.arange(70, dtype=np.float32)
