@@ -83,6 +83,7 @@ SIGNATURES = {
     "gs_knn_destroy": [_vp],
     "gs_knn_download": [_vp, _vp, _up, _fp],
     "gs_knn_device_arrays": [_vp, C.POINTER(_up), C.POINTER(_fp)],
+    "gs_knn_upload": [_vp, _vp, _up, _fp],
     "gs_walls_create": [_fp, _fp, _fp, _u, _vp, _u, C.POINTER(_vp)],
     "gs_walls_load": [C.c_char_p, _vp, _u, C.POINTER(_vp)],
     "gs_walls_destroy": [_vp],
@@ -102,6 +103,8 @@ SIGNATURES = {
     "gs_steer_to_avoid_walls": [_vp, _vp, _vp, _f, _f, _u],
     "gs_update_group": [_vp, _f],
     "gs_anti_penetration_agents": [_vp, _vp, _vp, _u],
+    "gs_update_group_with_antipenetration": [_vp, _vp, _vp, _f],
+    "gs_anti_penetration_wall": [_vp, _vp, _vp, _f, _u],
     "gs_step": [_vp, _vp, _vp, C.POINTER(StepParams), _u],
     "gs_step_host": [_vp, _vp, _vp, C.POINTER(StepParams), _u, C.POINTER(AgentArrays), _u,
                      C.POINTER(AgentArrays)],

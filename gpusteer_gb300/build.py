@@ -81,10 +81,13 @@ def build_headless(force: bool = False, verbose: bool = False) -> Path:
     deps = [HEADLESS_SRC, LIB, inc / "GroupSteerLibrary.h", inc / "PlugIn.h", inc / "gpusteer.h"]
     if not force and not _stale(HEADLESS, deps):
         return HEADLESS
-    cuda_inc = Path(nvcc()).resolve().parent.parent / "include"
+    cuda = Path(nvcc()).resolve().parent.parent
+    # The plugins make their own CUDA runtime calls (cudaMemset on the device
+    # arrays), as the reference's do: the static runtime needs no library path.
     cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-ffp-contract=off",
-           "-I", str(inc), "-I", str(cuda_inc), str(HEADLESS_SRC), "-o", str(HEADLESS),
-           "-L", str(BUILD), "-lgpusteer", "-Wl,-rpath,$ORIGIN"]
+           "-I", str(inc), "-I", str(cuda / "include"), str(HEADLESS_SRC), "-o", str(HEADLESS),
+           "-L", str(BUILD), "-lgpusteer", "-Wl,-rpath,$ORIGIN", "-L", str(cuda / "lib64"),
+           "-lcudart_static", "-ldl", "-lpthread", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if verbose or r.returncode != 0:
         sys.stderr.write(r.stdout + r.stderr)

@@ -635,9 +635,11 @@ gs_status gs_group_device_arrays(gs_group g, gs_agent_arrays* d) {
     d->radius = g->radius;
     d->mass = g->mass;
     d->applied = g->applied;
-    // The caller may write through these pointers.
+    // The caller may write through these pointers.  The KNN database keeps
+    // the positions of its last update (the binned search reads only its own
+    // sorted copies), as the reference's does: a plugin may fetch the
+    // pointers between updateKNNDatabase and findKNearestNeighbors.
     touched(g);
-    g->db.valid = false;
     return GS_OK;
 }
 
@@ -701,6 +703,16 @@ gs_status gs_knn_download(gs_knn kd, gs_group g, unsigned* idx, float* dist) {
     const size_t cnt = size_t(kd->n) * kd->k;
     if (idx) GS_CUDA(cudaMemcpyAsync(idx, kd->idx, cnt * 4, cudaMemcpyDeviceToHost, st));
     if (dist) GS_CUDA(cudaMemcpyAsync(dist, kd->dist, cnt * 4, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    return GS_OK;
+}
+
+gs_status gs_knn_upload(gs_knn kd, gs_group g, const unsigned* idx, const float* dist) {
+    if (!kd) return fail(GS_ERR_INVALID_ARG, "null knn");
+    cudaStream_t st = g ? g->stream : nullptr;
+    const size_t cnt = size_t(kd->n) * kd->k;
+    if (idx) GS_CUDA(cudaMemcpyAsync(kd->idx, idx, cnt * 4, cudaMemcpyHostToDevice, st));
+    if (dist) GS_CUDA(cudaMemcpyAsync(kd->dist, dist, cnt * 4, cudaMemcpyHostToDevice, st));
     GS_CUDA(cudaStreamSynchronize(st));
     return GS_OK;
 }
@@ -1105,6 +1117,31 @@ gs_status gs_update_group(gs_group g, float elapsed_time) {
     return GS_OK;
 }
 
+gs_status gs_update_group_with_antipenetration(gs_group g, gs_knn knw, gs_walls walls,
+                                               float elapsed_time) {
+    if (!g || !knw || !walls) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knw->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    if (!std::isfinite(elapsed_time)) return fail(GS_ERR_NONFINITE, "elapsed time is not finite");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_update_antipen_wall(view(g), knw->idx, knw->k, walls->start, walls->end,
+                                      walls->normal, walls->n, elapsed_time, g->stream));
+    g->fused_current = false;
+    g->accum_dirty = false;
+    return GS_OK;
+}
+
+gs_status gs_anti_penetration_wall(gs_group g, gs_knn knw, gs_walls walls, float elapsed_time,
+                                   unsigned /*do_not_apply_with: unused, as in the reference*/) {
+    if (!g || !knw || !walls) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knw->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    if (!std::isfinite(elapsed_time)) return fail(GS_ERR_NONFINITE, "elapsed time is not finite");
+    GS_TRY(ensure_reference(g));
+    GS_TRY(launch_antipen_wall(view(g), knw->idx, knw->k, walls->start, walls->end,
+                               walls->normal, walls->n, elapsed_time, g->stream));
+    touched(g);
+    return GS_OK;
+}
+
 gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, unsigned mask) {
     if (!g || !knn || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
     if (knn->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
@@ -1287,8 +1324,10 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
     // configuration (which also performs one-time kernel set-up).
     const bool cfg_same = g->graph_exec && std::memcmp(&g->graph_L, &L, sizeof(L)) == 0 &&
                           std::memcmp(&g->graph_d, &d, sizeof(d)) == 0 && g->graph_C == C;
-    if (dirty || hook || !g->use_graph || !cfg_same) {
-        const unsigned eager = (hook || !g->use_graph) ? steps : 1u;
+    // The legacy default stream cannot be captured: a group on it runs eagerly.
+    const bool graphs = g->use_graph && st != cudaStreamLegacy && st != nullptr;
+    if (dirty || hook || !graphs || !cfg_same) {
+        const unsigned eager = (hook || !graphs) ? steps : 1u;
         for (; step < eager && step < steps; ++step) {
             d.dirty = dirty ? 1 : 0;
             GS_TRY(step_body(g, L, d, C, hook));

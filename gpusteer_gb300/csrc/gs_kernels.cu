@@ -816,6 +816,134 @@ gs_status launch_update(GroupView g, float dt, cudaStream_t st) {
     return GS_OK;
 }
 
+// updateGroupWithAntiPenetration (UpdateCUDAKernelNew.cu:95-268): the update
+// with the walls' anti-penetration.  Behaviour kept from the reference kernel:
+// the wall list is read row-major, knl[i*k + s] (:149-150), although
+// findKNearestNeighbors writes it column-major; the overlap test measures the
+// distance to lineStart + (lineEnd - lineStart), the segment's end, because
+// ClosestPointOnLine's clamp(0.f, 1.f, t) returns 1 (:67-80); the last listed
+// line within the radius pushes the agent out (:215-229); the nearest crossing
+// of the move turns the velocity parallel to that wall (:201-237); applied
+// bits are kept.  An agent whose new speed is 0 keeps its side vector.
+__global__ void k_update_antipen_wall(GroupView g, const unsigned* __restrict__ knl, unsigned k,
+                                      const float4* __restrict__ start,
+                                      const float4* __restrict__ end,
+                                      const float4* __restrict__ normal, unsigned n_lines,
+                                      float dt) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    Self me = load_self(g, i);
+    const V3 steer = truncate_length(v3(g.steering[i]), me.max_force);
+    const V3 acc = dvd(steer, me.mass);
+    V3 vel = add(mul(me.dir, me.speed), mul(acc, dt));
+    vel = truncate_length(vel, me.max_speed);
+    const V3 future = add(me.pos, mul(vel, dt));
+    const float r = me.radius;
+    float line_d = FLT_MAX, hit_d = FLT_MAX;
+    unsigned line = UINT_MAX, hit = UINT_MAX;
+    V3 line_n = v3(0.f, 0.f, 0.f), hit_n = v3(0.f, 0.f, 0.f);
+    for (unsigned s = 0; s < k; ++s) {
+        const unsigned li = knl[size_t(i) * k + s];
+        if (li >= n_lines) break;
+        const V3 ls = v3(start[li]), le = v3(end[li]), ln = v3(normal[li]);
+        V3 ip;
+        if (lines_intersect(me.pos, future, ls, le, ip)) {
+            const float d = distance(me.pos, ip);
+            if (d < hit_d) {
+                hit_d = d;
+                hit = li;
+                hit_n = ln;
+            }
+        }
+        const V3 o = sub(add(ls, sub(le, ls)), me.pos);
+        const float dsq = dot(o, o);
+        if (dsq < r * r) {
+            line_d = sqrtf(dsq);
+            line = li;
+            line_n = ln;
+        }
+    }
+    unsigned applied = g.applied[i];
+    if (line != UINT_MAX) {
+        me.pos = add(me.pos, mul(neg(line_n), line_d - r));
+        applied |= ANTI_PENETRATION_WALL;
+    }
+    if (hit != UINT_MAX) {
+        vel = perpendicular_component(vel, hit_n);
+        applied |= ANTI_PENETRATION_WALL;
+    }
+    me.speed = length(vel);
+    if (me.speed > 0.f) {
+        me.dir = dvd(vel, me.speed);
+        me.side = normalize(cross(me.dir, me.up));
+        me.up = cross(me.side, me.dir);
+    }
+    me.pos = add(me.pos, mul(vel, dt));
+    g.side[i] = make_float3(me.side.x, me.side.y, me.side.z);
+    g.up[i] = make_float3(me.up.x, me.up.y, me.up.z);
+    g.direction[i] = f4(me.dir, 0.f);
+    g.position[i] = f4(me.pos, 0.f);
+    g.steering[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    g.speed[i] = me.speed;
+    g.applied[i] = applied;
+}
+
+gs_status launch_update_antipen_wall(GroupView g, const unsigned* knl, unsigned k,
+                                     const float4* start, const float4* end,
+                                     const float4* normal, unsigned n_lines, float dt,
+                                     cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_update_antipen_wall<<<blocks_for(g.n), kBlock, 0, st>>>(g, knl, k, start, end, normal,
+                                                              n_lines, dt);
+    GS_LAUNCHED("update_group_with_antipenetration");
+    return GS_OK;
+}
+
+// antiPenetrationWall (AntiPenetrationWallCUDAKernel.cu:52-134): an agent
+// whose move velocity * dt crosses a listed wall turns its heading parallel
+// to the nearest crossed wall.  As the reference kernel: every agent is
+// tested (its early-out `! applied & KERNEL_AVOID_WALLS_BIT`, :73, is never
+// true), the wall list is read row-major (:88-91), every direction is
+// rewritten with w = 0 (:133).
+__global__ void k_antipen_wall(GroupView g, const unsigned* __restrict__ knl, unsigned k,
+                               const float4* __restrict__ start, const float4* __restrict__ end,
+                               const float4* __restrict__ normal, unsigned n_lines, float dt) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    const V3 pos = v3(g.position[i]);
+    V3 dir = v3(g.direction[i]);
+    const V3 future = add(pos, mul(mul(dir, g.speed[i]), dt));
+    float hit_d = FLT_MAX;
+    unsigned hit = UINT_MAX;
+    for (unsigned s = 0; s < k; ++s) {
+        const unsigned li = knl[size_t(i) * k + s];
+        if (li >= n_lines) break;
+        V3 ip;
+        if (lines_intersect(pos, future, v3(start[li]), v3(end[li]), ip)) {
+            const float d = distance(pos, ip);
+            if (d < hit_d) {
+                hit_d = d;
+                hit = li;
+            }
+        }
+    }
+    if (hit != UINT_MAX) {
+        dir = normalize(perpendicular_component(dir, v3(normal[hit])));
+        g.applied[i] |= ANTI_PENETRATION_WALL;
+    }
+    g.direction[i] = f4(dir, 0.f);
+}
+
+gs_status launch_antipen_wall(GroupView g, const unsigned* knl, unsigned k, const float4* start,
+                              const float4* end, const float4* normal, unsigned n_lines,
+                              float dt, cudaStream_t st) {
+    if (g.n == 0) return GS_OK;
+    k_antipen_wall<<<blocks_for(g.n), kBlock, 0, st>>>(g, knl, k, start, end, normal, n_lines,
+                                                       dt);
+    GS_LAUNCHED("anti_penetration_wall");
+    return GS_OK;
+}
+
 // AntiPenetrationAgentsCUDAKernel.cu:72-108.  Positions are read from the
 // group and written to pos_out (the reference's m_pdPositionNew); the other
 // group's applied bits are read from a snapshot taken before the launch (the

@@ -59,6 +59,13 @@ gs_status launch_avoid_walls(GroupView g, const unsigned* knw, unsigned kw, cons
                              const float4* end, const float4* normal, unsigned n_lines,
                              float min_time, float w, unsigned mask, cudaStream_t st);
 gs_status launch_update(GroupView g, float dt, cudaStream_t st);
+gs_status launch_update_antipen_wall(GroupView g, const unsigned* knl, unsigned k,
+                                     const float4* start, const float4* end,
+                                     const float4* normal, unsigned n_lines, float dt,
+                                     cudaStream_t st);
+gs_status launch_antipen_wall(GroupView g, const unsigned* knl, unsigned k, const float4* start,
+                              const float4* end, const float4* normal, unsigned n_lines,
+                              float dt, cudaStream_t st);
 gs_status launch_follow_path(GroupView g, const PathDev& path, float prediction_time, float w,
                              unsigned mask, cudaStream_t st);
 gs_status launch_antipenetration(GroupView g, const unsigned* knn, const float* knn_dist,

@@ -218,6 +218,18 @@ class KNNData:
              _ptr(dist))
         return idx, dist
 
+    def upload(self, idx: np.ndarray | None, dist: np.ndarray | None = None,
+               group: AgentGroup | None = None) -> None:
+        """Writes the lists (column-major, k * n) from the host, as a caller of
+        the reference writes pdKNNIndices() / pdKNNDistances()."""
+        cnt = self.k * self.n
+        i = None if idx is None else np.ascontiguousarray(idx, np.uint32).reshape(-1)
+        d = None if dist is None else np.ascontiguousarray(dist, np.float32).reshape(-1)
+        if (i is not None and i.size != cnt) or (d is not None and d.size != cnt):
+            raise ValueError(f"KNN arrays must hold k * n = {cnt} entries")
+        call("gs_knn_upload", self._h, group.handle if group else None,
+             None if i is None else _ptr(i, C.c_uint), None if d is None else _ptr(d))
+
     def __del__(self):
         if getattr(self, "_h", None) and _lib._lib is not None:
             _lib._lib.gs_knn_destroy(self._h)
@@ -461,6 +473,20 @@ def updateGroup(group, elapsed_time) -> None:
 
 def antiPenetrationAgents(group, knn, other, do_not_apply_with=0) -> None:
     call("gs_anti_penetration_agents", group.handle, knn.handle, other.handle,
+         int(do_not_apply_with))
+
+
+def updateGroupWithAntiPenetration(group, knw, walls, elapsed_time) -> None:
+    """updateGroupWithAntiPenetration (UpdateCUDAKernelNew.cu:95-268); reads
+    the wall list row-major, as the reference kernel does."""
+    call("gs_update_group_with_antipenetration", group.handle, knw.handle, walls.handle,
+         elapsed_time)
+
+
+def antiPenetrationWall(group, knw, walls, elapsed_time, do_not_apply_with=0) -> None:
+    """antiPenetrationWall (AntiPenetrationWallCUDAKernel.cu:52-134); reads the
+    wall list row-major and ignores do_not_apply_with, as the reference does."""
+    call("gs_anti_penetration_wall", group.handle, knw.handle, walls.handle, elapsed_time,
          int(do_not_apply_with))
 
 

@@ -15,8 +15,13 @@
 //
 //   ChokePointNew  CtfGroup::update as ChokePointNew.cpp:586-630 has it, with
 //               path following and anti-penetration (below)
+//   ChokePointGroup  CtfEnemyGroup::update (plugins/ChokePointGroup.cpp:683-728):
+//               the applied bits cleared with cudaMemset, walls, path
+//               following, seek, flocking, updateGroupWithAntiPenetration,
+//               antiPenetrationAgents
 //
-//   gs_headless <Boids|ChokePoint|ChokePointNew> <state_in> <state_out> <frames> [key=value ...]
+//   gs_headless <Boids|ChokePoint|ChokePointNew|ChokePointGroup> <state_in> <state_out> <frames>
+//               [key=value ...]
 //
 // State files: uint32 n, then position (4n f32), direction (4n), steering
 // (4n), side (3n), up (3n), speed, max_speed, max_force, radius, mass (n
@@ -31,6 +36,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime_api.h>
 #include <vector_functions.h>
 
 #include "GroupSteerLibrary.h"
@@ -350,16 +356,114 @@ private:
     std::unique_ptr<KNNData> m_knnSelf, m_knnWalls;
 };
 
+// CtfEnemyGroup::update (plugins/ChokePointGroup.cpp:683-728): the older
+// choke-point group, which integrates with updateGroupWithAntiPenetration.
+// That update keeps the applied bits, so the frame starts by clearing them
+// with a cudaMemset on the group's device array (:689-690), ordered with the
+// library's launches on the legacy default stream.  The path and the goal
+// come from the parameters (path=x,y,z;...  path_radius=  goal=x,y,z).
+class ChokePointGroupPlugIn : public HeadlessPlugIn {
+public:
+    const char* name() { return "ChokePointGroup"; }
+    void open() {
+        const Params& p = params;
+        m_worldSize = f3param(p, "world", make_float3(512.f, 10.f, 512.f));
+        m_worldCells = u3param(p, "cells", make_uint3(256, 1, 256));
+        m_k = uparam(p, "k", 16);
+        m_knw = uparam(p, "knw", 3);
+        m_radius = uparam(p, "radius", 1);
+        m_bins.reset(new KNNBinData(m_worldCells, m_worldSize, m_radius));
+        m_walls.reset(new WallGroup(m_worldCells, m_knw));
+        auto it = p.find("map");
+        if (it == p.end() || !m_walls->LoadFromFile(it->second.c_str()))
+            throw std::runtime_error("ChokePointGroup needs map=<file.map>");
+        m_walls->SplitWalls(m_bins->hvCells());
+        m_walls->SyncDevice();
+        updateKNNDatabase(m_walls.get(), m_bins.get());
+        std::vector<float3> pts;
+        auto pp = p.find("path");
+        if (pp == p.end()) throw std::runtime_error("ChokePointGroup needs path=x,y,z;x,y,z...");
+        std::istringstream in(pp->second);
+        std::string item;
+        while (std::getline(in, item, ';')) {
+            std::istringstream v(item);
+            float3 q;
+            char c;
+            v >> q.x >> c >> q.y >> c >> q.z;
+            pts.push_back(q);
+        }
+        m_path.reset(new PolylinePathwayCUDA(pts, fparam(p, "path_radius", 23.5f), false));
+        m_group.reset(new AgentGroup(m_worldCells, m_k));
+        for (const AgentData& a : read_state(in_path.c_str())) m_group->AddAgent(a);
+        m_group->SyncDevice();
+        m_knnSelf.reset(new KNNData(m_group->Size(), m_k));
+        m_knnWalls.reset(new KNNData(m_group->Size(), m_knw));
+    }
+    void update(const float, const float elapsedTime) {
+        const Params& p = params;
+        AgentGroup* g = m_group.get();
+        wrapWorld(g, m_worldSize);
+        updateKNNDatabase(g, m_bins.get());
+        if (cudaMemset(g->GetAgentGroupData().pdAppliedKernels(), 0, g->Size() * sizeof(uint)) !=
+            cudaSuccess)
+            throw std::runtime_error("cudaMemset of the applied bits failed");
+        findKNearestNeighbors(g, m_knnSelf.get(), m_bins.get(), g, m_radius);
+        findKNearestNeighbors(g, m_knnWalls.get(), m_bins.get(), m_walls.get(), m_radius);
+        steerToAvoidWalls(g, m_knnWalls.get(), m_walls.get(), fparam(p, "min_time_wall", 10.f),
+                          fparam(p, "w_walls", 1.f), uparam(p, "mask_walls", 0));
+        steerToFollowPath(g, m_path.get(), fparam(p, "path_time", 5.f), fparam(p, "w_path", 1.f),
+                          uparam(p, "mask_path", KERNEL_SEPARATION_BIT));
+        steerForSeek(g, f3param(p, "goal", make_float3(0.f, 0.f, -93.5f)),
+                     fparam(p, "w_seek", 1.f), uparam(p, "mask_seek", KERNEL_AVOID_WALLS_BIT));
+        steerForSeparation(g, m_knnSelf.get(), g, fparam(p, "sep_min", 0.5f),
+                           fparam(p, "sep_max", 1.2f), fparam(p, "sep_cos", -0.8660254f),
+                           fparam(p, "w_sep", 10.f),
+                           uparam(p, "mask_sep", KERNEL_ANTI_PENETRATION_WALL));
+        steerForAlignment(g, m_knnSelf.get(), g, fparam(p, "ali_min", 0.5f),
+                          fparam(p, "ali_max", 7.f), fparam(p, "ali_cos", -0.8660254f),
+                          fparam(p, "w_ali", 2.5f),
+                          uparam(p, "mask_ali", KERNEL_AVOID_WALLS_BIT | KERNEL_SEPARATION_BIT));
+        steerForCohesion(g, m_knnSelf.get(), g, fparam(p, "coh_min", 0.5f),
+                         fparam(p, "coh_max", 7.f), fparam(p, "coh_cos", -0.8660254f),
+                         fparam(p, "w_coh", 1.f),
+                         uparam(p, "mask_coh", KERNEL_AVOID_WALLS_BIT | KERNEL_SEPARATION_BIT));
+        updateGroupWithAntiPenetration(g, m_knnWalls.get(), m_walls.get(), elapsedTime);
+        antiPenetrationAgents(g, m_knnSelf.get(), g,
+                              uparam(p, "mask_antipen",
+                                     KERNEL_AVOID_WALLS_BIT | KERNEL_ANTI_PENETRATION_WALL));
+    }
+    void redraw(const float, const float) { write_state(out_path.c_str(), *m_group); }
+    void close() {
+        m_knnSelf.reset();
+        m_knnWalls.reset();
+        m_group.reset();
+        m_path.reset();
+        m_walls.reset();
+        m_bins.reset();
+    }
+
+private:
+    float3 m_worldSize;
+    uint3 m_worldCells;
+    uint m_k = 16, m_knw = 3, m_radius = 1;
+    std::unique_ptr<KNNBinData> m_bins;
+    std::unique_ptr<WallGroup> m_walls;
+    std::unique_ptr<PolylinePathwayCUDA> m_path;
+    std::unique_ptr<AgentGroup> m_group;
+    std::unique_ptr<KNNData> m_knnSelf, m_knnWalls;
+};
+
 BoidsPlugIn gBoidsPlugIn;
 ChokePointPlugIn gChokePointPlugIn;
 ChokePointNewPlugIn gChokePointNewPlugIn;
+ChokePointGroupPlugIn gChokePointGroupPlugIn;
 
 }  // namespace
 
 int main(int argc, char** argv) {
     if (argc < 5) {
         std::fprintf(stderr,
-                     "usage: %s <Boids|ChokePoint|ChokePointNew> <state_in> <state_out> <frames> "
+                     "usage: %s <Boids|ChokePoint|ChokePointNew|ChokePointGroup> <state_in> <state_out> <frames> "
                      "[key=value ...]\n",
                      argv[0]);
         return 2;

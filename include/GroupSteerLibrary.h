@@ -10,15 +10,20 @@
  *   - errors throw OpenSteer::GpuSteerError (the reference aborts through
  *     CUDA_SAFE_CALL);
  *   - the behaviours outside the GB300 path (flee, pursuit, evade, stay-on-
- *     path, obstacles, wall anti-penetration) are not declared, so a plugin
- *     that calls them fails to compile rather than at run time;
+ *     path, obstacles) are not declared, so a plugin that calls them fails to
+ *     compile rather than at run time;
  *   - WallGroup::SplitWalls takes the cell list of a KNNBinData made by this
  *     header (the split runs in the library, on that grid).
+ * Every AgentGroup made here runs its work on the legacy default stream, as
+ * the reference's kernels do, so a plugin's own CUDA calls on the pd*()
+ * device pointers (a cudaMemset of the applied bits, a kernel of its own)
+ * are ordered with the library's launches as they are in the reference.
  * Results are bit-identical to the reference kernels' restatement (oracle/). */
 #ifndef GPUSTEER_GROUP_STEER_LIBRARY_H
 #define GPUSTEER_GROUP_STEER_LIBRARY_H
 
 #include <vector_types.h> /* float3, float4, uint3 (CUDA toolkit) */
+#include <driver_types.h> /* cudaStreamLegacy */
 
 #include <climits>
 #include <cstddef>
@@ -327,7 +332,7 @@ public:
             while (cap < n) cap *= 2;
             if (m_group) gs_group_destroy(m_group);
             m_group = nullptr;
-            gsCheck(gs_group_create(m_k, unsigned(cap), nullptr, &m_group));
+            gsCheck(gs_group_create(m_k, unsigned(cap), cudaStreamLegacy, &m_group));
             m_capacity = cap;
         }
         std::vector<float> pos(4 * n), dir(4 * n), steer(4 * n), side(3 * n), up(3 * n);
@@ -652,6 +657,20 @@ inline void steerForCohesion(AgentGroup* pAgentGroup, KNNData* pKNNData, AgentGr
 /* :189 */
 inline void updateGroup(AgentGroup* pAgentGroup, const float elapsedTime) {
     gsCheck(gs_update_group(detail::group(pAgentGroup), elapsedTime));
+}
+/* :198 (UpdateCUDAKernelNew.cu:95-268; the wall list is read row-major, as
+ * that kernel reads it) */
+inline void updateGroupWithAntiPenetration(AgentGroup* pAgentGroup, KNNData* pKNNData,
+                                           WallGroup* pWallGroup, const float elapsedTime) {
+    gsCheck(gs_update_group_with_antipenetration(detail::group(pAgentGroup), pKNNData->handle(),
+                                                 pWallGroup->gsWalls(), elapsedTime));
+}
+/* :207 (AntiPenetrationWallCUDAKernel.cu:52-134; doNotApplyWith is not used,
+ * as in the reference) */
+inline void antiPenetrationWall(AgentGroup* pAgentGroup, KNNData* pKNNData, WallGroup* pWallGroup,
+                                float const elapsedTime, uint const doNotApplyWith) {
+    gsCheck(gs_anti_penetration_wall(detail::group(pAgentGroup), pKNNData->handle(),
+                                     pWallGroup->gsWalls(), elapsedTime, doNotApplyWith));
 }
 /* :216 */
 inline void antiPenetrationAgents(AgentGroup* pAgentGroup, KNNData* pKNNData,

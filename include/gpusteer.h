@@ -178,6 +178,10 @@ gs_status gs_knn_destroy(gs_knn knn);
 /* KNNData::syncHost + hvKNNIndices/hvKNNDistances (column-major, k*n). */
 gs_status gs_knn_download(gs_knn knn, gs_group g, unsigned* idx, float* dist);
 gs_status gs_knn_device_arrays(gs_knn knn, unsigned** idx, float** dist);
+/* Writes the lists from the host (column-major, k*n; either array may be
+ * NULL): what a caller of the reference does through pdKNNIndices() /
+ * pdKNNDistances() (KNNData.cuh:37-38) with a cudaMemcpy. */
+gs_status gs_knn_upload(gs_knn knn, gs_group g, const unsigned* idx, const float* dist);
 
 /* ---- WallGroup: WallGroup::LoadFromFile + SplitWalls + SyncDevice
  *      (WallGroupData.cu:73-206, plugins/ChokePointNew.cpp:107-119) ------------- */
@@ -258,6 +262,22 @@ gs_status gs_update_group(gs_group g, float elapsed_time);
 /* antiPenetrationAgents (GroupSteerLibrary.cuh:216-223). */
 gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other,
                                      unsigned do_not_apply_with);
+/* updateGroupWithAntiPenetration (GroupSteerLibrary.cuh:198-205,
+ * UpdateCUDAKernelNew.cu:95-268): updateGroup that also pushes an agent out of
+ * a wall it overlaps and removes the velocity component that would carry it
+ * across a wall this step.  As the reference kernel: `knw` is read row-major
+ * (entry i*k + s for agent i), the overlap test uses each segment's end point,
+ * and appliedKernels is not cleared (bit KERNEL_ANTI_PENETRATION_WALL is
+ * added). */
+gs_status gs_update_group_with_antipenetration(gs_group g, gs_knn knw, gs_walls walls,
+                                               float elapsed_time);
+/* antiPenetrationWall (GroupSteerLibrary.cuh:207-214,
+ * AntiPenetrationWallCUDAKernel.cu:52-134): an agent whose next move crosses a
+ * listed wall turns its heading parallel to the nearest such wall.  `knw` is
+ * read row-major as in the reference kernel; do_not_apply_with is accepted and,
+ * as in the reference, not used. */
+gs_status gs_anti_penetration_wall(gs_group g, gs_knn knw, gs_walls walls, float elapsed_time,
+                                   unsigned do_not_apply_with);
 
 /* ---- fused step -------------------------------------------------------------- */
 /* Runs `steps` whole steps; the result equals the per-function sequence

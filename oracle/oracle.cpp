@@ -93,6 +93,7 @@ constexpr unsigned AVOID_WALLS_BIT = 1u << 8;
 constexpr unsigned AVOID_NEIGHBORS_BIT = 1u << 9;
 constexpr unsigned AVOID_CLOSE_NEIGHBORS_BIT = 1u << 10;
 constexpr unsigned ANTI_PENETRATION_WALL = 1u << 12;
+constexpr unsigned ANTI_PENETRATION_AGENT = 1u << 13;
 constexpr unsigned FOLLOW_PATH_BIT = 1u << 11;
 
 inline int nthreads(int t) {
@@ -676,6 +677,154 @@ template <class T> void update(Group<T> g, T dt, int threads) {
     }
 }
 
+// ---- UpdateCUDAKernelNew.cu:95-268 (updateGroupWithAntiPenetration) ----------
+// The update with the walls' anti-penetration, as the reference kernel
+// behaves:
+//  * the wall list is read row-major, knl[i*k + s] (:149-150), whereas
+//    findKNearestNeighbors writes it column-major, so an agent reads the
+//    entries the column-major array holds at those positions;
+//  * ClosestPointOnLine (:73-80) calls clamp(0.f, 1.f, t), whose argument
+//    order (:67-71) returns 1: the point tested is lineStart + (lineEnd -
+//    lineStart), the segment's end;
+//  * the overlap test keeps the last listed line within the radius (:215-221),
+//    the crossing test the nearest crossing (strict <, :205);
+//  * appliedKernels is not cleared (:152-153);
+//  * an agent whose new speed is 0 keeps its side vector (the reference then
+//    writes a shared-memory side it never loaded, :155 and :261).
+template <class T>
+void update_antipen_wall(Group<T> g, const unsigned* knl, unsigned k, const orc_walls* walls,
+                         T dt, int threads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (long long ii = 0; ii < (long long)g.n; ++ii) {
+        const size_t i = size_t(ii);
+        V3<T> dir = ld4<T>(g.direction, i), pos = ld4<T>(g.position, i);
+        V3<T> side = ld3<T>(g.side, i), up = ld3<T>(g.up, i);
+        T speed = g.speed[i];
+        const T r = g.radius[i];
+        const V3<T> steer = truncate_length(ld4<T>(g.steering, i), T(g.max_force[i]));
+        const V3<T> acc = dvd(steer, T(g.mass[i]));
+        V3<T> vel = add(mul(dir, speed), mul(acc, dt));
+        vel = truncate_length(vel, T(g.max_speed[i]));
+        const V3<T> future = add(pos, mul(vel, dt));
+        T line_d = T(FLT_MAX), hit_d = T(FLT_MAX);
+        unsigned line = UINT_MAX, hit = UINT_MAX;
+        V3<T> line_n{0, 0, 0}, hit_n{0, 0, 0};
+        for (unsigned s = 0; s < k; ++s) {
+            const unsigned li = knl[i * k + s];
+            if (li >= walls->n) break;
+            const V3<T> ls = ld4<T>(walls->start, li), le = ld4<T>(walls->end, li);
+            const V3<T> ln = ld4<T>(walls->normal, li);
+            V3<T> ip{0, 0, 0};
+            if (lines_intersect(pos, future, ls, le, ip)) {
+                const T d = distance(pos, ip);
+                if (d < hit_d) {
+                    hit_d = d;
+                    hit = li;
+                    hit_n = ln;
+                }
+            }
+            const V3<T> end_pt = add(ls, mul(sub(le, ls), T(1)));
+            const V3<T> o = sub(end_pt, pos);
+            const T dsq = dot(o, o);
+            if (dsq < r * r) {
+                line_d = std::sqrt(dsq);
+                line = li;
+                line_n = ln;
+            }
+        }
+        if (line != UINT_MAX) {
+            pos = add(pos, mul(neg(line_n), line_d - r));
+            g.applied[i] |= ANTI_PENETRATION_WALL;
+        }
+        if (hit != UINT_MAX) {
+            vel = perpendicular_component(vel, hit_n);
+            g.applied[i] |= ANTI_PENETRATION_WALL;
+        }
+        speed = length(vel);
+        if (speed > 0) {
+            dir = dvd(vel, speed);
+            side = normalize(cross(dir, up));
+            up = cross(side, dir);
+        }
+        pos = add(pos, mul(vel, dt));
+        st3(g.side, i, side);
+        st3(g.up, i, up);
+        st4(g.direction, i, dir);
+        st4(g.position, i, pos);
+        st4(g.steering, i, V3<T>{0, 0, 0});
+        g.speed[i] = speed;
+    }
+}
+
+// ---- AntiPenetrationWallKernel (AntiPenetrationWallCUDAKernel.cu:52-134) ------
+// Turns the heading of an agent whose next move (velocity * dt) crosses one
+// of its listed walls parallel to the nearest such wall.  As the reference:
+// the early-out test `! applied & KERNEL_AVOID_WALLS_BIT` (:73) is always
+// false, so every agent is tested; the wall list is read row-major,
+// knl[i*k + s] (:88-91); every agent's direction is rewritten with w = 0
+// (:133); the doNotApplyWith mask is not used.
+template <class T>
+void antipen_wall(Group<T> g, const unsigned* knl, unsigned k, const orc_walls* walls, T dt,
+                  int threads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (long long ii = 0; ii < (long long)g.n; ++ii) {
+        const size_t i = size_t(ii);
+        const V3<T> pos = ld4<T>(g.position, i);
+        V3<T> dir = ld4<T>(g.direction, i);
+        const V3<T> future = add(pos, mul(mul(dir, T(g.speed[i])), dt));
+        T hit_d = T(FLT_MAX);
+        unsigned hit = UINT_MAX;
+        for (unsigned s = 0; s < k; ++s) {
+            const unsigned li = knl[i * k + s];
+            if (li >= walls->n) break;
+            V3<T> ip{0, 0, 0};
+            if (lines_intersect(pos, future, ld4<T>(walls->start, li), ld4<T>(walls->end, li), ip)) {
+                const T d = distance(pos, ip);
+                if (d < hit_d) {
+                    hit_d = d;
+                    hit = li;
+                }
+            }
+        }
+        if (hit != UINT_MAX) {
+            dir = normalize(perpendicular_component(dir, ld4<T>(walls->normal, hit)));
+            g.applied[i] |= ANTI_PENETRATION_WALL;
+        }
+        st4(g.direction, i, dir);
+    }
+}
+
+// ---- AntiPenetrationAgentsCUDAKernel.cu:57-109 with AntiPenetrationAgentsCUDA::run
+// (AntiPenetrationAgentsCUDA.cu:62-98) ------------------------------------------
+// Each agent not masked by its own bits moves away from its nearest neighbour
+// (the first KNN entry) when their radii overlap: by the whole overlap when
+// the neighbour's bits hit the mask, else by half.  The new positions go to a
+// copy of the positions (w = 0 where moved) that replaces them afterwards;
+// the neighbour's position and bits are the ones before this pass (posB4 and
+// appliedB are read only).
+template <class T>
+void antipen_agents(Group<T> g, const unsigned* knn_idx, const T* knn_dist, const T* posB4,
+                    const T* radiusB, const unsigned* appliedB, unsigned nB, unsigned mask,
+                    int threads) {
+    std::vector<T> out(g.position, g.position + size_t(4) * g.n);
+#pragma omp parallel for schedule(static) num_threads(nthreads(threads))
+    for (long long ii = 0; ii < (long long)g.n; ++ii) {
+        const size_t i = size_t(ii);
+        if (g.applied[i] & mask) continue;
+        const unsigned b = knn_idx[i];
+        if (b >= nB) continue;
+        const T sum_radii = g.radius[i] + radiusB[b];
+        const T overlap = sum_radii - knn_dist[i];
+        if (overlap < T(0)) continue;
+        const V3<T> pos = ld4<T>(g.position, i);
+        const V3<T> unit = normalize(sub(pos, ld4<T>(posB4, b)));
+        const T move = (appliedB[b] & mask) ? overlap : T(0.5f) * overlap;
+        st4(out.data(), i, add(pos, mul(unit, move)));
+        g.applied[i] |= ANTI_PENETRATION_AGENT;
+    }
+    std::copy(out.begin(), out.end(), g.position);
+}
+
 // ---- one whole step (plugins/ChokePointNew.cpp:586-630, BoidsGroup.cpp:606-637)
 template <class T>
 int run_steps(Group<T> g, const orc_walls* walls, const orc_step_params* p, unsigned steps,
@@ -899,6 +1048,22 @@ void orc_steer_avoid_walls(orc_group* g, const unsigned* knw_idx, unsigned knw,
 }
 
 void orc_update(orc_group* g, float dt) { update(view<float>(g), dt, 0); }
+
+void orc_update_with_antipenetration(orc_group* g, const unsigned* knl, unsigned k,
+                                     const orc_walls* walls, float dt) {
+    update_antipen_wall(view<float>(g), knl, k, walls, dt, 0);
+}
+
+void orc_antipenetration_wall(orc_group* g, const unsigned* knl, unsigned k,
+                              const orc_walls* walls, float dt) {
+    antipen_wall(view<float>(g), knl, k, walls, dt, 0);
+}
+
+void orc_antipenetration_agents(orc_group* g, const unsigned* knn_idx, const float* knn_dist,
+                                const float* posB4, const float* radiusB,
+                                const unsigned* appliedB, unsigned nB, unsigned mask) {
+    antipen_agents(view<float>(g), knn_idx, knn_dist, posB4, radiusB, appliedB, nB, mask, 0);
+}
 
 // PolylinePathwayCUDA::Initialize (PolylinePathwayCUDA.cu:17-56): binary32
 // host arithmetic, in the reference's order.

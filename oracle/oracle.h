@@ -187,6 +187,19 @@ void orc_steer_avoid_walls(orc_group* g, const unsigned* knw_idx, unsigned knw,
                            const orc_walls* walls, float min_time, float w,
                            unsigned mask);
 void orc_update(orc_group* g, float dt);
+/* updateGroupWithAntiPenetration (UpdateCUDAKernelNew.cu:95-268) and
+ * antiPenetrationWall (AntiPenetrationWallCUDAKernel.cu:52-134).  knl is the
+ * walls' KNN array (k * n), read row-major as the reference kernels read it. */
+void orc_update_with_antipenetration(orc_group* g, const unsigned* knl, unsigned k,
+                                     const orc_walls* walls, float dt);
+void orc_antipenetration_wall(orc_group* g, const unsigned* knl, unsigned k,
+                              const orc_walls* walls, float dt);
+/* antiPenetrationAgents (AntiPenetrationAgentsCUDAKernel.cu:57-109): posB4,
+ * radiusB and appliedB are the other group's positions, radii and bits before
+ * the pass (for a group with itself: copies taken before the call). */
+void orc_antipenetration_agents(orc_group* g, const unsigned* knn_idx, const float* knn_dist,
+                                const float* posB4, const float* radiusB,
+                                const unsigned* appliedB, unsigned nB, unsigned mask);
 
 /* PolylinePathwayCUDA::Initialize: from n_in float3 points, writes the path's
  * points, lengths and normals (n_in + cyclic entries, caller capacity n_in + 1)

@@ -121,6 +121,12 @@ namespace ref_antipen { GSREF_DYNAMIC_SHARED
 namespace ref_path { GSREF_DYNAMIC_SHARED
 #include "SteerToFollowPathCUDAKernel.cu"
 }
+namespace ref_update_ap { GSREF_DYNAMIC_SHARED
+#include "UpdateCUDAKernelNew.cu"
+}
+namespace ref_antipen_wall { GSREF_DYNAMIC_SHARED
+#include "AntiPenetrationWallCUDAKernel.cu"
+}
 
 namespace {
 constexpr unsigned TPB = THREADSPERBLOCK;  // AbstractCUDAKernel.cuh:46-54
@@ -380,6 +386,40 @@ void gsref_antipenetration_agents(float* pos4, const float* radius, unsigned nA,
     });
     AntiPenetrationAgentsKernelUnbindTextures();
     std::copy(out.begin(), out.end(), f4(pos4));
+}
+
+// UpdateWithAntiPenetrationCUDA::run, UpdateCUDA.cu:125-190 (dynamic shared
+// memory k * THREADSPERBLOCK words for the wall list).
+int gsref_update_antipen_wall(float* side3, float* up3, float* dir4, float* pos4, float* steer4,
+                              float* speed, const float* maxForce, const float* maxSpeed,
+                              const float* mass, const float* radius, const unsigned* knl,
+                              unsigned k, const float* start4, const float* end4,
+                              const float* normal4, unsigned nLines, float dt, unsigned n,
+                              unsigned* applied) {
+    using namespace ref_update_ap;
+    if (TPB * k > (1u << 14)) return -1;
+    UpdateCUDAKernelBindTextures(f4(start4), f4(end4), f4(normal4), nLines);
+    launch(blocks(n, TPB), TPB, [&] {
+        UpdateCUDAKernelNew(f3(side3), f3(up3), f4(dir4), f4(pos4), f4(steer4), speed, maxForce,
+                            maxSpeed, mass, radius, knl, k, nLines, dt, n, applied);
+    });
+    UpdateCUDAKernelUnbindTextures();
+    return 0;
+}
+
+// AntiPenetrationWALLCUDA::run, AntiPenetrationWallCUDA.cu:45-87.
+int gsref_antipenetration_wall(const float* pos4, float* dir4, const float* speed,
+                               const unsigned* knl, unsigned k, const float* start4,
+                               const float* end4, const float* normal4, unsigned nLines,
+                               float dt, unsigned n, unsigned* applied) {
+    using namespace ref_antipen_wall;
+    if (TPB * k > (1u << 14)) return -1;
+    AntiPenetrationWallKernelBindTextures(f4(start4), f4(end4), f4(normal4), nLines);
+    launch(blocks(n, TPB), TPB, [&] {
+        AntiPenetrationWallKernel(f4(pos4), f4(dir4), speed, knl, k, dt, n, nLines, applied);
+    });
+    AntiPenetrationWallKernelUnbindTextures();
+    return 0;
 }
 
 }  // extern "C"

@@ -186,6 +186,47 @@ def avoid_case(ref):
          ap_out_applied=s.applied)
 
 
+def wall_antipen_case(ref):
+    """updateGroupWithAntiPenetration (UpdateCUDAKernelNew.cu:95-268) and
+    antiPenetrationWall (AntiPenetrationWallCUDAKernel.cu:52-134) on agents
+    moving at and along the choke point's walls.  Both kernels read the wall
+    list row-major; each runs on the wall KNN as findKNearestNeighbors writes
+    it (column-major) and on its transpose, with which every agent tests its
+    own nearest walls."""
+    ws, wc = (128.0, 10.0, 128.0), (64, 1, 64)
+    walls = choke_walls(10.0, ws, wc)
+    nl = walls[0].shape[0]
+    n = 1500
+    s0 = sc.chokepoint_agents(n, x_range=(-24, 24), z_range=(-16, 16), seed=61)
+    u = sc.uniform01(62, 4 * n).reshape(4, n)
+    s0.speed[:] = u[0] * np.float32(4.0)
+    s0.steering[:, 0] = (u[1] - np.float32(0.5)) * np.float32(6.0)
+    s0.steering[:, 2] = (u[2] - np.float32(0.5)) * np.float32(6.0)
+    s0.radius[:] = np.float32(0.3) + u[3] * np.float32(0.6)
+    s0.applied[:] = (u[3] < 0.25).astype(np.uint32) * 256
+    kw, dt = 4, 0.5
+    widx, _ = ref_knn_binned(ref, s0.position, walls[1], False, ws, wc, 1, kw)
+    widx_t = np.ascontiguousarray(widx.reshape(kw, n).T).ravel()
+    out = {}
+    for name, knl in (("col", widx), ("row", widx_t)):
+        s = s0.copy()
+        rc = ref.gsref_update_antipen_wall(
+            fp(s.side), fp(s.up), fp(s.direction), fp(s.position), fp(s.steering), fp(s.speed),
+            fp(s.max_force), fp(s.max_speed), fp(s.mass), fp(s.radius), up(knl), kw,
+            fp(walls[0]), fp(walls[2]), fp(walls[3]), nl, C.c_float(dt), n, up(s.applied))
+        assert rc == 0
+        out.update(state_arrays(f"upd_{name}_", s))
+        s = s0.copy()
+        rc = ref.gsref_antipenetration_wall(
+            fp(s.position), fp(s.direction), fp(s.speed), up(knl), kw, fp(walls[0]),
+            fp(walls[2]), fp(walls[3]), nl, C.c_float(dt), n, up(s.applied))
+        assert rc == 0
+        out.update(state_arrays(f"apw_{name}_", s))
+    save("wall_antipen", {"ws": ws, "wc": wc, "knw": kw, "dt": dt},
+         knw_col=widx, knw_row=widx_t, wall_start=walls[0], wall_mid=walls[1],
+         wall_end=walls[2], wall_normal=walls[3], **state_arrays("in_", s0), **out)
+
+
 def flock_steps(ref):
     """20 whole flock steps (KNN, separation, cohesion, alignment, update),
     each kernel the reference's, composed as BoidsGroup::update."""
@@ -287,16 +328,16 @@ def path_case(ref):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", nargs="*", default=None, help="case functions to run")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle" / "ref"), f"REF={a.ref}"], check=True)
     ref = ol.ref_harness()
     assert ref is not None
-    knn_cases(ref)
-    flock_case(ref)
-    avoid_case(ref)
-    flock_steps(ref)
-    choke_steps(ref)
-    path_case(ref)
+    cases = [knn_cases, flock_case, avoid_case, flock_steps, choke_steps, path_case,
+             wall_antipen_case]
+    for case in cases:
+        if a.only is None or case.__name__ in a.only:
+            case(ref)
 
 
 if __name__ == "__main__":

@@ -159,6 +159,8 @@ void (*h)(AgentGroup*, const float) = updateGroup;
 void (*i)(AgentGroup*, KNNData*, AgentGroup*, uint const) = antiPenetrationAgents;
 void (*j)(AgentGroup*, PolylinePathwayCUDA*, float const, float const, uint const) =
     steerToFollowPath;
+void (*k1)(AgentGroup*, KNNData*, WallGroup*, const float) = updateGroupWithAntiPenetration;
+void (*k2)(AgentGroup*, KNNData*, WallGroup*, float const, uint const) = antiPenetrationWall;
 int main() {
     AgentGroup* grp = nullptr;
     (void)grp;

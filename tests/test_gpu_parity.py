@@ -300,6 +300,35 @@ def test_avoid_stages_match_oracle_on_golden_inputs():
     np.testing.assert_array_equal(out.applied, z["ap_out_applied"])
 
 
+def test_wall_antipenetration_matches_reference_golden():
+    """updateGroupWithAntiPenetration and antiPenetrationWall against the
+    reference kernels' outputs, bit for bit: on the wall lists as
+    findKNearestNeighbors writes them (found here on the GPU) and on their
+    transpose (uploaded), both read row-major as the reference kernels do."""
+    z, m = load("wall_antipen")
+    s0 = gstate(z, "in_")
+    n, kw, dt = s0.n, m["knw"], m["dt"]
+    rows = np.concatenate([z["wall_start"][:, :3], z["wall_end"][:, :3],
+                           z["wall_normal"][:, :3]], 1)
+    walls = gs.WallGroup(rows, bins=None, knw=kw)  # already split
+    bins = gs.KNNBinData(m["wc"], m["ws"], 1)
+    calls = {"upd": lambda g, knw: gs.updateGroupWithAntiPenetration(g, knw, walls, dt),
+             "apw": lambda g, knw: gs.antiPenetrationWall(g, knw, walls, dt, 0)}
+    for layout in ("col", "row"):
+        for name, call in calls.items():
+            g = group_of(s0)
+            knw = gs.KNNData(n, kw)
+            if layout == "col":
+                gs.updateKNNDatabase(g, bins)
+                gs.findKNearestNeighbors(g, knw, bins, walls, 1)
+                np.testing.assert_array_equal(knw.download(g)[0], z["knw_col"])
+            else:
+                knw.upload(z["knw_row"], None, g)
+                np.testing.assert_array_equal(knw.download(g)[0], z["knw_row"])
+            call(g, knw)
+            assert_state(g.download(), gstate(z, f"{name}_{layout}_"))
+
+
 def test_wall_split_matches_oracle():
     for gap in (7.5, 10.0, 32.5):
         for ws, wc in (((128.0, 10.0, 128.0), (64, 1, 64)), ((512.0, 10.0, 512.0), (256, 1, 256))):

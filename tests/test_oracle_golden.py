@@ -140,6 +140,43 @@ def test_avoid_stages_match_reference():
             assert (want.applied & 1024).any()
 
 
+def test_agent_antipenetration_matches_reference():
+    """antiPenetrationAgents on the choke-point crowd, a third of it masked."""
+    z, m = load("avoid_stages")
+    s = state(z, "in_")
+    s.applied[:] = z["ap_in_applied"]
+    pos_b, rad_b, app_b = s.position.copy(), s.radius.copy(), s.applied.copy()
+    ol.oracle().orc_antipenetration_agents(
+        C.byref(ol.group_struct(s)), ol.ptr(z["knn_idx"], C.c_uint), ol.ptr(z["knn_dist"]),
+        ol.ptr(pos_b), ol.ptr(rad_b), ol.ptr(app_b, C.c_uint), s.n, 4096)
+    np.testing.assert_array_equal(s.position, z["ap_out_position"])
+    np.testing.assert_array_equal(s.applied, z["ap_out_applied"])
+    assert ((s.applied & 8192) != 0).sum() > 20
+
+
+def test_wall_antipenetration_matches_reference():
+    """updateGroupWithAntiPenetration and antiPenetrationWall, bit for bit,
+    on the wall KNN as written (column-major) and on its transpose."""
+    z, m = load("wall_antipen")
+    o = ol.oracle()
+    walls = ol.walls_struct(z["wall_start"], z["wall_mid"], z["wall_end"], z["wall_normal"])
+    for layout in ("col", "row"):
+        knl = ol.ptr(z[f"knw_{layout}"], C.c_uint)
+        s = state(z, "in_")
+        o.orc_update_with_antipenetration(C.byref(ol.group_struct(s)), knl, m["knw"],
+                                          C.byref(walls), C.c_float(m["dt"]))
+        want = state(z, f"upd_{layout}_")
+        assert (want.speed > 0).all()
+        assert_state_equal(s, want)
+        s = state(z, "in_")
+        o.orc_antipenetration_wall(C.byref(ol.group_struct(s)), knl, m["knw"], C.byref(walls),
+                                   C.c_float(m["dt"]))
+        assert_state_equal(s, state(z, f"apw_{layout}_"))
+    # the transposed lists reach the walls: both kernels fire on many agents
+    assert ((z["upd_row_applied"] & 4096) != 0).sum() > 50
+    assert ((z["apw_row_applied"] & 4096) != 0).sum() > 30
+
+
 def test_flock_steps_match_reference():
     z, m = load("flock_steps")
     s = state(z, "in_")

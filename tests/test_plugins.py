@@ -169,3 +169,78 @@ def test_chokepoint_new_plugin_with_path_and_antipenetration(tmp_path):
     dropin = g2.download()
     for k in FIELDS:
         np.testing.assert_array_equal(getattr(got, k), getattr(dropin, k), err_msg=k)
+
+
+# CtfEnemyGroup's values (plugins/ChokePointGroup.cpp:148-203): weights, masks,
+# neighbourhoods; the path and the goal are the test's.
+CPG = {"min_time_wall": 10.0, "w_walls": 1.0, "mask_walls": 0, "path_time": 5.0, "w_path": 1.0,
+       "mask_path": 16, "w_seek": 1.0, "mask_seek": 256, "sep_min": 0.5, "sep_max": 1.2,
+       "sep_cos": -0.8660254, "w_sep": 10.0, "mask_sep": 4096, "ali_min": 0.5, "ali_max": 7.0,
+       "ali_cos": -0.8660254, "w_ali": 2.5, "mask_ali": 272, "coh_min": 0.5, "coh_max": 7.0,
+       "coh_cos": -0.8660254, "w_coh": 1.0, "mask_coh": 272, "mask_antipen": 4352}
+
+
+def oracle_chokepoint_group(s, p, walls, path, goal, frames, dt):
+    """CtfEnemyGroup::update (ChokePointGroup.cpp:683-728), one oracle call per
+    reference call, on a copy of s."""
+    C = ol.C
+    o = ol.oracle()
+    st, mid, en, nm = walls
+    W = ol.walls_struct(st, mid, en, nm)
+    s = s.copy()
+    n, k, kw = s.n, p.k, p.knw
+    c = CPG
+    f = C.c_float
+    for _ in range(frames):
+        G = C.byref(ol.group_struct(s))
+        o.orc_wrap_world(G, ol.f3(p.world_size), sc.WRAP_REFERENCE)
+        s.applied[:] = 0
+        idx, dist = ol.knn_binned(s.position, s.position, True, p.world_size, p.world_cells, 1, k)
+        widx, _ = ol.knn_binned(s.position, mid, False, p.world_size, p.world_cells, 1, kw)
+        ip, wp = ol.ptr(idx, C.c_uint), ol.ptr(widx, C.c_uint)
+        o.orc_steer_avoid_walls(G, wp, kw, C.byref(W), f(c["min_time_wall"]), f(c["w_walls"]),
+                                c["mask_walls"])
+        o.orc_steer_follow_path(G, C.byref(path), f(c["path_time"]), f(c["w_path"]),
+                                c["mask_path"])
+        o.orc_steer_seek(G, ol.f3(goal), f(c["w_seek"]), c["mask_seek"])
+        o.orc_steer_separation(G, ip, k, ol.ptr(s.position), n, f(c["sep_min"]),
+                               f(c["sep_max"]), f(c["sep_cos"]), f(c["w_sep"]), c["mask_sep"])
+        o.orc_steer_alignment(G, ip, k, ol.ptr(s.position), ol.ptr(s.direction), n,
+                              f(c["ali_min"]), f(c["ali_max"]), f(c["ali_cos"]), f(c["w_ali"]),
+                              c["mask_ali"])
+        o.orc_steer_cohesion(G, ip, k, ol.ptr(s.position), n, f(c["coh_min"]), f(c["coh_max"]),
+                             f(c["coh_cos"]), f(c["w_coh"]), c["mask_coh"])
+        o.orc_update_with_antipenetration(G, wp, kw, C.byref(W), f(dt))
+        pb, rb, ab = s.position.copy(), s.radius.copy(), s.applied.copy()
+        o.orc_antipenetration_agents(G, ip, ol.ptr(dist), ol.ptr(pb), ol.ptr(rb),
+                                     ol.ptr(ab, C.c_uint), n, c["mask_antipen"])
+    return s
+
+
+def test_chokepoint_group_plugin_with_wall_antipenetration(tmp_path):
+    """CtfEnemyGroup::update (ChokePointGroup.cpp:683-728) through the C++
+    drop-in: the applied bits cleared by the plugin's own cudaMemset on the
+    group's device array, updateGroupWithAntiPenetration and
+    antiPenetrationAgents; bit for bit the oracle composed call for call."""
+    p = sc.chokepoint_params()
+    pts, radius, goal, dt, frames = [(0.0, 0.0, 13.5), (0.0, 0.0, -1650.0)], 23.5, \
+        (0.0, 0.0, -93.5), 0.1, 25
+    s = sc.chokepoint_agents(5000, x_range=(-45.0, 45.0), z_range=(14.0, 44.0), seed=23)
+    s.speed[:] = np.float32(2.0)
+    rows = sc.chokepoint_walls(10.0)
+    mp = tmp_path / "ChokePoint10.map"
+    mp.write_text("\n".join(" ".join(f32(x) for x in r) for r in rows) + "\n")
+    args = {"world": v3(p.world_size), "cells": ",".join(str(c) for c in p.world_cells),
+            "k": p.k, "knw": p.knw, "map": str(mp), "path": ";".join(v3(q) for q in pts),
+            "path_radius": f32(radius), "goal": v3(goal), "dt": f32(dt)}
+    args.update({key: (f32(v) if isinstance(v, float) else v) for key, v in CPG.items()})
+    got = run_driver(tmp_path, "ChokePointGroup", s, frames, args)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    walls = gs.WallGroup(rows, bins=bins, knw=p.knw).download()
+    want = oracle_chokepoint_group(s, p, walls, ol.path_init(pts, radius, False), goal, frames,
+                                   np.float32(dt))
+    for k in FIELDS:
+        np.testing.assert_array_equal(getattr(got, k), getattr(want, k), err_msg=k)
+    # the frame's wall anti-penetration and agent anti-penetration both fired
+    assert ((want.applied & 4096) != 0).sum() > 20
+    assert ((want.applied & 8192) != 0).sum() > 20
