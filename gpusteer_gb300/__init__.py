@@ -9,7 +9,8 @@ from ._lib import GpuSteerError, load  # noqa: F401
 from .groups import (  # noqa: F401
     AgentGroup, Batch, KNNBinData, KNNData, Path, Rollout, WallGroup, antiPenetrationAgents,
     antiPenetrationWall, updateGroupWithAntiPenetration,
-    findKNearestNeighbors, findKNearestNeighborsBruteForce, set_block, set_graphs,
+    findKNearestNeighbors, findKNearestNeighborsBruteForce, findKNearestNeighborsGroups,
+    set_block, set_graphs,
     set_knn_capacity, step, step_host, steerForAlignment, steerForCohesion,
     steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, steerToFollowPath,
     updateGroup,

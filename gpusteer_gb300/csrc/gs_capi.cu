@@ -823,6 +823,66 @@ gs_status gs_find_knn(gs_group g, gs_knn out, gs_bins bins, gs_group other,
     return GS_OK;
 }
 
+gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins bins,
+                             gs_knn* out) {
+    if (!groups || !bins || !out || n_groups == 0) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (size_t(n_groups) * n_groups > kMaxKnnPairs)
+        return fail(GS_ERR_INVALID_ARG, "at most 7 groups (49 pairs) per batched KNN");
+    for (unsigned i = 0; i < n_groups; ++i) {
+        gs_group g = groups[i];
+        if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+        if (!g->db.valid || g->db.cells != bins->cells)
+            return fail(GS_ERR_STATE, "call gs_update_knn_database on every group first");
+    }
+    KnnPairs P;
+    std::memset(&P, 0, sizeof(P));
+    P.grid = bins->grid;
+    P.r = bins->radius;
+    for (unsigned i = 0; i < n_groups; ++i)
+        for (unsigned j = 0; j < n_groups; ++j) {
+            gs_knn o = out[size_t(i) * n_groups + j];
+            if (!o) continue;
+            gs_group a = groups[i], b = groups[j];
+            if (o->n != a->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from its group");
+            KnnPair& q = P.pair[P.n_pairs++];
+            q.a_sorted = a->db.sorted;
+            q.a_pos_id = a->db.pos_id;
+            q.b_start = b->db.start;
+            q.b_pos_id = b->db.pos_id;
+            q.idx = o->idx;
+            q.dist = o->dist;
+            q.nA = a->n;
+            q.k = o->k;
+            q.self = a == b;
+        }
+    if (P.n_pairs == 0) return GS_OK;
+    // One launch on the first group's stream, after every group's database
+    // build; every group's stream then waits for it.
+    cudaStream_t st = groups[0]->stream;
+    for (unsigned i = 1; i < n_groups; ++i)
+        if (groups[i]->stream != st) GS_CUDA(cudaStreamSynchronize(groups[i]->stream));
+    GS_TRY(launch_knn_binned_pairs(P, st));
+    cudaEvent_t done = nullptr;
+    for (unsigned i = 1; i < n_groups; ++i) {
+        if (groups[i]->stream == st) continue;
+        if (!done) {
+            GS_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+            const cudaError_t e = cudaEventRecord(done, st);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(done);
+                return cuda_fail(e, "cudaEventRecord");
+            }
+        }
+        const cudaError_t e = cudaStreamWaitEvent(groups[i]->stream, done, 0);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(done);
+            return cuda_fail(e, "cudaStreamWaitEvent");
+        }
+    }
+    if (done) cudaEventDestroy(done);
+    return GS_OK;
+}
+
 gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls,
                             unsigned search_radius) {
     (void)search_radius;

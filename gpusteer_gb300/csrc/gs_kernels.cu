@@ -281,6 +281,63 @@ static gs_status knn_binned_k(const Database& A, unsigned nA, const Database& B,
     return GS_OK;
 }
 
+// ---- batched binned KNN over group pairs --------------------------------------
+// The k_knn_binned search for several (A, B) database pairs in one launch: the
+// pair table rides in the kernel parameters, each pair owns a contiguous run
+// of blocks, and a block finds its pair by a scan of the (few) block offsets.
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_knn_binned_pairs(KnnPairs P) {
+    unsigned q = 0;
+    while (q + 1 < P.n_pairs && blockIdx.x >= P.pair[q + 1].block_begin) ++q;
+    const KnnPair& pr = P.pair[q];
+    const unsigned s = (blockIdx.x - pr.block_begin) * blockDim.x + threadIdx.x;
+    if (s >= pr.nA) return;
+    const unsigned a = pr.a_sorted[s];
+    const V3 p = v3(pr.a_pos_id[s]);
+    unsigned ix, iy, iz;
+    cell_coords(P.grid, p, ix, iy, iz);
+    const Box box = cell_box(P.grid, ix, iy, iz, P.r);
+    extern __shared__ unsigned sh_col[];
+    unsigned* col = sh_col + threadIdx.x;
+    const unsigned bd = blockDim.x;
+    knn_neighbours<KMAX, 64>(int(pr.k), p, pr.self ? a : UINT_MAX, P.grid, box, 0u, pr.b_start,
+                             pr.b_pos_id, col, bd);
+    for (unsigned r = 0; r < pr.k; ++r) {
+        const unsigned bs = col[r * bd];
+        const float4 v = bs == UINT_MAX ? make_float4(0.f, 0.f, 0.f, 0.f) : pr.b_pos_id[bs];
+        pr.idx[a + size_t(r) * pr.nA] = bs == UINT_MAX ? UINT_MAX : __float_as_uint(v.w);
+        pr.dist[a + size_t(r) * pr.nA] = bs == UINT_MAX ? FLT_MAX : distance(p, v3(v));
+    }
+}
+
+template <int KMAX>
+static gs_status knn_pairs_k(const KnnPairs& P, unsigned blocks, cudaStream_t st) {
+    const size_t smem = size_t(2 * 64) * kBlock * sizeof(unsigned);
+    if (smem > 48 * 1024)
+        GS_CUDA(cudaFuncSetAttribute(k_knn_binned_pairs<KMAX>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    k_knn_binned_pairs<KMAX><<<blocks, kBlock, smem, st>>>(P);
+    GS_LAUNCHED("knn_binned_pairs");
+    return GS_OK;
+}
+static_assert(sizeof(KnnPairs) <= 4096, "batched KNN parameters exceed 4 KiB");
+
+gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st) {
+    if (P.n_pairs == 0 || P.n_pairs > kMaxKnnPairs)
+        return fail(GS_ERR_INVALID_ARG, "between 1 and 49 group pairs per batched KNN");
+    unsigned blocks = 0, kmax = 0;
+    for (unsigned q = 0; q < P.n_pairs; ++q) {
+        P.pair[q].block_begin = blocks;
+        blocks += blocks_for(P.pair[q].nA);
+        kmax = std::max(kmax, P.pair[q].k);
+    }
+    if (blocks == 0) return GS_OK;
+    if (kmax <= 8) return knn_pairs_k<8>(P, blocks, st);
+    if (kmax <= 16) return knn_pairs_k<16>(P, blocks, st);
+    if (kmax <= 32) return knn_pairs_k<32>(P, blocks, st);
+    return knn_pairs_k<64>(P, blocks, st);
+}
+
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
                             unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
     if (nA == 0) return GS_OK;

@@ -21,6 +21,26 @@ gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid
 // ---- per-function (drop-in) kernels -----------------------------------------
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
                             unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
+// Batched binned KNN over (A, B) database pairs of one grid (every group pair
+// of a MultiGroup frame): one launch, results as launch_knn_binned per pair.
+// 49 pairs (seven groups, every pair) keep the parameter block under 4 KiB.
+constexpr unsigned kMaxKnnPairs = 49;
+struct KnnPair {
+    const unsigned* a_sorted;
+    const float4* a_pos_id;
+    const unsigned* b_start;
+    const float4* b_pos_id;
+    unsigned* idx;
+    float* dist;
+    unsigned nA, k, block_begin;
+    bool self;
+};
+struct KnnPairs {
+    KnnPair pair[kMaxKnnPairs];
+    Grid grid;
+    unsigned r, n_pairs;
+};
+gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st);
 // seed (may be null, k <= 32 only): per query of A an upper bound of its k-th distance.
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
                            bool self, unsigned k, const float* seed, unsigned* idx, float* dist,

@@ -428,6 +428,16 @@ def findKNearestNeighbors(group: AgentGroup, knn: KNNData, bins: KNNBinData, oth
              int(search_radius))
 
 
+def findKNearestNeighborsGroups(groups, bins: KNNBinData, knns) -> None:
+    """findKNearestNeighbors for every group pair of a MultiGroup frame in one
+    launch: knns[i][j] (None to skip) gets group i's lists against group j."""
+    G = len(groups)
+    hs = (C.c_void_p * G)(*[grp.handle for grp in groups])
+    out = (C.c_void_p * (G * G))(*[(knns[i][j].handle if knns[i][j] is not None else None)
+                                   for i in range(G) for j in range(G)])
+    call("gs_find_knn_groups", hs, G, bins.handle, out)
+
+
 def findKNearestNeighborsBruteForce(group: AgentGroup, knn: KNNData, other: AgentGroup) -> None:
     call("gs_knn_bruteforce", group.handle, knn.handle, other.handle)
 

@@ -672,6 +672,21 @@ inline void antiPenetrationWall(AgentGroup* pAgentGroup, KNNData* pKNNData, Wall
     gsCheck(gs_anti_penetration_wall(detail::group(pAgentGroup), pKNNData->handle(),
                                      pWallGroup->gsWalls(), elapsedTime, doNotApplyWith));
 }
+/* No counterpart in the reference: findKNearestNeighbors for every group
+ * pair of a MultiGroup frame (MultiGroup.cpp:560-564) in one launch;
+ * ppKNNData[i * nGroups + j] (null to skip) receives group i against group j,
+ * equal to the per-pair calls. */
+inline void findKNearestNeighborsGroups(AgentGroup* const* ppGroups, uint const nGroups,
+                                        KNNBinData* pKNNBinData, KNNData* const* ppKNNData) {
+    std::vector<gs_group> g(nGroups);
+    for (uint i = 0; i < nGroups; ++i) g[i] = ppGroups[i]->gsGroup();
+    std::vector<gs_knn> out(size_t(nGroups) * nGroups, nullptr);
+    for (size_t q = 0; q < out.size(); ++q)
+        if (ppKNNData[q]) out[q] = ppKNNData[q]->handle();
+    gsCheck(gs_find_knn_groups(g.data(), nGroups, pKNNBinData->handle(), out.data()));
+    for (size_t q = 0; q < out.size(); ++q)
+        if (ppKNNData[q]) ppKNNData[q]->setSyncHost(g[q / nGroups]);
+}
 /* :216 */
 inline void antiPenetrationAgents(AgentGroup* pAgentGroup, KNNData* pKNNData,
                                   AgentGroup* pOtherGroup, uint const doNotApplyWith) {

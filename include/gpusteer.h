@@ -209,6 +209,14 @@ gs_status gs_walls_update_knn_database(gs_walls w, gs_bins bins);
 gs_status gs_find_knn(gs_group g, gs_knn out, gs_bins bins, gs_group other,
                       unsigned search_radius);
 /* findKNearestNeighbors against a WallGroup (plugins/ChokePointNew.cpp:600). */
+/* findKNearestNeighbors for every group pair of a MultiGroup frame
+ * (plugins/MultiGroup.cpp:560-564 calls it once per pair) in one launch:
+ * out[i * n_groups + j] (NULL to skip a pair) receives group i's lists against
+ * group j.  Every pair reads only the databases of gs_update_knn_database, so
+ * the lists equal the per-pair calls' bit for bit, also when the groups are
+ * stepped in turn between the calls as MultiGroup does.  At most 7 groups. */
+gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins bins,
+                             gs_knn* out);
 gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls,
                             unsigned search_radius);
 /* KNNBruteForceCUDAV2 (KNNBruteForceCUDA.cu:163-187). */

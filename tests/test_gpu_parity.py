@@ -694,6 +694,50 @@ def test_multigroup_cross_group_steps_match_oracle():
         assert_state(g.download(), s, skip_side=s.speed == 0)
 
 
+def test_multigroup_batched_knn_equals_per_pair_calls():
+    """gs_find_knn_groups: every group pair's lists in one launch, taken at the
+    start of a MultiGroup frame, equal the per-pair findKNearestNeighbors calls
+    that Group::update makes in turn after the earlier groups have moved, and
+    the oracle's.  Pairs carry different k, one pair is skipped, and one group
+    appears twice (its pairs with itself are self searches)."""
+    p = sc.boids_params(k=8, world=96.0, cell=4.0)
+    states = [sc.boids_sphere(3000, radius=18.0, seed=41), sc.boids_sphere(2000, radius=18.0, seed=42),
+              sc.boids_sphere(1200, radius=12.0, seed=43)]
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    groups = [group_of(s, 16) for s in states]
+    seq = groups + [groups[1]]  # group 1 listed twice
+    sizes = [st.n for st in states] + [states[1].n]
+    G = len(seq)
+    kk = [[16 if (i + j) % 2 else 8 for j in range(G)] for i in range(G)]
+    for frame in range(4):
+        for g in groups:
+            gs.wrapWorld(g, p.world_size, sc.WRAP_REFERENCE)
+            gs.updateKNNDatabase(g, bins)
+        snap = [g.download().position.copy() for g in seq]
+        batched = [[gs.KNNData(sizes[i], kk[i][j]) if (i, j) != (2, 0) else None
+                    for j in range(G)] for i in range(G)]
+        gs.findKNearestNeighborsGroups(seq, bins, batched)
+        for i in range(G):
+            for j in range(G):
+                if batched[i][j] is None:
+                    continue
+                single = gs.KNNData(sizes[i], kk[i][j])
+                gs.findKNearestNeighbors(seq[i], single, bins, seq[j], 1)
+                bi, bd = batched[i][j].download(seq[i])
+                si, sd = single.download(seq[i])
+                np.testing.assert_array_equal(bi, si)
+                np.testing.assert_array_equal(bd, sd)
+                if frame == 0 and i < 3:
+                    oi, od = ol.knn_binned(snap[i], snap[j], seq[i] is seq[j], p.world_size,
+                                           p.world_cells, 1, kk[i][j])
+                    np.testing.assert_array_equal(bi, oi)
+                    np.testing.assert_array_equal(bd, od)
+            if i < 3:  # this group steps before the next group's per-pair calls
+                gs.steerForSeparation(seq[i], batched[i][i], seq[i], p.sep_min, p.sep_max,
+                                      p.sep_cos, p.w_sep, 0)
+                gs.updateGroup(seq[i], p.dt)
+
+
 # ---- path following (SteerToFollowPathCUDAKernel.cu, PolylinePathwayCUDA.cu) ----------
 
 @pytest.mark.parametrize("name", ["line", "loop", "bend"])
