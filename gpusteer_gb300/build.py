@@ -78,7 +78,8 @@ def build_headless(force: bool = False, verbose: bool = False) -> Path:
     """The headless plugin driver: C++ plugins on include/GroupSteerLibrary.h,
     linked against libgpusteer.so (found next to it at run time)."""
     inc = PKG.parent / "include"
-    deps = [HEADLESS_SRC, LIB, inc / "GroupSteerLibrary.h", inc / "PlugIn.h", inc / "gpusteer.h"]
+    deps = [HEADLESS_SRC, LIB, inc / "GroupSteerLibrary.h", inc / "PlugIn.h", inc / "gpusteer.h",
+            inc / "SimulationParams.h"]
     if not force and not _stale(HEADLESS, deps):
         return HEADLESS
     cuda = Path(nvcc()).resolve().parent.parent

@@ -21,7 +21,11 @@
 //               antiPenetrationAgents
 //
 //   gs_headless <Boids|ChokePoint|ChokePointNew|ChokePointGroup> <state_in> <state_out> <frames>
-//               [key=value ...]
+//               [params=<file.params>] [key=value ...]
+//
+// params= loads a scenario file with SimulationParams (include/SimulationParams.h)
+// and supplies the values the reference's plugins read from it; key=value
+// arguments override single values.
 //
 // State files: uint32 n, then position (4n f32), direction (4n), steering
 // (4n), side (3n), up (3n), speed, max_speed, max_force, radius, mass (n
@@ -41,6 +45,7 @@
 
 #include "GroupSteerLibrary.h"
 #include "PlugIn.h"
+#include "SimulationParams.h"
 
 using namespace OpenSteer;
 
@@ -71,6 +76,74 @@ uint3 u3param(const Params& p, const char* k, uint3 def) {
     char c;
     in >> def.x >> c >> def.y >> c >> def.z;
     return def;
+}
+
+// The values a plugin reads from its SimulationParams (ChokePointNew.cpp:589-629
+// reads m_pSimulationParams->...), as this driver's key=value parameters; keys
+// given on the command line win.  Floats are printed with 9 significant
+// digits, which read back to the same binary32 value.  A relative map file
+// name is taken relative to the .params file.
+void apply_simulation_params(const char* file, Params& p) {
+    SimulationParams sp;
+    sp.load(file);
+    const std::string f(file);
+    const size_t slash = f.find_last_of('/');
+    const std::string dir = slash == std::string::npos ? std::string(".") : f.substr(0, slash);
+    auto put = [&](const char* k, std::string const& v) {
+        if (!p.count(k)) p[k] = v;
+    };
+    auto fl = [](float v) {
+        char b[32];
+        std::snprintf(b, sizeof(b), "%.9g", v);
+        return std::string(b);
+    };
+    auto un = [](unsigned v) { return std::to_string(v); };
+    auto f3s = [&](float3 v) { return fl(v.x) + "," + fl(v.y) + "," + fl(v.z); };
+    const WorldParams& w = sp.m_WorldParams;
+    put("world", f3s(w.m_f3Dimensions));
+    put("cells", un(w.m_u3Cells.x) + "," + un(w.m_u3Cells.y) + "," + un(w.m_u3Cells.z));
+    put("k", un(sp.m_nKNN));
+    put("knw", un(sp.m_nKNW));
+    put("radius", un(sp.m_nSearchRadius));
+    if (!w.m_strMapFilename.empty())
+        put("map", w.m_strMapFilename[0] == '/' ? w.m_strMapFilename : dir + "/" + w.m_strMapFilename);
+    put("min_time_wall", fl(sp.m_fMinTimeToWall));
+    put("w_walls", fl(sp.m_fWeightAvoidWalls));
+    put("mask_walls", un(sp.m_nMaskAvoidWalls));
+    put("min_time_col", fl(sp.m_fMinTimeToCollision));
+    put("min_sep", fl(sp.m_fMinSeparationDistance));
+    put("avoid_close", un(sp.m_bAvoidCloseNeighbors ? 1u : 0u));
+    put("w_avoid", fl(sp.m_fWeightAvoidNeighbors));
+    put("mask_avoid", un(sp.m_nMaskAvoidNeighbors));
+    put("sep_min", fl(sp.m_fMinSeparationDistance));
+    put("sep_max", fl(sp.m_fMaxSeparationDistance));
+    put("sep_cos", fl(sp.m_fCosMaxFlockingAngle));
+    put("w_sep", fl(sp.m_fWeightSeparation));
+    put("mask_sep", un(sp.m_nMaskSeparation));
+    for (const char* b : {"ali", "coh"}) {
+        const std::string pre(b);
+        put((pre + "_min").c_str(), fl(sp.m_fMinFlockingDistance));
+        put((pre + "_max").c_str(), fl(sp.m_fMaxFlockingDistance));
+        put((pre + "_cos").c_str(), fl(sp.m_fCosMaxFlockingAngle));
+    }
+    put("w_ali", fl(sp.m_fWeightAlignment));
+    put("mask_ali", un(sp.m_nMaskAlignment));
+    put("w_coh", fl(sp.m_fWeightCohesion));
+    put("mask_coh", un(sp.m_nMaskCohesion));
+    put("path_time", fl(sp.m_fPathPredictionTime));
+    put("w_path", fl(sp.m_fWeightFollowPath));
+    put("mask_path", un(sp.m_nMaskFollowPath));
+    put("w_seek", fl(sp.m_fWeightSeek));
+    put("mask_seek", un(sp.m_nMaskSeek));
+    put("mask_antipen", un(sp.m_nMaskAntiPenetrationAgents));
+    if (!sp.m_vecGroupParams.empty()) {
+        const GroupParams& g = sp.m_vecGroupParams[0];
+        std::string path;
+        for (float3 const& q : g.m_vecPathPoints) path += (path.empty() ? "" : ";") + f3s(q);
+        if (!path.empty()) put("path", path);
+        put("path_radius", fl(g.m_fPathRadius));
+        put("path_cyclic", un(g.m_bPathIsCyclic ? 1u : 0u));
+    }
 }
 
 // ---- state files ---------------------------------------------------------------------
@@ -485,6 +558,11 @@ int main(int argc, char** argv) {
         plugin->params[std::string(argv[i], size_t(eq - argv[i]))] = eq + 1;
     }
     try {
+        auto pf = plugin->params.find("params");
+        if (pf != plugin->params.end()) {
+            const std::string file = pf->second;
+            apply_simulation_params(file.c_str(), plugin->params);
+        }
         const float dt = fparam(plugin->params, "dt", 1.f / 60.f);
         runHeadless(*plugin, frames, dt, frames ? frames : 1);
     } catch (const std::exception& e) {

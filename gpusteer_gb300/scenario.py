@@ -412,6 +412,37 @@ def params_from_file(sim: SimulationParams, dt: float) -> StepParams:
         dt=dt)
 
 
+def chokepoint_new_from_file(sim: SimulationParams, dt: float = 1.0 / 30.0, group: int = 0):
+    """CtfGroup::update (plugins/ChokePointNew.cpp:586-630) with a parsed
+    .params file: (StepParams, path points, path radius, cyclic).  Walls,
+    separation (mask KERNEL_ANTI_PENETRATION_WALL, as the plugin passes it,
+    :615), alignment, cohesion, follow path, seek the path's second point;
+    the closing antiPenetrationAgents takes maskAntiPenetrationAgents."""
+    v, w, g = sim.values, sim.world, sim.groups[group]
+    pts = [tuple(float(c) for c in q) for q in g["path"]]
+    if len(pts) < 2:
+        raise ParamsError("the group needs a path of at least two points")
+    cos = v["cosMaxFlockingAngle"]
+    p = StepParams(
+        world_size=tuple(w["dimensions"]), world_cells=tuple(w["cells"]),
+        search_radius=v["searchRadius"], wrap_mode=WRAP_REFERENCE, k=v["knn"], knw=v["knw"],
+        clear_applied=1,
+        min_time_to_wall=v["minTimeToWall"], w_walls=v["weightAvoidWalls"],
+        mask_walls=v["maskAvoidWalls"],
+        sep_min=v["minSeparationDistance"], sep_max=v["maxSeparationDistance"], sep_cos=cos,
+        w_sep=v["weightSeparation"], mask_sep=KERNEL_ANTI_PENETRATION_WALL,
+        ali_min=v["minFlockingDistance"], ali_max=v["maxFlockingDistance"], ali_cos=cos,
+        w_ali=v["weightAlignment"], mask_ali=v["maskAlignment"],
+        coh_min=v["minFlockingDistance"], coh_max=v["maxFlockingDistance"], coh_cos=cos,
+        w_coh=v["weightCohesion"], mask_coh=v["maskCohesion"],
+        seek_target=pts[1], w_seek=v["weightSeek"], mask_seek=v["maskSeek"],
+        path_prediction_time=v["pathPredictionTime"], w_path=v["weightFollowPath"],
+        mask_path=v["maskFollowPath"],
+        order=(B_AVOID_WALLS, B_SEPARATION, B_ALIGNMENT, B_COHESION, B_FOLLOW_PATH, B_SEEK),
+        dt=dt)
+    return p, pts, float(g.get("pathRadius", 0.0)), bool(g.get("cyclic", 0))
+
+
 CHOKEPOINT_GAPS = (7.5, 10.0, 12.5, 15.0, 17.5, 20.0, 22.5, 25.0, 27.5, 30.0, 32.5)
 
 

@@ -186,3 +186,156 @@ def test_headless_driver_builds_and_links():
     gb.build()
     r = subprocess.run([str(gb.HEADLESS)], capture_output=True, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+PARAMS_DUMP = r'''
+#include <cstdio>
+#include "SimulationParams.h"
+using namespace OpenSteer;
+static void f3(const char* k, float3 v) { std::printf("%s %.9g %.9g %.9g\n", k, v.x, v.y, v.z); }
+int main(int argc, char** argv) {
+    SimulationParams p;
+    try {
+        p.load(argv[1]);
+    } catch (ParamsError const& e) {
+        std::printf("error %s\n", e.what());
+        return 0;
+    }
+#define U(m, k) std::printf("%s %u\n", k, unsigned(p.m));
+#define F(m, k) std::printf("%s %.9g\n", k, p.m);
+    U(m_nSeed, "seed") U(m_nKNN, "knn") U(m_nKNO, "kno") U(m_nKNW, "knw")
+    U(m_nSearchRadius, "searchRadius") U(m_bAvoidCloseNeighbors, "avoidCloseNeighbors")
+    F(m_fMaxPursuitPredictionTime, "maxPursuitPredictionTime")
+    F(m_fMinTimeToCollision, "minTimeToCollision") F(m_fMinTimeToObstacle, "minTimeToObstacle")
+    F(m_fMinTimeToWall, "minTimeToWall") F(m_fPathPredictionTime, "pathPredictionTime")
+    F(m_fMinSeparationDistance, "minSeparationDistance")
+    F(m_fMaxSeparationDistance, "maxSeparationDistance")
+    F(m_fMinFlockingDistance, "minFlockingDistance") F(m_fMaxFlockingDistance, "maxFlockingDistance")
+    F(m_fCosMaxFlockingAngle, "cosMaxFlockingAngle")
+    F(m_fWeightAlignment, "weightAlignment") F(m_fWeightCohesion, "weightCohesion")
+    F(m_fWeightSeparation, "weightSeparation") F(m_fWeightPursuit, "weightPursuit")
+    F(m_fWeightSeek, "weightSeek") F(m_fWeightFollowPath, "weightFollowPath")
+    F(m_fWeightAvoidObstacles, "weightAvoidObstacles") F(m_fWeightAvoidWalls, "weightAvoidWalls")
+    F(m_fWeightAvoidNeighbors, "weightAvoidNeighbors")
+    U(m_nMaskAlignment, "maskAlignment") U(m_nMaskAntiPenetrationAgents, "maskAntiPenetrationAgents")
+    U(m_nMaskCohesion, "maskCohesion") U(m_nMaskSeparation, "maskSeparation")
+    U(m_nMaskSeek, "maskSeek") U(m_nMaskFlee, "maskFlee") U(m_nMaskPursuit, "maskPursuit")
+    U(m_nMaskEvade, "maskEvade") U(m_nMaskFollowPath, "maskFollowPath")
+    U(m_nMaskAvoidObstacles, "maskAvoidObstacles") U(m_nMaskAvoidWalls, "maskAvoidWalls")
+    U(m_nMaskAvoidNeighbors, "maskAvoidNeighbors")
+    f3("world.dimensions", p.m_WorldParams.m_f3Dimensions);
+    std::printf("world.cells %u %u %u\n", p.m_WorldParams.m_u3Cells.x, p.m_WorldParams.m_u3Cells.y,
+                p.m_WorldParams.m_u3Cells.z);
+    std::printf("world.obstacleCount %u\n", p.m_WorldParams.m_nObstacleCount);
+    std::printf("world.mapFilename %s\n", p.m_WorldParams.m_strMapFilename.c_str());
+    for (GroupParams const& g : p.m_vecGroupParams) {
+        std::printf("group %u %.9g %.9g %.9g %.9g %.9g %u\n", g.m_nNumAgents, g.m_fMaxSpeed,
+                    g.m_fMaxForce, g.m_fMinStartRadius, g.m_fMaxStartRadius, g.m_fPathRadius,
+                    unsigned(g.m_bPathIsCyclic));
+        f3("group.startPosition", g.m_f3StartPosition);
+        f3("group.bodyColor", g.m_f3BodyColor);
+        for (float3 const& q : g.m_vecPathPoints) f3("group.point", q);
+    }
+    return 0;
+}
+'''
+
+
+def _params_dump_binary(tmp_path):
+    import shutil
+    import subprocess
+
+    from gpusteer_gb300 import build as gb
+
+    src = tmp_path / "dump.cpp"
+    src.write_text(PARAMS_DUMP)
+    exe = tmp_path / "dump"
+    cuda_inc = Path(gb.nvcc()).resolve().parent.parent / "include"
+    r = subprocess.run([shutil.which("g++"), "-std=c++17", "-Wall", "-Werror", "-O1",
+                        "-I", str(REPO / "include"), "-I", str(cuda_inc), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def _python_dump(p) -> list:
+    f32 = lambda x: float(np.float32(x))  # noqa: E731
+    g9 = lambda x: f"{f32(x):.9g}"  # noqa: E731
+    v = p.values
+    lines = []
+    for k in ("seed", "knn", "kno", "knw", "searchRadius", "avoidCloseNeighbors"):
+        lines.append(f"{k} {int(v.get(k, 0))}")
+    for k in ("maxPursuitPredictionTime", "minTimeToCollision", "minTimeToObstacle",
+              "minTimeToWall", "pathPredictionTime", "minSeparationDistance",
+              "maxSeparationDistance", "minFlockingDistance", "maxFlockingDistance",
+              "cosMaxFlockingAngle", "weightAlignment", "weightCohesion", "weightSeparation",
+              "weightPursuit", "weightSeek", "weightFollowPath", "weightAvoidObstacles",
+              "weightAvoidWalls", "weightAvoidNeighbors"):
+        lines.append(f"{k} {g9(v.get(k, 0.0))}")
+    for k in ("maskAlignment", "maskAntiPenetrationAgents", "maskCohesion", "maskSeparation",
+              "maskSeek", "maskFlee", "maskPursuit", "maskEvade", "maskFollowPath",
+              "maskAvoidObstacles", "maskAvoidWalls", "maskAvoidNeighbors"):
+        lines.append(f"{k} {int(v.get(k, 0))}")
+    w = p.world
+    lines.append("world.dimensions " + " ".join(g9(x) for x in w.get("dimensions", (0, 0, 0))))
+    lines.append("world.cells " + " ".join(str(x) for x in w.get("cells", (0, 0, 0))))
+    lines.append(f"world.obstacleCount {w.get('obstacleCount', 0)}")
+    lines.append(f"world.mapFilename {w.get('mapFilename', '')}")
+    for g in p.groups:
+        lines.append(f"group {g.get('numAgents', 0)} {g9(g.get('maxSpeed', 0))} "
+                     f"{g9(g.get('maxForce', 0))} {g9(g.get('minStartRadius', 0))} "
+                     f"{g9(g.get('maxStartRadius', 0))} {g9(g.get('pathRadius', 0))} "
+                     f"{int(g.get('cyclic', 0))}")
+        lines.append("group.startPosition " + " ".join(g9(x) for x in g.get("startPosition", (0, 0, 0))))
+        lines.append("group.bodyColor " + " ".join(g9(x) for x in g.get("bodyColor", (0, 0, 0))))
+        for q in g["path"]:
+            lines.append("group.point " + " ".join(g9(x) for x in q))
+    return lines
+
+
+def test_cpp_simulation_params_loader_matches_python_reader(tmp_path):
+    """include/SimulationParams.h (SimulationParams::load, Simulation.cpp:7-250)
+    and the Python reader agree on every value of a scenario file, and of the
+    reference's own data/*.params files where the reference tree is present."""
+    import subprocess
+
+    exe = _params_dump_binary(tmp_path)
+    text = """# header
+    seed = 7
+    knn = 6 # comment after a value
+    cosMaxFlockingAngle = -0.86602540378443864676372317075294
+    avoidCloseNeighbors = 1
+    maskSeek = 4480
+    weightSeek = 1.5
+    <world>
+        dimensions = 2048 10 2048
+        cells = 512 1 512
+        mapFilename = ChokePoint20.map
+    </world>
+    <group>
+        numAgents = 100
+        maxSpeed = 3
+        <path>
+            point = 0 0 13.5
+            #radius = 5
+            point = 0 0 -1650
+            radius = 20
+            cyclic = 0
+        </path>
+        bodyColor = 0.4 0.4 0.6 # Bluish
+    </group>
+    </simulation>
+    """
+    files = [tmp_path / "synthetic.params"]
+    files[0].write_text(text)
+    data = Path("/root/reference/data")
+    if data.exists():
+        files += sorted(data.glob("*.params"))
+    for f in files:
+        got = subprocess.run([str(exe), str(f)], capture_output=True, text=True).stdout.split("\n")
+        want = _python_dump(sc.load_params(f.read_text()))
+        assert got[:len(want)] == want, f.name
+    bad = tmp_path / "bad.params"
+    bad.write_text("bogusKey = 1\n</simulation>\n")
+    out = subprocess.run([str(exe), str(bad)], capture_output=True, text=True).stdout
+    assert out.startswith("error unknown key bogusKey")

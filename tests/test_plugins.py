@@ -244,3 +244,81 @@ def test_chokepoint_group_plugin_with_wall_antipenetration(tmp_path):
     # the frame's wall anti-penetration and agent anti-penetration both fired
     assert ((want.applied & 4096) != 0).sum() > 20
     assert ((want.applied & 8192) != 0).sum() > 20
+
+
+SCENARIO = """# choke-point scenario: the values of the reference's data/ChokePoint.params
+# on a 512 x 512 world
+    seed = 1
+    knn = 16
+    knw = 3
+    searchRadius = 1
+    minTimeToWall = 10
+    pathPredictionTime = 5
+    minSeparationDistance = 0.5
+    maxSeparationDistance = 1.2
+    minFlockingDistance = 0.5
+    maxFlockingDistance = 7
+    cosMaxFlockingAngle = -0.86602540378443864676372317075294
+    weightAlignment = 2.5   # per-value comment
+    weightCohesion = 1
+    weightSeparation = 10
+    weightSeek = 1.5
+    weightFollowPath = 1
+    weightAvoidWalls = 1
+    maskAlignment = 272
+    maskAntiPenetrationAgents = 4096
+    maskCohesion = 272
+    maskSeparation = 4096
+    maskSeek = 4480
+    maskFollowPath = 16
+    maskAvoidWalls = 0
+    <world>
+        dimensions = 512 10 512
+        cells = 256 1 256
+        obstacleCount = 0
+        mapFilename = ChokePoint10.map
+    </world>
+    <group>
+        numAgents = 6000
+        maxSpeed = 3
+        maxForce = 3
+        <path>
+            point = 0 0 13.5
+            point = 0 0 -1650
+            cyclic = 0
+            radius = 20
+        </path>
+    </group>
+</simulation>
+"""
+
+
+def test_chokepoint_new_plugin_from_params_file(tmp_path):
+    """ChokePointNew configured by a .params file, read by the C++ plugin through
+    include/SimulationParams.h and by the Python reader for gs_step
+    (scenario.chokepoint_new_from_file): the plugin, the fused step and the
+    oracle agree bit for bit (closing anti-penetration off)."""
+    pf = tmp_path / "scenario.params"
+    pf.write_text(SCENARIO)
+    rows = sc.chokepoint_walls(10.0)
+    (tmp_path / "ChokePoint10.map").write_text(
+        "\n".join(" ".join(f32(x) for x in r) for r in rows) + "\n")
+    dt = np.float32(1.0 / 30.0)
+    p, pts, radius, cyclic = sc.chokepoint_new_from_file(sc.load_params(SCENARIO), float(dt))
+    assert p.k == 16 and p.mask_seek == 4480 and radius == 20.0 and not cyclic
+    s = sc.chokepoint_agents(6000, seed=29)
+    s.speed[:] = np.float32(1.0)
+    frames = 20
+    got = run_driver(tmp_path, "ChokePointNew", s, frames,
+                     {"params": str(pf), "antipen": 0, "dt": f32(dt)})
+    bins = gs.KNNBinData(p.world_cells, p.world_size, p.search_radius)
+    walls = gs.WallGroup(rows, bins=bins, knw=p.knw)
+    g = gs.AgentGroup(p.k, s.n)
+    g.upload(s)
+    gs.step(g, bins, walls, p, frames, path=gs.Path(pts, radius, cyclic))
+    fused = g.download()
+    want = s.copy()
+    ol.run(want, p, frames, walls=walls.download(), path=ol.path_init(pts, radius, cyclic))
+    for k in FIELDS:
+        np.testing.assert_array_equal(getattr(got, k), getattr(fused, k), err_msg=k)
+        np.testing.assert_array_equal(getattr(got, k), getattr(want, k), err_msg=k)
