@@ -122,6 +122,8 @@ SIGNATURES = {
     "gs_knn_binned_noalloc": [_vp, _u, _up, _fp, _u, _u, _vp, _vp, _vp],
     "gs_cell_density": [_vp, _vp, _up],
     "gs_cell_avg_velocity": [_vp, _vp, _fp],
+    "gs_batch_cell_density": [_vp, _up],
+    "gs_batch_cell_avg_velocity": [_vp, _fp],
     "gs_path_create": [_fp, _u, _f, _i, C.POINTER(_vp)],
     "gs_path_destroy": [_vp],
     "gs_path_get": [_vp, _fp, _fp, _fp, _u, _up, _fp],

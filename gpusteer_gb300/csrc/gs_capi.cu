@@ -71,6 +71,7 @@ static gs_status ensure_reference(gs_group g) {
 static void touched(gs_group g) {
     g->fused_current = false;
     g->accum_dirty = true;
+    g->frame_cells = 0;
 }
 
 static bool finite3(const float* v) {
@@ -501,6 +502,7 @@ gs_status gs_group_destroy(gs_group g) {
     db_release(g->bf_a);
     db_release(g->bf_b);
     dfree(g->bf_tmp);
+    if (g->diag) cudaFree(g->diag);
     release_fused(g);
     if (g->prof_events) {
         prof_collect(g);
@@ -1000,42 +1002,78 @@ gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float mi
 }
 
 // ---- ExtractData diagnostics ----------------------------------------------------------
-static gs_status diag_check(gs_group g, gs_bins bins) {
-    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
-    if (!g->db.valid || g->db.cells != bins->cells ||
-        std::memcmp(&g->db.grid, &bins->grid, sizeof(Grid)) != 0)
-        return fail(GS_ERR_STATE, "call gs_update_knn_database on this grid first");
+// The database the diagnostics read: the per-function one when it is current
+// on this grid (gs_update_knn_database since the last change), else the fused
+// step's own when the state is still that step's result (the reference reads
+// the database its plugin built at the start of the frame, ChokePointNew.cpp:
+// 592 and :422-426, which is the fused step's start-of-step buckets).
+enum DiagSource { DIAG_NONE, DIAG_DB, DIAG_FRAME };
+static DiagSource diag_source(gs_group g, gs_bins bins) {
+    if (g->db.valid && g->db.cells == bins->cells &&
+        std::memcmp(&g->db.grid, &bins->grid, sizeof(Grid)) == 0)
+        return DIAG_DB;
+    if (g->frame_cells != 0 && g->frame_cells == bins->cells &&
+        std::memcmp(&g->fdb.grid, &bins->grid, sizeof(Grid)) == 0)
+        return DIAG_FRAME;
+    return DIAG_NONE;
+}
+
+// Scratch of the diagnostics, kept with the group (no allocation per call).
+static gs_status diag_scratch(gs_group g, size_t bytes, void** p) {
+    if (g->diag_bytes < bytes) {
+        if (g->diag) cudaFree(g->diag);
+        g->diag = nullptr;
+        g->diag_bytes = 0;
+        GS_CUDA(cudaMalloc(&g->diag, bytes));
+        g->diag_bytes = bytes;
+    }
+    *p = g->diag;
     return GS_OK;
 }
 
-gs_status gs_cell_density(gs_group g, gs_bins bins, unsigned* counts) {
-    GS_TRY(diag_check(g, bins));
-    if (!counts) return fail(GS_ERR_INVALID_ARG, "null output");
-    unsigned* d = nullptr;
-    GS_TRY(dalloc(&d, g->db.cells));
-    gs_status s = launch_cell_density(g->db, d, g->stream);
-    if (s == GS_OK && cudaMemcpyAsync(counts, d, size_t(g->db.cells) * 4, cudaMemcpyDeviceToHost,
-                                      g->stream) != cudaSuccess)
-        s = fail(GS_ERR_CUDA, "cell density copy");
+static gs_status diag_copy_out(gs_group g, void* host, const void* dev, size_t bytes,
+                               gs_status s) {
+    if (s == GS_OK && cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, g->stream) !=
+                          cudaSuccess)
+        s = fail(GS_ERR_CUDA, "cell diagnostics copy");
     if (cudaStreamSynchronize(g->stream) != cudaSuccess && s == GS_OK)
-        s = fail(GS_ERR_CUDA, "cell density");
-    dfree(d);
+        s = fail(GS_ERR_CUDA, "cell diagnostics");
     return s;
 }
 
+gs_status gs_cell_density(gs_group g, gs_bins bins, unsigned* counts) {
+    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (!counts) return fail(GS_ERR_INVALID_ARG, "null output");
+    const DiagSource src = diag_source(g, bins);
+    if (src == DIAG_NONE)
+        return fail(GS_ERR_STATE, "call gs_update_knn_database on this grid, or gs_step, first");
+    const unsigned C = bins->cells;
+    void* d = nullptr;
+    GS_TRY(diag_scratch(g, size_t(C) * 4, &d));
+    const gs_status s = src == DIAG_DB
+                            ? launch_cell_density(g->db, static_cast<unsigned*>(d), g->stream)
+                            : launch_frame_cell_density(g->fdb.start, C,
+                                                        static_cast<unsigned*>(d), g->stream);
+    return diag_copy_out(g, counts, d, size_t(C) * 4, s);
+}
+
 gs_status gs_cell_avg_velocity(gs_group g, gs_bins bins, float* avg3) {
-    GS_TRY(diag_check(g, bins));
+    if (!g || !bins) return fail(GS_ERR_INVALID_ARG, "null argument");
     if (!avg3) return fail(GS_ERR_INVALID_ARG, "null output");
-    float3* d = nullptr;
-    GS_TRY(dalloc(&d, g->db.cells));
-    gs_status s = launch_cell_avg_velocity(g->db, g->direction, g->speed, d, g->stream);
-    if (s == GS_OK && cudaMemcpyAsync(avg3, d, size_t(g->db.cells) * 12, cudaMemcpyDeviceToHost,
-                                      g->stream) != cudaSuccess)
-        s = fail(GS_ERR_CUDA, "cell velocity copy");
-    if (cudaStreamSynchronize(g->stream) != cudaSuccess && s == GS_OK)
-        s = fail(GS_ERR_CUDA, "cell velocity");
-    dfree(d);
-    return s;
+    const DiagSource src = diag_source(g, bins);
+    if (src == DIAG_NONE)
+        return fail(GS_ERR_STATE, "call gs_update_knn_database on this grid, or gs_step, first");
+    const unsigned C = bins->cells;
+    void* d = nullptr;
+    GS_TRY(diag_scratch(g, size_t(C) * 12, &d));
+    float3* out = static_cast<float3*>(d);
+    gs_status s;
+    if (src == DIAG_DB) {
+        s = launch_cell_avg_velocity(g->db, g->direction, g->speed, out, g->stream);
+    } else {
+        s = launch_frame_cell_avg_velocity(g->fdb.start, C, g->A.f[0], g->A.f[1], out, g->stream);
+    }
+    return diag_copy_out(g, avg3, d, size_t(C) * 12, s);
 }
 
 // ---- PolylinePathwayCUDA ------------------------------------------------------------
@@ -1173,6 +1211,7 @@ gs_status gs_update_group(gs_group g, float elapsed_time) {
     GS_TRY(ensure_reference(g));
     GS_TRY(launch_update(view(g), elapsed_time, g->stream));
     g->fused_current = false;
+    g->frame_cells = 0;
     g->accum_dirty = false;
     return GS_OK;
 }
@@ -1186,6 +1225,7 @@ gs_status gs_update_group_with_antipenetration(gs_group g, gs_knn knw, gs_walls 
     GS_TRY(launch_update_antipen_wall(view(g), knw->idx, knw->k, walls->start, walls->end,
                                       walls->normal, walls->n, elapsed_time, g->stream));
     g->fused_current = false;
+    g->frame_cells = 0;
     g->accum_dirty = false;
     return GS_OK;
 }
@@ -1375,6 +1415,7 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
     cudaStream_t st = g->stream;
     FusedLaunch L;
     bool dirty = false;
+    g->frame_cells = 0;
     GS_TRY(fused_setup(g, d, grid, C, agent_scene, w, L, dirty));
     Profiler prof(g);
     PhaseHook* hook = g->profiling ? &prof : nullptr;
@@ -1422,6 +1463,7 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
     }
     g->accum_dirty = false;
     g->db.valid = false;
+    g->frame_cells = C;
     return GS_OK;
 }
 
@@ -1642,6 +1684,40 @@ gs_status gs_batch_group(gs_batch b, gs_group* g) {
     return GS_OK;
 }
 
+// ExtractData of the last gs_batch_step's frame for every scene, from the
+// step's own buckets: cells scene after scene (scene s at s * cells).
+static gs_status batch_frame(gs_batch b, unsigned& Ct) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
+    Ct = b->cells * unsigned(b->scenes.size());
+    if (b->g->frame_cells == 0 || b->g->frame_cells != Ct)
+        return fail(GS_ERR_STATE, "run gs_batch_step first");
+    return GS_OK;
+}
+
+gs_status gs_batch_cell_density(gs_batch b, unsigned* counts) {
+    unsigned Ct = 0;
+    GS_TRY(batch_frame(b, Ct));
+    if (!counts) return fail(GS_ERR_INVALID_ARG, "null output");
+    gs_group g = b->g;
+    void* d = nullptr;
+    GS_TRY(diag_scratch(g, size_t(Ct) * 4, &d));
+    const gs_status s =
+        launch_frame_cell_density(g->fdb.start, Ct, static_cast<unsigned*>(d), g->stream);
+    return diag_copy_out(g, counts, d, size_t(Ct) * 4, s);
+}
+
+gs_status gs_batch_cell_avg_velocity(gs_batch b, float* avg3) {
+    unsigned Ct = 0;
+    GS_TRY(batch_frame(b, Ct));
+    if (!avg3) return fail(GS_ERR_INVALID_ARG, "null output");
+    gs_group g = b->g;
+    void* d = nullptr;
+    GS_TRY(diag_scratch(g, size_t(Ct) * 12, &d));
+    const gs_status s = launch_frame_cell_avg_velocity(g->fdb.start, Ct, g->A.f[0], g->A.f[1],
+                                                       static_cast<float3*>(d), g->stream);
+    return diag_copy_out(g, avg3, d, size_t(Ct) * 12, s);
+}
+
 gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
     if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
     StepDev d;
@@ -1805,6 +1881,7 @@ static gs_status rollout_restore(gs_rollout r, unsigned c) {
     GS_CUDA(cudaMemsetAsync(g->steering, 0, n * 16, st));
     GS_CUDA(cudaMemsetAsync(g->applied, 0, n * 4, st));
     g->fused_current = false;
+    g->frame_cells = 0;
     g->accum_dirty = false;
     g->db.valid = false;
     return GS_OK;
@@ -1829,6 +1906,7 @@ gs_status gs_rollout_forward(gs_rollout r, const gs_step_params* p) {
     GS_CUDA(cudaMemsetAsync(g->steering, 0, size_t(g->n) * 16, g->stream));
     GS_CUDA(cudaMemsetAsync(g->applied, 0, size_t(g->n) * 4, g->stream));
     g->fused_current = false;
+    g->frame_cells = 0;
     g->accum_dirty = false;
     GS_TRY(rollout_save(r, 0));
     for (unsigned c = 0; c < r->n_seg; ++c) {

@@ -171,6 +171,12 @@ struct gs_group_s {
     bool auto_cap_valid;
     gs::Grid auto_cap_grid;
     bool fused_current;    // true: A holds the state, reference arrays stale
+    // cells of the last completed fused step's database while the state is still
+    // that step's result (0 once anything changes it): fdb.start then holds the
+    // step's start-of-step buckets and A the agents' new state per slot
+    unsigned frame_cells;
+    void* diag;            // scratch of the cell diagnostics, grown on demand
+    size_t diag_bytes;
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with
     unsigned fused_k_alloc;

@@ -630,6 +630,52 @@ __global__ void k_cell_avg_velocity(const unsigned* __restrict__ start,
     out[c] = make_float3(avg.x, avg.y, avg.z);
 }
 
+// The same average over the fused step's frame: slot s of the start-of-step
+// buckets holds the agent whose new state the step wrote to A[s] (its index
+// in f0.w, heading and speed in f1).  A cell's agents belong to one scene, so
+// ascending index is the reference's order here too.
+__global__ void k_cell_avg_velocity_frame(const unsigned* __restrict__ start, unsigned C,
+                                          const float4* __restrict__ f0,
+                                          const float4* __restrict__ f1,
+                                          float3* __restrict__ out) {
+    const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const unsigned s0 = start[c], s1 = start[c + 1];
+    V3 sum = v3(0.f, 0.f, 0.f);
+    unsigned last = 0;
+    for (unsigned t = 0; t < s1 - s0; ++t) {
+        unsigned next = UINT_MAX, at = s0;
+        for (unsigned s = s0; s < s1; ++s) {
+            const unsigned id = __float_as_uint(f0[s].w);
+            if ((t == 0 || id > last) && id < next) {
+                next = id;
+                at = s;
+            }
+        }
+        last = next;
+        const float4 h = f1[at];
+        sum = add(sum, mul(v3(h), h.w));
+    }
+    const V3 avg = s1 > s0 ? dvd(sum, float(s1 - s0)) : v3(0.f, 0.f, 0.f);
+    out[c] = make_float3(avg.x, avg.y, avg.z);
+}
+
+gs_status launch_frame_cell_density(const unsigned* start, unsigned C, unsigned* out,
+                                    cudaStream_t st) {
+    if (C == 0) return GS_OK;
+    k_cell_density<<<blocks_for(C), kBlock, 0, st>>>(start, C, out);
+    GS_LAUNCHED("cell_density");
+    return GS_OK;
+}
+
+gs_status launch_frame_cell_avg_velocity(const unsigned* start, unsigned C, const float4* f0,
+                                         const float4* f1, float3* out, cudaStream_t st) {
+    if (C == 0) return GS_OK;
+    k_cell_avg_velocity_frame<<<blocks_for(C), kBlock, 0, st>>>(start, C, f0, f1, out);
+    GS_LAUNCHED("cell_avg_velocity");
+    return GS_OK;
+}
+
 gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st) {
     if (db.cells == 0) return GS_OK;
     k_cell_density<<<blocks_for(db.cells), kBlock, 0, st>>>(db.start, db.cells, out);

@@ -52,6 +52,11 @@ gs_status launch_wrap(float4* pos, unsigned n, const float ws[3], int mode, cuda
 gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st);
 gs_status launch_cell_avg_velocity(const Database& db, const float4* dir, const float* speed,
                                    float3* out, cudaStream_t st);
+// The same diagnostics over a fused step's frame (start-of-step buckets, new state in A).
+gs_status launch_frame_cell_density(const unsigned* start, unsigned C, unsigned* out,
+                                    cudaStream_t st);
+gs_status launch_frame_cell_avg_velocity(const unsigned* start, unsigned C, const float4* f0,
+                                         const float4* f1, float3* out, cudaStream_t st);
 
 struct GroupView {
     float4 *position, *direction, *steering;

@@ -327,6 +327,7 @@ class Batch:
         self._h = h
         self.counts = counts
         self.n = int(counts.sum())
+        self.cells_per_scene = int(np.prod(np.asarray(world_cells, np.uint64)))
         g = C.c_void_p()
         call("gs_batch_group", h, C.byref(g))
         self.group = _GroupRef(g)
@@ -364,6 +365,18 @@ class Batch:
     def step(self, params: StepParams, steps: int = 1) -> None:
         p = step_params_c(params)
         call("gs_batch_step", self._h, C.byref(p), int(steps))
+
+    def cell_density(self) -> np.ndarray:
+        """Agents per cell of the last step's frame, (scenes, cells)."""
+        out = np.zeros((len(self.counts), self.cells_per_scene), np.uint32)
+        call("gs_batch_cell_density", self._h, _ptr(out, C.c_uint))
+        return out
+
+    def cell_avg_velocity(self) -> np.ndarray:
+        """Mean velocity per cell of the last step's frame, (scenes, cells, 3)."""
+        out = np.zeros((len(self.counts), self.cells_per_scene, 3), np.float32)
+        call("gs_batch_cell_avg_velocity", self._h, _ptr(out))
+        return out
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib._lib is not None:

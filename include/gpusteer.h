@@ -234,11 +234,16 @@ gs_status gs_steer_for_cohesion(gs_group g, gs_knn knn, gs_group other, float mi
                                 unsigned do_not_apply_with);
 /* steerForSeek (GroupSteerLibrary.cuh:52-59). */
 /* ---- ExtractData diagnostics: ComputeCellDensity / ComputeAvgCellVelocity
- *      (ProcessData.cu:74-237, used by src/ExtractData.cpp).  On the group's KNN
- *      database (gs_update_knn_database with these bins first): agents per cell,
- *      and each cell's mean velocity (direction * speed summed in ascending agent
- *      index, divided by the count; zero when empty).  Host outputs: one unsigned
- *      / one float3 per cell.  Synchronous. */
+ *      (ProcessData.cu:74-237, used by src/ExtractData.cpp).  Agents per cell of
+ *      the group's KNN database, and each cell's mean velocity (direction * speed
+ *      of its agents now, summed in ascending agent index, divided by the count;
+ *      zero when empty).  The database is the one gs_update_knn_database built
+ *      with these bins when it is current; otherwise, after gs_step and before
+ *      anything else changes the group, the last step's own buckets, which are
+ *      the database the reference's plugin built at the start of that frame
+ *      (ChokePointNew.cpp:592, extracted after the frame at :422-426): no
+ *      rebuild.  Host outputs: one unsigned / one float3 per cell.
+ *      Synchronous. */
 gs_status gs_cell_density(gs_group g, gs_bins bins, unsigned* counts);
 gs_status gs_cell_avg_velocity(gs_group g, gs_bins bins, float* avg3);
 
@@ -332,6 +337,11 @@ gs_status gs_batch_download(gs_batch b, const gs_agent_arrays* host);
 /* The batch's underlying group (stream, profiling, graphs, block size). */
 gs_status gs_batch_group(gs_batch b, gs_group* g);
 gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps);
+/* ExtractData (gs_cell_density / gs_cell_avg_velocity) for every scene after
+ * gs_batch_step, from that step's own buckets on the batch grid: cells scene
+ * after scene (scene s at s * cells). */
+gs_status gs_batch_cell_density(gs_batch b, unsigned* counts);
+gs_status gs_batch_cell_avg_velocity(gs_batch b, float* avg3);
 
 /* ---- differentiable rollouts --------------------------------------------------------
  * No counterpart in the reference.  A rollout runs `steps` fused steps of a

@@ -821,3 +821,55 @@ def test_cell_diagnostics_match_oracle(case):
     np.testing.assert_array_equal(cell_density(g, bins), ol.cell_density(s.position, ws, wc))
     np.testing.assert_array_equal(cell_avg_velocity(g, bins),
                                   ol.cell_avg_velocity(s.position, s.direction, s.speed, ws, wc))
+
+
+def frame_diagnostics_oracle(s, p, walls, steps):
+    """ExtractData after `steps` frames: the database the last frame built
+    (positions after its wrap) and the velocities after that frame."""
+    pre = s.copy()
+    if steps > 1:
+        ol.run(pre, p, steps - 1, walls=walls)
+    db = pre.copy()
+    ol.oracle().orc_wrap_world(ol.C.byref(ol.group_struct(db)), ol.f3(p.world_size), p.wrap_mode)
+    post = pre.copy()
+    ol.run(post, p, 1, walls=walls)
+    return (ol.cell_density(db.position, p.world_size, p.world_cells),
+            ol.cell_avg_velocity(db.position, post.direction, post.speed, p.world_size,
+                                 p.world_cells))
+
+
+def test_cell_diagnostics_of_a_fused_frame():
+    """After gs_step, ExtractData reads the step's own buckets (the database the
+    reference's plugin builds at the start of the frame) and the agents' new
+    velocities, with no rebuild; once gs_update_knn_database runs again, its
+    database takes over.  The same per scene after gs_batch_step."""
+    from gpusteer_gb300.groups import cell_avg_velocity, cell_density
+
+    p = sc.chokepoint_params(world=256.0, cell=2.0)
+    s = sc.chokepoint_agents(12000, seed=31)
+    s.speed[:] = (sc.uniform01(7, s.n) * 2.0).astype(np.float32)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    walls = gs.WallGroup(sc.chokepoint_walls(10.0), bins=bins, knw=p.knw)
+    g = group_of(s, p.k)
+    steps = 12
+    gs.step(g, bins, walls, p, steps)
+    want_d, want_v = frame_diagnostics_oracle(s, p, walls.download(), steps)
+    got_d = cell_density(g, bins)
+    np.testing.assert_array_equal(got_d, want_d)
+    np.testing.assert_array_equal(cell_avg_velocity(g, bins), want_v)
+    assert got_d.max() >= 4
+    gs.updateKNNDatabase(g, bins)
+    cur = g.download()
+    np.testing.assert_array_equal(cell_density(g, bins),
+                                  ol.cell_density(cur.position, p.world_size, p.world_cells))
+    # batched: every scene's frame at once
+    states, gaps = sc.batched_chokepoint(4, seed=5, n_range=(800, 4000))
+    b = batch_setup(states, gaps, p)
+    b.step(p, steps)
+    dens, vel = b.cell_density(), b.cell_avg_velocity()
+    for i, (st, gap) in enumerate(zip(states, gaps)):
+        wb = gs.KNNBinData(p.world_cells, p.world_size, 1)
+        sw = gs.WallGroup(sc.chokepoint_walls(gap), bins=wb, knw=p.knw).download()
+        wd, wv = frame_diagnostics_oracle(st, p, sw, steps)
+        np.testing.assert_array_equal(dens[i], wd)
+        np.testing.assert_array_equal(vel[i], wv.reshape(-1, 3))
