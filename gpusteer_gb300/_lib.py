@@ -123,6 +123,7 @@ SIGNATURES = {
     "gs_cell_density": [_vp, _vp, _up],
     "gs_cell_avg_velocity": [_vp, _vp, _fp],
     "gs_batch_cell_density": [_vp, _up],
+    "gs_batches_step_host": [C.POINTER(_vp), _u, _vp, _u, _vp, _vp],
     "gs_batch_cell_avg_velocity": [_vp, _fp],
     "gs_path_create": [_fp, _u, _f, _i, C.POINTER(_vp)],
     "gs_path_destroy": [_vp],

@@ -47,6 +47,7 @@ static void release_fused(gs_group g) {
     dfree(g->d_scene);
     dfree(g->d_err);
     dfree(g->retry);
+    dfree(g->slot_of);
     dfree(g->retry_count);
     dfree(g->d_stat);
     db_release(g->fdb);
@@ -61,7 +62,7 @@ static void drop_graph(gs_group g) {
 // Brings the reference-layout arrays up to date after fused steps.
 static gs_status ensure_reference(gs_group g) {
     if (!g->fused_current) return GS_OK;
-    GS_TRY(fused_to_reference(g->A, g->n, g->d_scene, view(g), g->stream));
+    GS_TRY(fused_to_reference(g->A, g->n, g->d_scene, g->slot_of, view(g), g->stream));
     g->fused_current = false;
     g->db.valid = false;
     return GS_OK;
@@ -503,6 +504,7 @@ gs_status gs_group_destroy(gs_group g) {
     db_release(g->bf_b);
     dfree(g->bf_tmp);
     if (g->diag) cudaFree(g->diag);
+    if (g->ap) cudaFree(g->ap);
     release_fused(g);
     if (g->prof_events) {
         prof_collect(g);
@@ -559,12 +561,24 @@ gs_status gs_group_create(unsigned k, unsigned capacity, void* stream, gs_group*
     return GS_OK;
 }
 
+static gs_status upload_enqueue(gs_group g, const gs_agent_arrays* h, unsigned n);
+
 gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
     if (!g || !h) return fail(GS_ERR_INVALID_ARG, "null argument");
     if (n > g->capacity) return fail(GS_ERR_INVALID_ARG, "more agents than the group's capacity");
     if (!h->position || !h->direction || !h->steering || !h->side || !h->up || !h->speed ||
         !h->max_speed || !h->max_force || !h->radius || !h->mass || !h->applied)
         return fail(GS_ERR_INVALID_ARG, "upload needs every array");
+    GS_TRY(upload_enqueue(g, h, n));
+    g->n = n;
+    g->db.valid = false;
+    g->auto_cap_valid = false;
+    touched(g);
+    return GS_OK;
+}
+
+// Queues the copies of gs_group_upload on the group's stream.
+static gs_status upload_enqueue(gs_group g, const gs_agent_arrays* h, unsigned n) {
     cudaStream_t st = g->stream;
     auto cp = [&](void* dst, const void* src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
@@ -582,18 +596,23 @@ gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
     if (e == cudaSuccess) e = cp(g->mass, h->mass, f1b);
     if (e == cudaSuccess) e = cp(g->applied, h->applied, f1b);
     if (e != cudaSuccess) return cuda_fail(e, "upload");
-    g->n = n;
-    g->db.valid = false;
-    g->auto_cap_valid = false;
-    touched(g);
     return GS_OK;
 }
 
 static gs_status check_device_flags(gs_group g);
 
-gs_status gs_group_download(gs_group g, const gs_agent_arrays* h) {
-    if (!g || !h) return fail(GS_ERR_INVALID_ARG, "null argument");
+// Queues the copies of gs_group_download on the group's stream.  With
+// skip_constants the per-agent constants (maxSpeed, maxForce, radius, mass),
+// which no step changes, are not copied.
+static gs_status download_copies(gs_group g, const gs_agent_arrays* h, bool skip_constants);
+static gs_status download_enqueue(gs_group g, const gs_agent_arrays* h,
+                                  bool skip_constants = false) {
     GS_TRY(ensure_reference(g));
+    return download_copies(g, h, skip_constants);
+}
+
+// The device-to-host copies of the reference-layout arrays.
+static gs_status download_copies(gs_group g, const gs_agent_arrays* h, bool skip_constants) {
     cudaStream_t st = g->stream;
     const unsigned n = g->n;
     auto cp = [&](void* dst, const void* src, size_t bytes) {
@@ -607,13 +626,21 @@ gs_status gs_group_download(gs_group g, const gs_agent_arrays* h) {
     if (e == cudaSuccess) e = cp(h->side, g->side, f3b);
     if (e == cudaSuccess) e = cp(h->up, g->up, f3b);
     if (e == cudaSuccess) e = cp(h->speed, g->speed, f1b);
-    if (e == cudaSuccess) e = cp(h->max_speed, g->max_speed, f1b);
-    if (e == cudaSuccess) e = cp(h->max_force, g->max_force, f1b);
-    if (e == cudaSuccess) e = cp(h->radius, g->radius, f1b);
-    if (e == cudaSuccess) e = cp(h->mass, g->mass, f1b);
+    if (!skip_constants) {
+        if (e == cudaSuccess) e = cp(h->max_speed, g->max_speed, f1b);
+        if (e == cudaSuccess) e = cp(h->max_force, g->max_force, f1b);
+        if (e == cudaSuccess) e = cp(h->radius, g->radius, f1b);
+        if (e == cudaSuccess) e = cp(h->mass, g->mass, f1b);
+    }
     if (e == cudaSuccess) e = cp(h->applied, g->applied, f1b);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "download");
+    return GS_OK;
+}
+
+gs_status gs_group_download(gs_group g, const gs_agent_arrays* h) {
+    if (!g || !h) return fail(GS_ERR_INVALID_ARG, "null argument");
+    GS_TRY(download_enqueue(g, h));
+    GS_CUDA(cudaStreamSynchronize(g->stream));
     return check_device_flags(g);
 }
 
@@ -1251,23 +1278,27 @@ gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, uns
         GS_CUDA(cudaStreamSynchronize(other->stream));
     }
     if (g->n == 0) return GS_OK;
-    // Scratch: the new positions and a snapshot of the other group's bits,
-    // from the fused-step buffers when they exist, else allocated here.
-    float4* pos_out = nullptr;
-    unsigned* snap = nullptr;
-    GS_TRY(dalloc(&pos_out, g->n));
-    gs_status s = dalloc(&snap, other->n ? other->n : 1);
-    if (s == GS_OK && other->n)
-        s = cudaMemcpyAsync(snap, other->applied, size_t(other->n) * 4, cudaMemcpyDeviceToDevice,
-                            g->stream) == cudaSuccess ? GS_OK : fail(GS_ERR_CUDA, "snapshot");
-    if (s == GS_OK)
-        s = launch_antipenetration(view(g), knn->idx, knn->dist, knn->k, other_view(other), snap,
-                                   pos_out, mask, g->stream);
-    cudaStreamSynchronize(g->stream);
-    dfree(pos_out);
-    dfree(snap);
-    if (s == GS_OK) touched(g);
-    return s;
+    // Scratch kept with the group (grown on demand, not allocated per call as
+    // the reference's AntiPenetrationAgentsCUDA does): the new positions, then
+    // a snapshot of the other group's bits.
+    const size_t pos_bytes = size_t(g->n) * 16, snap_bytes = size_t(other->n ? other->n : 1) * 4;
+    if (g->ap_bytes < pos_bytes + snap_bytes) {
+        GS_CUDA(cudaStreamSynchronize(g->stream));
+        if (g->ap) cudaFree(g->ap);
+        g->ap = nullptr;
+        g->ap_bytes = 0;
+        GS_CUDA(cudaMalloc(&g->ap, pos_bytes + snap_bytes));
+        g->ap_bytes = pos_bytes + snap_bytes;
+    }
+    float4* pos_out = static_cast<float4*>(g->ap);
+    unsigned* snap = reinterpret_cast<unsigned*>(static_cast<char*>(g->ap) + pos_bytes);
+    if (other->n)
+        GS_CUDA(cudaMemcpyAsync(snap, other->applied, size_t(other->n) * 4,
+                                cudaMemcpyDeviceToDevice, g->stream));
+    GS_TRY(launch_antipenetration(view(g), knn->idx, knn->dist, knn->k, other_view(other), snap,
+                                  pos_out, mask, g->stream));
+    touched(g);
+    return GS_OK;
 }
 
 // ---- fused step ------------------------------------------------------------------
@@ -1281,6 +1312,7 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         GS_TRY(dalloc(&g->cellrank, n));
         GS_TRY(dalloc(&g->d_err, 1));
         GS_TRY(dalloc(&g->retry, n));
+        GS_TRY(dalloc(&g->slot_of, n));
         GS_TRY(dalloc(&g->retry_count, 1));
         GS_TRY(dalloc(&g->d_stat, 1));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
@@ -1342,6 +1374,8 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
     return GS_OK;
 }
 
+static void fill_launch(gs_group g, const StepDev& d, const WallsDev& w, FusedLaunch& L);
+
 // Brings the fused engine's bucketed state and pending cell counts up to
 // date for steps on `grid` and fills the launch block L; picks the KNN
 // capacity into d.  dirty: the first step must add the steering and applied
@@ -1382,6 +1416,12 @@ static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned 
         d.enum_cap = g->auto_cap;
     }
 
+    fill_launch(g, d, w, L);
+    return GS_OK;
+}
+
+// The launch block of the fused kernels for the group's current buffers.
+static void fill_launch(gs_group g, const StepDev& d, const WallsDev& w, FusedLaunch& L) {
     std::memset(static_cast<void*>(&L), 0, sizeof(L));  // byte-compared as a graph key
     L.A = g->A;
     L.B = g->B;
@@ -1405,7 +1445,6 @@ static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned 
         L.knn_slot = g->knn_slot;
         L.knn_dist = g->knn_dist;
     }
-    return GS_OK;
 }
 
 // The fused engine for a group whose scene table is in g->h_scenes / d_scene
@@ -1533,6 +1572,7 @@ gs_status gs_group_set_block(gs_group g, unsigned threads) {
 // ---- batched scenes ---------------------------------------------------------------
 gs_status gs_batch_destroy(gs_batch b) {
     if (!b) return GS_OK;
+    if (b->io_exec) cudaGraphExecDestroy(b->io_exec);
     gs_group_destroy(b->g);
     dfree(b->agent_scene);
     dfree(b->w_start);
@@ -1684,6 +1724,214 @@ gs_status gs_batch_group(gs_batch b, gs_group* g) {
     return GS_OK;
 }
 
+// Host arrays of agents [off, ...) of `h`.
+static gs_agent_arrays host_at(const gs_agent_arrays& h, size_t off) {
+    gs_agent_arrays v = h;
+    v.position = h.position + 4 * off;
+    v.direction = h.direction + 4 * off;
+    v.steering = h.steering + 4 * off;
+    v.side = h.side + 3 * off;
+    v.up = h.up + 3 * off;
+    v.speed = h.speed + off;
+    v.max_speed = h.max_speed + off;
+    v.max_force = h.max_force + off;
+    v.radius = h.radius + off;
+    v.mass = h.mass + off;
+    v.applied = h.applied + off;
+    return v;
+}
+
+static gs_status batch_prepare(gs_batch b, const gs_step_params* p, StepDev& d, Grid& grid,
+                               unsigned& Ct, WallsDev& w);
+
+// True when every array of h is page-locked host memory (copies from it can
+// be captured in a graph and overlap with other work).
+static bool host_pinned(const gs_agent_arrays& h) {
+    const void* ptrs[] = {h.position, h.direction, h.steering, h.side, h.up, h.speed,
+                          h.max_speed, h.max_force, h.radius, h.mass, h.applied};
+    for (const void* q : ptrs) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();  // clear the query's error
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
+
+// One part's plan for gs_batches_step_host: its launch set-up and host views.
+struct IoPart {
+    gs_batch b;
+    StepDev d;
+    Grid grid;
+    unsigned Ct;
+    WallsDev w;
+    FusedLaunch L;
+    gs_agent_arrays hi, ho;
+};
+
+// One part's upload, then its steps, conversion back and download, queued on
+// its stream: the eager sequence (the upload marks steering and applied bits
+// as carried in, so the first step adds them), as a graph captures it.
+static gs_status io_upload(IoPart& q) { return upload_enqueue(q.b->g, &q.hi, q.b->g->n); }
+
+static gs_status io_compute_and_download(IoPart& q, unsigned steps, bool in_place) {
+    gs_group g = q.b->g;
+    cudaStream_t st = g->stream;
+    GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(q.Ct) * 4, st));
+    GS_TRY(fused_from_reference(view(g), q.b->agent_scene, g->d_scene, g->A, g->cellrank,
+                                g->fdb.count, q.d.wrap_mode, true, st));
+    for (unsigned i = 0; i < steps; ++i) {
+        StepDev di = q.d;
+        di.dirty = i == 0 ? 1 : 0;
+        GS_TRY(step_body(g, q.L, di, q.Ct, nullptr));
+    }
+    GS_TRY(fused_to_reference(g->A, g->n, g->d_scene, g->slot_of, view(g), st));
+    return download_copies(g, &q.ho, in_place);
+}
+
+// The parts of gs_batches_step_host as one graph over the parts' streams:
+// part i's uploads follow part i-1's (so the first part's data arrive first
+// and its steps start early), its steps follow its uploads, its download its
+// steps.  One launch per call, kept while the key (parts, host arrays,
+// buffers, parameters) holds; cached on the first part.
+static gs_status io_graph(std::vector<IoPart>& parts, unsigned steps, bool in_place) {
+    gs_batch b0 = parts[0].b;
+    cudaStream_t st0 = b0->g->stream;
+    std::vector<unsigned char> key;
+    auto put = [&](const void* v, size_t bytes) {
+        const unsigned char* c = static_cast<const unsigned char*>(v);
+        key.insert(key.end(), c, c + bytes);
+    };
+    for (const IoPart& q : parts) {
+        put(&q.b, sizeof(q.b));
+        put(&q.hi, sizeof(q.hi));
+        put(&q.ho, sizeof(q.ho));
+        put(&q.L, sizeof(q.L));
+        put(&q.d, sizeof(q.d));
+        const unsigned extra[2] = {q.b->g->n, q.Ct};
+        put(extra, sizeof(extra));
+    }
+    const unsigned call[2] = {steps, in_place ? 1u : 0u};
+    put(call, sizeof(call));
+    if (!b0->io_exec || key != b0->io_key) {
+        if (b0->io_exec) cudaGraphExecDestroy(b0->io_exec);
+        b0->io_exec = nullptr;
+        b0->io_key.clear();
+        const size_t P = parts.size();
+        std::vector<cudaEvent_t> ev(2 * P, nullptr);  // uploaded_i, done_i
+        gs_status s = GS_OK;
+        for (cudaEvent_t& e : ev)
+            if (s == GS_OK && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+                s = fail(GS_ERR_CUDA, "cudaEventCreate");
+        cudaGraph_t graph_h = nullptr;
+        if (s == GS_OK && cudaStreamBeginCapture(st0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            s = fail(GS_ERR_CUDA, "cudaStreamBeginCapture");
+        const bool capturing = s == GS_OK;
+        for (size_t i = 0; i < P && s == GS_OK; ++i) {
+            cudaStream_t st = parts[i].b->g->stream;
+            if (i > 0 && cudaStreamWaitEvent(st, ev[i - 1], 0) != cudaSuccess)
+                s = fail(GS_ERR_CUDA, "cudaStreamWaitEvent");
+            if (s == GS_OK) s = io_upload(parts[i]);
+            if (s == GS_OK && cudaEventRecord(ev[i], st) != cudaSuccess)
+                s = fail(GS_ERR_CUDA, "cudaEventRecord");
+            if (s == GS_OK) s = io_compute_and_download(parts[i], steps, in_place);
+            if (s == GS_OK && i > 0 && cudaEventRecord(ev[P + i], st) != cudaSuccess)
+                s = fail(GS_ERR_CUDA, "cudaEventRecord");
+        }
+        for (size_t i = 1; i < P && s == GS_OK; ++i)
+            if (cudaStreamWaitEvent(st0, ev[P + i], 0) != cudaSuccess)
+                s = fail(GS_ERR_CUDA, "cudaStreamWaitEvent");
+        if (capturing) {
+            const cudaError_t e = cudaStreamEndCapture(st0, &graph_h);
+            if (s == GS_OK && e != cudaSuccess) s = cuda_fail(e, "cudaStreamEndCapture");
+        }
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+        if (s == GS_OK) {
+            const cudaError_t ei = cudaGraphInstantiate(&b0->io_exec, graph_h, 0);
+            if (ei != cudaSuccess) {
+                b0->io_exec = nullptr;
+                s = cuda_fail(ei, "cudaGraphInstantiate");
+            }
+        }
+        if (graph_h) cudaGraphDestroy(graph_h);
+        if (s != GS_OK) return s;
+        b0->io_key = key;
+    }
+    GS_CUDA(cudaGraphLaunch(b0->io_exec, st0));
+    return GS_OK;
+}
+
+gs_status gs_batches_step_host(const gs_batch* parts, unsigned n_parts, const gs_step_params* p,
+                               unsigned steps, const gs_agent_arrays* in,
+                               const gs_agent_arrays* out) {
+    if (!parts || !p || !in || !out || n_parts == 0)
+        return fail(GS_ERR_INVALID_ARG, "null argument");
+    for (unsigned i = 0; i < n_parts; ++i) {
+        if (!parts[i]) return fail(GS_ERR_INVALID_ARG, "null batch");
+        for (unsigned j = 0; j < i; ++j)
+            if (parts[j] == parts[i] || parts[j]->g->stream == parts[i]->g->stream)
+                return fail(GS_ERR_INVALID_ARG, "every part needs a batch and a stream of its own");
+    }
+    // When out is in, the constants no step changes are already in place on
+    // the host and are not copied back.
+    const bool in_place = out->max_speed == in->max_speed && out->max_force == in->max_force &&
+                          out->radius == in->radius && out->mass == in->mass;
+    const bool pinned = host_pinned(*in) && host_pinned(*out);
+    std::vector<IoPart> plan(n_parts);
+    bool graph = pinned && steps > 0;
+    size_t off = 0;
+    for (unsigned i = 0; i < n_parts; ++i) {
+        IoPart& q = plan[i];
+        q.b = parts[i];
+        q.hi = host_at(*in, off);
+        q.ho = host_at(*out, off);
+        off += q.b->total;
+        GS_TRY(batch_prepare(q.b, p, q.d, q.grid, q.Ct, q.w));
+        gs_group g = q.b->g;
+        graph = graph && g->knn_cap != 0 && !g->profiling && g->use_graph &&
+                g->stream != cudaStreamLegacy && g->stream != nullptr;
+    }
+    if (graph) {
+        for (IoPart& q : plan) {
+            gs_group g = q.b->g;
+            g->n = q.b->total;
+            q.d.enum_cap = g->knn_cap;
+            fill_launch(g, q.d, q.w, q.L);
+        }
+        GS_TRY(io_graph(plan, steps, in_place));
+        // the result is in the reference arrays and, with the step's buckets, in A
+        for (IoPart& q : plan) {
+            gs_group g = q.b->g;
+            g->fused_current = false;
+            g->accum_dirty = false;
+            g->db.valid = false;
+            g->auto_cap_valid = false;
+            g->fdb.grid = q.grid;
+            g->fdb.valid = true;
+            g->pending_wrap = q.d.wrap_mode;
+            g->frame_cells = q.Ct;
+        }
+    } else {
+        // call by call: each part's upload, steps and download on its stream
+        for (IoPart& q : plan) {
+            GS_TRY(gs_group_upload(q.b->g, &q.hi, q.b->total));
+            if (steps) GS_TRY(fused_run(q.b->g, q.d, q.grid, q.Ct, q.b->agent_scene, q.w, steps));
+            GS_TRY(download_enqueue(q.b->g, &q.ho, in_place));
+        }
+    }
+    gs_status s = GS_OK;
+    for (unsigned i = 0; i < n_parts; ++i) {
+        const cudaError_t e = cudaStreamSynchronize(parts[i]->g->stream);
+        if (e != cudaSuccess && s == GS_OK) s = cuda_fail(e, "batches step");
+    }
+    for (unsigned i = 0; i < n_parts && s == GS_OK; ++i) s = check_device_flags(parts[i]->g);
+    return s;
+}
+
 // ExtractData of the last gs_batch_step's frame for every scene, from the
 // step's own buckets: cells scene after scene (scene s at s * cells).
 static gs_status batch_frame(gs_batch b, unsigned& Ct) {
@@ -1718,20 +1966,19 @@ gs_status gs_batch_cell_avg_velocity(gs_batch b, float* avg3) {
     return diag_copy_out(g, avg3, d, size_t(Ct) * 12, s);
 }
 
-gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
-    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
-    StepDev d;
+// gs_batch_step's checks and set-up (buffers, walls, scene table), without
+// launching: the step parameters d, grid, cells over all scenes and walls.
+static gs_status batch_prepare(gs_batch b, const gs_step_params* p, StepDev& d, Grid& grid,
+                               unsigned& Ct, WallsDev& w) {
     GS_TRY(validate_step(p, nullptr, d));
-    Grid grid;
     unsigned C;
     GS_TRY(check_grid(p->world_cells, p->world_size, grid, C));
     if (std::memcmp(&grid, &b->grid, sizeof(Grid)) != 0)
         return fail(GS_ERR_INVALID_ARG, "step grid differs from the batch grid");
     if (d.r != b->radius) return fail(GS_ERR_INVALID_ARG, "search radius differs from the batch");
-    if (steps == 0) return GS_OK;
     gs_group g = b->g;
     const unsigned S = unsigned(b->scenes.size());
-    const unsigned Ct = b->cells * S;
+    Ct = b->cells * S;
     const bool has_walls = d.need & NEED_WALLS;
     GS_TRY(reserve_fused(g, Ct, has_walls, d.k, S));
     if (has_walls) GS_TRY(batch_walls(b));
@@ -1740,7 +1987,7 @@ gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
         for (Scene& sc : scenes) sc.n_walls = 0;
     GS_TRY(put_scenes(g, scenes));
     d.block = g->block;
-    WallsDev w;
+    w = WallsDev();
     if (has_walls) {
         w.start = b->w_start;
         w.end = b->w_end;
@@ -1748,7 +1995,18 @@ gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
         w.pos_id = b->w_pos_id;
         w.cell_start = b->w_cell_start;
     }
-    return fused_run(g, d, grid, Ct, b->agent_scene, w, steps);
+    return GS_OK;
+}
+
+gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "null batch");
+    StepDev d;
+    Grid grid;
+    unsigned Ct = 0;
+    WallsDev w;
+    GS_TRY(batch_prepare(b, p, d, grid, Ct, w));
+    if (steps == 0) return GS_OK;
+    return fused_run(b->g, d, grid, Ct, b->agent_scene, w, steps);
 }
 
 }  // extern "C"

@@ -162,6 +162,7 @@ struct gs_group_s {
     std::vector<gs::Scene>* h_scenes;  // host copy of the table on the device
     unsigned* d_err;       // device error flags (see FusedLaunch::err)
     unsigned* retry;       // [capacity] exact-redo list and its counter
+    unsigned* slot_of;     // [capacity] each agent's slot (conversion to the reference layout)
     unsigned* retry_count;
     unsigned* d_stat;      // one word of scratch for device-side statistics
     // candidate capacity of the fused KNN scan: knn_cap fixed by the caller
@@ -177,6 +178,8 @@ struct gs_group_s {
     unsigned frame_cells;
     void* diag;            // scratch of the cell diagnostics, grown on demand
     size_t diag_bytes;
+    void* ap;              // scratch of anti-penetration (new positions, bit snapshot)
+    size_t ap_bytes;
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with
     unsigned fused_k_alloc;
@@ -220,4 +223,9 @@ struct gs_batch_s {
     unsigned* agent_scene = nullptr;
     float4 *w_start = nullptr, *w_end = nullptr, *w_normal = nullptr, *w_pos_id = nullptr;
     unsigned* w_cell_start = nullptr;
+    // gs_batches_step_host: this batch's upload, steps and download captured
+    // as one graph, replayed while its key (host arrays, buffers, parameters)
+    // stays the same
+    cudaGraphExec_t io_exec = nullptr;
+    std::vector<unsigned char> io_key;
 };

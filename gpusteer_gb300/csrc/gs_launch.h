@@ -159,8 +159,9 @@ struct PhaseHook {
 };
 gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
                      PhaseHook* hook = nullptr);
-gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView g,
-                             cudaStream_t st);
+// slot_of: capacity words of scratch (each agent's slot, then the gather).
+gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, unsigned* slot_of,
+                             GroupView g, cudaStream_t st);
 // ---- adjoint of the fused flocking step -------------------------------------------
 // Inputs recorded by a forward step (FusedLaunch::rec_*), the agents' constant
 // limits, and the adjoints of the step's outputs; accumulates the adjoints of

@@ -428,7 +428,6 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev
     const unsigned id = u(w0.w), scene = u(f4v.w);
     unsigned applied = u(w2.w);
     V3 steer = v3(w2);
-    const Scene sc = L.scenes[scene];
     const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
     Accs a;
     init_accs(a, p);
@@ -445,6 +444,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev
     }
     finish_all(a, p, 1, fs, fa, fc, me, applied, steer);
     integrate(me, steer, p.dt);
+    const Scene sc = L.scenes[scene];  // loaded here: not held through the neighbour loop
     store_next(L, s, me, id, scene, sc, p.wrap_mode);
 }
 
@@ -519,14 +519,24 @@ gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st, Ph
     return launch_fused<32>(L, p, st, hook);
 }
 
-// A -> reference layout (scatter by agent index).
-__global__ void k_to_reference(Fused A, unsigned n, const Scene* __restrict__ scenes,
-                               GroupView g) {
+// A -> reference layout.  Slot order is bucket order, a shuffle of the agent
+// order, so the conversion first records each agent's slot (one scattered
+// 4-byte store per agent), then writes the reference arrays in agent order,
+// coalesced, reading each agent's five float4 from its slot.
+__global__ void k_slot_of(Fused A, unsigned n, const Scene* __restrict__ scenes,
+                          unsigned* __restrict__ slot_of) {
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
+    const unsigned id = u(A.f[0][s].w), scene = u(A.f[4][s].w);
+    slot_of[scenes[scene].agent_offset + id] = s;
+}
+
+__global__ void k_to_reference(Fused A, unsigned n, const unsigned* __restrict__ slot_of,
+                               GroupView g) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned s = slot_of[i];
     const float4 f0 = A.f[0][s], f1 = A.f[1][s], f2 = A.f[2][s], f3 = A.f[3][s], f4v = A.f[4][s];
-    const Scene sc = scenes[u(f4v.w)];
-    const unsigned i = sc.agent_offset + u(f0.w);
     g.position[i] = make_float4(f0.x, f0.y, f0.z, 0.f);
     g.direction[i] = make_float4(f1.x, f1.y, f1.z, 0.f);
     g.speed[i] = f1.w;
@@ -540,10 +550,11 @@ __global__ void k_to_reference(Fused A, unsigned n, const Scene* __restrict__ sc
     g.steering[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, GroupView g,
-                             cudaStream_t st) {
+gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, unsigned* slot_of,
+                             GroupView g, cudaStream_t st) {
     if (n == 0) return GS_OK;
-    k_to_reference<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, g);
+    k_slot_of<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, slot_of);
+    k_to_reference<<<blocks_for(n), kBlock, 0, st>>>(A, n, slot_of, g);
     GS_LAUNCHED("fused_to_reference");
     return GS_OK;
 }

@@ -384,6 +384,46 @@ class Batch:
             self._h = None
 
 
+def pinned_state(n: int) -> AgentState:
+    """An AgentState whose arrays live in page-locked host memory
+    (gs_host_alloc), freed with the state; host copies from it overlap with
+    device work and can be captured in graphs."""
+    import weakref
+
+    shapes = {"position": (n, 4), "direction": (n, 4), "steering": (n, 4), "side": (n, 3),
+              "up": (n, 3), "speed": (n,), "max_speed": (n,), "max_force": (n,),
+              "radius": (n,), "mass": (n,), "applied": (n,)}
+    arrays, ptrs = {}, []
+    for k, shp in shapes.items():
+        count = max(1, int(np.prod(shp)))
+        p = C.c_void_p()
+        call("gs_host_alloc", count * 4, C.byref(p))
+        ptrs.append(p)
+        ctype = C.c_uint if k == "applied" else C.c_float
+        buf = (ctype * count).from_address(p.value)
+        arrays[k] = np.ctypeslib.as_array(buf)[:int(np.prod(shp))].reshape(shp)
+    st = AgentState(**arrays)
+    lib = _lib.load()
+    weakref.finalize(st, lambda ps=ptrs: [lib.gs_host_free(q) for q in ps])
+    return st
+
+
+def batches_step_host(parts, params: StepParams, steps: int, state_in: AgentState,
+                      state_out: AgentState) -> None:
+    """gs_batches_step_host: host state in, `steps` steps, host state out for
+    several Batch objects (the parts of one workload) with their copies and
+    steps overlapped across the parts' streams.  The states hold the parts'
+    agents one part after another."""
+    total = sum(b.n for b in parts)
+    if state_in.n != total or state_out.n != total:
+        raise ValueError("host states must hold every part's agents")
+    p = step_params_c(params)
+    hs = (C.c_void_p * len(parts))(*[b.handle for b in parts])
+    a_in, a_out = host_arrays(state_in), host_arrays(state_out)
+    call("gs_batches_step_host", hs, len(parts), C.byref(p), int(steps), C.byref(a_in),
+         C.byref(a_out))
+
+
 class Rollout:
     """Checkpointed differentiable rollout of a plain flock (gs_rollout_*):
     `steps` fused steps from the group's state, then the adjoint backwards

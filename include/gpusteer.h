@@ -337,6 +337,22 @@ gs_status gs_batch_download(gs_batch b, const gs_agent_arrays* host);
 /* The batch's underlying group (stream, profiling, graphs, block size). */
 gs_status gs_batch_group(gs_batch b, gs_group* g);
 gs_status gs_batch_step(gs_batch b, const gs_step_params* p, unsigned steps);
+/* Host state in, `steps` steps, host state out for several batches at once,
+ * e.g. consecutive ranges of one workload's scenes: each part's upload, steps
+ * and download are queued on its own stream, part after part, so that the
+ * copies of one part run while another part steps (host<->device copies in
+ * both directions and the steps overlap).  `in` and `out` hold the parts'
+ * agents one part after another, each in its scene order; they may be the same
+ * arrays (then maxSpeed, maxForce, radius and mass, which no step changes, are
+ * not copied back), and page-locked host memory (gs_host_alloc) lets the
+ * copies overlap.
+ * Returns once every part's state is in `out`.  Each scene's result equals
+ * gs_batch_step's.  A fixed KNN capacity (gs_group_set_knn_capacity on each
+ * part's group) keeps the parts from waiting on the host for the automatic
+ * capacity measurement that follows an upload. */
+gs_status gs_batches_step_host(const gs_batch* parts, unsigned n_parts, const gs_step_params* p,
+                               unsigned steps, const gs_agent_arrays* in,
+                               const gs_agent_arrays* out);
 /* ExtractData (gs_cell_density / gs_cell_avg_velocity) for every scene after
  * gs_batch_step, from that step's own buckets on the batch grid: cells scene
  * after scene (scene s at s * cells). */
