@@ -85,6 +85,7 @@ SIGNATURES = {
     "gs_knn_device_arrays": [_vp, C.POINTER(_up), C.POINTER(_fp)],
     "gs_knn_upload": [_vp, _vp, _up, _fp],
     "gs_find_knn_groups": [C.POINTER(_vp), _u, _vp, C.POINTER(_vp)],
+    "gs_multigroup_step": [C.POINTER(_vp), _u, _vp, C.POINTER(_vp), C.POINTER(_vp), _vp, _u],
     "gs_walls_create": [_fp, _fp, _fp, _u, _vp, _u, C.POINTER(_vp)],
     "gs_walls_load": [C.c_char_p, _vp, _u, C.POINTER(_vp)],
     "gs_walls_destroy": [_vp],

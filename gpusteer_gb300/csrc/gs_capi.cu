@@ -75,6 +75,17 @@ static void touched(gs_group g) {
     g->frame_cells = 0;
 }
 
+// A call queued on g's stream reads `other`'s arrays (it waited for other's
+// earlier work first).  Later work on other's stream must not overwrite them
+// before that read: other's stream waits for g's stream up to here.
+static gs_status read_done(gs_group g, gs_group other) {
+    if (other == g || other->stream == g->stream) return GS_OK;
+    if (!g->read_ev) GS_CUDA(cudaEventCreateWithFlags(&g->read_ev, cudaEventDisableTiming));
+    GS_CUDA(cudaEventRecord(g->read_ev, g->stream));
+    GS_CUDA(cudaStreamWaitEvent(other->stream, g->read_ev, 0));
+    return GS_OK;
+}
+
 static bool finite3(const float* v) {
     return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
 }
@@ -505,6 +516,7 @@ gs_status gs_group_destroy(gs_group g) {
     dfree(g->bf_tmp);
     if (g->diag) cudaFree(g->diag);
     if (g->ap) cudaFree(g->ap);
+    if (g->read_ev) cudaEventDestroy(g->read_ev);
     release_fused(g);
     if (g->prof_events) {
         prof_collect(g);
@@ -849,21 +861,12 @@ gs_status gs_find_knn(gs_group g, gs_knn out, gs_bins bins, gs_group other,
     if (other != g) GS_CUDA(cudaStreamSynchronize(other->stream));
     GS_TRY(launch_knn_binned(g->db, g->n, other->db, other == g, bins->radius, out->k, out->idx,
                              out->dist, g->stream));
-    return GS_OK;
+    return read_done(g, other);
 }
 
-gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins bins,
-                             gs_knn* out) {
-    if (!groups || !bins || !out || n_groups == 0) return fail(GS_ERR_INVALID_ARG, "null argument");
-    if (size_t(n_groups) * n_groups > kMaxKnnPairs)
-        return fail(GS_ERR_INVALID_ARG, "at most 7 groups (49 pairs) per batched KNN");
-    for (unsigned i = 0; i < n_groups; ++i) {
-        gs_group g = groups[i];
-        if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
-        if (!g->db.valid || g->db.cells != bins->cells)
-            return fail(GS_ERR_STATE, "call gs_update_knn_database on every group first");
-    }
-    KnnPairs P;
+// The pair table of a batched KNN over groups (out[i * n + j], NULL skips).
+static gs_status knn_pairs(const gs_group* groups, unsigned n_groups, gs_bins bins,
+                           gs_knn* out, KnnPairs& P) {
     std::memset(&P, 0, sizeof(P));
     P.grid = bins->grid;
     P.r = bins->radius;
@@ -884,6 +887,22 @@ gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins 
             q.k = o->k;
             q.self = a == b;
         }
+    return GS_OK;
+}
+
+gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins bins,
+                             gs_knn* out) {
+    if (!groups || !bins || !out || n_groups == 0) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (size_t(n_groups) * n_groups > kMaxKnnPairs)
+        return fail(GS_ERR_INVALID_ARG, "at most 7 groups (49 pairs) per batched KNN");
+    for (unsigned i = 0; i < n_groups; ++i) {
+        gs_group g = groups[i];
+        if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+        if (!g->db.valid || g->db.cells != bins->cells)
+            return fail(GS_ERR_STATE, "call gs_update_knn_database on every group first");
+    }
+    KnnPairs P;
+    GS_TRY(knn_pairs(groups, n_groups, bins, out, P));
     if (P.n_pairs == 0) return GS_OK;
     // One launch on the first group's stream, after every group's database
     // build; every group's stream then waits for it.
@@ -893,6 +912,118 @@ gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins 
     GS_TRY(launch_knn_binned_pairs(P, st));
     cudaEvent_t done = nullptr;
     for (unsigned i = 1; i < n_groups; ++i) {
+        if (groups[i]->stream == st) continue;
+        if (!done) {
+            GS_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+            const cudaError_t e = cudaEventRecord(done, st);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(done);
+                return cuda_fail(e, "cudaEventRecord");
+            }
+        }
+        const cudaError_t e = cudaStreamWaitEvent(groups[i]->stream, done, 0);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(done);
+            return cuda_fail(e, "cudaStreamWaitEvent");
+        }
+    }
+    if (done) cudaEventDestroy(done);
+    return GS_OK;
+}
+
+static gs_status antipen_enqueue(gs_group g, gs_knn knn, gs_group other, unsigned mask,
+                                 cudaStream_t st);
+
+gs_status gs_multigroup_step(const gs_group* groups, unsigned n_groups, gs_bins bins,
+                             const gs_path* paths, gs_knn* knn, const gs_multigroup_params* p,
+                             unsigned steps) {
+    if (!groups || !bins || !knn || !p || n_groups == 0)
+        return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (n_groups > kMaxGroups) return fail(GS_ERR_INVALID_ARG, "at most 7 groups");
+    if (p->wrap_mode < 0 || p->wrap_mode > 2) return fail(GS_ERR_INVALID_ARG, "bad wrap mode");
+    if (!finite3(p->world_size) || !std::isfinite(p->dt))
+        return fail(GS_ERR_NONFINITE, "non-finite parameter");
+    const unsigned G = n_groups;
+    for (unsigned i = 0; i < G; ++i) {
+        if (!groups[i]) return fail(GS_ERR_INVALID_ARG, "null group");
+        for (unsigned j = 0; j < i; ++j)
+            if (groups[j] == groups[i]) return fail(GS_ERR_INVALID_ARG, "a group appears twice");
+        for (unsigned j = 0; j < G; ++j) {
+            gs_knn o = knn[size_t(i) * G + j];
+            if (!o) return fail(GS_ERR_INVALID_ARG, "every group pair needs its KNNData");
+            if (o->n != groups[i]->n)
+                return fail(GS_ERR_INVALID_ARG, "KNNData size differs from its group");
+        }
+        if (paths && paths[i] && paths[i]->n < 2)
+            return fail(GS_ERR_INVALID_ARG, "follow-path needs a path of 2+ points");
+    }
+    // Everything runs on the first group's stream, after the other groups'
+    // pending work; their streams wait for it at the end.
+    cudaStream_t st = groups[0]->stream;
+    for (unsigned i = 0; i < G; ++i) {
+        GS_TRY(ensure_reference(groups[i]));
+        if (groups[i]->stream != st) GS_CUDA(cudaStreamSynchronize(groups[i]->stream));
+        GS_TRY(db_reserve(groups[i]->db, groups[i]->capacity, bins->cells));
+    }
+    for (unsigned step = 0; step < steps; ++step) {
+        // Group::preUpdate for every group (MultiGroup.cpp:545-556)
+        for (unsigned i = 0; i < G; ++i) {
+            gs_group g = groups[i];
+            GS_TRY(launch_wrap(g->position, g->n, p->world_size, p->wrap_mode, st));
+            GS_TRY(db_build(g->db, g->position, g->n, bins->grid, st));
+            if (g->n) GS_CUDA(cudaMemsetAsync(g->applied, 0, size_t(g->n) * 4, st));
+        }
+        // every pair's KNN reads only those databases: one launch (:561-564)
+        KnnPairs P;
+        GS_TRY(knn_pairs(groups, G, bins, knn, P));
+        if (P.n_pairs) GS_TRY(launch_knn_binned_pairs(P, st));
+        // Group::update of each group in turn (:558-610)
+        for (unsigned i = 0; i < G; ++i) {
+            gs_group g = groups[i];
+            MultiSteer M;
+            std::memset(static_cast<void*>(&M), 0, sizeof(M));
+            M.g = view(g);
+            for (unsigned j = 0; j < G; ++j) {
+                M.o[j] = other_view(groups[j]);
+                gs_knn o = knn[size_t(i) * G + j];
+                M.idx[j] = o->idx;
+                M.dist[j] = o->dist;
+                M.k[j] = o->k;
+            }
+            M.n_groups = G;
+            M.self = i;
+            M.min_time = p->min_time_to_collision;
+            M.min_sep = p->min_separation_distance;
+            M.w_avoid = p->w_avoid;
+            M.mask_avoid = p->mask_avoid;
+            M.avoid_close = p->avoid_close;
+            M.sep = FlockParams{p->sep_min, p->sep_max, p->sep_cos, p->w_sep, p->mask_sep};
+            M.ali = FlockParams{p->ali_min, p->ali_max, p->ali_cos, p->w_ali, p->mask_ali};
+            M.coh = FlockParams{p->coh_min, p->coh_max, p->coh_cos, p->w_coh, p->mask_coh};
+            const gs_path P_i = paths ? paths[i] : nullptr;
+            if (P_i) {
+                M.has_path = 1;
+                M.path = PathDev{P_i->d_points, P_i->d_lengths, P_i->d_normals, P_i->n,
+                                 P_i->radius, P_i->cyclic, P_i->total};
+                M.path_time = p->path_prediction_time;
+                M.w_path = p->w_path;
+                M.mask_path = p->mask_path;
+                M.w_seek = p->w_seek;
+                M.mask_seek = p->mask_seek;
+                for (int c = 0; c < 3; ++c) M.seek_target[c] = P_i->h_points[3 + c];
+            }
+            GS_TRY(launch_multigroup_steer(M, st));
+            GS_TRY(launch_update(view(g), p->dt, st));
+            for (unsigned j = 0; j < G; ++j)
+                GS_TRY(antipen_enqueue(g, knn[size_t(i) * G + j], groups[j], p->mask_antipen, st));
+        }
+    }
+    for (unsigned i = 0; i < G; ++i) {
+        touched(groups[i]);
+        groups[i]->db.valid = true;  // built this frame, as the reference's stays
+    }
+    cudaEvent_t done = nullptr;
+    for (unsigned i = 1; i < G; ++i) {
         if (groups[i]->stream == st) continue;
         if (!done) {
             GS_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
@@ -994,7 +1125,7 @@ gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
     }
     GS_TRY(launch_knn_brute(g->position, g->n, other->position, other->n, other == g, out->k,
                             seed, out->idx, out->dist, st));
-    return GS_OK;
+    return read_done(g, other);
 }
 
 static gs_status flock_call(int kind, gs_group g, gs_knn knn, gs_group other, float a, float b,
@@ -1009,7 +1140,7 @@ static gs_status flock_call(int kind, gs_group g, gs_knn knn, gs_group other, fl
     GS_TRY(launch_flock(kind, view(g), knn->idx, knn->k, other_view(other), a, b, c, w, mask,
                         g->stream));
     touched(g);
-    return GS_OK;
+    return read_done(g, other);
 }
 
 gs_status gs_steer_for_separation(gs_group g, gs_knn knn, gs_group other, float min_distance,
@@ -1218,7 +1349,7 @@ gs_status gs_steer_to_avoid_neighbors(gs_group g, gs_knn knn, gs_group other,
                                   min_time_to_collision, min_separation_distance,
                                   avoid_close != 0, weight, mask, g->stream));
     touched(g);
-    return GS_OK;
+    return read_done(g, other);
 }
 
 gs_status gs_steer_to_avoid_walls(gs_group g, gs_knn knw, gs_walls walls, float min_time,
@@ -1269,21 +1400,17 @@ gs_status gs_anti_penetration_wall(gs_group g, gs_knn knw, gs_walls walls, float
     return GS_OK;
 }
 
-gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, unsigned mask) {
-    if (!g || !knn || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
-    if (knn->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
-    GS_TRY(ensure_reference(g));
-    if (other != g) {
-        GS_TRY(ensure_reference(other));
-        GS_CUDA(cudaStreamSynchronize(other->stream));
-    }
+// antiPenetrationAgents on g's stream, with the scratch kept with the group
+// (grown on demand, not allocated per call as the reference's
+// AntiPenetrationAgentsCUDA does): the new positions, then a snapshot of the
+// other group's bits.  Queued on st; the groups' earlier work must be complete
+// or on st.
+static gs_status antipen_enqueue(gs_group g, gs_knn knn, gs_group other, unsigned mask,
+                                 cudaStream_t st) {
     if (g->n == 0) return GS_OK;
-    // Scratch kept with the group (grown on demand, not allocated per call as
-    // the reference's AntiPenetrationAgentsCUDA does): the new positions, then
-    // a snapshot of the other group's bits.
     const size_t pos_bytes = size_t(g->n) * 16, snap_bytes = size_t(other->n ? other->n : 1) * 4;
     if (g->ap_bytes < pos_bytes + snap_bytes) {
-        GS_CUDA(cudaStreamSynchronize(g->stream));
+        GS_CUDA(cudaStreamSynchronize(st));
         if (g->ap) cudaFree(g->ap);
         g->ap = nullptr;
         g->ap_bytes = 0;
@@ -1294,11 +1421,22 @@ gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, uns
     unsigned* snap = reinterpret_cast<unsigned*>(static_cast<char*>(g->ap) + pos_bytes);
     if (other->n)
         GS_CUDA(cudaMemcpyAsync(snap, other->applied, size_t(other->n) * 4,
-                                cudaMemcpyDeviceToDevice, g->stream));
-    GS_TRY(launch_antipenetration(view(g), knn->idx, knn->dist, knn->k, other_view(other), snap,
-                                  pos_out, mask, g->stream));
+                                cudaMemcpyDeviceToDevice, st));
+    return launch_antipenetration(view(g), knn->idx, knn->dist, knn->k, other_view(other), snap,
+                                  pos_out, mask, st);
+}
+
+gs_status gs_anti_penetration_agents(gs_group g, gs_knn knn, gs_group other, unsigned mask) {
+    if (!g || !knn || !other) return fail(GS_ERR_INVALID_ARG, "null argument");
+    if (knn->n != g->n) return fail(GS_ERR_INVALID_ARG, "KNNData size differs from the group");
+    GS_TRY(ensure_reference(g));
+    if (other != g) {
+        GS_TRY(ensure_reference(other));
+        GS_CUDA(cudaStreamSynchronize(other->stream));
+    }
+    GS_TRY(antipen_enqueue(g, knn, other, mask, g->stream));
     touched(g);
-    return GS_OK;
+    return read_done(g, other);
 }
 
 // ---- fused step ------------------------------------------------------------------

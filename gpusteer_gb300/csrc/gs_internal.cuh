@@ -179,6 +179,7 @@ struct gs_group_s {
     void* diag;            // scratch of the cell diagnostics, grown on demand
     size_t diag_bytes;
     void* ap;              // scratch of anti-penetration (new positions, bit snapshot)
+    cudaEvent_t read_ev;   // marks this group's reads of another group (read_done)
     size_t ap_bytes;
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with

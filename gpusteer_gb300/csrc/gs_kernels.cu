@@ -1047,6 +1047,101 @@ gs_status launch_antipen_wall(GroupView g, const unsigned* knl, unsigned k, cons
     return GS_OK;
 }
 
+// One group's behaviour calls of a MultiGroup frame (Group::update,
+// plugins/MultiGroup.cpp:558-601), per agent in the calls' order: avoid the
+// neighbours of every other group (close pass, then main pass, per group,
+// :573-580), separation from every group (:583-588), alignment and cohesion
+// with this group (:590-591), then path following and seek of the path's
+// second point when the group has a path (:593-597).  Each call keeps its own
+// mask test and normalisation, and the applied bits accumulate from call to
+// call, as the per-call kernels do.  Only steering and applied bits are
+// written (positions move in the update that follows), so every read of a
+// group's state sees the state the per-call kernels see.
+__global__ void k_multigroup_steer(MultiSteer M) {
+    const unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
+    const GroupView& g = M.g;
+    if (a >= g.n) return;
+    const unsigned n = g.n;
+    unsigned applied = g.applied[a];
+    V3 steer = v3(g.steering[a]);
+    const Self me = load_self(g, a);
+    for (unsigned j = 0; j < M.n_groups; ++j) {
+        if (j == M.self) continue;
+        const OtherView& o = M.o[j];
+        const unsigned* idx = M.idx[j];
+        if (M.avoid_close && !(applied & M.mask_avoid)) {
+            CloseAcc acc;
+            close_init(acc);
+            for (unsigned s = 0; s < M.k[j]; ++s) {
+                const unsigned b = idx[a + size_t(s) * n];
+                if (b >= o.n) break;
+                close_add(acc, me, M.min_sep, M.dist[j][a + size_t(s) * n], v3(o.position[b]),
+                          o.radius[b]);
+                if (acc.found) break;
+            }
+            close_finish(acc, M.w_avoid, M.mask_avoid, applied, steer);
+        }
+        if (!(applied & (M.mask_avoid | AVOID_CLOSE_NEIGHBORS_BIT))) {
+            AvoidAcc acc;
+            avoid_init(acc, M.min_time);
+            for (unsigned s = 0; s < M.k[j]; ++s) {
+                const unsigned b = idx[a + size_t(s) * n];
+                if (b >= o.n) break;
+                avoid_add(acc, me, b, v3(o.position[b]), v3(o.direction[b]), o.speed[b],
+                          o.radius[b]);
+            }
+            if (acc.threat != UINT_MAX) avoid_finish(acc, M.w_avoid, M.mask_avoid, me, applied, steer);
+        }
+    }
+    for (unsigned j = 0; j < M.n_groups; ++j) {
+        if (applied & M.sep.mask) continue;
+        const OtherView& o = M.o[j];
+        FlockAcc acc;
+        flock_init(acc);
+        for (unsigned s = 0; s < M.k[j]; ++s) {
+            const unsigned b = M.idx[j][a + size_t(s) * n];
+            if (b >= o.n) break;
+            const V3 offset = sub(v3(o.position[b]), me.pos);
+            const float dsq = dot(offset, offset);
+            separation_add(acc, M.sep, me.dir, offset, dsq, sqrtf(dsq));
+        }
+        flock_finish(0, acc, M.sep, me, applied, steer);
+    }
+    for (int kind = 1; kind <= 2; ++kind) {
+        const FlockParams& fp = kind == 1 ? M.ali : M.coh;
+        if (applied & fp.mask) continue;
+        const OtherView& o = M.o[M.self];
+        FlockAcc acc;
+        flock_init(acc);
+        for (unsigned s = 0; s < M.k[M.self]; ++s) {
+            const unsigned b = M.idx[M.self][a + size_t(s) * n];
+            if (b >= o.n) break;
+            const V3 bp = v3(o.position[b]);
+            const V3 offset = sub(bp, me.pos);
+            const float d = sqrtf(dot(offset, offset));
+            if (kind == 1) alignment_add(acc, fp, me.dir, offset, d, v3(o.direction[b]));
+            else cohesion_add(acc, fp, me.dir, offset, d, bp);
+        }
+        flock_finish(kind, acc, fp, me, applied, steer);
+    }
+    if (M.has_path) {
+        if (!(applied & M.mask_path))
+            follow_path_finish(M.path, M.path_time, M.w_path, M.mask_path, me, applied, steer);
+        if (!(applied & M.mask_seek))
+            seek_finish(v3(M.seek_target[0], M.seek_target[1], M.seek_target[2]), M.w_seek,
+                        M.mask_seek, me, applied, steer);
+    }
+    g.steering[a] = f4(steer, 0.f);
+    g.applied[a] = applied;
+}
+
+gs_status launch_multigroup_steer(const MultiSteer& M, cudaStream_t st) {
+    if (M.g.n == 0) return GS_OK;
+    k_multigroup_steer<<<blocks_for(M.g.n), kBlock, 0, st>>>(M);
+    GS_LAUNCHED("multigroup_steer");
+    return GS_OK;
+}
+
 // AntiPenetrationAgentsCUDAKernel.cu:72-108.  Positions are read from the
 // group and written to pos_out (the reference's m_pdPositionNew); the other
 // group's applied bits are read from a snapshot taken before the launch (the

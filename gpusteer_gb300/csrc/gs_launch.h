@@ -84,6 +84,28 @@ gs_status launch_avoid_walls(GroupView g, const unsigned* knw, unsigned kw, cons
                              const float4* end, const float4* normal, unsigned n_lines,
                              float min_time, float w, unsigned mask, cudaStream_t st);
 gs_status launch_update(GroupView g, float dt, cudaStream_t st);
+// MultiGroup (plugins/MultiGroup.cpp:558-601): one group's behaviour calls of
+// a frame in one pass, reading every group's current state and this group's
+// KNN lists against each of them.
+constexpr unsigned kMaxGroups = 7;
+struct MultiSteer {
+    GroupView g;
+    OtherView o[kMaxGroups];
+    const unsigned* idx[kMaxGroups];
+    const float* dist[kMaxGroups];
+    unsigned k[kMaxGroups];
+    unsigned n_groups, self;
+    float min_time, min_sep, w_avoid;
+    unsigned mask_avoid;
+    int avoid_close;
+    FlockParams sep, ali, coh;
+    int has_path;
+    PathDev path;
+    float path_time, w_path, w_seek;
+    unsigned mask_path, mask_seek;
+    float seek_target[3];
+};
+gs_status launch_multigroup_steer(const MultiSteer& M, cudaStream_t st);
 gs_status launch_update_antipen_wall(GroupView g, const unsigned* knl, unsigned k,
                                      const float4* start, const float4* end,
                                      const float4* normal, unsigned n_lines, float dt,

@@ -491,6 +491,43 @@ def findKNearestNeighborsGroups(groups, bins: KNNBinData, knns) -> None:
     call("gs_find_knn_groups", hs, G, bins.handle, out)
 
 
+class MultiGroupParams(C.Structure):
+    """gs_multigroup_params: the values a MultiGroup frame reads."""
+    _fields_ = [("world_size", C.c_float * 3), ("wrap_mode", C.c_int),
+                ("min_time_to_collision", C.c_float), ("min_separation_distance", C.c_float),
+                ("avoid_close", C.c_int), ("w_avoid", C.c_float), ("mask_avoid", C.c_uint),
+                ("sep_min", C.c_float), ("sep_max", C.c_float), ("sep_cos", C.c_float),
+                ("w_sep", C.c_float), ("mask_sep", C.c_uint),
+                ("ali_min", C.c_float), ("ali_max", C.c_float), ("ali_cos", C.c_float),
+                ("w_ali", C.c_float), ("mask_ali", C.c_uint),
+                ("coh_min", C.c_float), ("coh_max", C.c_float), ("coh_cos", C.c_float),
+                ("w_coh", C.c_float), ("mask_coh", C.c_uint),
+                ("path_prediction_time", C.c_float), ("w_path", C.c_float),
+                ("mask_path", C.c_uint), ("w_seek", C.c_float), ("mask_seek", C.c_uint),
+                ("mask_antipen", C.c_uint), ("dt", C.c_float)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        for k, v in kw.items():
+            if k == "world_size":
+                self.world_size = (C.c_float * 3)(*v)
+            else:
+                setattr(self, k, v)
+
+
+def multigroup_step(groups, bins: KNNBinData, knns, params: MultiGroupParams, steps: int = 1,
+                    paths=None) -> None:
+    """gs_multigroup_step: `steps` MultiGroup frames; knns[i][j] are group i's
+    lists against group j (all pairs), paths[i] a Path or None."""
+    G = len(groups)
+    hs = (C.c_void_p * G)(*[grp.handle for grp in groups])
+    ps = None
+    if paths is not None:
+        ps = (C.c_void_p * G)(*[(q.handle if q is not None else None) for q in paths])
+    ks = (C.c_void_p * (G * G))(*[knns[i][j].handle for i in range(G) for j in range(G)])
+    call("gs_multigroup_step", hs, G, bins.handle, ps, ks, C.byref(params), int(steps))
+
+
 def findKNearestNeighborsBruteForce(group: AgentGroup, knn: KNNData, other: AgentGroup) -> None:
     call("gs_knn_bruteforce", group.handle, knn.handle, other.handle)
 

@@ -217,6 +217,43 @@ gs_status gs_find_knn(gs_group g, gs_knn out, gs_bins bins, gs_group other,
  * stepped in turn between the calls as MultiGroup does.  At most 7 groups. */
 gs_status gs_find_knn_groups(const gs_group* groups, unsigned n_groups, gs_bins bins,
                              gs_knn* out);
+
+/* The values a MultiGroup frame reads from its SimulationParams
+ * (plugins/MultiGroup.cpp:545-610; data/MultiGroup*.params). */
+typedef struct gs_multigroup_params {
+    float    world_size[3];
+    int      wrap_mode;                      /* GS_WRAP_*                               */
+    float    min_time_to_collision, min_separation_distance;
+    int      avoid_close;
+    float    w_avoid;
+    unsigned mask_avoid;
+    float    sep_min, sep_max, sep_cos, w_sep;  /* minSeparationDistance, maxSeparation... */
+    unsigned mask_sep;
+    float    ali_min, ali_max, ali_cos, w_ali;  /* minFlockingDistance, maxFlocking...     */
+    unsigned mask_ali;
+    float    coh_min, coh_max, coh_cos, w_coh;
+    unsigned mask_coh;
+    float    path_prediction_time, w_path;
+    unsigned mask_path;
+    float    w_seek;
+    unsigned mask_seek;
+    unsigned mask_antipen;                   /* maskAntiPenetrationAgents               */
+    float    dt;
+} gs_multigroup_params;
+
+/* `steps` frames of a MultiGroup simulation (MultiGroupSimulation::update):
+ * Group::preUpdate for every group (wrap, updateKNNDatabase, applied bits
+ * cleared), every group pair's KNN in one launch into knn[i * n_groups + j]
+ * (all n_groups^2 lists, owned by the caller), then Group::update of each
+ * group in turn: avoid the other groups' neighbours, separation from every
+ * group, alignment and cohesion with itself, path following and seek of the
+ * path's second point when paths[i] is set (paths may be NULL), update, and
+ * anti-penetration against every group.  One steering launch per group
+ * replaces its per-call launches; results equal the per-function sequence
+ * bit for bit.  At most 7 groups. */
+gs_status gs_multigroup_step(const gs_group* groups, unsigned n_groups, gs_bins bins,
+                             const gs_path* paths, gs_knn* knn, const gs_multigroup_params* p,
+                             unsigned steps);
 gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls,
                             unsigned search_radius);
 /* KNNBruteForceCUDAV2 (KNNBruteForceCUDA.cu:163-187). */

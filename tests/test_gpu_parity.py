@@ -781,6 +781,75 @@ def test_multigroup_batched_knn_equals_per_pair_calls():
                 gs.updateGroup(seq[i], p.dt)
 
 
+def test_multigroup_fused_frames_equal_per_function_frames():
+    """gs_multigroup_step (one steering launch per group) against the same
+    frames through the per-function API, call for call as MultiGroup.cpp:545-610
+    runs them: three groups, two with paths, close-neighbour avoidance and
+    anti-penetration between all groups; bit for bit over six frames."""
+    p = sc.boids_params(k=8, world=96.0, cell=4.0)
+    states = [sc.boids_sphere(2500, radius=16.0, seed=51), sc.boids_sphere(1800, radius=16.0, seed=52),
+              sc.boids_sphere(900, radius=12.0, seed=53)]
+    for st in states:
+        st.radius[:] = np.float32(0.9)
+    G = len(states)
+    pts = [[(0.0, 0.0, 0.0), (30.0, 5.0, -20.0), (-10.0, 20.0, 30.0)], None,
+           [(5.0, -5.0, 5.0), (-25.0, 0.0, 10.0)]]
+    mp = dict(world_size=p.world_size, wrap_mode=sc.WRAP_REFERENCE, min_time_to_collision=2.0,
+              min_separation_distance=0.5, avoid_close=1, w_avoid=1.0, mask_avoid=0,
+              sep_min=p.sep_min, sep_max=p.sep_max, sep_cos=p.sep_cos, w_sep=p.w_sep,
+              mask_sep=4096, ali_min=p.ali_min, ali_max=p.ali_max, ali_cos=p.ali_cos,
+              w_ali=p.w_ali, mask_ali=272, coh_min=p.coh_min, coh_max=p.coh_max,
+              coh_cos=p.coh_cos, w_coh=p.w_coh, mask_coh=272, path_prediction_time=5.0,
+              w_path=1.0, mask_path=16, w_seek=1.5, mask_seek=4480, mask_antipen=4096,
+              dt=1.0 / 30.0)
+    frames = 6
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    paths = [gs.Path(q, 6.0) if q is not None else None for q in pts]
+    # fused
+    fused = [group_of(s, p.k) for s in states]
+    kf = [[gs.KNNData(states[i].n, p.k) for _ in range(G)] for i in range(G)]
+    gs.multigroup_step(fused, bins, kf, gs.MultiGroupParams(**mp), frames, paths=paths)
+    # per function
+    groups = [group_of(s, p.k) for s in states]
+    kp = [[gs.KNNData(states[i].n, p.k) for _ in range(G)] for i in range(G)]
+    m = mp
+    for _ in range(frames):
+        for g in groups:
+            gs.wrapWorld(g, p.world_size, sc.WRAP_REFERENCE)
+            st = g.download()
+            st.applied[:] = 0
+            g.upload(st)
+            gs.updateKNNDatabase(g, bins)
+        for i, g in enumerate(groups):
+            for j, o in enumerate(groups):
+                gs.findKNearestNeighbors(g, kp[i][j], bins, o, 1)
+            for j, o in enumerate(groups):
+                if j != i:
+                    gs.steerToAvoidNeighbors(g, kp[i][j], o, m["min_time_to_collision"],
+                                             m["min_separation_distance"], m["avoid_close"],
+                                             m["w_avoid"], m["mask_avoid"])
+            for j, o in enumerate(groups):
+                gs.steerForSeparation(g, kp[i][j], o, m["sep_min"], m["sep_max"], m["sep_cos"],
+                                      m["w_sep"], m["mask_sep"])
+            gs.steerForAlignment(g, kp[i][i], g, m["ali_min"], m["ali_max"], m["ali_cos"],
+                                 m["w_ali"], m["mask_ali"])
+            gs.steerForCohesion(g, kp[i][i], g, m["coh_min"], m["coh_max"], m["coh_cos"],
+                                m["w_coh"], m["mask_coh"])
+            if paths[i] is not None:
+                gs.steerToFollowPath(g, paths[i], m["path_prediction_time"], m["w_path"],
+                                     m["mask_path"])
+                gs.steerForSeek(g, pts[i][1], m["w_seek"], m["mask_seek"])
+            gs.updateGroup(g, m["dt"])
+            for j, o in enumerate(groups):
+                gs.antiPenetrationAgents(g, kp[i][j], o, m["mask_antipen"])
+    for i in range(G):
+        assert_state(fused[i].download(), groups[i].download())
+        np.testing.assert_array_equal(kf[i][(i + 1) % G].download(fused[i])[0],
+                                      kp[i][(i + 1) % G].download(groups[i])[0])
+    got = fused[0].download()
+    assert ((got.applied & 8192) != 0).sum() > 50  # anti-penetration fired
+
+
 # ---- path following (SteerToFollowPathCUDAKernel.cu, PolylinePathwayCUDA.cu) ----------
 
 @pytest.mark.parametrize("name", ["line", "loop", "bend"])
