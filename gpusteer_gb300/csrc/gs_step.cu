@@ -137,45 +137,48 @@ struct Accs {
     CloseAcc close;
 };
 
-__device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, const FlockParams& fs,
-                                           const FlockParams& fa, const FlockParams& fc,
-                                           const Self& me, unsigned bid, float knn_d, V3 bpos,
-                                           V3 bdir, float bspeed, float bradius) {
+// `need` is p.need, or a compile-time mask equal to it in a kernel
+// specialised for one configuration (the unused accumulators then vanish).
+__device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned need,
+                                           const FlockParams& fs, const FlockParams& fa,
+                                           const FlockParams& fc, const Self& me, unsigned bid,
+                                           float knn_d, V3 bpos, V3 bdir, float bspeed,
+                                           float bradius) {
     const V3 offset = sub(bpos, me.pos);
     const float dsq = dot(offset, offset);
     const float d = sqrtf(dsq);
-    if (p.need & (NEED_SEP | NEED_ALI | NEED_COH)) {
+    if (need & (NEED_SEP | NEED_ALI | NEED_COH)) {
         // inBoidNeighborhood (FlockingCommon.cuh:4-30) for the three flocking
         // behaviours: the unit offset and its dot with the heading are the
         // same operands for all three, so they are computed once.
-        const bool ang_s = (p.need & NEED_SEP) && !(d < fs.min_d) && !(d > fs.max_d);
-        const bool ang_a = (p.need & NEED_ALI) && !(d < fa.min_d) && !(d > fa.max_d);
-        const bool ang_c = (p.need & NEED_COH) && !(d < fc.min_d) && !(d > fc.max_d);
+        const bool ang_s = (need & NEED_SEP) && !(d < fs.min_d) && !(d > fs.max_d);
+        const bool ang_a = (need & NEED_ALI) && !(d < fa.min_d) && !(d > fa.max_d);
+        const bool ang_c = (need & NEED_COH) && !(d < fc.min_d) && !(d > fc.max_d);
         float fwd = 0.f;
         if (ang_s || ang_a || ang_c) fwd = dot(me.dir, dvd(offset, d));
-        if (p.need & NEED_SEP) {
+        if (need & NEED_SEP) {
             if ((d < fs.min_d) || (ang_s && fwd > fs.cos_max)) {
                 a.sep.sum = add(a.sep.sum, dvd(offset, -dsq));
                 a.sep.n++;
             }
         }
-        if (p.need & NEED_ALI) {
+        if (need & NEED_ALI) {
             if ((d < fa.min_d) || (ang_a && fwd > fa.cos_max)) {
                 a.ali.sum = add(a.ali.sum, bdir);
                 a.ali.n++;
             }
         }
-        if (p.need & NEED_COH) {
+        if (need & NEED_COH) {
             if ((d < fc.min_d) || (ang_c && fwd > fc.cos_max)) {
                 a.coh.sum = add(a.coh.sum, bpos);
                 a.coh.n++;
             }
         }
     }
-    if (p.need & NEED_AVOID) avoid_add(a.avoid, me, bid, bpos, bdir, bspeed, bradius);
+    if (need & NEED_AVOID) avoid_add(a.avoid, me, bid, bpos, bdir, bspeed, bradius);
     // the KNN distance equals d unless the neighbour moved after the KNN
     // (avoid-walls); the caller passes it then, else -1
-    if (p.need & NEED_CLOSE)
+    if (need & NEED_CLOSE)
         close_add(a.close, me, p.min_sep, knn_d < 0.f ? d : knn_d, bpos, bradius);
 }
 
@@ -296,8 +299,13 @@ __device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, u
 }
 
 // ---- whole step without walls -------------------------------------------------------
-template <int KMAX, unsigned ENUM, bool EXACT>
+// NEEDC: the behaviours that read the neighbour list, fixed at compile time
+// (kNeedRuntime: taken from p.need).
+constexpr unsigned kNeedRuntime = ~0u;
+constexpr unsigned kNeedList = NEED_SEP | NEED_ALI | NEED_COH | NEED_AVOID | NEED_CLOSE;
+template <int KMAX, unsigned ENUM, bool EXACT, unsigned NEEDC = kNeedRuntime>
 __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
+    const unsigned need = NEEDC == kNeedRuntime ? p.need : NEEDC;
     extern __shared__ unsigned sh_col[];
     const unsigned bd = blockDim.x;
     unsigned* col = sh_col + threadIdx.x;
@@ -323,8 +331,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
                           fc = flock_params(p.coh);
         Accs a;
         init_accs(a, p);
-        const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
-        const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
+        const bool need_dir = need & (NEED_ALI | NEED_AVOID);
+        const bool need_rad = need & (NEED_AVOID | NEED_CLOSE);
         unsigned* rec_knn = L.rec_knn ? L.rec_knn + size_t(id) * p.k : nullptr;
         unsigned r = 0;
         for (; r < p.k; ++r) {
@@ -334,7 +342,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
             const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float br = need_rad ? L.B.f[2][bs].w : 0.f;
             if (rec_knn) rec_knn[r] = u(b0.w);
-            accumulate(a, p, fs, fa, fc, me, u(b0.w), -1.f, v3(b0), v3(b1), b1.w, br);
+            accumulate(a, p, need, fs, fa, fc, me, u(b0.w), -1.f, v3(b0), v3(b1), b1.w, br);
         }
         if (rec_knn) {
             for (; r < p.k; ++r) rec_knn[r] = UINT_MAX;
@@ -409,8 +417,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
 }
 
 // ---- rest of the step after the wall phase --------------------------------------------
-template <int KMAX>
+template <int KMAX, unsigned NEEDC>
 __global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev p) {
+    const unsigned need = NEEDC == kNeedRuntime ? p.need : NEEDC;
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.n) return;
     const float4 w0 = L.w0[s], w1 = L.w1[s], w2 = L.w2[s];
@@ -431,16 +440,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev
     const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
     Accs a;
     init_accs(a, p);
-    const bool need_dir = p.need & (NEED_ALI | NEED_AVOID);
-    const bool need_rad = p.need & (NEED_AVOID | NEED_CLOSE);
+    const bool need_dir = need & (NEED_ALI | NEED_AVOID);
+    const bool need_rad = need & (NEED_AVOID | NEED_CLOSE);
     for (unsigned i = 0; i < p.k; ++i) {
         const unsigned bs = L.knn_slot[size_t(i) * L.n + s];
         if (bs == UINT_MAX) break;
         const float4 b0 = L.w0[bs];
         const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float br = need_rad ? L.B.f[2][bs].w : 0.f;
-        const float kd = (p.need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
-        accumulate(a, p, fs, fa, fc, me, u(b0.w), kd, v3(b0), v3(b1), b1.w, br);
+        const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
+        accumulate(a, p, need, fs, fa, fc, me, u(b0.w), kd, v3(b0), v3(b1), b1.w, br);
     }
     finish_all(a, p, 1, fs, fa, fc, me, applied, steer);
     integrate(me, steer, p.dt);
@@ -488,12 +497,26 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
         k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
-        k_fused_rest<KMAX><<<nb, bs, 0, st>>>(L, p);
+        // the choke-point step (separation and neighbour avoidance) has its own build
+        if ((p.need & kNeedList) == (NEED_SEP | NEED_AVOID))
+            k_fused_rest<KMAX, NEED_SEP | NEED_AVOID><<<nb, bs, 0, st>>>(L, p);
+        else
+            k_fused_rest<KMAX, kNeedRuntime><<<nb, bs, 0, st>>>(L, p);
         if (hook) hook->mark(3, false);
     } else {
         GS_TRY(allow_smem(k_fused<KMAX, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
-        k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
+        // the flock (separation, alignment, cohesion) on the collecting scan has
+        // its own build
+        bool done = false;
+        if constexpr (ENUM == 32) {
+            if ((p.need & kNeedList) == (NEED_SEP | NEED_ALI | NEED_COH)) {
+                GS_TRY(allow_smem(k_fused<KMAX, 32, false, NEED_SEP | NEED_ALI | NEED_COH>, smem));
+                k_fused<KMAX, 32, false, NEED_SEP | NEED_ALI | NEED_COH><<<nb, bs, smem, st>>>(L, p);
+                done = true;
+            }
+        }
+        if (!done) k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
         k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
     }
