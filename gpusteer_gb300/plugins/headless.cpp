@@ -20,8 +20,11 @@
 //               following, seek, flocking, updateGroupWithAntiPenetration,
 //               antiPenetrationAgents
 //
-//   gs_headless <Boids|ChokePoint|ChokePointNew|ChokePointGroup> <state_in> <state_out> <frames>
-//               [params=<file.params>] [key=value ...]
+//   MultiGroup  MultiGroupSimulation::update (plugins/MultiGroup.cpp:545-610)
+//               over several groups (below)
+//
+//   gs_headless <Boids|ChokePoint|ChokePointNew|ChokePointGroup|MultiGroup> <state_in> <state_out>
+//               <frames> [params=<file.params>] [key=value ...]
 //
 // params= loads a scenario file with SimulationParams (include/SimulationParams.h)
 // and supplies the values the reference's plugins read from it; key=value
@@ -136,6 +139,12 @@ void apply_simulation_params(const char* file, Params& p) {
     put("w_seek", fl(sp.m_fWeightSeek));
     put("mask_seek", un(sp.m_nMaskSeek));
     put("mask_antipen", un(sp.m_nMaskAntiPenetrationAgents));
+    for (size_t gi = 0; gi < sp.m_vecGroupParams.size(); ++gi) {
+        const GroupParams& g = sp.m_vecGroupParams[gi];
+        std::string path;
+        for (float3 const& q : g.m_vecPathPoints) path += (path.empty() ? "" : ";") + f3s(q);
+        if (!path.empty()) put(("path" + std::to_string(gi)).c_str(), path);
+    }
     if (!sp.m_vecGroupParams.empty()) {
         const GroupParams& g = sp.m_vecGroupParams[0];
         std::string path;
@@ -215,6 +224,26 @@ void write_state(const char* path, AgentGroup& g) {
         std::fwrite(v->data(), 4, v->size(), f);
     std::fwrite(ap.data(), 4, ap.size(), f);
     std::fclose(f);
+}
+
+std::vector<std::string> split(const std::string& s, char sep) {
+    std::vector<std::string> out;
+    std::istringstream in(s);
+    std::string item;
+    while (std::getline(in, item, sep)) out.push_back(item);
+    return out;
+}
+
+std::vector<float3> parse_points(const std::string& s) {
+    std::vector<float3> pts;
+    for (const std::string& item : split(s, ';')) {
+        std::istringstream v(item);
+        float3 q;
+        char c;
+        v >> q.x >> c >> q.y >> c >> q.z;
+        pts.push_back(q);
+    }
+    return pts;
 }
 
 // ---- plugins -------------------------------------------------------------------------
@@ -526,17 +555,118 @@ private:
     std::unique_ptr<KNNData> m_knnSelf, m_knnWalls;
 };
 
+// MultiGroupSimulation::update (plugins/MultiGroup.cpp:545-610): several groups
+// in one world.  Every frame runs Group::preUpdate for every group (wrap,
+// updateKNNDatabase, the applied bits cleared with cudaMemset), then
+// Group::update of each group in turn: KNN against every group, avoid the
+// other groups' neighbours, separation from every group, alignment and
+// cohesion with itself, path following and seek of the path's second point
+// when the group has a path (path<i>=x,y,z;...), update, anti-penetration
+// against every group.  state_in / state_out list one file per group,
+// separated by commas.
+class MultiGroupPlugIn : public HeadlessPlugIn {
+public:
+    const char* name() { return "MultiGroup"; }
+    void open() {
+        const Params& p = params;
+        m_worldSize = f3param(p, "world", make_float3(200.f, 200.f, 200.f));
+        m_worldCells = u3param(p, "cells", make_uint3(50, 50, 50));
+        m_k = uparam(p, "k", 16);
+        m_radius = uparam(p, "radius", 1);
+        m_bins.reset(new KNNBinData(m_worldCells, m_worldSize, m_radius));
+        const std::vector<std::string> files = split(in_path, ',');
+        for (size_t i = 0; i < files.size(); ++i) {
+            m_groups.emplace_back(new AgentGroup(m_worldCells, m_k));
+            for (const AgentData& a : read_state(files[i].c_str())) m_groups.back()->AddAgent(a);
+            m_groups.back()->SyncDevice();
+            auto pp = p.find("path" + std::to_string(i));
+            m_paths.emplace_back(pp == p.end() ? nullptr
+                                               : new PolylinePathwayCUDA(parse_points(pp->second),
+                                                                         fparam(p, "path_radius", 23.f),
+                                                                         false));
+        }
+        const size_t G = m_groups.size();
+        for (size_t i = 0; i < G; ++i)
+            for (size_t j = 0; j < G; ++j)
+                m_knn.emplace_back(new KNNData(m_groups[i]->Size(), m_k));
+    }
+    void update(const float, const float elapsedTime) {
+        const Params& p = params;
+        const size_t G = m_groups.size();
+        for (auto& g : m_groups) {  // Group::preUpdate (:545-556)
+            wrapWorld(g.get(), m_worldSize);
+            updateKNNDatabase(g.get(), m_bins.get());
+            if (cudaMemset(g->GetAgentGroupData().pdAppliedKernels(), 0, g->Size() * sizeof(uint)) !=
+                cudaSuccess)
+                throw std::runtime_error("cudaMemset of the applied bits failed");
+        }
+        for (size_t i = 0; i < G; ++i) {  // Group::update (:558-610)
+            AgentGroup* gi = m_groups[i].get();
+            for (size_t j = 0; j < G; ++j)
+                findKNearestNeighbors(gi, knn(i, j), m_bins.get(), m_groups[j].get(), m_radius);
+            for (size_t j = 0; j < G; ++j)
+                if (j != i)
+                    steerToAvoidNeighbors(gi, knn(i, j), m_groups[j].get(),
+                                          fparam(p, "min_time_col", 2.f), fparam(p, "min_sep", 0.5f),
+                                          uparam(p, "avoid_close", 0) != 0, fparam(p, "w_avoid", 1.f),
+                                          uparam(p, "mask_avoid", 0));
+            for (size_t j = 0; j < G; ++j)
+                steerForSeparation(gi, knn(i, j), m_groups[j].get(), fparam(p, "sep_min", 0.5f),
+                                   fparam(p, "sep_max", 1.2f), fparam(p, "sep_cos", -0.8660254f),
+                                   fparam(p, "w_sep", 10.f), uparam(p, "mask_sep", 0));
+            steerForAlignment(gi, knn(i, i), gi, fparam(p, "ali_min", 0.5f), fparam(p, "ali_max", 7.f),
+                              fparam(p, "ali_cos", -0.8660254f), fparam(p, "w_ali", 2.5f),
+                              uparam(p, "mask_ali", 0));
+            steerForCohesion(gi, knn(i, i), gi, fparam(p, "coh_min", 0.5f), fparam(p, "coh_max", 7.f),
+                             fparam(p, "coh_cos", -0.8660254f), fparam(p, "w_coh", 1.f),
+                             uparam(p, "mask_coh", 0));
+            if (PolylinePathwayCUDA* path = m_paths[i].get()) {
+                steerToFollowPath(gi, path, fparam(p, "path_time", 5.f), fparam(p, "w_path", 1.f),
+                                  uparam(p, "mask_path", 0));
+                steerForSeek(gi, path->hvPoints()[1], fparam(p, "w_seek", 1.f),
+                             uparam(p, "mask_seek", 0));
+            }
+            updateGroup(gi, elapsedTime);
+            for (size_t j = 0; j < G; ++j)
+                antiPenetrationAgents(gi, knn(i, j), m_groups[j].get(), uparam(p, "mask_antipen", 0));
+        }
+    }
+    void redraw(const float, const float) {
+        const std::vector<std::string> files = split(out_path, ',');
+        for (size_t i = 0; i < m_groups.size() && i < files.size(); ++i)
+            write_state(files[i].c_str(), *m_groups[i]);
+    }
+    void close() {
+        m_knn.clear();
+        m_paths.clear();
+        m_groups.clear();
+        m_bins.reset();
+    }
+
+private:
+    KNNData* knn(size_t i, size_t j) { return m_knn[i * m_groups.size() + j].get(); }
+    float3 m_worldSize;
+    uint3 m_worldCells;
+    uint m_k = 16, m_radius = 1;
+    std::unique_ptr<KNNBinData> m_bins;
+    std::vector<std::unique_ptr<AgentGroup>> m_groups;
+    std::vector<std::unique_ptr<PolylinePathwayCUDA>> m_paths;
+    std::vector<std::unique_ptr<KNNData>> m_knn;
+};
+
 BoidsPlugIn gBoidsPlugIn;
 ChokePointPlugIn gChokePointPlugIn;
 ChokePointNewPlugIn gChokePointNewPlugIn;
 ChokePointGroupPlugIn gChokePointGroupPlugIn;
+MultiGroupPlugIn gMultiGroupPlugIn;
 
 }  // namespace
 
 int main(int argc, char** argv) {
     if (argc < 5) {
         std::fprintf(stderr,
-                     "usage: %s <Boids|ChokePoint|ChokePointNew|ChokePointGroup> <state_in> <state_out> <frames> "
+                     "usage: %s <Boids|ChokePoint|ChokePointNew|ChokePointGroup|MultiGroup> <state_in> <state_out> "
+                     "<frames> "
                      "[key=value ...]\n",
                      argv[0]);
         return 2;

@@ -322,3 +322,58 @@ def test_chokepoint_new_plugin_from_params_file(tmp_path):
     for k in FIELDS:
         np.testing.assert_array_equal(getattr(got, k), getattr(fused, k), err_msg=k)
         np.testing.assert_array_equal(getattr(got, k), getattr(want, k), err_msg=k)
+
+
+def test_multigroup_plugin_equals_fused_multigroup_frames(tmp_path):
+    """MultiGroupSimulation::update (MultiGroup.cpp:545-610) through the C++
+    drop-in, call for call over three groups with two paths, against
+    gs_multigroup_step on the same groups: bit for bit."""
+    p = sc.boids_params(k=8, world=96.0, cell=4.0)
+    states = [sc.boids_sphere(2200, radius=16.0, seed=61), sc.boids_sphere(1500, radius=16.0, seed=62),
+              sc.boids_sphere(700, radius=12.0, seed=63)]
+    for s in states:
+        s.radius[:] = np.float32(0.9)
+    pts = [[(0.0, 0.0, 0.0), (30.0, 5.0, -20.0)], None, [(5.0, -5.0, 5.0), (-25.0, 0.0, 10.0)]]
+    radius, dt, frames = 6.0, np.float32(1.0 / 30.0), 8
+    mp = dict(world_size=p.world_size, wrap_mode=sc.WRAP_REFERENCE, min_time_to_collision=2.0,
+              min_separation_distance=0.5, avoid_close=1, w_avoid=1.0, mask_avoid=0,
+              sep_min=p.sep_min, sep_max=p.sep_max, sep_cos=p.sep_cos, w_sep=p.w_sep,
+              mask_sep=4096, ali_min=p.ali_min, ali_max=p.ali_max, ali_cos=p.ali_cos,
+              w_ali=p.w_ali, mask_ali=272, coh_min=p.coh_min, coh_max=p.coh_max,
+              coh_cos=p.coh_cos, w_coh=p.w_coh, mask_coh=272, path_prediction_time=5.0,
+              w_path=1.0, mask_path=16, w_seek=1.5, mask_seek=4480, mask_antipen=4096,
+              dt=float(dt))
+    ins = [tmp_path / f"in{i}.bin" for i in range(3)]
+    outs = [tmp_path / f"out{i}.bin" for i in range(3)]
+    for f, s in zip(ins, states):
+        write_state(f, s)
+    args = {"world": v3(p.world_size), "cells": ",".join(str(c) for c in p.world_cells),
+            "k": p.k, "radius": 1, "min_time_col": f32(2.0), "min_sep": f32(0.5),
+            "avoid_close": 1, "w_avoid": f32(1.0), "mask_avoid": 0, "sep_min": f32(p.sep_min),
+            "sep_max": f32(p.sep_max), "sep_cos": f32(p.sep_cos), "w_sep": f32(p.w_sep),
+            "mask_sep": 4096, "ali_min": f32(p.ali_min), "ali_max": f32(p.ali_max),
+            "ali_cos": f32(p.ali_cos), "w_ali": f32(p.w_ali), "mask_ali": 272,
+            "coh_min": f32(p.coh_min), "coh_max": f32(p.coh_max), "coh_cos": f32(p.coh_cos),
+            "w_coh": f32(p.w_coh), "mask_coh": 272, "path_time": f32(5.0), "w_path": f32(1.0),
+            "mask_path": 16, "w_seek": f32(1.5), "mask_seek": 4480, "mask_antipen": 4096,
+            "path_radius": f32(radius), "dt": f32(dt),
+            "path0": ";".join(v3(q) for q in pts[0]), "path2": ";".join(v3(q) for q in pts[2])}
+    gb.build()
+    cmd = [str(gb.HEADLESS), "MultiGroup", ",".join(map(str, ins)), ",".join(map(str, outs)),
+           str(frames)] + [f"{k}={v}" for k, v in args.items()]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    got = [read_state(f) for f in outs]
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    groups = []
+    for s in states:
+        g = gs.AgentGroup(p.k, s.n)
+        g.upload(s)
+        groups.append(g)
+    knns = [[gs.KNNData(states[i].n, p.k) for _ in range(3)] for i in range(3)]
+    paths = [gs.Path(q, radius) if q is not None else None for q in pts]
+    gs.multigroup_step(groups, bins, knns, gs.MultiGroupParams(**mp), frames, paths=paths)
+    for i in range(3):
+        want = groups[i].download()
+        for k in FIELDS:
+            np.testing.assert_array_equal(getattr(got[i], k), getattr(want, k), err_msg=f"{i} {k}")
