@@ -339,3 +339,36 @@ def test_cpp_simulation_params_loader_matches_python_reader(tmp_path):
     bad.write_text("bogusKey = 1\n</simulation>\n")
     out = subprocess.run([str(exe), str(bad)], capture_output=True, text=True).stdout
     assert out.startswith("error unknown key bogusKey")
+
+
+def test_parameter_blocks_match_the_header(tmp_path):
+    """The ctypes mirrors of gs_step_params and gs_multigroup_params have the C
+    header's size and field offsets."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    from gpusteer_gb300 import build as gb
+    from gpusteer_gb300.groups import MultiGroupParams, _StepParamsC
+
+    checks = {"gs_multigroup_params": MultiGroupParams, "gs_step_params": _StepParamsC}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "gpusteer.h"', "int main(void) {"]
+    for cname, cls in checks.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in cls._fields_:
+            lines.append(f'printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    cuda_inc = Path(gb.nvcc()).resolve().parent.parent / "include"
+    r = subprocess.run([shutil.which("gcc"), "-std=c99", "-Wall", "-I", str(REPO / "include"),
+                        "-I", str(cuda_inc), str(src), "-o", str(exe)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line.strip()}
+    for cname, cls in checks.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for field, _ in cls._fields_:
+            assert got[(cname, field)] == getattr(cls, field).offset, (cname, field)
