@@ -375,24 +375,11 @@ def run_reference_batched(args):
 # ---- GPU arm ------------------------------------------------------------------------
 
 def pinned_state(lib, n):
-    """AgentState whose arrays live in page-locked host memory."""
-    from gpusteer_gb300.state import AgentState
+    """AgentState whose arrays live in page-locked host memory, in the
+    library's three blocks (one pitched copy per block); freed with the state."""
+    import gpusteer_gb300 as gs
 
-    shapes = {"position": (n, 4), "direction": (n, 4), "steering": (n, 4), "side": (n, 3),
-              "up": (n, 3), "speed": (n,), "max_speed": (n,), "max_force": (n,),
-              "radius": (n,), "mass": (n,), "applied": (n,)}
-    arrays, ptrs = {}, []
-    for k, shp in shapes.items():
-        count = int(np.prod(shp))
-        p = C.c_void_p()
-        from gpusteer_gb300._lib import check
-
-        check(lib.gs_host_alloc(count * 4, C.byref(p)))
-        ptrs.append(p)
-        ctype = C.c_uint if k == "applied" else C.c_float
-        buf = (ctype * count).from_address(p.value)
-        arrays[k] = np.ctypeslib.as_array(buf).reshape(shp)
-    return AgentState(**arrays), ptrs
+    return gs.pinned_state(n), []
 
 
 def read_peaks():

@@ -499,17 +499,10 @@ gs_status gs_bins_get_cells(gs_bins bins, float* min3, float* max3, float* centr
 gs_status gs_group_destroy(gs_group g) {
     if (!g) return GS_OK;
     if (g->stream) cudaStreamSynchronize(g->stream);
+    // the reference-layout arrays live in three blocks (see gs_group_create)
     dfree(g->position);
-    dfree(g->direction);
-    dfree(g->steering);
     dfree(g->side);
-    dfree(g->up);
     dfree(g->speed);
-    dfree(g->max_speed);
-    dfree(g->max_force);
-    dfree(g->radius);
-    dfree(g->mass);
-    dfree(g->applied);
     db_release(g->db);
     db_release(g->bf_a);
     db_release(g->bf_b);
@@ -551,18 +544,25 @@ gs_status gs_group_create(unsigned k, unsigned capacity, void* stream, gs_group*
         if (e != cudaSuccess) s = cuda_fail(e, "cudaStreamCreate");
         g->own_stream = true;
     }
+    // The reference-layout arrays, one block per element size: position,
+    // direction, steering (float4); side, up (float3); speed, maxSpeed,
+    // maxForce, radius, mass, applied (4 bytes).  Arrays of one block sit at a
+    // fixed stride, so a host state laid out the same way moves in one pitched
+    // copy per block (copy_arrays).
     const size_t n = capacity;
-    if (s == GS_OK) s = dalloc(&g->position, n);
-    if (s == GS_OK) s = dalloc(&g->direction, n);
-    if (s == GS_OK) s = dalloc(&g->steering, n);
-    if (s == GS_OK) s = dalloc(&g->side, n);
-    if (s == GS_OK) s = dalloc(&g->up, n);
-    if (s == GS_OK) s = dalloc(&g->speed, n);
-    if (s == GS_OK) s = dalloc(&g->max_speed, n);
-    if (s == GS_OK) s = dalloc(&g->max_force, n);
-    if (s == GS_OK) s = dalloc(&g->radius, n);
-    if (s == GS_OK) s = dalloc(&g->mass, n);
-    if (s == GS_OK) s = dalloc(&g->applied, n);
+    if (s == GS_OK) s = dalloc(&g->position, 3 * n);
+    if (s == GS_OK) s = dalloc(&g->side, 2 * n);
+    if (s == GS_OK) s = dalloc(&g->speed, 6 * n);
+    if (s == GS_OK) {
+        g->direction = g->position + n;
+        g->steering = g->position + 2 * n;
+        g->up = g->side + n;
+        g->max_speed = g->speed + n;
+        g->max_force = g->speed + 2 * n;
+        g->radius = g->speed + 3 * n;
+        g->mass = g->speed + 4 * n;
+        g->applied = reinterpret_cast<unsigned*>(g->speed + 5 * n);
+    }
     if (s != GS_OK) {
         const std::string msg = g_last_error;
         gs_group_destroy(g);
@@ -571,6 +571,44 @@ gs_status gs_group_create(unsigned k, unsigned capacity, void* stream, gs_group*
     }
     *out = g;
     return GS_OK;
+}
+
+// Copies n elements of `count` arrays (elem bytes each) from src[i] to dst[i]:
+// one pitched copy when both sides hold the arrays at one fixed, increasing
+// stride (then the copy engine pays its fixed cost once, not per array), else
+// one copy per array.
+static cudaError_t copy_arrays(void* const* dst, const void* const* src, int count, size_t elem,
+                               unsigned n, cudaMemcpyKind kind, cudaStream_t st) {
+    const size_t width = size_t(n) * elem;
+    if (width == 0) return cudaSuccess;
+    static int max_pitch = -1;
+    if (max_pitch < 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&v, cudaDevAttrMaxPitch, dev) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        max_pitch = v;
+    }
+    if (count > 1) {
+        auto gap = [](const void* a, const void* b) {
+            return static_cast<const char*>(b) - static_cast<const char*>(a);
+        };
+        const ptrdiff_t dp = gap(dst[0], dst[1]), sp = gap(src[0], src[1]);
+        bool ok = dp >= ptrdiff_t(width) && sp >= ptrdiff_t(width) && dp <= max_pitch &&
+                  sp <= max_pitch;
+        for (int i = 2; i < count && ok; ++i)
+            ok = gap(dst[i - 1], dst[i]) == dp && gap(src[i - 1], src[i]) == sp;
+        if (ok)
+            return cudaMemcpy2DAsync(dst[0], size_t(dp), src[0], size_t(sp), width, size_t(count),
+                                     kind, st);
+    }
+    for (int i = 0; i < count; ++i) {
+        const cudaError_t e = cudaMemcpyAsync(dst[i], src[i], width, kind, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 static gs_status upload_enqueue(gs_group g, const gs_agent_arrays* h, unsigned n);
@@ -592,21 +630,15 @@ gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
 // Queues the copies of gs_group_upload on the group's stream.
 static gs_status upload_enqueue(gs_group g, const gs_agent_arrays* h, unsigned n) {
     cudaStream_t st = g->stream;
-    auto cp = [&](void* dst, const void* src, size_t bytes) {
-        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
-    };
-    const size_t f4b = size_t(n) * 16, f3b = size_t(n) * 12, f1b = size_t(n) * 4;
-    cudaError_t e = cp(g->position, h->position, f4b);
-    if (e == cudaSuccess) e = cp(g->direction, h->direction, f4b);
-    if (e == cudaSuccess) e = cp(g->steering, h->steering, f4b);
-    if (e == cudaSuccess) e = cp(g->side, h->side, f3b);
-    if (e == cudaSuccess) e = cp(g->up, h->up, f3b);
-    if (e == cudaSuccess) e = cp(g->speed, h->speed, f1b);
-    if (e == cudaSuccess) e = cp(g->max_speed, h->max_speed, f1b);
-    if (e == cudaSuccess) e = cp(g->max_force, h->max_force, f1b);
-    if (e == cudaSuccess) e = cp(g->radius, h->radius, f1b);
-    if (e == cudaSuccess) e = cp(g->mass, h->mass, f1b);
-    if (e == cudaSuccess) e = cp(g->applied, h->applied, f1b);
+    void* d4[] = {g->position, g->direction, g->steering};
+    const void* h4[] = {h->position, h->direction, h->steering};
+    void* d3[] = {g->side, g->up};
+    const void* h3[] = {h->side, h->up};
+    void* d1[] = {g->speed, g->max_speed, g->max_force, g->radius, g->mass, g->applied};
+    const void* h1[] = {h->speed, h->max_speed, h->max_force, h->radius, h->mass, h->applied};
+    cudaError_t e = copy_arrays(d4, h4, 3, 16, n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = copy_arrays(d3, h3, 2, 12, n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = copy_arrays(d1, h1, 6, 4, n, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "upload");
     return GS_OK;
 }
@@ -623,28 +655,49 @@ static gs_status download_enqueue(gs_group g, const gs_agent_arrays* h,
     return download_copies(g, h, skip_constants);
 }
 
-// The device-to-host copies of the reference-layout arrays.
+// The device-to-host copies of the reference-layout arrays (a NULL host
+// array is left out).
 static gs_status download_copies(gs_group g, const gs_agent_arrays* h, bool skip_constants) {
     cudaStream_t st = g->stream;
     const unsigned n = g->n;
-    auto cp = [&](void* dst, const void* src, size_t bytes) {
-        if (!dst || bytes == 0) return cudaSuccess;
-        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+    const bool all4 = h->position && h->direction && h->steering, all3 = h->side && h->up;
+    const bool all1 = h->speed && h->max_speed && h->max_force && h->radius && h->mass && h->applied;
+    cudaError_t e = cudaSuccess;
+    auto cp = [&](void* dst, const void* src, size_t elem) {
+        if (e == cudaSuccess && dst && n)
+            e = cudaMemcpyAsync(dst, src, size_t(n) * elem, cudaMemcpyDeviceToHost, st);
     };
-    const size_t f4b = size_t(n) * 16, f3b = size_t(n) * 12, f1b = size_t(n) * 4;
-    cudaError_t e = cp(h->position, g->position, f4b);
-    if (e == cudaSuccess) e = cp(h->direction, g->direction, f4b);
-    if (e == cudaSuccess) e = cp(h->steering, g->steering, f4b);
-    if (e == cudaSuccess) e = cp(h->side, g->side, f3b);
-    if (e == cudaSuccess) e = cp(h->up, g->up, f3b);
-    if (e == cudaSuccess) e = cp(h->speed, g->speed, f1b);
-    if (!skip_constants) {
-        if (e == cudaSuccess) e = cp(h->max_speed, g->max_speed, f1b);
-        if (e == cudaSuccess) e = cp(h->max_force, g->max_force, f1b);
-        if (e == cudaSuccess) e = cp(h->radius, g->radius, f1b);
-        if (e == cudaSuccess) e = cp(h->mass, g->mass, f1b);
+    if (all4) {
+        void* h4[] = {h->position, h->direction, h->steering};
+        const void* d4[] = {g->position, g->direction, g->steering};
+        e = copy_arrays(h4, d4, 3, 16, n, cudaMemcpyDeviceToHost, st);
+    } else {
+        cp(h->position, g->position, 16);
+        cp(h->direction, g->direction, 16);
+        cp(h->steering, g->steering, 16);
     }
-    if (e == cudaSuccess) e = cp(h->applied, g->applied, f1b);
+    if (all3) {
+        void* h3[] = {h->side, h->up};
+        const void* d3[] = {g->side, g->up};
+        if (e == cudaSuccess) e = copy_arrays(h3, d3, 2, 12, n, cudaMemcpyDeviceToHost, st);
+    } else {
+        cp(h->side, g->side, 12);
+        cp(h->up, g->up, 12);
+    }
+    if (all1 && !skip_constants) {
+        void* h1[] = {h->speed, h->max_speed, h->max_force, h->radius, h->mass, h->applied};
+        const void* d1[] = {g->speed, g->max_speed, g->max_force, g->radius, g->mass, g->applied};
+        if (e == cudaSuccess) e = copy_arrays(h1, d1, 6, 4, n, cudaMemcpyDeviceToHost, st);
+    } else {
+        cp(h->speed, g->speed, 4);
+        if (!skip_constants) {
+            cp(h->max_speed, g->max_speed, 4);
+            cp(h->max_force, g->max_force, 4);
+            cp(h->radius, g->radius, 4);
+            cp(h->mass, g->mass, 4);
+        }
+        cp(h->applied, g->applied, 4);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "download");
     return GS_OK;
 }

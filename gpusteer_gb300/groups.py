@@ -386,24 +386,28 @@ class Batch:
 
 def pinned_state(n: int) -> AgentState:
     """An AgentState whose arrays live in page-locked host memory
-    (gs_host_alloc), freed with the state; host copies from it overlap with
-    device work and can be captured in graphs."""
+    (gs_host_alloc), freed with the state.  Host copies from it overlap with
+    device work and can be captured in graphs; its arrays are laid out in the
+    library's three blocks (position, direction, steering | side, up | speed,
+    maxSpeed, maxForce, radius, mass, applied), so each block moves in one
+    pitched copy."""
     import weakref
 
-    shapes = {"position": (n, 4), "direction": (n, 4), "steering": (n, 4), "side": (n, 3),
-              "up": (n, 3), "speed": (n,), "max_speed": (n,), "max_force": (n,),
-              "radius": (n,), "mass": (n,), "applied": (n,)}
+    blocks = [(("position", "direction", "steering"), 4), (("side", "up"), 3),
+              (("speed", "max_speed", "max_force", "radius", "mass", "applied"), 1)]
     arrays, ptrs = {}, []
-    for k, shp in shapes.items():
-        count = max(1, int(np.prod(shp)))
+    lib = _lib.load()
+    for names, width in blocks:
+        count = max(1, len(names) * n * width)
         p = C.c_void_p()
         call("gs_host_alloc", count * 4, C.byref(p))
         ptrs.append(p)
-        ctype = C.c_uint if k == "applied" else C.c_float
-        buf = (ctype * count).from_address(p.value)
-        arrays[k] = np.ctypeslib.as_array(buf)[:int(np.prod(shp))].reshape(shp)
+        for j, k in enumerate(names):
+            ctype = C.c_uint if k == "applied" else C.c_float
+            buf = (ctype * (n * width)).from_address(p.value + 4 * j * n * width)
+            a = np.ctypeslib.as_array(buf) if n else np.zeros(0, np.float32)
+            arrays[k] = a.reshape((n, width)) if width > 1 else a
     st = AgentState(**arrays)
-    lib = _lib.load()
     weakref.finalize(st, lambda ps=ptrs: [lib.gs_host_free(q) for q in ps])
     return st
 
