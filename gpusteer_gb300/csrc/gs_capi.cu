@@ -49,6 +49,7 @@ static void release_fused(gs_group g) {
     dfree(g->retry);
     dfree(g->slot_of);
     dfree(g->retry_count);
+    dfree(g->retry_knn);
     dfree(g->d_stat);
     db_release(g->fdb);
     g->fused_k_alloc = 0;
@@ -1505,6 +1506,7 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         GS_TRY(dalloc(&g->retry, n));
         GS_TRY(dalloc(&g->slot_of, n));
         GS_TRY(dalloc(&g->retry_count, 1));
+        GS_TRY(dalloc(&g->retry_knn, size_t(std::min<size_t>(n, kRetryListCap)) * kRetryListK));
         GS_TRY(dalloc(&g->d_stat, 1));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
         GS_CUDA(cudaMemset(g->retry_count, 0, sizeof(unsigned)));
@@ -1624,6 +1626,8 @@ static void fill_launch(gs_group g, const StepDev& d, const WallsDev& w, FusedLa
     L.err = g->d_err;
     L.retry = g->retry;
     L.retry_count = g->retry_count;
+    L.retry_knn = g->retry_knn;
+    L.retry_cap = unsigned(std::min<size_t>(g->capacity, kRetryListCap));
     if (d.need & NEED_WALLS) {
         L.w_start = w.start;
         L.w_end = w.end;

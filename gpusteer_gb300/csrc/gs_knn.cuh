@@ -126,15 +126,18 @@ constexpr unsigned KEY32_EMPTY = 0xffffffffu;
 template <int KMAX>
 struct KList32 {
     unsigned key[KMAX];
-    // Inserts c; returns the largest key, which leaves the list.
+    // Inserts c; returns the largest key, which leaves the list.  In a sorted
+    // list the entry at i after the insertion is min(key[i], max(key[i-1], c)):
+    // key[i-1] when c goes below it, c when it falls between, else key[i].
+    // Every entry comes from the old list and c alone, so the KMAX
+    // min/max pairs are independent (dependency depth 2) instead of one
+    // chain through c of 2 * KMAX steps.
     __device__ __forceinline__ unsigned insert(unsigned c) {
+        const unsigned out = max(key[KMAX - 1], c);
 #pragma unroll
-        for (int i = 0; i < KMAX; ++i) {
-            const unsigned lo = min(key[i], c);
-            c = max(key[i], c);
-            key[i] = lo;
-        }
-        return c;
+        for (int i = KMAX - 1; i > 0; --i) key[i] = min(key[i], max(key[i - 1], c));
+        key[0] = min(key[0], c);
+        return out;
     }
     // Ascending bitonic sort (compare-exchange = min + max).
     __device__ __forceinline__ void sort() {

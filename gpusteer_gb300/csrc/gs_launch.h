@@ -145,6 +145,12 @@ struct StepDev {
 constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
                    NEED_WALLS = 32;
 
+// The exact redo's precomputed neighbour lists: kRetryListK slots per entry
+// (the largest KMAX), for up to kRetryListCap entries per step.
+constexpr unsigned kRetryListK = 32;
+constexpr unsigned kRetryListCap = 16384;
+constexpr unsigned kRetryNotListed = 0xfffffffeu;
+
 struct FusedLaunch {
     Fused A, B;
     uint2* cellrank;
@@ -161,6 +167,12 @@ struct FusedLaunch {
     unsigned* err;  // device flag: bit 0 = a bucketed slot fell outside [0, n)
     unsigned* retry;        // [n] slots the fast KNN handed to the exact redo
     unsigned* retry_count;  // zeroed by the permute launch of each step
+    // [retry_cap * kRetryListK] the exact neighbour slots of the first
+    // retry_cap redo entries, written by the warp-per-agent exact search
+    // (entry 0 = kRetryNotListed when that search left the entry to the
+    // redo's own thread)
+    unsigned* retry_knn;
+    unsigned retry_cap;
     // optional record of the step's inputs by agent index (rollouts for the
     // adjoint; walls-free steps only): null when not recording
     float4* rec_pos;    // [n] position | speed before the step (after the wrap)

@@ -231,12 +231,19 @@ __device__ __forceinline__ void store_next(const FusedLaunch& L, unsigned s, con
     L.cellrank[s] = make_uint2(cell, rank);
 }
 
-__device__ __forceinline__ Self load_fused(const Fused& B, unsigned s, float4& f0, float4& f4v) {
-    f0 = B.f[0][s];
+// The scene number alone (f4.w): the KNN needs position, index and scene;
+// the rest of the state is loaded after it, so it is not held in registers
+// through the scan.
+__device__ __forceinline__ unsigned load_scene(const Fused& B, unsigned s) {
+    return __float_as_uint(reinterpret_cast<const float*>(B.f[4] + s)[3]);
+}
+
+// Everything but position and index, after the KNN.
+__device__ __forceinline__ Self load_rest(const Fused& B, unsigned s, V3 pos, float4& f4v) {
     const float4 f1 = B.f[1][s], f2 = B.f[2][s], f3 = B.f[3][s];
     f4v = B.f[4][s];
     Self me;
-    me.pos = v3(f0);
+    me.pos = pos;
     me.dir = v3(f1);
     me.speed = f1.w;
     me.side = v3(f2);
@@ -255,9 +262,18 @@ __device__ __forceinline__ Self load_fused(const Fused& B, unsigned s, float4& f
 // gave up and the agent was appended to the retry list.
 template <int KMAX, unsigned ENUM, bool EXACT>
 __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDev& p, unsigned s,
-                                              V3 pos, unsigned id, const Scene& sc,
+                                              unsigned it, V3 pos, unsigned id, const Scene& sc,
                                               const Box& box, unsigned* col, unsigned bd) {
     if (EXACT) {
+        // redo entry `it`: the list the warp-per-agent search stored, else a
+        // search by this thread
+        if (it < L.retry_cap) {
+            const unsigned* pre = L.retry_knn + size_t(it) * kRetryListK;
+            if (pre[0] != kRetryNotListed) {
+                for (unsigned r = 0; r < p.k; ++r) col[r * bd] = pre[r];
+                return 0;
+            }
+        }
         knn_neighbours_exact<KMAX>(int(p.k), pos, id, sc.grid, box, sc.cell_offset, L.start,
                                    L.B.f[0], col, bd);
         return 0;
@@ -298,6 +314,94 @@ __device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, u
     return true;
 }
 
+// ---- exact redo: one warp per agent ------------------------------------------------
+// The exact (distance, index) list of each redo entry, found by a whole warp:
+// the lanes compute the 64-bit keys of the box's candidates side by side
+// (row by row, 32 candidates at a time) into a per-warp shared table, then
+// k rounds of a warp arg-min take the smallest key left and retire it.  The
+// list equals knn_neighbours_exact's: the keys are unique (distinct agent
+// indices), a candidate is listed only below KEY_EMPTY, the agent itself is
+// skipped, and empty ranks hold UINT_MAX.  A redo entry costs a few
+// arg-min rounds of latency instead of one thread's serial pass over every
+// candidate.  Entries with more than kRetryWarpKeys candidates are marked
+// kRetryNotListed and searched by the redo's own thread.
+constexpr unsigned kRetryWarpKeys = 256;
+
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) {
+    __shared__ unsigned long long sk[kBlock / 32][kRetryWarpKeys];
+    __shared__ unsigned ss[kBlock / 32][kRetryWarpKeys];
+    const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const unsigned nw = gridDim.x * (blockDim.x >> 5);
+    const unsigned count = min(*L.retry_count, L.retry_cap);
+    unsigned long long* keys = sk[w];
+    unsigned* slots = ss[w];
+    // warp w of block b takes entries w * gridDim.x + b, + nw, ...: a few
+    // hundred entries land one per block across every SM
+    for (unsigned e = w * gridDim.x + blockIdx.x; e < count; e += nw) {
+        const unsigned s = L.retry[e];
+        const float4 f0 = L.B.f[0][s];
+        const V3 pos = v3(f0);
+        const unsigned id = u(f0.w);
+        const Scene sc = L.scenes[load_scene(L.B, s)];
+        unsigned ix, iy, iz;
+        cell_coords(sc.grid, pos, ix, iy, iz);
+        const Box b = cell_box(sc.grid, ix, iy, iz, p.r);
+        unsigned total = 0;
+        for (unsigned cy = b.y0; cy <= b.y1; ++cy) {
+            for (unsigned cz = b.z0; cz <= b.z1; ++cz) {
+                const unsigned c0 = sc.cell_offset + cell_label(sc.grid, b.x0, cy, cz);
+                const unsigned c1 = sc.cell_offset + cell_label(sc.grid, b.x1, cy, cz) + 1;
+                const unsigned s0 = L.start[c0], len = L.start[c1] - s0;
+                for (unsigned t = lane; t < len; t += 32) {
+                    const unsigned j = total + t;
+                    if (j < kRetryWarpKeys) {
+                        const float4 q = L.B.f[0][s0 + t];
+                        const unsigned qid = u(q.w);
+                        keys[j] = qid == id ? ~0ull : knn_key(distance(pos, v3(q)), qid);
+                        slots[j] = s0 + t;
+                    }
+                }
+                total += len;
+            }
+        }
+        __syncwarp();
+        unsigned* out = L.retry_knn + size_t(e) * kRetryListK;
+        if (total > kRetryWarpKeys) {
+            if (lane == 0) out[0] = kRetryNotListed;
+            __syncwarp();
+            continue;
+        }
+        for (unsigned r = 0; r < p.k; ++r) {
+            unsigned long long best = ~0ull;
+            unsigned bj = 0;
+            for (unsigned j = lane; j < total; j += 32) {
+                const unsigned long long kk = keys[j];
+                if (kk < best) {
+                    best = kk;
+                    bj = j;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const unsigned oj = __shfl_xor_sync(0xffffffffu, bj, off);
+                if (ob < best) {
+                    best = ob;
+                    bj = oj;
+                }
+            }
+            // every lane holds the same (best, bj): the keys are unique
+            const bool listed = best < KEY_EMPTY;
+            if (lane == 0) {
+                out[r] = listed ? slots[bj] : UINT_MAX;
+                if (listed) keys[bj] = ~0ull;
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // ---- whole step without walls -------------------------------------------------------
 // NEEDC: the behaviours that read the neighbour list, fixed at compile time
 // (kNeedRuntime: taken from p.need).
@@ -313,18 +417,17 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
     for (unsigned it = first_agent<EXACT>();; it += step) {
         unsigned s;
         if (!next_agent<EXACT>(L, it, s)) return;
-        float4 f0, f4v;
-        Self me = load_fused(L.B, s, f0, f4v);
-        const unsigned id = u(f0.w), scene = u(f4v.w);
+        const float4 f0 = L.B.f[0][s];
+        const V3 pos = v3(f0);
+        const unsigned id = u(f0.w), scene = load_scene(L.B, s);
         const Scene sc = L.scenes[scene];
         unsigned ix, iy, iz;
-        cell_coords(sc.grid, me.pos, ix, iy, iz);
+        cell_coords(sc.grid, pos, ix, iy, iz);
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
-        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, me.pos, id, sc, box, col, bd);
-        if (base == UINT_MAX) {
-            if (EXACT) return;
-            return;
-        }
+        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, it, pos, id, sc, box, col, bd);
+        if (base == UINT_MAX) return;
+        float4 f4v;
+        Self me = load_rest(L.B, s, pos, f4v);
         unsigned applied = p.clear_applied ? 0u : u(f4v.z);
         V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
         const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali),
@@ -366,15 +469,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
     for (unsigned it = first_agent<EXACT>();; it += step) {
         unsigned s;
         if (!next_agent<EXACT>(L, it, s)) return;
-        float4 f0, f4v;
-        Self me = load_fused(L.B, s, f0, f4v);
-        const unsigned id = u(f0.w), scene = u(f4v.w);
+        const float4 f0 = L.B.f[0][s];
+        const V3 pos = v3(f0);
+        const unsigned id = u(f0.w), scene = load_scene(L.B, s);
         const Scene sc = L.scenes[scene];
         unsigned ix, iy, iz;
-        cell_coords(sc.grid, me.pos, ix, iy, iz);
+        cell_coords(sc.grid, pos, ix, iy, iz);
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
-        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, me.pos, id, sc, box, col, bd);
+        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, it, pos, id, sc, box, col, bd);
         if (base == UINT_MAX) return;
+        float4 f4v;
+        Self me = load_rest(L.B, s, pos, f4v);
         unsigned applied = p.clear_applied ? 0u : u(f4v.z);
         V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
         for (unsigned r = 0; r < p.k; ++r) {
@@ -494,6 +599,7 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
         GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
         k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
+        k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
         k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
@@ -517,6 +623,7 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
             }
         }
         if (!done) k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
+        k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
         k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         if (hook) hook->mark(2, false);
     }
