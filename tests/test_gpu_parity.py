@@ -441,6 +441,41 @@ def test_knn_capacity_does_not_change_results(capacity):
         assert_state(g.download(), want, skip_side=want.speed == 0)
 
 
+@pytest.mark.parametrize("case", ["lattice_past_list_cap", "crowd_warp_lists", "clump_thread_lists"])
+def test_exact_redo_routes(case):
+    """Every route of the exact redo gives the oracle's result bit for bit:
+    lists found by one warp per agent (boxes of up to 256 candidates),
+    lists left to the redo's own thread (larger boxes), and redo entries
+    past the 16,384 stored lists (a 27,000-agent lattice, where ties send
+    every agent to the redo), with and without walls."""
+    if case == "lattice_past_list_cap":
+        g3 = np.stack(np.meshgrid(*(np.arange(30),) * 3, indexing="ij"), -1)
+        pts = g3.reshape(-1, 3).astype(np.float32) - 15.0
+        s = sc.boids_sphere(pts.shape[0], seed=4)
+        s.position[:, :3] = pts
+        p = sc.boids_params(k=16, world=64.0, cell=2.0)
+        bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+        g = group_of(s, p.k)
+        gs.set_knn_capacity(g, 32)
+        gs.step(g, bins, None, p, 2)
+        want = s.copy()
+        ol.run(want, p, 2)
+    else:
+        # 4,000 agents in a square: 10 per cell (90 candidates, past the
+        # collecting scan's 32) or 40 per cell (360, past the warp's 256)
+        p = sc.chokepoint_params()
+        bins, walls = choke_walls(p)
+        half = 10.0 if case == "clump_thread_lists" else 20.0
+        s = sc.chokepoint_agents(4000, x_range=(-half, half), z_range=(20.0, 20.0 + 2 * half),
+                                 seed=6)
+        g = group_of(s, p.k)
+        gs.set_knn_capacity(g, 128 if case == "clump_thread_lists" else 32)
+        gs.step(g, bins, walls, p, 3)
+        want = s.copy()
+        ol.run(want, p, 3, walls=walls.download())
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
 def test_streaming_scan_in_3d_matches_oracle():
     s = sc.boids_sphere(20000, radius=25.0, seed=8)
     p = sc.boids_params(k=16, world=64.0, cell=2.0)
