@@ -149,7 +149,8 @@ struct gs_group_s {
     // fused-step state
     gs::Fused A, B;
     uint2* cellrank;       // next cell and rank per slot of A
-    float4 *w0, *w1, *w2;  // wall-phase outputs (corrected pos/dir, steering+applied)
+    float4 *w0, *w1, *w2;  // wall-phase outputs: corrected position | radius,
+                           // direction | speed, steering | applied
     unsigned* knn_slot;    // [k * n] neighbour slots (wall phase)
     float* knn_dist;       // [k * n]
     gs::Database fdb;      // counts / starts of the fused step

@@ -514,7 +514,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
         } else if (!(applied & p.mask_walls)) {
             steer = add(mul(v3(0.f, 0.f, 0.f), p.w_walls), steer);
         }
-        L.w0[s] = make_float4(me.pos.x, me.pos.y, me.pos.z, f0.w);
+        // the radius rides with the position: a neighbour costs the rest
+        // phase two gathers (w0, w1) instead of three
+        L.w0[s] = make_float4(me.pos.x, me.pos.y, me.pos.z, me.radius);
         L.w1[s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
         L.w2[s] = make_float4(steer.x, steer.y, steer.z, fb(applied));
         if (!EXACT) return;
@@ -539,22 +541,22 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev
     me.mass = f3.w;
     me.max_speed = f4v.x;
     me.max_force = f4v.y;
-    const unsigned id = u(w0.w), scene = u(f4v.w);
+    const unsigned id = u(reinterpret_cast<const float*>(L.B.f[0] + s)[3]), scene = u(f4v.w);
     unsigned applied = u(w2.w);
     V3 steer = v3(w2);
     const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
     Accs a;
     init_accs(a, p);
     const bool need_dir = need & (NEED_ALI | NEED_AVOID);
-    const bool need_rad = need & (NEED_AVOID | NEED_CLOSE);
     for (unsigned i = 0; i < p.k; ++i) {
         const unsigned bs = L.knn_slot[size_t(i) * L.n + s];
         if (bs == UINT_MAX) break;
         const float4 b0 = L.w0[bs];
         const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float br = need_rad ? L.B.f[2][bs].w : 0.f;
         const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
-        accumulate(a, p, need, fs, fa, fc, me, u(b0.w), kd, v3(b0), v3(b1), b1.w, br);
+        // neighbour avoidance keeps only whether a threat was found, so the
+        // list rank stands in for the neighbour's index
+        accumulate(a, p, need, fs, fa, fc, me, i, kd, v3(b0), v3(b1), b1.w, b0.w);
     }
     finish_all(a, p, 1, fs, fa, fc, me, applied, steer);
     integrate(me, steer, p.dt);
