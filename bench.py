@@ -672,7 +672,7 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
                 "identical_to_one_batch": parts_identical,
                 "one_batch": {"value": e2e_one, "ms_per_step": one_s * 1e3 / e2e_steps,
                               "api": "gs_batch_upload, gs_batch_step, gs_batch_download"}},
-        "gpu_launches": 8 * args.steps,  # scan (3), permute, walls, exact lists, redo, rest
+        "gpu_launches": gs.step_launches(b.group, True) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": read_traffic("batched"),
                      "kernel": "k_fused_walls+k_fused_rest",
@@ -816,8 +816,6 @@ def run_gpu(args, dist, rank, world, local_rank):
     group.upload(state)
     stream = torch.cuda.ExternalStream(group.stream)
     has_walls = walls is not None
-    # scan (3), permute, fused (walls + rest with walls), exact lists, redo
-    launches_per_step = 3 + 1 + (4 if has_walls else 3)
 
     # warm-up, then K timed steps (state resident in HBM)
     gs.step(group, bins, walls, p, args.warmup)
@@ -892,7 +890,7 @@ def run_gpu(args, dist, rank, world, local_rank):
                    "l2": "inputs larger than L2 (about 200 MB of bucketed state per step)"},
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state},
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": gs.step_launches(group, has_walls) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_fused" + ("_walls+k_fused_rest" if has_walls else ""),

@@ -12,7 +12,8 @@ from .groups import (  # noqa: F401
     antiPenetrationWall, updateGroupWithAntiPenetration,
     findKNearestNeighbors, findKNearestNeighborsBruteForce, findKNearestNeighborsGroups,
     set_block, set_graphs,
-    set_knn_capacity, step, step_host, steerForAlignment, steerForCohesion,
+    knn_capacity, set_knn_capacity, step, step_host, step_launches, steerForAlignment,
+    steerForCohesion,
     steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, steerToFollowPath,
     updateGroup,
     updateKNNDatabase, wrapWorld)

@@ -113,6 +113,7 @@ SIGNATURES = {
     "gs_group_set_graphs": [_vp, _i],
     "gs_group_set_block": [_vp, _u],
     "gs_group_set_knn_capacity": [_vp, _u],
+    "gs_group_knn_capacity": [_vp, _up],
     "gs_batch_create": [_u, _up, _u, _up, _fp, _u, _vp, C.POINTER(_vp)],
     "gs_batch_destroy": [_vp],
     "gs_batch_set_walls": [_vp, _u, _fp, _fp, _fp, _u],

@@ -1756,6 +1756,12 @@ gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity) {
     return GS_OK;
 }
 
+gs_status gs_group_knn_capacity(gs_group g, unsigned* capacity) {
+    if (!g || !capacity) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *capacity = g->knn_cap ? g->knn_cap : (g->auto_cap_valid ? g->auto_cap : 0u);
+    return GS_OK;
+}
+
 gs_status gs_group_set_block(gs_group g, unsigned threads) {
     if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
     if (threads != 64 && threads != 128 && threads != 256)

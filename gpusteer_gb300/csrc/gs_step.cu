@@ -324,7 +324,8 @@ __device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, u
 // skipped, and empty ranks hold UINT_MAX.  A redo entry costs a few
 // arg-min rounds of latency instead of one thread's serial pass over every
 // candidate.  Entries with more than kRetryWarpKeys candidates are marked
-// kRetryNotListed and searched by the redo's own thread.
+// kRetryNotListed and searched by the redo's own thread.  Launched after the
+// streaming scan only (crowded boxes, where the serial pass is long).
 constexpr unsigned kRetryWarpKeys = 256;
 
 template <int KMAX>
@@ -524,8 +525,11 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
 }
 
 // ---- rest of the step after the wall phase --------------------------------------------
+// Five blocks per SM (48 registers): the rest phase waits on neighbour
+// gathers, and the extra resident warps hide more of that than the spills
+// cost (0.604 -> 0.585 ms per 256-scene step against four blocks).
 template <int KMAX, unsigned NEEDC>
-__global__ void __launch_bounds__(kBlock, 4) k_fused_rest(FusedLaunch L, StepDev p) {
+__global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev p) {
     const unsigned need = NEEDC == kNeedRuntime ? p.need : NEEDC;
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.n) return;
@@ -597,12 +601,18 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
     const size_t smem = ENUM > 64 ? size_t(KMAX > 8 ? KMAX : 8) * bs * sizeof(unsigned)
                                   : size_t(2 * ENUM) * bs * sizeof(unsigned);
     const size_t smem_x = size_t(KMAX > 8 ? KMAX : 8) * kBlock * sizeof(unsigned);
+    // The warp-per-agent exact lists pay off for crowded boxes (the streaming
+    // scan, 40-250 candidates); with the collecting scan (sparse boxes, mostly
+    // distance ties among a dozen candidates) the redo thread's own search is
+    // shorter than the extra launch, and the redo reads no stored lists.
+    FusedLaunch Lx = L;
+    if (ENUM <= 64) Lx.retry_cap = 0;
     if (p.need & NEED_WALLS) {
         GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
         k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
-        k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
-        k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
+        if (ENUM > 64) k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
+        k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(Lx, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
         // the choke-point step (separation and neighbour avoidance) has its own build
@@ -625,8 +635,8 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
             }
         }
         if (!done) k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
-        k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
-        k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
+        if (ENUM > 64) k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
+        k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(Lx, p);
         if (hook) hook->mark(2, false);
     }
     GS_LAUNCHED("fused_step");

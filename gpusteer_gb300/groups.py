@@ -312,6 +312,21 @@ def set_knn_capacity(group, capacity: int) -> None:
     call("gs_group_set_knn_capacity", group.handle, int(capacity))
 
 
+def knn_capacity(group) -> int:
+    """The capacity the fused step uses (the fixed one, else the one measured
+    at the last step; 0 before the first step)."""
+    out = C.c_uint(0)
+    call("gs_group_knn_capacity", group.handle, C.byref(out))
+    return int(out.value)
+
+
+def step_launches(group, walls: bool) -> int:
+    """Kernel launches of one fused step: the counting-sort scan (3), the
+    permute, the fused kernel (two with walls), the exact redo, and with the
+    streaming scan (capacity 128 or 256) the warp-per-agent exact lists."""
+    return 3 + 1 + (2 if walls else 1) + 1 + (1 if knn_capacity(group) > 64 else 0)
+
+
 class Batch:
     """Many independent scenes advanced together (gs_batch_*): agents are
     concatenated in scene order, each scene keeps scene-local indices, cells

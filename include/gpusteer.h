@@ -353,6 +353,11 @@ gs_status gs_group_set_block(gs_group g, unsigned threads);
  * upload).  Results do not depend on it: agents with more candidates are
  * redone by the exact scan.  Not part of the reference. */
 gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity);
+/* The capacity the fused step uses: the fixed one, else the one measured at
+ * the last step (0 before the first).  With 128 or 256 a step makes one more
+ * launch: the exact lists of the agents the fast scan hands to the redo,
+ * found by one warp per agent. */
+gs_status gs_group_knn_capacity(gs_group g, unsigned* capacity);
 
 /* ---- batched scenes -------------------------------------------------------------
  * Many independent worlds (e.g. one ChokePoint plugin instance each) advanced

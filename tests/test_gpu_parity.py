@@ -443,11 +443,13 @@ def test_knn_capacity_does_not_change_results(capacity):
 
 @pytest.mark.parametrize("case", ["lattice_past_list_cap", "crowd_warp_lists", "clump_thread_lists"])
 def test_exact_redo_routes(case):
-    """Every route of the exact redo gives the oracle's result bit for bit:
-    lists found by one warp per agent (boxes of up to 256 candidates),
-    lists left to the redo's own thread (larger boxes), and redo entries
-    past the 16,384 stored lists (a 27,000-agent lattice, where ties send
-    every agent to the redo), with and without walls."""
+    """Every route of the exact redo after the streaming scan (capacity 128)
+    gives the oracle's result bit for bit: lists found by one warp per agent
+    (boxes of up to 256 candidates), lists left to the redo's own thread
+    (larger boxes), and redo entries past the 16,384 stored lists (a
+    27,000-agent lattice, 216 candidates per box: every agent overflows into
+    the redo), with and without walls.  The collecting scans' redo (capacity
+    32 and 64, no stored lists) is covered by the lattice test above."""
     if case == "lattice_past_list_cap":
         g3 = np.stack(np.meshgrid(*(np.arange(30),) * 3, indexing="ij"), -1)
         pts = g3.reshape(-1, 3).astype(np.float32) - 15.0
@@ -456,24 +458,46 @@ def test_exact_redo_routes(case):
         p = sc.boids_params(k=16, world=64.0, cell=2.0)
         bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
         g = group_of(s, p.k)
-        gs.set_knn_capacity(g, 32)
+        gs.set_knn_capacity(g, 128)
         gs.step(g, bins, None, p, 2)
         want = s.copy()
         ol.run(want, p, 2)
     else:
-        # 4,000 agents in a square: 10 per cell (90 candidates, past the
-        # collecting scan's 32) or 40 per cell (360, past the warp's 256)
+        # 4,000 agents in a square: about 20 per cell (184 candidates, past
+        # the streaming scan's 128) or 40 per cell (360, past the warp's 256)
         p = sc.chokepoint_params()
         bins, walls = choke_walls(p)
-        half = 10.0 if case == "clump_thread_lists" else 20.0
+        half = 10.0 if case == "clump_thread_lists" else 14.0
         s = sc.chokepoint_agents(4000, x_range=(-half, half), z_range=(20.0, 20.0 + 2 * half),
                                  seed=6)
         g = group_of(s, p.k)
-        gs.set_knn_capacity(g, 128 if case == "clump_thread_lists" else 32)
+        gs.set_knn_capacity(g, 128)
         gs.step(g, bins, walls, p, 3)
         want = s.copy()
         ol.run(want, p, 3, walls=walls.download())
     assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+def test_knn_capacity_reads_back():
+    """The capacity a step used: the fixed one, or the measured choice
+    (streaming scan for a dense crowd, collecting scan for a sparse flock);
+    the step's launch count follows it."""
+    p = sc.chokepoint_params()
+    bins, walls = choke_walls(p)
+    g = group_of(sc.chokepoint_agents(10000, seed=5), p.k)
+    assert gs.knn_capacity(g) == 0
+    gs.step(g, bins, walls, p, 1)
+    assert gs.knn_capacity(g) in (128, 256)
+    assert gs.step_launches(g, True) == 8
+    gs.set_knn_capacity(g, 64)
+    assert gs.knn_capacity(g) == 64
+    assert gs.step_launches(g, True) == 7
+    s = sc.boids_sphere(4096, seed=0)
+    pb = sc.boids_params(k=7)
+    fb = group_of(s, pb.k)
+    gs.step(fb, gs.KNNBinData(pb.world_cells, pb.world_size, 1), None, pb, 1)
+    assert gs.knn_capacity(fb) in (32, 64)
+    assert gs.step_launches(fb, False) == 6
 
 
 def test_streaming_scan_in_3d_matches_oracle():
