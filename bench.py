@@ -504,6 +504,7 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     ms_max = allreduce_max(dist, ev0.elapsed_time(ev1))
     value = n * args.steps * world / (ms_max / 1e3)
     phases = phase_times(lib, b.group, lambda k: b.step(p, k), max(3, min(args.steps, 10)))
+    launches_per_step = gs.step_launches(b.group, True)
     del b
 
     # the same scenes, one gs_step call per scene per step (same grid, block,
@@ -672,7 +673,7 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
                 "identical_to_one_batch": parts_identical,
                 "one_batch": {"value": e2e_one, "ms_per_step": one_s * 1e3 / e2e_steps,
                               "api": "gs_batch_upload, gs_batch_step, gs_batch_download"}},
-        "gpu_launches": gs.step_launches(b.group, True) * args.steps,
+        "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": read_traffic("batched"),
                      "kernel": "k_fused_walls+k_fused_rest",
