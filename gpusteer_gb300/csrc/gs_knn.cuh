@@ -139,6 +139,41 @@ struct KList32 {
         key[0] = min(key[0], c);
         return out;
     }
+    // Merges the 4 keys c into the list, keeping the KMAX smallest, and
+    // returns the smallest key that does not stay.  The chunk is sorted (5
+    // compare-exchanges) and laid reversed against the list's last 4
+    // entries: the elementwise minimum of an ascending and a descending
+    // sequence is bitonic and holds the KMAX smallest keys of both, and the
+    // elementwise maxima are the keys that leave.  log2(KMAX) half-cleaner
+    // stages then sort the bitonic list.  Equal to inserting the 4 keys one
+    // after another, at about two thirds of the min/max work per key.
+    __device__ __forceinline__ unsigned merge4(unsigned (&c)[4]) {
+        static_assert(KMAX >= 4, "chunk merge needs KMAX >= 4");
+        cmpx(c[0], c[1]);
+        cmpx(c[2], c[3]);
+        cmpx(c[0], c[2]);
+        cmpx(c[1], c[3]);
+        cmpx(c[1], c[2]);
+        unsigned out = KEY32_EMPTY;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const unsigned a = key[KMAX - 4 + j], b = c[3 - j];
+            key[KMAX - 4 + j] = min(a, b);
+            out = min(out, max(a, b));
+        }
+#pragma unroll
+        for (int stride = KMAX / 2; stride > 0; stride >>= 1) {
+#pragma unroll
+            for (int i = 0; i < KMAX; ++i)
+                if ((i ^ stride) > i) cmpx(key[i], key[i ^ stride]);
+        }
+        return out;
+    }
+    __device__ __forceinline__ static void cmpx(unsigned& a, unsigned& b) {
+        const unsigned lo = min(a, b);
+        b = max(a, b);
+        a = lo;
+    }
     // Ascending bitonic sort (compare-exchange = min + max).
     __device__ __forceinline__ void sort() {
 #pragma unroll
@@ -270,9 +305,10 @@ __device__ __forceinline__ bool knn_neighbours_fast(int k, V3 p, unsigned self_i
 // exact path.
 __device__ constexpr int kRowOrder[9] = {4, 1, 3, 5, 7, 0, 2, 6, 8};
 
-// Streaming fast path for crowded boxes: the same 32-bit keys, but every
-// candidate goes straight into the register list (no per-candidate shared
-// memory), so the enumeration capacity is 2^EBITS whatever the block size.
+// Streaming fast path for crowded boxes: the same 32-bit keys, but the
+// candidates go straight into the register list, four at a time (no
+// per-candidate shared memory), so the enumeration capacity is 2^EBITS
+// whatever the block size.
 // e numbers every candidate of the box in row order, the agent itself
 // included, so a listed key's e is decoded back to its slot from the nine
 // row starts and the running row offsets alone.  Boxes of more than 3 x 3
@@ -310,13 +346,22 @@ __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self
     for (int ii = 0; ii < 9; ++ii) {
         const int i = kRowOrder[ii];
         const unsigned n_row = pre[i + 1] - pre[i];
-        for (unsigned t = 0; t < n_row; ++t) {
-            const float4 q = __ldg(pos_id + rs[i] + t);
-            const unsigned bits = __float_as_uint(distance(p, v3(q)));
-            if (__float_as_uint(q.w) != self_id && bits < 0x7f7fffffu) {
-                const unsigned c = (bits & ~mask) | (pre[i] + t);
-                out_min = min(out_min, c < L.key[KMAX - 1] ? L.insert(c) : c);
+        // four candidates at a time: their loads and distances overlap, and
+        // one chunk merge costs less than four insertions
+        for (unsigned t0 = 0; t0 < n_row; t0 += 4) {
+            unsigned c[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const unsigned t = t0 + unsigned(j);
+                c[j] = KEY32_EMPTY;
+                if (t < n_row) {
+                    const float4 q = __ldg(pos_id + rs[i] + t);
+                    const unsigned bits = __float_as_uint(distance(p, v3(q)));
+                    if (__float_as_uint(q.w) != self_id && bits < 0x7f7fffffu)
+                        c[j] = (bits & ~mask) | (pre[i] + t);
+                }
             }
+            out_min = min(out_min, L.merge4(c));
         }
     }
     const unsigned last = L.key[KMAX - 1];
