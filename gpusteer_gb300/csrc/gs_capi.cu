@@ -274,6 +274,7 @@ static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev&
     if (!std::isfinite(p->dt)) return fail(GS_ERR_NONFINITE, "dt is not finite");
     std::memset(&d, 0, sizeof(d));
     d.k = p->k;
+    d.flat = p->world_cells[1] == 1 ? 1u : 0u;
     d.knw = p->knw;
     d.r = p->search_radius;
     d.wrap_mode = p->wrap_mode;

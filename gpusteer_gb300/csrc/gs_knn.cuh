@@ -297,13 +297,14 @@ __device__ __forceinline__ bool knn_neighbours_fast(int k, V3 p, unsigned self_i
 }
 
 // The order the streaming scan visits the nine rows of a 3 x 3 x 3 (or
-// 3 x 3) box in: the middle row first, then the rows beside it, then the
-// corners, so the list fills with near candidates early and later candidates
+// 3 x 3) box in (kRowOrderFlat: the three rows of a flat box): the middle
+// row first, then the rows beside it, then the corners, so the list fills with near candidates early and later candidates
 // insert less (1.5 % of a 256-scene choke-point step).  The result does not
 // depend on it: the list ends as the k smallest keys, whose enumeration
 // indices do not change, and ties of truncated distance send the agent to the
 // exact path.
 __device__ constexpr int kRowOrder[9] = {4, 1, 3, 5, 7, 0, 2, 6, 8};
+__device__ constexpr int kRowOrderFlat[3] = {1, 0, 2};
 
 // Streaming fast path for crowded boxes: the same 32-bit keys, but the
 // candidates go straight into the register list, four at a time (no
@@ -314,8 +315,12 @@ __device__ constexpr int kRowOrder[9] = {4, 1, 3, 5, 7, 0, 2, 6, 8};
 // row starts and the running row offsets alone.  Boxes of more than 3 x 3
 // rows (search radius above 1) are left to the exact path.  Writes the k
 // slots to out[r * stride]; returns false when the exact path must redo the
-// agent, on the same conditions as the collecting scan.
-template <int KMAX, unsigned EBITS>
+// agent, on the same conditions as the collecting scan.  FLAT: the grid is
+// one cell high in y (the 2D worlds on the x-z plane), so a box has at most 3
+// rows; that build keeps 3 row starts instead of 9 (no register spills at
+// 64 registers) and drops the 6 empty row loops.  The rows and their
+// enumeration are those of the 9-row build (rows 3-8 are empty there).
+template <int KMAX, unsigned EBITS, bool FLAT = false>
 __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self_id,
                                                       const Grid& g, const Box& b,
                                                       unsigned cell_offset,
@@ -323,13 +328,14 @@ __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self
                                                       const float4* __restrict__ pos_id,
                                                       unsigned* out, unsigned stride) {
     constexpr unsigned ENUM = 1u << EBITS, mask = ENUM - 1;
-    if (b.y1 - b.y0 > 2 || b.z1 - b.z0 > 2) return false;
+    constexpr int R = FLAT ? 3 : 9;
+    if ((FLAT ? b.y1 != b.y0 : b.y1 - b.y0 > 2) || b.z1 - b.z0 > 2) return false;
     const unsigned span = b.x1 - b.x0 + 1;
-    unsigned rs[9], pre[10];
+    unsigned rs[R], pre[R + 1];
     pre[0] = 0;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) {
-        const unsigned cy = b.y0 + unsigned(i / 3), cz = b.z0 + unsigned(i % 3);
+    for (int i = 0; i < R; ++i) {
+        const unsigned cy = b.y0 + unsigned(FLAT ? 0 : i / 3), cz = b.z0 + unsigned(i % 3);
         const bool ok = cy <= b.y1 && cz <= b.z1;
         const unsigned c0 = cell_offset + cell_label(g, b.x0, ok ? cy : b.y0, ok ? cz : b.z0);
         const unsigned s0 = ok ? __ldg(cell_start + c0) : 0u;
@@ -337,14 +343,14 @@ __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self
         rs[i] = s0;
         pre[i + 1] = pre[i] + (s1 - s0);
     }
-    if (pre[9] > ENUM) return false;
+    if (pre[R] > ENUM) return false;
     KList32<KMAX> L;
 #pragma unroll
     for (int i = 0; i < KMAX; ++i) L.key[i] = i < KMAX - k ? 0u : KEY32_EMPTY;
     unsigned out_min = KEY32_EMPTY;  // smallest key not (or no longer) in the list
 #pragma unroll
-    for (int ii = 0; ii < 9; ++ii) {
-        const int i = kRowOrder[ii];
+    for (int ii = 0; ii < R; ++ii) {
+        const int i = FLAT ? kRowOrderFlat[ii] : kRowOrder[ii];
         const unsigned n_row = pre[i + 1] - pre[i];
         // four candidates at a time: their loads and distances overlap, and
         // one chunk merge costs less than four insertions
@@ -379,7 +385,7 @@ __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self
             const unsigned e = key & mask;
             slot = rs[0] + e;
 #pragma unroll
-            for (int j = 1; j < 9; ++j)
+            for (int j = 1; j < R; ++j)
                 if (e >= pre[j]) slot = rs[j] + (e - pre[j]);
         }
         out[(i - (KMAX - k)) * stride] = slot;

@@ -138,6 +138,7 @@ struct StepDev {
     unsigned need;      // NEED_* bits
     unsigned enum_cap;  // candidate capacity of the fast KNN scan (32, 64: collecting; 128, 256: streaming)
     unsigned block;     // threads per block of the fused launches (0: 256)
+    unsigned flat;      // the grid is one cell high (y): boxes hold 3 rows of cells
     PathDev path;       // path following (GS_B_FOLLOW_PATH)
     float path_time, w_path;
     unsigned mask_path;

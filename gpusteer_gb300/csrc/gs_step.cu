@@ -260,7 +260,7 @@ __device__ __forceinline__ Self load_rest(const Fused& B, unsigned s, V3 pos, fl
 // column: at col[(ENUM + r) * bd] on the fast path, col[r * bd] on the exact
 // path; returns the column offset of entry 0, or UINT_MAX when the fast path
 // gave up and the agent was appended to the retry list.
-template <int KMAX, unsigned ENUM, bool EXACT>
+template <int KMAX, unsigned ENUM, bool EXACT, bool FLAT>
 __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDev& p, unsigned s,
                                               unsigned it, V3 pos, unsigned id, const Scene& sc,
                                               const Box& box, unsigned* col, unsigned bd) {
@@ -281,7 +281,7 @@ __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDe
     if constexpr (ENUM > 64) {
         // crowded boxes: streaming scan, result at col[r * bd]
         constexpr unsigned EBITS = ENUM >= 256 ? 8u : 7u;
-        if (knn_neighbours_stream<KMAX, EBITS>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
+        if (knn_neighbours_stream<KMAX, EBITS, FLAT>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
                                                L.start, L.B.f[0], col, bd))
             return 0;
     } else if (knn_neighbours_fast<KMAX, ENUM>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) 
 // (kNeedRuntime: taken from p.need).
 constexpr unsigned kNeedRuntime = ~0u;
 constexpr unsigned kNeedList = NEED_SEP | NEED_ALI | NEED_COH | NEED_AVOID | NEED_CLOSE;
-template <int KMAX, unsigned ENUM, bool EXACT, unsigned NEEDC = kNeedRuntime>
+template <int KMAX, unsigned ENUM, bool EXACT, unsigned NEEDC = kNeedRuntime, bool FLAT = false>
 __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
     const unsigned need = NEEDC == kNeedRuntime ? p.need : NEEDC;
     extern __shared__ unsigned sh_col[];
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
         unsigned ix, iy, iz;
         cell_coords(sc.grid, pos, ix, iy, iz);
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
-        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, it, pos, id, sc, box, col, bd);
+        const unsigned base = agent_knn<KMAX, ENUM, EXACT, FLAT>(L, p, s, it, pos, id, sc, box, col, bd);
         if (base == UINT_MAX) return;
         float4 f4v;
         Self me = load_rest(L.B, s, pos, f4v);
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
 }
 
 // ---- wall phase: KNN, wall KNN and avoid-walls ---------------------------------------
-template <int KMAX, int KW, unsigned ENUM, bool EXACT>
+template <int KMAX, int KW, unsigned ENUM, bool EXACT, bool FLAT = false>
 __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDev p) {
     extern __shared__ unsigned sh_col[];
     const unsigned bd = blockDim.x;
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
         unsigned ix, iy, iz;
         cell_coords(sc.grid, pos, ix, iy, iz);
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
-        const unsigned base = agent_knn<KMAX, ENUM, EXACT>(L, p, s, it, pos, id, sc, box, col, bd);
+        const unsigned base = agent_knn<KMAX, ENUM, EXACT, FLAT>(L, p, s, it, pos, id, sc, box, col, bd);
         if (base == UINT_MAX) return;
         float4 f4v;
         Self me = load_rest(L.B, s, pos, f4v);
@@ -608,9 +608,20 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
     FusedLaunch Lx = L;
     if (ENUM <= 64) Lx.retry_cap = 0;
     if (p.need & NEED_WALLS) {
-        GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
         if (hook) hook->mark(2, true);
-        k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
+        // flat grids (one cell high) have a 3-row build of the streaming scan
+        bool launched = false;
+        if constexpr (ENUM > 64) {
+            if (p.flat) {
+                GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false, true>, smem));
+                k_fused_walls<KMAX, 8, ENUM, false, true><<<nb, bs, smem, st>>>(L, p);
+                launched = true;
+            }
+        }
+        if (!launched) {
+            GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
+            k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
+        }
         if (ENUM > 64) k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
         k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(Lx, p);
         if (hook) hook->mark(2, false);
@@ -631,6 +642,13 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
             if ((p.need & kNeedList) == (NEED_SEP | NEED_ALI | NEED_COH)) {
                 GS_TRY(allow_smem(k_fused<KMAX, 32, false, NEED_SEP | NEED_ALI | NEED_COH>, smem));
                 k_fused<KMAX, 32, false, NEED_SEP | NEED_ALI | NEED_COH><<<nb, bs, smem, st>>>(L, p);
+                done = true;
+            }
+        }
+        if constexpr (ENUM > 64) {
+            if (p.flat) {
+                GS_TRY(allow_smem(k_fused<KMAX, ENUM, false, kNeedRuntime, true>, smem));
+                k_fused<KMAX, ENUM, false, kNeedRuntime, true><<<nb, bs, smem, st>>>(L, p);
                 done = true;
             }
         }

@@ -500,6 +500,21 @@ def test_knn_capacity_reads_back():
     assert gs.step_launches(fb, False) == 6
 
 
+@pytest.mark.parametrize("capacity", [128, 256])
+def test_flat_streaming_scan_without_walls(capacity):
+    """A 2D crowd (grid one cell high) without walls: the 3-row build of the
+    streaming scan in the single fused kernel gives the oracle's result."""
+    p = sc.chokepoint_params().replace(order=(sc.B_AVOID_NEIGHBORS, sc.B_SEPARATION, sc.B_SEEK))
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    s = sc.chokepoint_agents(10000, seed=9)
+    g = group_of(s, p.k)
+    gs.set_knn_capacity(g, capacity)
+    gs.step(g, bins, None, p, 10)
+    want = s.copy()
+    ol.run(want, p, 10)
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
 def test_streaming_scan_in_3d_matches_oracle():
     s = sc.boids_sphere(20000, radius=25.0, seed=8)
     p = sc.boids_params(k=16, world=64.0, cell=2.0)
