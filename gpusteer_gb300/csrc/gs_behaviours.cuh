@@ -281,6 +281,58 @@ GS_HD void avoid_finish(const AvoidAcc& a, float w, unsigned mask, const Self& s
     steer = add(r, steer);
 }
 
+// The same behaviour with a four-word accumulator, for kernels that can
+// read their neighbours again after the pass: the smallest accepted time,
+// the threat's list rank, and the rank and time of the last neighbour that
+// passed the time test (whose nearest-approach position the reference keeps
+// in threat_at).  avoid_lite_full rebuilds AvoidAcc from those two
+// neighbours with the expressions avoid_add evaluates, so the result is the
+// same bit for bit; the pass itself holds 4 words instead of 12.
+struct AvoidLite {
+    float min_t, last_t;
+    unsigned threat, last;  // list ranks, UINT_MAX for none
+};
+GS_HD void avoid_lite_init(AvoidLite& a, float min_time) {
+    a.min_t = min_time;
+    a.last_t = 0.f;
+    a.threat = a.last = UINT_MAX;
+}
+GS_HD void avoid_lite_add(AvoidLite& a, const Self& s, unsigned rank, V3 bpos, V3 bdir,
+                          float bspeed, float bradius) {
+    const float danger = s.radius + bradius;
+    const float time = nearest_approach_time(s.pos, s.dir, s.speed, bpos, bdir, bspeed);
+    if (time >= 0.f && time < a.min_t) {
+        V3 at;
+        a.last = rank;
+        a.last_t = time;
+        if (nearest_approach_positions(s.pos, s.dir, s.speed, bpos, bdir, bspeed, time, at) <
+            danger) {
+            a.min_t = time;
+            a.threat = rank;
+        }
+    }
+}
+// fetch(rank, pos, dir, speed) reads list entry `rank` as the pass saw it.
+template <class Fetch>
+GS_HD AvoidAcc avoid_lite_full(const AvoidLite& a, Fetch&& fetch) {
+    AvoidAcc f;
+    avoid_init(f, a.min_t);
+    f.threat = a.threat;
+    V3 pos, dir;
+    float speed;
+    if (a.last != UINT_MAX) {
+        fetch(a.last, pos, dir, speed);
+        f.threat_at = add(pos, mul(dir, speed * a.last_t));  // nearest_approach_positions
+    }
+    if (a.threat != UINT_MAX) {
+        fetch(a.threat, pos, dir, speed);
+        f.threat_pos = pos;
+        f.threat_dir = dir;
+        f.threat_speed = speed;
+    }
+    return f;
+}
+
 // ---- SteerToAvoidWallsCUDAKernel (AvoidWallsCUDAKernel.cu:89-244) -----------------
 struct WallAcc {
     V3 feelers[3];

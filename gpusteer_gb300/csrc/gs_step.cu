@@ -133,7 +133,7 @@ gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStr
 // Neighbour accumulators of every behaviour that reads the KNN list.
 struct Accs {
     FlockAcc sep, ali, coh;
-    AvoidAcc avoid;
+    AvoidLite avoid;
     CloseAcc close;
 };
 
@@ -141,7 +141,7 @@ struct Accs {
 // specialised for one configuration (the unused accumulators then vanish).
 __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned need,
                                            const FlockParams& fs, const FlockParams& fa,
-                                           const FlockParams& fc, const Self& me, unsigned bid,
+                                           const FlockParams& fc, const Self& me, unsigned rank,
                                            float knn_d, V3 bpos, V3 bdir, float bspeed,
                                            float bradius) {
     const V3 offset = sub(bpos, me.pos);
@@ -175,18 +175,20 @@ __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned n
             }
         }
     }
-    if (need & NEED_AVOID) avoid_add(a.avoid, me, bid, bpos, bdir, bspeed, bradius);
+    if (need & NEED_AVOID) avoid_lite_add(a.avoid, me, rank, bpos, bdir, bspeed, bradius);
     // the KNN distance equals d unless the neighbour moved after the KNN
     // (avoid-walls); the caller passes it then, else -1
     if (need & NEED_CLOSE)
         close_add(a.close, me, p.min_sep, knn_d < 0.f ? d : knn_d, bpos, bradius);
 }
 
-// Behaviours order[first..] in order, then nothing else.
+// Behaviours order[first..] in order, then nothing else.  fetch(rank, pos,
+// dir, speed) reads neighbour list entry `rank` again (neighbour avoidance).
+template <class Fetch>
 __device__ __forceinline__ void finish_all(const Accs& a, const StepDev& p, unsigned first,
                                            const FlockParams& fs, const FlockParams& fa,
                                            const FlockParams& fc, const Self& me,
-                                           unsigned& applied, V3& steer) {
+                                           unsigned& applied, V3& steer, Fetch&& fetch) {
 #pragma unroll
     for (unsigned o = 0; o < 8; ++o) {
         if (o < first || o >= p.n_order) continue;
@@ -200,7 +202,8 @@ __device__ __forceinline__ void finish_all(const Accs& a, const StepDev& p, unsi
                 break;
             case GS_B_AVOID_NEIGHBORS:
                 if (p.avoid_close) close_finish(a.close, p.w_avoid, p.mask_avoid, applied, steer);
-                avoid_finish(a.avoid, p.w_avoid, p.mask_avoid, me, applied, steer);
+                avoid_finish(avoid_lite_full(a.avoid, fetch), p.w_avoid, p.mask_avoid, me,
+                             applied, steer);
                 break;
             case GS_B_FOLLOW_PATH:
                 follow_path_finish(p.path, p.path_time, p.w_path, p.mask_path, me, applied, steer);
@@ -214,7 +217,7 @@ __device__ __forceinline__ void init_accs(Accs& a, const StepDev& p) {
     flock_init(a.sep);
     flock_init(a.ali);
     flock_init(a.coh);
-    avoid_init(a.avoid, p.min_time_col);
+    avoid_lite_init(a.avoid, p.min_time_col);
     close_init(a.close);
 }
 
@@ -446,14 +449,21 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
             const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float br = need_rad ? L.B.f[2][bs].w : 0.f;
             if (rec_knn) rec_knn[r] = u(b0.w);
-            accumulate(a, p, need, fs, fa, fc, me, u(b0.w), -1.f, v3(b0), v3(b1), b1.w, br);
+            accumulate(a, p, need, fs, fa, fc, me, r, -1.f, v3(b0), v3(b1), b1.w, br);
         }
         if (rec_knn) {
             for (; r < p.k; ++r) rec_knn[r] = UINT_MAX;
             L.rec_pos[id] = make_float4(me.pos.x, me.pos.y, me.pos.z, me.speed);
             L.rec_dir[id] = make_float4(me.dir.x, me.dir.y, me.dir.z, 0.f);
         }
-        finish_all(a, p, 0, fs, fa, fc, me, applied, steer);
+        finish_all(a, p, 0, fs, fa, fc, me, applied, steer,
+                   [&](unsigned rank, V3& bp, V3& bh, float& bsp) {
+                       const unsigned bs = col[(base + rank) * bd];
+                       const float4 b0 = L.B.f[0][bs], b1 = L.B.f[1][bs];
+                       bp = v3(b0);
+                       bh = v3(b1);
+                       bsp = b1.w;
+                   });
         integrate(me, steer, p.dt);
         store_next(L, s, me, id, scene, sc, p.wrap_mode);
         if (!EXACT) return;
@@ -533,21 +543,14 @@ __global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev
     const unsigned need = NEEDC == kNeedRuntime ? p.need : NEEDC;
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= L.n) return;
-    const float4 w0 = L.w0[s], w1 = L.w1[s], w2 = L.w2[s];
-    const float4 f2 = L.B.f[2][s], f3 = L.B.f[3][s], f4v = L.B.f[4][s];
+    // the neighbour pass reads position, radius, heading and speed only; the
+    // rest of the state is loaded after it, so it is not held through the pass
+    const float4 w0 = L.w0[s], w1 = L.w1[s];
     Self me;
     me.pos = v3(w0);
+    me.radius = w0.w;
     me.dir = v3(w1);
     me.speed = w1.w;
-    me.side = v3(f2);
-    me.radius = f2.w;
-    me.up = v3(f3);
-    me.mass = f3.w;
-    me.max_speed = f4v.x;
-    me.max_force = f4v.y;
-    const unsigned id = u(reinterpret_cast<const float*>(L.B.f[0] + s)[3]), scene = u(f4v.w);
-    unsigned applied = u(w2.w);
-    V3 steer = v3(w2);
     const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
     Accs a;
     init_accs(a, p);
@@ -558,13 +561,28 @@ __global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev
         const float4 b0 = L.w0[bs];
         const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
-        // neighbour avoidance keeps only whether a threat was found, so the
-        // list rank stands in for the neighbour's index
         accumulate(a, p, need, fs, fa, fc, me, i, kd, v3(b0), v3(b1), b1.w, b0.w);
     }
-    finish_all(a, p, 1, fs, fa, fc, me, applied, steer);
+    const float4 w2 = L.w2[s];
+    const float4 f2 = L.B.f[2][s], f3 = L.B.f[3][s], f4v = L.B.f[4][s];
+    me.side = v3(f2);
+    me.up = v3(f3);
+    me.mass = f3.w;
+    me.max_speed = f4v.x;
+    me.max_force = f4v.y;
+    const unsigned id = u(reinterpret_cast<const float*>(L.B.f[0] + s)[3]), scene = u(f4v.w);
+    unsigned applied = u(w2.w);
+    V3 steer = v3(w2);
+    finish_all(a, p, 1, fs, fa, fc, me, applied, steer,
+               [&](unsigned rank, V3& bp, V3& bh, float& bsp) {
+                   const unsigned bs = L.knn_slot[size_t(rank) * L.n + s];
+                   const float4 b0 = L.w0[bs], b1 = L.w1[bs];
+                   bp = v3(b0);
+                   bh = v3(b1);
+                   bsp = b1.w;
+               });
     integrate(me, steer, p.dt);
-    const Scene sc = L.scenes[scene];  // loaded here: not held through the neighbour loop
+    const Scene sc = L.scenes[scene];
     store_next(L, s, me, id, scene, sc, p.wrap_mode);
 }
 
