@@ -505,6 +505,7 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     value = n * args.steps * world / (ms_max / 1e3)
     phases = phase_times(lib, b.group, lambda k: b.step(p, k), max(3, min(args.steps, 10)))
     launches_per_step = gs.step_launches(b.group, True)
+    measured_cap = gs.knn_capacity(b.group)  # the scan the resident steps used
     del b
 
     # the same scenes, one gs_step call per scene per step (same grid, block,
@@ -599,7 +600,9 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     for lo, hi in zip(cuts[:-1], cuts[1:]):
         bp = autotune.batch_for(states[lo:hi], gaps[lo:hi], p, walls_rows)
         gs.set_block(bp.group, tr.block)
-        gs.set_knn_capacity(bp.group, tr.capacity or 256)
+        # a fixed capacity (the host-stepping graph needs one): the one the
+        # resident batch used
+        gs.set_knn_capacity(bp.group, tr.capacity or measured_cap or 256)
         parts.append(bp)
     # one step from the initial state: the parts equal the single batch
     for k in hio.names():
@@ -611,11 +614,17 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
     parts_identical = all(np.array_equal(getattr(hio, k), getattr(want, k)) for k in want.names())
     gs.batches_step_host(parts, p, 1, hio, hio)
     barrier(dist)
-    t0 = time.perf_counter()
+    # each call is synchronous (its results are in host memory when it
+    # returns): timed one by one, the median per step discounts a host-side
+    # stall in one call; the mean is reported beside it
+    step_s = []
     for _ in range(e2e_steps):
+        t0 = time.perf_counter()
         gs.batches_step_host(parts, p, 1, hio, hio)
-    e2e_s = allreduce_max(dist, time.perf_counter() - t0)
-    e2e = n * e2e_steps * world / e2e_s
+        step_s.append(time.perf_counter() - t0)
+    e2e_med = allreduce_max(dist, statistics.median(step_s))
+    e2e_mean = allreduce_max(dist, sum(step_s) / len(step_s))
+    e2e = n * world / e2e_med
     bytes_state = n * (16 * 3 + 12 * 2 + 4 * 5 + 4)
     # in place, the four per-agent constants (16 B) are not copied back
     bytes_back = n * (16 * 3 + 12 * 2 + 4 * 2)
@@ -666,7 +675,9 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         "autotune": {"seconds": tune_s, "trials": tr.trials},
         "adjoint": adjoint,
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
-                "d2h_bytes_per_step": bytes_back, "ms_per_step": e2e_s * 1e3 / e2e_steps,
+                "d2h_bytes_per_step": bytes_back, "ms_per_step": e2e_med * 1e3,
+                "ms_per_step_mean": e2e_mean * 1e3,
+                "timing": f"median of {e2e_steps} host-timed calls, one step each",
                 "api": f"gs_batches_step_host over {len(cuts) - 1} parts (scene ranges) in "
                        "place, one graph: each part's copies in, steps and copies out, "
                        "overlapped across the parts",
