@@ -97,11 +97,12 @@ static gs_status check_grid(const unsigned wc[3], const float ws[3], Grid& g, un
         if (wc[a] == 0) return fail(GS_ERR_INVALID_ARG, "world cells must be positive");
         if (!(ws[a] > 0.f) || !std::isfinite(ws[a]))
             return fail(GS_ERR_INVALID_ARG, "world size must be positive and finite");
+        // checked after every factor: the running product stays below 2^62
         c *= wc[a];
+        if (c > (1ull << 30)) return fail(GS_ERR_INVALID_ARG, "too many cells");
         g.wc[a] = wc[a];
         g.ws[a] = ws[a];
     }
-    if (c > (1ull << 30)) return fail(GS_ERR_INVALID_ARG, "too many cells");
     cells = unsigned(c);
     return GS_OK;
 }

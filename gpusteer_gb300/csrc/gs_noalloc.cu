@@ -24,8 +24,14 @@
 // the array and must be serialised by the caller.
 //
 // The array's device address is looked up with cudaGetSymbolAddress the first
-// time a call is made on a device (with that device current); make that first
-// call before starting any stream capture on that device.
+// time a call is made in a CUDA context (with that context's device current)
+// and kept for that context only: a context created later on the same device
+// (after cudaDeviceReset, say) loads the library's module again, possibly at
+// another address, and its first call looks the address up again.  Make the
+// first call on each device, and the first after a reset, before starting any
+// stream capture on that device.
+#include <cuda.h>
+
 #include <cmath>
 #include <cstdint>
 #include <mutex>
@@ -41,18 +47,56 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_knn_scratch[kScratchBytes];
 
 std::mutex g_mu;
+// Per device: the context the address was looked up in (0: none) and the address.
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
 void* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_knn_scratch on the current device (looked up once).
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (the
+// library links the static runtime, not libcuda).  Null when unavailable.
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrent g_ctx_current = nullptr;
+CtxGetId g_ctx_id = nullptr;
+std::once_flag g_entry_once;
+
+void resolve_entry_points() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+        g_ctx_current = reinterpret_cast<CtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+        g_ctx_id = reinterpret_cast<CtxGetId>(f);
+}
+
+// Unique id of the calling thread's current context, 0 if none is current or
+// the driver cannot say.
+unsigned long long current_context_id() {
+    if (!g_ctx_current || !g_ctx_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (g_ctx_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_knn_scratch in the current context of the current
+// device: looked up once per context, again whenever the context changed.
 gs_status scratch_address(void** out) {
+    std::call_once(g_entry_once, resolve_entry_points);
     int dev = 0;
     GS_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return fail(GS_ERR_UNSUPPORTED, "device index too large");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (ctx == 0 || ctx != g_scratch_ctx[dev] || !g_scratch_addr[dev]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_knn_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(knn scratch)");
+        // the lookup made the device's primary context current if none was
+        g_scratch_ctx[dev] = current_context_id();
         g_scratch_addr[dev] = p;
     }
     *out = g_scratch_addr[dev];
@@ -82,9 +126,10 @@ extern "C" gs_status gs_knn_binned_noalloc(const float* positions4, unsigned n,
             return fail(GS_ERR_INVALID_ARG, "bad world size or cell count");
         grid.wc[a] = world_cells[a];
         grid.ws[a] = world_size[a];
+        // checked after every factor: the running product stays below 2^62
         cells *= world_cells[a];
+        if (cells > (1ull << 30)) return fail(GS_ERR_INVALID_ARG, "too many cells");
     }
-    if (cells > (1ull << 30)) return fail(GS_ERR_INVALID_ARG, "too many cells");
     const unsigned C = unsigned(cells);
     const unsigned T = scan_tile_count(C);
     // layout inside the fixed array

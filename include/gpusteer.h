@@ -454,9 +454,12 @@ gs_status gs_flock_adjoint_step(const float* position_speed, const float* headin
  * that loads it, until exit): problems needing more than
  * 8 * (cells + 1) + 4 * ceil(cells / 4096) + 28 * n bytes (plus alignment) of
  * it return GS_ERR_INVALID_ARG.  Calls share that array: calls that overlap
- * on the GPU race and must be serialised by the caller.  The first call on a
- * device looks up the array's address (cudaGetSymbolAddress) with that device
- * current; make it before any stream capture.  Asynchronous on `stream`. */
+ * on the GPU race and must be serialised by the caller.  The first call in a
+ * CUDA context looks up the array's address (cudaGetSymbolAddress) with that
+ * context's device current and keeps it for that context: the first call on
+ * each device, and the first after a cudaDeviceReset (which reloads the
+ * library's module, possibly at another address), do the look-up; make them
+ * before any stream capture.  Asynchronous on `stream`. */
 gs_status gs_knn_binned_noalloc(const float* positions4, unsigned n,
                                 const unsigned world_cells[3], const float world_size[3],
                                 unsigned search_radius, unsigned k, unsigned* idx_out,

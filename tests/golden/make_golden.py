@@ -327,7 +327,7 @@ def path_case(ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=str(ol.reference_root()))
     ap.add_argument("--only", nargs="*", default=None, help="case functions to run")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", str(REPO / "oracle" / "ref"), f"REF={a.ref}"], check=True)

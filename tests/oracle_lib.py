@@ -17,6 +17,18 @@ REPO = Path(__file__).resolve().parents[1]
 ORACLE_SO = REPO / "oracle" / "_build" / "liboracle.so"
 REF_SO = REPO / "oracle" / "_ref" / "libgsref.so"
 
+
+def reference_root() -> Path:
+    """The reference source tree: $GPUSTEER_REFERENCE, else the default of the
+    recipe that compiles it (oracle/ref/Makefile).  It may not exist."""
+    env = os.environ.get("GPUSTEER_REFERENCE")
+    if env:
+        return Path(env)
+    out = subprocess.run(["make", "-s", "--no-print-directory", "-C",
+                          str(REPO / "oracle" / "ref"), "print-ref"],
+                         capture_output=True, text=True)
+    return Path(out.stdout.strip() or "/nonexistent")
+
 _fp = C.POINTER(C.c_float)
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint)

@@ -9,6 +9,8 @@ import gpusteer_gb300 as gs
 from gpusteer_gb300 import _lib, scenario as sc
 from gpusteer_gb300.state import AgentState
 
+import oracle_lib as ol
+
 REPO = Path(__file__).resolve().parents[1]
 
 
@@ -51,7 +53,10 @@ def test_bins_host_side_matches_reference_cell_layout():
 
 
 @pytest.mark.parametrize("cells,size", [((0, 1, 1), (1, 1, 1)), ((1, 1, 1), (0, 1, 1)),
-                                        ((1, 1, 1), (float("nan"), 1, 1))])
+                                        ((1, 1, 1), (float("nan"), 1, 1)),
+                                        # 2^31 * 2^31 * 4 wraps a 64-bit product to 0
+                                        ((1 << 31, 1 << 31, 4), (1, 1, 1)),
+                                        ((1 << 20, 1 << 11, 1), (1, 1, 1))])
 def test_bins_reject_bad_grids(cells, size):
     with pytest.raises(gs.GpuSteerError) as e:
         gs.KNNBinData(cells, size, 1)
@@ -111,7 +116,7 @@ def test_params_reader_parses_reference_format():
 
 
 def test_reference_params_files_parse():
-    data = Path("/root/reference/data")
+    data = ol.reference_root() / "data"
     if not data.exists():
         pytest.skip("reference data not mounted")
     for name in ("BoidsGroup.params", "ChokePoint.params", "MultiGroup.params"):
@@ -328,7 +333,7 @@ def test_cpp_simulation_params_loader_matches_python_reader(tmp_path):
     """
     files = [tmp_path / "synthetic.params"]
     files[0].write_text(text)
-    data = Path("/root/reference/data")
+    data = ol.reference_root() / "data"
     if data.exists():
         files += sorted(data.glob("*.params"))
     for f in files:

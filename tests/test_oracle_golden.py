@@ -215,7 +215,7 @@ def test_wall_split_is_cell_bounded():
 
 @pytest.mark.parametrize("gap", ["7.5", "10", "20", "32.5"])
 def test_chokepoint_map_generator_matches_reference_files(gap):
-    path = Path("/root/reference/data") / f"ChokePoint{gap}.map"
+    path = ol.reference_root() / "data" / f"ChokePoint{gap}.map"
     if not path.exists():
         pytest.skip("reference data not mounted")
     np.testing.assert_array_equal(sc.read_map(str(path)), sc.chokepoint_walls(float(gap)))

@@ -44,14 +44,16 @@ def noalloc_knn(state, cells, size, r, k):
 
 
 @pytest.mark.parametrize("k", [7, 16])
-def test_noalloc_knn_equals_regular_path_on_two_calls(k):
+@pytest.mark.parametrize("r", [1, 2])
+def test_noalloc_knn_equals_regular_path_on_two_calls(k, r):
     cases = [
         (sc.boids_sphere(20000, radius=40.0, seed=1), (32, 32, 32), (128.0, 128.0, 128.0)),
+        # a flat grid (one cell high): the 2D worlds on the x-z plane
         (sc.chokepoint_agents(15000, seed=2), (128, 1, 128), (256.0, 10.0, 256.0)),
     ]
     for state, cells, size in cases:  # two calls in a row on the shared array
-        want_i, want_d = regular_knn(state, cells, size, 1, k)
-        got_i, got_d = noalloc_knn(state, cells, size, 1, k)
+        want_i, want_d = regular_knn(state, cells, size, r, k)
+        got_i, got_d = noalloc_knn(state, cells, size, r, k)
         np.testing.assert_array_equal(got_i, want_i)
         np.testing.assert_array_equal(got_d, want_d)
 
@@ -71,3 +73,12 @@ def test_noalloc_knn_rejects_problems_beyond_its_array():
                                    C.c_void_p(g.stream))
     assert st == 1  # GS_ERR_INVALID_ARG, nothing launched
     assert b"32 MiB" in lib.gs_last_error()
+    # a cell count whose 64-bit product wraps (2^31 * 2^31 * 4 = 2^64) is
+    # rejected before anything is launched
+    st = lib.gs_knn_binned_noalloc(C.c_void_p(g.device_arrays()["position"]), 4,
+                                   (C.c_uint * 3)(1 << 31, 1 << 31, 4),
+                                   (C.c_float * 3)(64.0, 64.0, 64.0), 1, 4,
+                                   C.cast(idx, C.c_void_p), C.cast(dist, C.c_void_p),
+                                   C.c_void_p(g.stream))
+    assert st == 1
+    assert b"too many cells" in lib.gs_last_error()
