@@ -127,6 +127,13 @@ namespace ref_update_ap { GSREF_DYNAMIC_SHARED
 namespace ref_antipen_wall { GSREF_DYNAMIC_SHARED
 #include "AntiPenetrationWallCUDAKernel.cu"
 }
+// ProcessData.cu's kernel section (ComputeCellDensityKernel, the texture
+// bindings and ComputeAvgCellVelocityKernel, ProcessData.cu:131-237), cut
+// unmodified out of the file by the recipe: the file's host functions use
+// <<<>>> launches and the AgentGroup class, which this harness does not build.
+namespace ref_diag { GSREF_DYNAMIC_SHARED
+#include "ProcessDataKernels.inc"
+}
 
 namespace {
 constexpr unsigned TPB = THREADSPERBLOCK;  // AbstractCUDAKernel.cuh:46-54
@@ -172,23 +179,25 @@ void update_db(BinDB& db, const float* pos4, unsigned n, unsigned numCells) {
     });
     ref_knn::KNNBinningV2ReorderDBUnbindTextures();
 }
-}  // namespace
 
-extern "C" {
+// KNNBinDataV2 construction (KNNBinDataV2.cu:30-168): the cells, the
+// constants and the 3D cell lookup array.  The lookup array is laid out so
+// that texel (x, y, z) holds the bin_cell label x + z*X + y*X*Z, the
+// labelling the neighbour table is indexed by.
+struct BinGrid {
+    std::vector<OpenSteer::bin_cell> cells;
+    std::vector<unsigned> lookup;
+    gsref_array3d arr;
+};
 
-// KNNBinDataV2 construction (KNNBinDataV2.cu:30-168) + KNNBinningV2UpdateDBCUDA
-// for both groups + KNNBinningV2CUDA::run (KNNBinningV2.cu:192-271).
-// The 3D lookup array is laid out so that texel (x, y, z) holds the bin_cell
-// label x + z*X + y*X*Z, the labelling the neighbour table is indexed by.
-int gsref_knn_binned(const float* posA4, unsigned nA, const float* posB4, unsigned nB,
-                     int self, const float ws[3], const unsigned wc[3], unsigned radius,
-                     unsigned k, unsigned* idx_out, float* dist_out) {
+void bin_grid(BinGrid& G, const float ws[3], const unsigned wc[3]) {
     using namespace ref_knn;
     const unsigned X = wc[0], Y = wc[1], Z = wc[2], C = X * Y * Z;
     const float3 worldSize = make_float3(ws[0], ws[1], ws[2]);
     const float3 step = make_float3(ws[0] / X, ws[1] / Y, ws[2] / Z);
     const float3 stepN = make_float3(step.x / ws[0], step.y / ws[1], step.z / ws[2]);
-    std::vector<OpenSteer::bin_cell> cells(C);
+    std::vector<OpenSteer::bin_cell>& cells = G.cells;
+    cells.resize(C);
     unsigned index = 0;
     for (size_t iH = 0; iH < Y; iH++)
         for (size_t iD = 0; iD < Z; iD++)
@@ -206,15 +215,33 @@ int gsref_knn_binned(const float* posA4, unsigned nA, const float* posB4, unsign
                 bc.maxBound.z = bc.minBound.z + step.z;
                 cells[index++] = bc;
             }
-    std::vector<unsigned> lookup(C);
+    G.lookup.resize(C);
     for (unsigned z = 0; z < Z; ++z)
         for (unsigned y = 0; y < Y; ++y)
-            for (unsigned x = 0; x < X; ++x) lookup[x + y * X + z * X * Y] = x + z * X + y * X * Z;
-    gsref_array3d arr{lookup.data(), X, Y, Z};
+            for (unsigned x = 0; x < X; ++x) G.lookup[x + y * X + z * X * Y] = x + z * X + y * X * Z;
+    G.arr = gsref_array3d{G.lookup.data(), X, Y, Z};
     constWorldSizeV2 = worldSize;
     constWorldStepV2 = step;
     constWorldStepNormalizedV2 = stepN;
     constWorldCellsV2 = make_uint3(X, Y, Z);
+}
+}  // namespace
+
+extern "C" {
+
+// KNNBinDataV2 construction + KNNBinningV2UpdateDBCUDA for both groups +
+// KNNBinningV2CUDA::run (KNNBinningV2.cu:192-271).
+int gsref_knn_binned(const float* posA4, unsigned nA, const float* posB4, unsigned nB,
+                     int self, const float ws[3], const unsigned wc[3], unsigned radius,
+                     unsigned k, unsigned* idx_out, float* dist_out) {
+    using namespace ref_knn;
+    const unsigned X = wc[0], Y = wc[1], Z = wc[2], C = X * Y * Z;
+    (void)X;
+    (void)Z;
+    BinGrid G;
+    bin_grid(G, ws, wc);
+    std::vector<OpenSteer::bin_cell>& cells = G.cells;
+    gsref_array3d& arr = G.arr;
 
     const bool b3D = Y > 1;
     const unsigned npc = ipow(radius * 2 + 1, b3D ? 3 : 2);
@@ -245,6 +272,33 @@ int gsref_knn_binned(const float* posA4, unsigned nA, const float* posB4, unsign
                            npc, radius, idx_out, dist_out, k, nA, nB, self != 0);
     });
     KNNBinningV2KernelUnbindTextures();
+    return 0;
+}
+
+// ExtractData's diagnostics: ComputeCellDensity and ComputeAvgCellVelocity
+// (ProcessData.cu:51-128) on the group's database as KNNBinningV2UpdateDBCUDA
+// builds it (KNNBinningV2.cu:87-142): cellStart of an empty cell is
+// 0xffffffff, pdAgentIndicesSorted is the stable sort's agent order.
+// density_out: one count per cell; avg_velocity_out: float3 per cell.
+int gsref_cell_diagnostics(const float* pos4, const float* dir4, const float* speed, unsigned n,
+                           const float ws[3], const unsigned wc[3], unsigned* density_out,
+                           float* avg_velocity_out) {
+    const unsigned C = wc[0] * wc[1] * wc[2];
+    BinGrid G;
+    bin_grid(G, ws, wc);
+    BinDB db;
+    ref_knn::KNNBinningV2BindTexture(reinterpret_cast<cudaArray*>(&G.arr));
+    update_db(db, pos4, n, C);
+    ref_knn::KNNBinningV2UnbindTexture();
+    launch(blocks(C, TPB), TPB, [&] {
+        ref_diag::ComputeCellDensityKernel(db.cellStart.data(), db.cellEnd.data(), density_out, C);
+    });
+    ref_diag::ComputeAvgCellVelocityBindTextures(f4(dir4), speed, db.agentSorted.data(), n);
+    launch(blocks(C, TPB), TPB, [&] {
+        ref_diag::ComputeAvgCellVelocityKernel(db.cellStart.data(), db.cellEnd.data(),
+                                               f3(avg_velocity_out), n, C);
+    });
+    ref_diag::ComputeAvgCellVelocityUnbindTextures();
     return 0;
 }
 

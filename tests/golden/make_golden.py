@@ -325,6 +325,35 @@ def path_case(ref):
              out_steering=out.steering, out_applied=out.applied)
 
 
+def cell_diag_case(ref):
+    """ExtractData's ComputeCellDensity / ComputeAvgCellVelocity
+    (ProcessData.cu:51-237) on the reference's database: a 2D crowd (some
+    agents outside the world, clamped into edge cells) and a 3D flock."""
+    arrays = {}
+    cases = {
+        "crowd2d": (sc.chokepoint_agents(3000, seed=21), (128.0, 10.0, 128.0), (64, 1, 64), 5),
+        "flock3d": (sc.boids_sphere(4000, radius=20.0, seed=24), (64.0, 64.0, 64.0),
+                    (16, 16, 16), 6),
+    }
+    meta = {}
+    for name, (s, ws, wc, sseed) in cases.items():
+        s.speed[:] = (sc.uniform01(sseed, s.n) * 3.0).astype(np.float32)
+        if name == "crowd2d":
+            s.position[:40, 0] = np.float32(70.0)  # beyond the +x face
+        C_ = wc[0] * wc[1] * wc[2]
+        dens = np.empty(C_, np.uint32)
+        vel = np.empty((C_, 3), np.float32)
+        rc = ref.gsref_cell_diagnostics(fp(s.position), fp(s.direction), fp(s.speed), s.n,
+                                        ol.f3(ws), ol.u3(wc), up(dens), fp(vel))
+        assert rc == 0, rc
+        assert dens.max() >= 4
+        arrays.update({f"{name}_position": s.position, f"{name}_direction": s.direction,
+                       f"{name}_speed": s.speed, f"{name}_density": dens,
+                       f"{name}_avg_velocity": vel})
+        meta[name] = {"ws": ws, "wc": wc}
+    save("cell_diag", meta, **arrays)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=str(ol.reference_root()))
@@ -334,7 +363,7 @@ def main():
     ref = ol.ref_harness()
     assert ref is not None
     cases = [knn_cases, flock_case, avoid_case, flock_steps, choke_steps, path_case,
-             wall_antipen_case]
+             wall_antipen_case, cell_diag_case]
     for case in cases:
         if a.only is None or case.__name__ in a.only:
             case(ref)

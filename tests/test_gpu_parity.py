@@ -1009,6 +1009,26 @@ def test_cell_diagnostics_match_oracle(case):
                                   ol.cell_avg_velocity(s.position, s.direction, s.speed, ws, wc))
 
 
+@pytest.mark.parametrize("case", ["crowd2d", "flock3d"])
+def test_cell_diagnostics_match_reference_golden(case):
+    """gs_cell_density / gs_cell_avg_velocity against the reference's own
+    ProcessData.cu kernels on the reference's database (cell_diag.npz)."""
+    from gpusteer_gb300.groups import cell_avg_velocity, cell_density
+
+    z, m = load("cell_diag")
+    ws, wc = m[case]["ws"], m[case]["wc"]
+    s = AgentState.zeros(z[f"{case}_position"].shape[0])
+    s.position[:] = z[f"{case}_position"]
+    s.direction[:] = z[f"{case}_direction"]
+    s.speed[:] = z[f"{case}_speed"]
+    bins = gs.KNNBinData(wc, ws, 1)
+    g = group_of(s)
+    gs.updateKNNDatabase(g, bins)
+    np.testing.assert_array_equal(cell_density(g, bins), z[f"{case}_density"])
+    np.testing.assert_array_equal(cell_avg_velocity(g, bins).reshape(-1, 3),
+                                  z[f"{case}_avg_velocity"])
+
+
 def frame_diagnostics_oracle(s, p, walls, steps):
     """ExtractData after `steps` frames: the database the last frame built
     (positions after its wrap) and the velocities after that frame."""

@@ -271,6 +271,19 @@ def test_path_initialize_restates_the_pathway(name):
 
 # ---- ExtractData diagnostics (ProcessData.cu:132-237) ---------------------------------
 
+@pytest.mark.parametrize("case", ["crowd2d", "flock3d"])
+def test_cell_diagnostics_match_reference_golden(case):
+    """Agents per cell and mean cell velocity against the reference's own
+    ComputeCellDensityKernel / ComputeAvgCellVelocityKernel run on its own
+    database (tests/golden/cell_diag.npz), bit for bit."""
+    z, m = load("cell_diag")
+    ws, wc = m[case]["ws"], m[case]["wc"]
+    pos = z[f"{case}_position"]
+    np.testing.assert_array_equal(ol.cell_density(pos, ws, wc), z[f"{case}_density"])
+    got = ol.cell_avg_velocity(pos, z[f"{case}_direction"], z[f"{case}_speed"], ws, wc)
+    np.testing.assert_array_equal(got.reshape(-1, 3), z[f"{case}_avg_velocity"])
+
+
 def test_cell_diagnostics_restate_processdata():
     """Agents per cell and the mean cell velocity, summed in ascending agent
     index (the stable sort's order) in binary32, against a plain loop."""
