@@ -74,6 +74,33 @@ def make_batched(n_scenes=256, seed=0):
     return states, gaps, sc.chokepoint_params(), sc.chokepoint_walls
 
 
+def batched_config(p, scenes: int, n: int, world: int) -> dict:
+    """The batched workload's config, as both arms print it."""
+    return {"workload": WORKLOADS["batched"] if scenes == 256 else
+            WORKLOADS["batched"].replace("256", str(scenes), 1),
+            "scenes": scenes, "agents": n, "k": p.k, "knw": p.knw,
+            "cell": p.world_size[0] / p.world_cells[0],
+            "cells_per_scene": int(np.prod(p.world_cells)),
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (about 270 MB of bucketed state per step)"}
+
+
+def single_config(name: str, p, n: int, world: int) -> dict:
+    """A single-group workload's config, as both arms print it."""
+    cfg = {"workload": WORKLOADS[name], "agents": n, "k": p.k,
+           "cell": p.world_size[0] / p.world_cells[0], "cells": int(np.prod(p.world_cells)),
+           "parallelism": f"replicas x{world}"}
+    if name == "large":
+        cfg["l2"] = "inputs larger than L2 (about 200 MB of bucketed state per step)"
+    return cfg
+
+
+def brute_config(n: int, k: int, world: int) -> dict:
+    return {"workload": WORKLOADS["brute"], "agents": n, "k": k,
+            "parallelism": f"replicas x{world}",
+            "l2": "1 MB of positions, L2-resident by design (compute-bound)"}
+
+
 def fused_bytes_per_agent(p) -> int:
     """Algorithmic DRAM bytes of the dominant fused kernel(s) per agent: its own
     bucketed state read once (5 float4 = 80 B), the new state written once
@@ -295,7 +322,7 @@ def run_reference(args, dist, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "agents": state.n, "k": p.k},
+        "config": single_config(args.workload, p, state.n, args.gpus),
         "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{steps} whole steps of the {state.n}-agent workload "
                                    f"(CPU oracle restating the reference kernels)"},
@@ -329,7 +356,7 @@ def run_reference_brute(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / args.steps * n / m, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS["brute"], "agents": n, "k": k},
+        "config": brute_config(n, k, args.gpus),
         "cpu_baseline": {"value": v, "unit": "agent-queries/s", "cores": threads, "kind": "port",
                          "sample": f"{m} of the {n} queries per step against all {n} agents "
                                    f"(CPU oracle restating KNNBruteForceCUDAV2, {threads} threads)"},
@@ -357,10 +384,7 @@ def run_reference_batched(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS["batched"] if args.scenes == 256 else
-                   WORKLOADS["batched"].replace("256", str(args.scenes), 1),
-                   "scenes": len(states), "agents": bo.n,
-                   "k": p.k},
+        "config": batched_config(p, len(states), bo.n, args.gpus),
         "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": bo.threads,
                          "kind": "port",
                          "sample": f"{steps} whole steps of all {len(states)} scenes "
@@ -459,7 +483,10 @@ def adjoint_timing(reps: int = 5):
             "timing": f"host clock around synchronised calls, median of {reps}"}
 
 
-def run_gpu_batched(args, dist, rank, world, local_rank):
+def gpu_batched_line(args, dist, rank, world, local_rank):
+    """The headline: 256 choke-point scenes batched, against per-scene
+    launches, end to end through host memory, with the large-flock and
+    brute-force records beside it.  Returns the JSON line (rank 0)."""
     import torch
 
     import gpusteer_gb300 as gs
@@ -633,9 +660,20 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         lib.gs_host_free(ptr)
     del b2
 
+    floor_ms = copy_floor_ms([s.n for s in states], cuts)
     adjoint = adjoint_timing() if not args.no_adjoint else None
+    # the other throughput configurations, as records of this line
+    large = brute = None
+    if not args.no_sub:
+        sub = argparse.Namespace(**vars(args))
+        sub.workload, sub.steps, sub.warmup = "large", args.large_steps, args.large_warmup
+        sub.cpu_seconds = min(args.cpu_seconds, 5.0)
+        large = gpu_single_line(sub, dist, rank, world, local_rank)
+        sub = argparse.Namespace(**vars(args))
+        sub.workload, sub.steps, sub.warmup = "brute", 5, 3
+        brute = gpu_brute_line(sub, dist, rank, world, local_rank)
     if rank != 0:
-        return
+        return None
     peak, peak_src = read_peaks()
     fused_ms = phases["fused"] + (phases["fused_rest"] or 0.0)
     fbytes = fused_bytes_per_agent(p) * n
@@ -660,14 +698,9 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOADS["batched"] if args.scenes == 256 else
-                   WORKLOADS["batched"].replace("256", str(args.scenes), 1),
-                   "scenes": len(states),
-                   "agents_per_gpu": n, "k": p.k, "knw": p.knw,
-                   "cell": p.world_size[0] / p.world_cells[0], "cells_per_scene": cells,
-                   "block": tr.block, "knn_capacity": tr.capacity or "auto",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (about 270 MB of bucketed state per step)"},
+        "config": batched_config(p, len(states), n, world),
+        "tuned": {"block": tr.block, "knn_capacity": tr.capacity or "auto",
+                  "cell": p.world_size[0] / p.world_cells[0]},
         "per_scene": per_scene,
         "identical_to_per_scene": None if identical is None else {
             "equal": bool(identical), "steps": total,
@@ -681,6 +714,11 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
                 "api": f"gs_batches_step_host over {len(cuts) - 1} parts (scene ranges) in "
                        "place, one graph: each part's copies in, steps and copies out, "
                        "overlapped across the parts",
+                "copy_floor_ms": floor_ms,
+                "e2e_over_copy_floor": e2e_med * 1e3 / floor_ms,
+                "copy_floor": "the same bytes in and out of the same page-locked arrays "
+                              "alone: one cudaMemcpyAsync per block and part, each part on "
+                              "its own stream (copies out after its copies in), no steps",
                 "identical_to_one_batch": parts_identical,
                 "one_batch": {"value": e2e_one, "ms_per_step": one_s * 1e3 / e2e_steps,
                               "api": "gs_batch_upload, gs_batch_step, gs_batch_download"}},
@@ -694,8 +732,59 @@ def run_gpu_batched(args, dist, rank, world, local_rank):
                           (ms_max / args.steps / 1e3) / 1e9,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
+        "large_flock": large,
+        "brute": brute,
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def copy_floor_ms(agents, cuts, reps: int = 5) -> float:
+    """Milliseconds to move the end-to-end step's bytes alone, with no steps:
+    per part (scene range cuts[i]..cuts[i+1]) the three state blocks in
+    (float4 x3, float3 x2, 4-byte x6: 96 B/agent) and out (80 B/agent: the
+    four per-agent constants stay), one cudaMemcpyAsync per block, each part
+    on its own stream.  Median of `reps`."""
+    import torch
+
+    blocks_in, blocks_out = (48, 24, 24), (48, 24, 8)
+    parts = []
+    for lo, hi in zip(cuts[:-1], cuts[1:]):
+        na = int(sum(agents[lo:hi]))
+        host = [torch.empty(na * b, dtype=torch.uint8, pin_memory=True) for b in blocks_in]
+        dev = [torch.empty(na * b, dtype=torch.uint8, device="cuda") for b in blocks_in]
+        parts.append((host, dev, torch.cuda.Stream(), na))
+    times = []
+    for _ in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for host, dev, st, na in parts:
+            with torch.cuda.stream(st):
+                for h, d in zip(host, dev):
+                    d.copy_(h, non_blocking=True)
+                for h, d, b in zip(host, dev, blocks_out):
+                    h[:na * b].copy_(d[:na * b], non_blocking=True)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    return statistics.median(times[1:]) * 1e3
+
+
+def issue_rate(workload: str, kernel_ms: float, clocks: dict, device: int):
+    """Warp instructions the dominant kernel(s) issue per launch (from the
+    committed ncu capture, profiles/issue_<workload>.json) over what the SMs
+    can issue in the measured time: SMs x 4 schedulers x median SM clock x
+    time.  An instruction-bound kernel is judged against this ceiling."""
+    path = REPO / "profiles" / f"issue_{workload}.json"
+    if not path.exists() or not kernel_ms or not clocks.get("sm_mhz"):
+        return None
+    import torch
+
+    rec = json.loads(path.read_text())
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    slots = sms * 4 * clocks["sm_mhz"] * 1e6 * kernel_ms / 1e3
+    return {"warp_instructions_per_launch": rec["warp_instructions_per_launch"],
+            "kernels": rec.get("kernels"), "sm_count": sms, "sm_mhz": clocks["sm_mhz"],
+            "kernel_ms": kernel_ms, "frac": rec["warp_instructions_per_launch"] / slots,
+            "source": f"profiles/issue_{workload}.json"}
 
 
 def fp32_peak_tflops():
@@ -724,8 +813,9 @@ def fp32_peak_tflops():
         torch.backends.cuda.matmul.allow_tf32 = prev
 
 
-def run_gpu_brute(args, dist, rank, world, local_rank):
-    """gs_knn_bruteforce (KNNBruteForceCUDAV2) over 65,536 agents, k = 16."""
+def gpu_brute_line(args, dist, rank, world, local_rank):
+    """gs_knn_bruteforce (KNNBruteForceCUDAV2) over 65,536 agents, k = 16.
+    Returns the JSON line (rank 0; None elsewhere)."""
     import torch
 
     import gpusteer_gb300 as gs
@@ -771,7 +861,7 @@ def run_gpu_brute(args, dist, rank, world, local_rank):
         knn.download(g)
     e2e_s = allreduce_max(dist, time.perf_counter() - t0)
     if rank != 0:
-        return
+        return None
     cpu = None
     if world == 1 and not args.no_cpu:
         sys.path.insert(0, str(REPO / "tests"))
@@ -790,9 +880,7 @@ def run_gpu_brute(args, dist, rank, world, local_rank):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": per,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOADS["brute"], "agents": n, "k": k,
-                   "parallelism": f"replicas x{world}",
-                   "l2": "1 MB of positions, L2-resident by design (compute-bound)"},
+        "config": brute_config(n, k, world),
         "e2e": {"value": n * e2e_steps * world / e2e_s, "unit": "agent-queries/s",
                 "h2d_bytes_per_step": n * 96, "d2h_bytes_per_step": n * k * 8},
         "gpu_launches": args.steps,
@@ -800,17 +888,27 @@ def run_gpu_brute(args, dist, rank, world, local_rank):
                      "frac": tflops / peak, "traffic": None, "kernel": "k_knn_brute3",
                      "algorithmic_flops_per_launch": 8.0 * pairs,
                      "peak_source": "measured here: cuBLAS SGEMM 8192^3 with TF32 off"},
+        "issue": issue_rate("brute", per, clocks.summary(), local_rank),
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_gpu(args, dist, rank, world, local_rank):
     if args.workload == "batched":
-        return run_gpu_batched(args, dist, rank, world, local_rank)
-    if args.workload == "brute":
-        return run_gpu_brute(args, dist, rank, world, local_rank)
+        line = gpu_batched_line(args, dist, rank, world, local_rank)
+    elif args.workload == "brute":
+        line = gpu_brute_line(args, dist, rank, world, local_rank)
+    else:
+        line = gpu_single_line(args, dist, rank, world, local_rank)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def gpu_single_line(args, dist, rank, world, local_rank):
+    """One group of the `large`, `chokepoint` or `boids` workload stepped K
+    times.  Returns the JSON line (rank 0; None elsewhere)."""
     import torch
 
     import gpusteer_gb300 as gs
@@ -876,7 +974,7 @@ def run_gpu(args, dist, rank, world, local_rank):
         lib.gs_host_free(ptr)
 
     if rank != 0:
-        return
+        return None
     cpu = None
     if world == 1 and not args.no_cpu:
         v, steps, threads, n_cpu = cpu_sample(state, p, walls_rows, args.cpu_seconds)
@@ -884,6 +982,7 @@ def run_gpu(args, dist, rank, world, local_rank):
                "sample": f"{steps} whole steps of the full {n_cpu}-agent workload, "
                          f"CPU oracle, {threads} threads"}
     cells = int(np.prod(p.world_cells))
+    step_model_gbs = step_model_bytes(n, p.k, cells) / (ms_max / args.steps / 1e3) / 1e9
     line = {
         "metric": "agent-steps/s",
         "value": value,
@@ -897,9 +996,7 @@ def run_gpu(args, dist, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "agents_per_gpu": n, "k": p.k,
-                   "cells": cells, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (about 200 MB of bucketed state per step)"},
+        "config": single_config(args.workload, p, n, world),
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state},
         "gpu_launches": gs.step_launches(group, has_walls) * args.steps,
@@ -908,11 +1005,13 @@ def run_gpu(args, dist, rank, world, local_rank):
                      "kernel": "k_fused" + ("_walls+k_fused_rest" if has_walls else ""),
                      "algorithmic_bytes_per_launch": fbytes, "peak_source": peak_src},
         "phases_ms": phases,
-        "step_model_gbs": step_model_bytes(n, p.k, cells) / (ms_max / args.steps / 1e3) / 1e9,
+        "step_model_gbs": step_model_gbs,
+        "step_model_frac": step_model_gbs / peak,
+        "issue": issue_rate(args.workload, fused_ms, clocks.summary(), local_rank),
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -935,6 +1034,12 @@ def main():
                     help="batched workload: scene ranges overlapped in the end-to-end run")
     ap.add_argument("--no-per-scene", action="store_true",
                     help="batched workload: skip the per-scene baselines")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="batched workload: skip the large-flock and brute-force records")
+    ap.add_argument("--large-steps", type=int, default=200,
+                    help="large-flock record: timed steps")
+    ap.add_argument("--large-warmup", type=int, default=100,
+                    help="large-flock record: untimed steps before (the flock clusters)")
     args = ap.parse_args()
     if args.steps is None:
         from gpusteer_gb300 import scenario as sc
