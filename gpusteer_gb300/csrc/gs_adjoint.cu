@@ -22,11 +22,16 @@
 //   g_u   = J_trunc(u, maxSpeed)^T g_v'            (u = v + a dt)
 //   g_S   = J_trunc(S, maxForce)^T (dt g_u / mass)
 //   dL/dw_b += g_S . F_b ;  g_q_b = (I - F_b F_b^T) w_b g_S / |q_b|
-// and scatters the neighbour terms with vector atomics:
+// and writes the neighbour terms of each KNN edge (agent i, rank r) to its
+// own slot:
 //   separation  g_o = (2 o (o . g) - |o|^2 g) / |o|^4,  g = g_q / n_members
 //   cohesion    g_q / n_members to each member's position
 //   alignment   g_q / n_members to each member's heading, turned into a
 //               velocity adjoint with (I - d d^T) / |v|
+// A second kernel gives each agent the sum of its own terms and of the terms
+// of every edge that points at it, found through a reverse-KNN index (edges
+// bucketed by their target) and added in ascending edge order.  No float
+// atomics: two backward passes give the same gradients bit for bit.
 // The derivative of the world wrap is the identity.
 #include <cfloat>
 #include <climits>
@@ -52,9 +57,7 @@ __device__ __forceinline__ V3 normalize_vjp(V3 F, float qlen, V3 g) {
     return dvd(sub(g, mul(F, dot(F, g))), qlen);
 }
 
-__device__ __forceinline__ void red_add(float4* a, V3 v) {
-    if (v.x != 0.f || v.y != 0.f || v.z != 0.f) atomicAdd(a, make_float4(v.x, v.y, v.z, 0.f));
-}
+__device__ __forceinline__ float4 f4z(V3 v) { return make_float4(v.x, v.y, v.z, 0.f); }
 
 struct Beh {
     bool on;
@@ -69,8 +72,8 @@ __global__ void __launch_bounds__(kAdjBlock) k_flock_adjoint(AdjointLaunch A, St
         const float4 P = A.pos[i], D = A.dir[i];
         const V3 pos = v3(P), dir = v3(D);
         const float speed = P.w;
-        const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali),
-                          fc = flock_params(p.coh);
+        const FlockParams fs = flock_params(p.sep, p.sep_dsq), fa = flock_params(p.ali, p.ali_dsq),
+                          fc = flock_params(p.coh, p.coh_dsq);
         const unsigned* nb = A.knn + size_t(i) * A.k;
 
         // forward: memberships (same operands and tests as the fused kernel)
@@ -164,12 +167,11 @@ __global__ void __launch_bounds__(kAdjBlock) k_flock_adjoint(AdjointLaunch A, St
         const V3 g_ali = ha.on ? mul(ha.gq, ha.inv_n) : v3(0.f, 0.f, 0.f);
         const unsigned m_sep = hs.on ? ms : 0u, m_ali = ha.on ? ma : 0u,
                        m_coh = hc.on ? mc : 0u;
-        const unsigned any = m_sep | m_ali | m_coh;
+        // every listed edge gets its slot written (zero where it adds nothing)
         for (unsigned r = 0; r < A.k; ++r) {
-            if (!(any >> r)) break;
-            if (!((any >> r) & 1u)) continue;
             const unsigned j = nb[r];
-            V3 gpj = v3(0.f, 0.f, 0.f);
+            if (j >= A.n) break;
+            V3 gpj = v3(0.f, 0.f, 0.f), gvj = v3(0.f, 0.f, 0.f);
             if ((m_sep >> r) & 1u) {
                 const V3 o = sub(v3(A.pos[j]), pos);
                 const float oo = dot(o, o);
@@ -178,16 +180,18 @@ __global__ void __launch_bounds__(kAdjBlock) k_flock_adjoint(AdjointLaunch A, St
                 own_p = sub(own_p, go);
             }
             if ((m_coh >> r) & 1u) gpj = add(gpj, g_coh);
-            red_add(A.lp_out + j, gpj);
             if ((m_ali >> r) & 1u) {
                 const float4 Pj = A.pos[j];
                 const V3 dj = v3(A.dir[j]);
-                if (Pj.w > 0.f) red_add(A.lv_out + j, dvd(sub(g_ali, mul(dj, dot(dj, g_ali))), Pj.w));
+                if (Pj.w > 0.f) gvj = dvd(sub(g_ali, mul(dj, dot(dj, g_ali))), Pj.w);
             }
+            const size_t e = size_t(i) * A.k + r;
+            A.edge_p[e] = f4z(gpj);
+            A.edge_v[e] = f4z(gvj);
         }
         if (speed > 0.f) own_v = add(own_v, dvd(sub(own_d, mul(dir, dot(dir, own_d))), speed));
-        red_add(A.lp_out + i, own_p);
-        red_add(A.lv_out + i, own_v);
+        A.own_p[i] = f4z(own_p);
+        A.own_v[i] = f4z(own_v);
     }
     // per-block sums of the weight adjoints (fixed order: deterministic)
     __shared__ float red[3][kAdjBlock / 32];
@@ -206,14 +210,118 @@ __global__ void __launch_bounds__(kAdjBlock) k_flock_adjoint(AdjointLaunch A, St
     }
 }
 
+// ---- reverse-KNN index of the recorded lists -------------------------------------
+// In-degree of every agent (edges e = i * k + r whose target knn[e] is an agent).
+__global__ void k_rev_count(const unsigned* __restrict__ knn, unsigned n, unsigned k,
+                            unsigned* __restrict__ indeg) {
+    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= size_t(n) * k) return;
+    const unsigned j = knn[e];
+    if (j < n) atomicAdd(indeg + j, 1u);
+}
+
+// Edges bucketed by target: redge[rstart[j] ..) holds the edges into j, in
+// the order the atomics hand out (the gather sorts each bucket).  fill is
+// zero on entry and holds the in-degrees on exit.
+__global__ void k_rev_fill(const unsigned* __restrict__ knn, unsigned n, unsigned k,
+                           const unsigned* __restrict__ rstart, unsigned* __restrict__ fill,
+                           unsigned* __restrict__ redge) {
+    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= size_t(n) * k) return;
+    const unsigned j = knn[e];
+    if (j < n) redge[rstart[j] + atomicAdd(fill + j, 1u)] = unsigned(e);
+}
+
+// Agent j's input adjoints: its own terms, then the terms of the edges into
+// it in ascending edge order, added to lp_out / lv_out.  Buckets of up to
+// kGatherSort edges are sorted in a local array; longer ones (not met in
+// practice: in-degrees stay near k) are walked by repeated minimum search.
+constexpr unsigned kGatherSort = 64;
+
+__global__ void __launch_bounds__(kAdjBlock) k_adjoint_gather(AdjointLaunch A) {
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.n) return;
+    const unsigned lo = A.rstart[j], hi = A.rstart[j + 1], deg = hi - lo;
+    V3 gp = v3(A.own_p[j]), gv = v3(A.own_v[j]);
+    auto add_edge = [&](unsigned e) {
+        gp = add(gp, v3(A.edge_p[e]));
+        gv = add(gv, v3(A.edge_v[e]));
+    };
+    if (deg <= kGatherSort) {
+        unsigned es[kGatherSort];
+        for (unsigned t = 0; t < deg; ++t) {  // insertion sort, ascending
+            const unsigned e = A.redge[lo + t];
+            unsigned q = t;
+            while (q > 0 && es[q - 1] > e) {
+                es[q] = es[q - 1];
+                --q;
+            }
+            es[q] = e;
+        }
+        for (unsigned t = 0; t < deg; ++t) add_edge(es[t]);
+    } else {
+        unsigned last = 0;
+        for (unsigned t = 0; t < deg; ++t) {
+            unsigned best = UINT_MAX;
+            for (unsigned q = lo; q < hi; ++q) {
+                const unsigned e = A.redge[q];
+                if ((t == 0 || e > last) && e < best) best = e;
+            }
+            add_edge(best);
+            last = best;
+        }
+    }
+    const float4 op = A.lp_out[j], ov = A.lv_out[j];
+    A.lp_out[j] = make_float4(op.x + gp.x, op.y + gp.y, op.z + gp.z, 0.f);
+    A.lv_out[j] = make_float4(ov.x + gv.x, ov.y + gv.y, ov.z + gv.z, 0.f);
+}
+
 }  // namespace
 
 unsigned adjoint_blocks(unsigned n) { return n ? (n + kAdjBlock - 1) / kAdjBlock : 1u; }
 
+size_t adjoint_scratch_bytes(unsigned n, unsigned k) {
+    const size_t nk = size_t(n) * k;
+    return nk * 32 + size_t(n) * 32 + (size_t(n) + 1) * 8 + nk * 4 +
+           (size_t(scan_tile_count(n + 1)) + 1) * 4 + 8 * 256;
+}
+
+// Carves the scratch of one adjoint step out of `base` (adjoint_scratch_bytes).
+void adjoint_scratch_bind(AdjointLaunch& A, void* base, unsigned n, unsigned k) {
+    auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+    char* b = static_cast<char*>(base);
+    const size_t nk = size_t(n) * k;
+    size_t o = 0;
+    A.edge_p = reinterpret_cast<float4*>(b + o);
+    o = align(o + nk * 16);
+    A.edge_v = reinterpret_cast<float4*>(b + o);
+    o = align(o + nk * 16);
+    A.own_p = reinterpret_cast<float4*>(b + o);
+    o = align(o + size_t(n) * 16);
+    A.own_v = reinterpret_cast<float4*>(b + o);
+    o = align(o + size_t(n) * 16);
+    A.indeg = reinterpret_cast<unsigned*>(b + o);
+    o = align(o + (size_t(n) + 1) * 4);
+    A.rstart = reinterpret_cast<unsigned*>(b + o);
+    o = align(o + (size_t(n) + 1) * 4);
+    A.redge = reinterpret_cast<unsigned*>(b + o);
+    o = align(o + nk * 4);
+    A.tile = reinterpret_cast<unsigned*>(b + o);
+}
+
 gs_status launch_flock_adjoint(const AdjointLaunch& A, const StepDev& p, cudaStream_t st) {
     if (A.k == 0 || A.k > 32) return fail(GS_ERR_INVALID_ARG, "adjoint needs 1 <= k <= 32");
     if (A.n == 0) return GS_OK;
+    const size_t nk = size_t(A.n) * A.k;
+    const unsigned eb = unsigned((nk + kAdjBlock - 1) / kAdjBlock);
+    // reverse-KNN index of this step's lists
+    GS_CUDA(cudaMemsetAsync(A.indeg, 0, (size_t(A.n) + 1) * 4, st));
+    k_rev_count<<<eb, kAdjBlock, 0, st>>>(A.knn, A.n, A.k, A.indeg);
+    GS_TRY(scan_counts(A.indeg, A.rstart, A.n, A.tile, st));  // zeroes indeg
+    k_rev_fill<<<eb, kAdjBlock, 0, st>>>(A.knn, A.n, A.k, A.rstart, A.indeg, A.redge);
+    // each agent's terms and its edges' terms, then the gather
     k_flock_adjoint<<<adjoint_blocks(A.n), kAdjBlock, 0, st>>>(A, p);
+    k_adjoint_gather<<<adjoint_blocks(A.n), kAdjBlock, 0, st>>>(A);
     GS_LAUNCHED("flock_adjoint");
     return GS_OK;
 }

@@ -28,11 +28,57 @@ struct FlockAcc {
 struct FlockParams {
     float min_d, max_d, cos_max, w;
     unsigned mask;
+    // squared-distance thresholds: d < min_d <=> dsq < lt, d > max_d <=> dsq > gt
+    float lt, gt;
 };
 
-// Packed (min, max, cos, weight, mask bits) as the fused step's parameters hold them.
-__device__ __forceinline__ FlockParams flock_params(const float v[5]) {
-    return FlockParams{v[0], v[1], v[2], v[3], __float_as_uint(v[4])};
+// Packed (min, max, cos, weight, mask bits) as the fused step's parameters
+// hold them, with the squared-distance thresholds (lt, gt).
+__device__ __forceinline__ FlockParams flock_params(const float v[5], const float dsq[2]) {
+    return FlockParams{v[0], v[1], v[2], v[3], __float_as_uint(v[4]), dsq[0], dsq[1]};
+}
+
+// ---- the angle test of inBoidNeighborhood without its divisions ----------------
+// FlockingCommon.cuh:24-27 tests f > c with f = dot(dir, offset / d), the unit
+// offset rounded componentwise (three IEEE divisions).  With g = dot(dir,
+// offset) (same operation order) and real arithmetic, d (F - c) = (a.o) - c d
+// for F the exact value of f; the rounding errors of f, of g and of c d are
+// bounded by standard floating-point error analysis:
+//   |f - F| <= gamma_4 S / d,  |g - a.o| <= gamma_3 S,  |fl(c d) - c d| <= u |c| d,
+// u = 2^-24, gamma_n = n u / (1 - n u), S = sum |dir_i offset_i| <= A d (1 + 3u)
+// with A = |dir_x| + |dir_y| + |dir_z|.  So when
+//   |g - c d| > (gamma_3 + gamma_4) A d (1 + 3u) + u |c| d + (error of d's estimate) |c|
+// the sign of g - c d is the sign of f - c, and f != c.  The margin used is
+// 2^-14 (A + |c|) d: over 100 times the A term (about 2^-21 A d) and, with d
+// estimated by sqrt.approx to better than 2^-20 relative, over 50 times the
+// c term; it holds for any estimate better than 2^-15.  The estimate is only
+// trusted for squared distances in [2^-60, 2^60] and A + |c| in [2^-60, 2^30]
+// (no underflow or overflow in any term).  Everywhere else, and inside the
+// margin, the reference's expression decides.  The result is the reference's
+// bit for bit; only the cost differs.
+struct AngleGate {
+    float k;  // 2^-14 (A + |c|), or +inf where the estimate is not trusted
+};
+
+__device__ __forceinline__ AngleGate angle_gate(V3 dir, float c) {
+    const float s = (fabsf(dir.x) + fabsf(dir.y) + fabsf(dir.z)) + fabsf(c);
+    return AngleGate{(s >= 0x1p-60f && s <= 0x1p30f) ? 0x1p-14f * s : __int_as_float(0x7f800000)};
+}
+
+// sqrt.approx of a squared distance in [2^-60, 2^60], NaN elsewhere (so that
+// no margin test passes and the exact expression decides).
+__device__ __forceinline__ float d_estimate(float dsq) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(dsq));
+    return (dsq >= 0x1p-60f && dsq <= 0x1p60f) ? r : __int_as_float(0x7fffffff);
+}
+
+// 1: f > c; 0: f <= c; -1: undecided (the caller evaluates the reference's
+// expression).  g = dot(dir, offset), de = d_estimate(dsq).
+__device__ __forceinline__ int angle_decide(float g, float de, float c, AngleGate gate) {
+    const float diff = g - c * de;
+    if (!(fabsf(diff) > gate.k * de)) return -1;
+    return diff > 0.f ? 1 : 0;
 }
 
 GS_HD void flock_init(FlockAcc& a) {

@@ -1,6 +1,8 @@
 // C ABI of libgpusteer (include/gpusteer.h): handle management, host <-> device
 // transfers, the GroupSteerLibrary.cuh free functions and the fused step.
 #include <cmath>
+#include <cstdint>
+#include <limits>
 #include <cstring>
 #include <fstream>
 #include <list>
@@ -51,6 +53,8 @@ static void release_fused(gs_group g) {
     dfree(g->retry_count);
     dfree(g->retry_knn);
     dfree(g->d_stat);
+    dfree(g->scan_state);
+    g->scan_state_cells = 0;
     db_release(g->fdb);
     g->fused_k_alloc = 0;
 }
@@ -265,6 +269,44 @@ static unsigned knn_capacity(unsigned n, unsigned occupied, const Grid& g, unsig
     return top <= 128.0 ? 128u : 256u;
 }
 
+// Exact squared-distance forms of the flocking tests' d < m and d > m, for
+// d = sqrtf(dsq) as the kernels round it (the host's float sqrt is the same
+// IEEE operation): d < m <=> dsq < lt and d > m <=> dsq > gt.  The square
+// root is monotone on the non-negative floats, so bisection over their bit
+// patterns (0 .. +inf, in value order) finds the smallest dsq whose root
+// reaches m and the largest whose root stays at or below m.  Squared
+// distances are never negative; NaN compares false on both sides, as its
+// root does.
+static float sqrt_reaches(float m) {  // lt: smallest x >= 0 with sqrt(x) >= m
+    if (!(m > 0.f)) return 0.f;        // m <= 0 or NaN: d < m never holds
+    uint32_t lo = 0, hi = 0x7f800000u;  // sqrt(+inf) = +inf >= m
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        float x;
+        std::memcpy(&x, &mid, 4);
+        if (std::sqrt(x) >= m) hi = mid;
+        else lo = mid + 1;
+    }
+    float r;
+    std::memcpy(&r, &lo, 4);
+    return r;
+}
+static float sqrt_stays(float m) {  // gt: largest x >= 0 with sqrt(x) <= m
+    if (std::isnan(m)) return std::numeric_limits<float>::infinity();  // d > NaN never holds
+    if (m < 0.f) return -1.f;  // every d >= 0 is above m
+    uint32_t lo = 0, hi = 0x7f800000u;  // sqrt(0) = 0 <= m
+    while (lo < hi) {
+        const uint32_t mid = hi - (hi - lo) / 2;
+        float x;
+        std::memcpy(&x, &mid, 4);
+        if (std::sqrt(x) <= m) lo = mid;
+        else hi = mid - 1;
+    }
+    float r;
+    std::memcpy(&r, &lo, 4);
+    return r;
+}
+
 static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev& d) {
     if (!p) return fail(GS_ERR_INVALID_ARG, "null step parameters");
     if (p->knn_mode != GS_KNN_BINNED)
@@ -290,6 +332,12 @@ static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev&
     fl(d.sep, p->sep_min, p->sep_max, p->sep_cos, p->w_sep, p->mask_sep);
     fl(d.ali, p->ali_min, p->ali_max, p->ali_cos, p->w_ali, p->mask_ali);
     fl(d.coh, p->coh_min, p->coh_max, p->coh_cos, p->w_coh, p->mask_coh);
+    d.sep_dsq[0] = sqrt_reaches(p->sep_min);
+    d.sep_dsq[1] = sqrt_stays(p->sep_max);
+    d.ali_dsq[0] = sqrt_reaches(p->ali_min);
+    d.ali_dsq[1] = sqrt_stays(p->ali_max);
+    d.coh_dsq[0] = sqrt_reaches(p->coh_min);
+    d.coh_dsq[1] = sqrt_stays(p->coh_max);
     std::memcpy(d.seek_target, p->seek_target, sizeof(d.seek_target));
     d.w_seek = p->w_seek;
     d.mask_seek = p->mask_seek;
@@ -755,6 +803,8 @@ static gs_status check_device_flags(gs_group g) {
     GS_CUDA(cudaStreamSynchronize(g->stream));
     if (flags) {
         GS_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned), g->stream));
+        if (flags & kErrScanTimeout)
+            return fail(GS_ERR_TIMEOUT, "fused step: a wait in the cell scan ran out (state void)");
         return fail(GS_ERR_STATE, "fused step: inconsistent cell counts (state not updated)");
     }
     return GS_OK;
@@ -1520,6 +1570,13 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         g->scene_alloc = n_scenes;
     }
     if (g->fdb.cells != C) GS_TRY(db_reserve(g->fdb, 0, C));
+    if (g->scan_state_cells != C) {
+        dfree(g->scan_state);
+        GS_TRY(dalloc(&g->scan_state, scan_state_bytes(C)));
+        GS_CUDA(cudaMemset(g->scan_state, 0, scan_state_bytes(C)));
+        GS_CUDA(cudaDeviceSynchronize());
+        g->scan_state_cells = C;
+    }
     if (walls && (!g->w0 || g->fused_k_alloc < k)) {
         const size_t n = g->capacity;
         dfree(g->w0);
@@ -1560,7 +1617,7 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
                            PhaseHook* hook) {
     cudaStream_t st = g->stream;
     if (hook) hook->mark(0, true);
-    GS_TRY(scan_counts(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
+    GS_TRY(scan_counts_onepass(g->fdb.count, g->fdb.start, C, g->scan_state, g->d_err, st));
     if (hook) hook->mark(0, false);
     if (hook) hook->mark(1, true);
     GS_TRY(fused_permute(L, d.wrap_mode, d.dirty != 0, st));
@@ -2232,6 +2289,7 @@ struct gs_rollout_s {
     // adjoint state, ping-pong: d loss / d (position, velocity)
     float4 *lp[2] = {nullptr, nullptr}, *lv[2] = {nullptr, nullptr};
     float* wpart = nullptr;  // [adjoint_blocks(cap) * 4]
+    unsigned char* adj_scratch = nullptr;  // adjoint_scratch_bytes(cap, k)
 };
 
 static void rollout_release(gs_rollout r) {
@@ -2248,6 +2306,7 @@ static void rollout_release(gs_rollout r) {
         dfree(r->lv[i]);
     }
     dfree(r->wpart);
+    dfree(r->adj_scratch);
 }
 
 gs_status gs_rollout_create(gs_group g, gs_bins bins, unsigned steps, unsigned checkpoint_every,
@@ -2280,6 +2339,7 @@ gs_status gs_rollout_create(gs_group g, gs_bins bins, unsigned steps, unsigned c
         if (s == GS_OK) s = dalloc(&r->lv[i], cap);
     }
     if (s == GS_OK) s = dalloc(&r->wpart, size_t(adjoint_blocks(r->cap)) * 4);
+    if (s == GS_OK) s = dalloc(&r->adj_scratch, adjoint_scratch_bytes(r->cap, r->k));
     if (s != GS_OK) {
         rollout_release(r);
         delete r;
@@ -2453,6 +2513,7 @@ gs_status gs_rollout_backward(gs_rollout r, const float* adj_position, const flo
             A.wpart = r->wpart;
             A.n = r->n;
             A.k = r->k;
+            adjoint_scratch_bind(A, r->adj_scratch, r->n, r->k);
             GS_TRY(launch_flock_adjoint(A, d, st));
             cur = 1 - cur;
         }
@@ -2510,5 +2571,15 @@ gs_status gs_flock_adjoint_step(const float* position_speed, const float* headin
     A.wpart = weight_partials;
     A.n = n;
     A.k = k;
-    return launch_flock_adjoint(A, d, static_cast<cudaStream_t>(stream));
+    // the step's scratch is stream-ordered: allocated and freed on `stream`,
+    // so calls on different streams never share it
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    void* scratch = nullptr;
+    GS_CUDA(cudaMallocAsync(&scratch, adjoint_scratch_bytes(n, k), st));
+    adjoint_scratch_bind(A, scratch, n, k);
+    const gs_status s = launch_flock_adjoint(A, d, st);
+    const cudaError_t e = cudaFreeAsync(scratch, st);
+    if (s != GS_OK) return s;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFreeAsync(adjoint scratch)");
+    return GS_OK;
 }

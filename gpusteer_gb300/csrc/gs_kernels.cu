@@ -162,6 +162,133 @@ gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* ti
     return GS_OK;
 }
 
+// ---- single-pass exclusive scan (the fused engine's counting sort) ---------------
+// Decoupled look-back: each block takes the next tile by ticket, so it only
+// ever waits on tiles that blocks already running hold; it publishes its tile
+// sum, then walks back over its predecessors' published words, 32 at a time,
+// until it meets one that carries an inclusive prefix, and publishes its own.
+// A word is (epoch:30 | flag:2 | value:32).  The epoch lives on the device
+// and the last block of each scan advances it (and resets the ticket), so
+// words left by earlier scans read as not ready without being cleared, also
+// across CUDA graph replays.  Every wait is bounded: a block that waits too
+// long sets kErrScanTimeout in err and goes on (the step is then void and the
+// host reports GS_ERR_TIMEOUT).  One launch reads each count once and writes
+// start and the zeroed count, against three launches and two reads.
+constexpr unsigned long long kScanAgg = 1ull << 32, kScanInc = 2ull << 32;
+constexpr unsigned kScanSpinLimit = 1u << 20;
+
+__device__ __forceinline__ unsigned long long ld_volatile64(const unsigned long long* p) {
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_onepass(unsigned* __restrict__ count, unsigned C,
+                                                         unsigned* __restrict__ start,
+                                                         unsigned long long* state, ScanCtl* ctl,
+                                                         unsigned T, unsigned* __restrict__ err) {
+    __shared__ unsigned sh[kScanTile + kScanTile / 32];
+    __shared__ unsigned ws[kBlock / 32];
+    __shared__ unsigned s_tile, s_epoch, s_prefix;
+    if (threadIdx.x == 0) {
+        s_tile = atomicAdd(&ctl->ticket, 1u);
+        s_epoch = *reinterpret_cast<volatile unsigned*>(&ctl->epoch);
+    }
+    __syncthreads();
+    const unsigned t = s_tile;
+    const unsigned long long ep = static_cast<unsigned long long>(s_epoch & 0x3fffffffu) << 34;
+    unsigned items[kScanItems];
+    load_tile(count, C, t, sh, items);
+    unsigned sum = 0;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) sum += items[j];
+    unsigned total;
+    unsigned run = block_exclusive_sum(sum, ws, total);
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+        if (lane == 0)
+            *reinterpret_cast<volatile unsigned long long*>(state + t) =
+                ep | (t == 0 ? kScanInc : kScanAgg) | total;
+        unsigned prefix = 0;
+        if (t > 0) {
+            int hi = int(t) - 1;  // the window is tiles hi, hi - 1, ..., hi - 31
+            for (;;) {
+                const int idx = hi - int(lane);
+                unsigned long long w = ep | kScanInc;  // before tile 0: an inclusive 0
+                if (idx >= 0) {
+                    unsigned spins = 0;
+                    for (;;) {
+                        w = ld_volatile64(state + idx);
+                        if ((w >> 34) == (ep >> 34) && (w & (3ull << 32)) != 0) break;
+                        if (++spins > kScanSpinLimit) {
+                            atomicOr(err, kErrScanTimeout);
+                            w = ep | kScanInc;
+                            break;
+                        }
+                        __nanosleep(64);
+                    }
+                }
+                const unsigned inc = __ballot_sync(0xffffffffu, (w & kScanInc) != 0);
+                const int first = inc ? __ffs(inc) - 1 : 32;  // the nearest inclusive word
+                unsigned part = int(lane) <= first ? unsigned(w) : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                prefix += part;
+                if (inc) break;
+                hi -= 32;
+            }
+        }
+        if (lane == 0) {
+            if (t > 0)
+                *reinterpret_cast<volatile unsigned long long*>(state + t) =
+                    ep | kScanInc | (prefix + total);
+            s_prefix = prefix;
+        }
+    }
+    __syncthreads();
+    run += s_prefix;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) {
+        const unsigned i = threadIdx.x * kScanItems + j;
+        sh[i + i / 32] = run;
+        run += items[j];
+    }
+    __syncthreads();
+    const unsigned base = t * kScanTile;
+#pragma unroll
+    for (unsigned j = 0; j < kScanItems; ++j) {
+        const unsigned i = j * kBlock + threadIdx.x;
+        if (base + i < C) {
+            start[base + i] = sh[i + i / 32];
+            count[base + i] = 0u;
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (t == T - 1) start[C] = s_prefix + total;
+        // the last block to finish readies the control block for the next scan
+        __threadfence();
+        if (atomicAdd(&ctl->done, 1u) == T - 1) {
+            ctl->ticket = 0;
+            ctl->done = 0;
+            atomicAdd(&ctl->epoch, 1u);
+        }
+    }
+}
+
+unsigned long long* scan_state_words(void* scan_state) {
+    return reinterpret_cast<unsigned long long*>(static_cast<char*>(scan_state) + sizeof(ScanCtl));
+}
+
+size_t scan_state_bytes(unsigned C) { return sizeof(ScanCtl) + size_t(scan_tile_count(C)) * 8; }
+
+gs_status scan_counts_onepass(unsigned* count, unsigned* start, unsigned C, void* scan_state,
+                              unsigned* err, cudaStream_t st) {
+    const unsigned T = scan_tile_count(C);
+    if (T == 0) return GS_OK;
+    k_scan_onepass<<<T, kBlock, 0, st>>>(count, C, start, scan_state_words(scan_state),
+                                         static_cast<ScanCtl*>(scan_state), T, err);
+    GS_LAUNCHED("scan_onepass");
+    return GS_OK;
+}
+
 // ---- database -----------------------------------------------------------------------
 gs_status db_reserve(Database& db, unsigned n, unsigned C) {
     if (db.cells != C) {

@@ -111,17 +111,65 @@ __device__ __forceinline__ void knn_scan_box(KList<KMAX>& L, V3 p, unsigned self
     }
 }
 
-// ---- fast scan: 32-bit keys ---------------------------------------------------------
-// key = distance bits with the low log2(ENUM) mantissa bits replaced by the
-// candidate's enumeration index e (slot and key kept in two per-thread
-// shared-memory tables at e).  Keys order candidates exactly like
-// (distance, index) whenever no two relevant candidates share the truncated
-// distance T = bits & ~(ENUM - 1): T(a) < T(b) implies d(a) < d(b).  The scan
-// records every way that assumption can fail - two list entries with equal T,
-// a candidate left out of a full list with T equal to the k-th entry's, more
-// than ENUM candidates - and then reports failure; the agent is then redone
-// with the exact 64-bit list (knn_scan_box).
+// ---- fast scan: 32-bit keys of squared distances --------------------------------
+// key = bits of the SQUARED distance (no square root per candidate) with the
+// low EBITS = log2(ENUM) mantissa bits replaced by the candidate's enumeration
+// index e.  T = key >> EBITS is the squared distance truncated to units of
+// 2^EBITS ulps.  Square root rounded to nearest is monotone, so smaller keys
+// never have larger distances, and two candidates whose T differ by two units
+// or more have DIFFERENT distances: their squared distances differ by more
+// than 2^EBITS ulps, a relative step of at least 2^(EBITS - 24), which leaves
+// at least 2^(EBITS - 2) ulps between the roots before rounding.  So the k
+// smallest keys are the k nearest candidates in (distance, index) order,
+// except where entries' T are within one unit of each other:
+//   - adjacent list entries that close are compared exactly ((distance,
+//     index) from their positions: near_pairs_ordered), and the agent is
+//     redone if they are out of order;
+//   - a candidate left out of a full list with T within one unit of the k-th
+//     entry's, or more than ENUM candidates, sends the agent to the exact
+//     64-bit list (knn_scan_box).
 constexpr unsigned KEY32_EMPTY = 0xffffffffu;
+
+template <unsigned N>
+struct Log2 {
+    static constexpr unsigned value = 1 + Log2<N / 2>::value;
+};
+template <>
+struct Log2<1> {
+    static constexpr unsigned value = 0;
+};
+
+// True when the candidate left out of a full list (smallest left-out key
+// out_min) may belong in it: its T is within one unit of the k-th entry's.
+template <unsigned EBITS>
+__device__ __forceinline__ bool boundary_unsure(unsigned last, unsigned out_min) {
+    return last != KEY32_EMPTY && (out_min >> EBITS) < (last >> EBITS) + 2u;
+}
+
+// The listed slots out[r * stride] (r < k, in key order, UINT_MAX after the
+// last neighbour) against the exact (distance, index) order, for the adjacent
+// entries whose T are within one unit (the others are ordered by their keys).
+template <int KMAX, unsigned EBITS>
+__device__ __forceinline__ bool near_pairs_ordered(const unsigned (&key)[KMAX], int k, V3 p,
+                                                   const float4* __restrict__ pos_id,
+                                                   const unsigned* out, unsigned stride) {
+    unsigned near = 0;
+#pragma unroll
+    for (int i = 1; i < KMAX; ++i)
+        if (i > KMAX - k && key[i] != KEY32_EMPTY && (key[i] >> EBITS) < (key[i - 1] >> EBITS) + 2u)
+            near |= 1u << i;
+    while (near) {
+        const int i = __ffs(near) - 1;
+        near &= near - 1;
+        const unsigned r = unsigned(i - (KMAX - k));
+        const float4 qa = __ldg(pos_id + out[(r - 1) * stride]);
+        const float4 qb = __ldg(pos_id + out[r * stride]);
+        if (!knn_less(distance(p, v3(qa)), __float_as_uint(qa.w), distance(p, v3(qb)),
+                      __float_as_uint(qb.w)))
+            return false;
+    }
+    return true;
+}
 
 template <int KMAX>
 struct KList32 {
@@ -195,18 +243,19 @@ struct KList32 {
     }
 };
 
-// Appends candidate slot s to the tables (self and non-finite distances
-// skip).  e counts past ENUM without storing; the caller checks it.  No early
-// exits: the warp's lanes reconverge after every candidate.
+// Appends candidate slot s to the tables (self and non-finite squared
+// distances skip).  e counts past ENUM without storing; the caller checks it.
+// No early exits: the warp's lanes reconverge after every candidate.
 template <unsigned ENUM>
 __device__ __forceinline__ void collect_one(unsigned s, V3 p, unsigned self_id,
                                             const float4* __restrict__ pos_id, unsigned& e,
                                             unsigned* slot_tab, unsigned* key_tab,
                                             unsigned stride) {
     const float4 q = __ldg(pos_id + s);
-    const unsigned bits = __float_as_uint(distance(p, v3(q)));
-    // never below FLT_MAX (inf, NaN): never listed
-    if (__float_as_uint(q.w) != self_id && bits < 0x7f7fffffu) {
+    const unsigned bits = __float_as_uint(dist_sq(p, v3(q)));
+    // inf or NaN (the distance is then inf or NaN: never below FLT_MAX, never
+    // listed); a finite square gives a finite root, which is
+    if (__float_as_uint(q.w) != self_id && bits <= 0x7f7fffffu) {
         if (e < ENUM) {
             slot_tab[e * stride] = s;
             key_tab[e * stride] = (bits & ~(ENUM - 1)) | e;
@@ -227,7 +276,10 @@ __device__ __forceinline__ unsigned collect_box(V3 p, unsigned self_id, const Gr
     unsigned e = 0;
     const unsigned span = b.x1 - b.x0 + 1;
     if (b.y1 - b.y0 <= 2 && b.z1 - b.z0 <= 2) {
-        // at most 3 x 3 rows: load every row's range first, then walk them
+        // At most 3 x 3 rows.  The rows' slots are first laid end to end in
+        // slot_tab (a short store loop per row), then one loop walks all of
+        // them: a warp runs as many iterations as its busiest lane has
+        // candidates, not the sum over rows of each row's busiest lane.
         unsigned rs[9], rn[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
@@ -239,10 +291,37 @@ __device__ __forceinline__ unsigned collect_box(V3 p, unsigned self_id, const Gr
             rs[i] = s0;
             rn[i] = s1 - s0;
         }
+        unsigned total = 0;
 #pragma unroll
-        for (int i = 0; i < 9; ++i)
+        for (int i = 0; i < 9; ++i) {
             for (unsigned t = 0; t < rn[i]; ++t)
-                collect_one<ENUM>(rs[i] + t, p, self_id, pos_id, e, slot_tab, key_tab, stride);
+                if (total + t < ENUM) slot_tab[(total + t) * stride] = rs[i] + t;
+            total += rn[i];
+        }
+        if (total > ENUM) return total;  // overflow: the exact path redoes the agent
+        // compacted in place (self and non-finite candidates dropped): entry
+        // e is written only after entries up to e were read.  Four at a
+        // time: the four slots, then the four positions, are loaded before
+        // any key is formed, so their loads overlap.
+        for (unsigned j0 = 0; j0 < total; j0 += 4) {
+            unsigned sl[4];
+            float4 q[4];
+#pragma unroll
+            for (unsigned u = 0; u < 4; ++u) sl[u] = j0 + u < total ? slot_tab[(j0 + u) * stride] : 0u;
+#pragma unroll
+            for (unsigned u = 0; u < 4; ++u)
+                q[u] = j0 + u < total ? __ldg(pos_id + sl[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (unsigned u = 0; u < 4; ++u) {
+                if (j0 + u >= total) break;
+                const unsigned bits = __float_as_uint(dist_sq(p, v3(q[u])));
+                if (__float_as_uint(q[u].w) != self_id && bits <= 0x7f7fffffu) {
+                    slot_tab[e * stride] = sl[u];
+                    key_tab[e * stride] = (bits & ~(ENUM - 1)) | e;
+                    ++e;
+                }
+            }
+        }
         return e;
     }
     for (unsigned cy = b.y0; cy <= b.y1; ++cy)
@@ -265,7 +344,7 @@ __device__ __forceinline__ bool knn_neighbours_fast(int k, V3 p, unsigned self_i
                                                     const float4* __restrict__ pos_id,
                                                     unsigned* slot_tab, unsigned* key_tab,
                                                     unsigned stride) {
-    constexpr unsigned mask = ENUM - 1;
+    constexpr unsigned mask = ENUM - 1, EBITS = Log2<ENUM>::value;
     const unsigned n = collect_box<ENUM>(p, self_id, g, b, cell_offset, cell_start, pos_id,
                                          slot_tab, key_tab, stride);
     if (n > ENUM) return false;
@@ -282,18 +361,13 @@ __device__ __forceinline__ bool knn_neighbours_fast(int k, V3 p, unsigned self_i
         const unsigned c = key_tab[e * stride];
         out_min = min(out_min, c < L.key[KMAX - 1] ? L.insert(c) : c);
     }
-    const unsigned last = L.key[KMAX - 1];
-    if (last != KEY32_EMPTY && (out_min & ~mask) == (last & ~mask)) return false;
-#pragma unroll
-    for (int i = KMAX - 1; i > 0; --i)
-        if (i > KMAX - k && L.key[i] != KEY32_EMPTY && (L.key[i] & ~mask) == (L.key[i - 1] & ~mask))
-            return false;
+    if (boundary_unsure<EBITS>(L.key[KMAX - 1], out_min)) return false;
 #pragma unroll
     for (int i = 0; i < KMAX; ++i)
         if (i >= KMAX - k)
             key_tab[(i - (KMAX - k)) * stride] =
                 L.key[i] != KEY32_EMPTY ? slot_tab[(L.key[i] & mask) * stride] : UINT_MAX;
-    return true;
+    return near_pairs_ordered<KMAX, EBITS>(L.key, k, p, pos_id, key_tab, stride);
 }
 
 // The order the streaming scan visits the nine rows of a 3 x 3 x 3 (or
@@ -362,20 +436,15 @@ __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self
                 c[j] = KEY32_EMPTY;
                 if (t < n_row) {
                     const float4 q = __ldg(pos_id + rs[i] + t);
-                    const unsigned bits = __float_as_uint(distance(p, v3(q)));
-                    if (__float_as_uint(q.w) != self_id && bits < 0x7f7fffffu)
+                    const unsigned bits = __float_as_uint(dist_sq(p, v3(q)));
+                    if (__float_as_uint(q.w) != self_id && bits <= 0x7f7fffffu)
                         c[j] = (bits & ~mask) | (pre[i] + t);
                 }
             }
             out_min = min(out_min, L.merge4(c));
         }
     }
-    const unsigned last = L.key[KMAX - 1];
-    if (last != KEY32_EMPTY && (out_min & ~mask) == (last & ~mask)) return false;
-#pragma unroll
-    for (int i = KMAX - 1; i > 0; --i)
-        if (i > KMAX - k && L.key[i] != KEY32_EMPTY && (L.key[i] & ~mask) == (L.key[i - 1] & ~mask))
-            return false;
+    if (boundary_unsure<EBITS>(L.key[KMAX - 1], out_min)) return false;
 #pragma unroll
     for (int i = 0; i < KMAX; ++i) {
         if (i < KMAX - k) continue;
@@ -390,7 +459,7 @@ __device__ __forceinline__ bool knn_neighbours_stream(int k, V3 p, unsigned self
         }
         out[(i - (KMAX - k)) * stride] = slot;
     }
-    return true;
+    return near_pairs_ordered<KMAX, EBITS>(L.key, k, p, pos_id, out, stride);
 }
 
 // Exact path: the ordered slots go to col[r * stride].

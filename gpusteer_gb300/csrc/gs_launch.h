@@ -11,6 +11,16 @@ namespace gs {
 gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
                       cudaStream_t st);
 unsigned scan_tile_count(unsigned C);
+// The same scan in one launch (decoupled look-back), for the fused engine.
+// scan_state: scan_state_bytes(C) bytes, zeroed once when allocated; err gets
+// kErrScanTimeout if a wait ran out.
+struct ScanCtl {
+    unsigned ticket, done, epoch, pad;
+};
+constexpr unsigned kErrScanTimeout = 4u;
+size_t scan_state_bytes(unsigned C);
+gs_status scan_counts_onepass(unsigned* count, unsigned* start, unsigned C, void* scan_state,
+                              unsigned* err, cudaStream_t st);
 // Allocates db for C cells and n agents (keeps existing buffers when large enough).
 gs_status db_reserve(Database& db, unsigned n, unsigned C);
 void db_release(Database& db);
@@ -124,6 +134,9 @@ struct StepDev {
     unsigned k, knw, r;
     int wrap_mode, clear_applied, dirty;
     float sep[5], ali[5], coh[5];  // min, max, cos, weight, mask bits
+    // exact squared-distance forms of each flocking test's d < min and
+    // d > max: (lt, gt) with d < min <=> dsq < lt and d > max <=> dsq > gt
+    float sep_dsq[2], ali_dsq[2], coh_dsq[2];
     float seek_target[3], w_seek;
     unsigned mask_seek;
     float min_time_wall, w_walls;
@@ -207,11 +220,16 @@ struct AdjointLaunch {
     const unsigned* knn; // [n * k] recorded neighbour indices
     const float *max_speed, *max_force, *mass;
     float4 *lp_in, *lv_in;    // d loss / d (position, velocity) after the step; zeroed
-    float4 *lp_out, *lv_out;  // d loss / d (position, velocity) before the step; += (atomic)
+    float4 *lp_out, *lv_out;  // d loss / d (position, velocity) before the step; +=
     float* wpart;             // [blocks * 4] per-block sums: separation, alignment, cohesion
     unsigned n, k;
+    // scratch (adjoint_scratch_bind): per-edge and own terms, reverse-KNN index
+    float4 *edge_p, *edge_v, *own_p, *own_v;
+    unsigned *indeg, *rstart, *redge, *tile;
 };
 unsigned adjoint_blocks(unsigned n);
+size_t adjoint_scratch_bytes(unsigned n, unsigned k);
+void adjoint_scratch_bind(AdjointLaunch& A, void* base, unsigned n, unsigned k);
 gs_status launch_flock_adjoint(const AdjointLaunch& A, const StepDev& p, cudaStream_t st);
 
 // Number of non-zero entries of count[0..C), read back to the host (syncs st).

@@ -41,6 +41,12 @@ GS_HD V3 cross(V3 a, V3 b) {
 }
 GS_HD bool is_zero(V3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
 GS_HD float distance(V3 a, V3 b) { return length(sub(a, b)); }
+// The squared distance under distance()'s square root: distance(a, b) is
+// sqrtf(dist_sq(a, b)) bit for bit.
+GS_HD float dist_sq(V3 a, V3 b) {
+    const V3 o = sub(a, b);
+    return dot(o, o);
+}
 GS_HD V3 perpendicular_component(V3 v, V3 u) { return sub(v, mul(u, dot(v, u))); }
 GS_HD V3 truncate_length(V3 v, float max_len) {
     const float max_sq = max_len * max_len;

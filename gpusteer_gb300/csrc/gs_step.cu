@@ -139,37 +139,60 @@ struct Accs {
 
 // `need` is p.need, or a compile-time mask equal to it in a kernel
 // specialised for one configuration (the unused accumulators then vanish).
+// gs, ga, gc: the agent's angle gates of the three flocking behaviours.
 __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned need,
                                            const FlockParams& fs, const FlockParams& fa,
-                                           const FlockParams& fc, const Self& me, unsigned rank,
+                                           const FlockParams& fc, AngleGate gs_, AngleGate ga,
+                                           AngleGate gc, const Self& me, unsigned rank,
                                            float knn_d, V3 bpos, V3 bdir, float bspeed,
                                            float bradius) {
     const V3 offset = sub(bpos, me.pos);
     const float dsq = dot(offset, offset);
-    const float d = sqrtf(dsq);
     if (need & (NEED_SEP | NEED_ALI | NEED_COH)) {
         // inBoidNeighborhood (FlockingCommon.cuh:4-30) for the three flocking
-        // behaviours: the unit offset and its dot with the heading are the
-        // same operands for all three, so they are computed once.
-        const bool ang_s = (need & NEED_SEP) && !(d < fs.min_d) && !(d > fs.max_d);
-        const bool ang_a = (need & NEED_ALI) && !(d < fa.min_d) && !(d > fa.max_d);
-        const bool ang_c = (need & NEED_COH) && !(d < fc.min_d) && !(d > fc.max_d);
-        float fwd = 0.f;
-        if (ang_s || ang_a || ang_c) fwd = dot(me.dir, dvd(offset, d));
+        // behaviours, without its square root and divisions where they cannot
+        // change the outcome: d < min and d > max are compared as squared
+        // distances against exact thresholds, and the angle test is decided
+        // from dot(dir, offset) unless it lies within the gate's margin (then
+        // the reference's unit offset and dot decide, computed once for all
+        // three, as they are the same operands).
+        const bool lt_s = (need & NEED_SEP) && dsq < fs.lt;
+        const bool lt_a = (need & NEED_ALI) && dsq < fa.lt;
+        const bool lt_c = (need & NEED_COH) && dsq < fc.lt;
+        const bool ang_s = (need & NEED_SEP) && !lt_s && !(dsq > fs.gt);
+        const bool ang_a = (need & NEED_ALI) && !lt_a && !(dsq > fa.gt);
+        const bool ang_c = (need & NEED_COH) && !lt_c && !(dsq > fc.gt);
+        bool in_s = lt_s, in_a = lt_a, in_c = lt_c;
+        if (ang_s || ang_a || ang_c) {
+            const float g = dot(me.dir, offset), de = d_estimate(dsq);
+            const int ds = ang_s ? angle_decide(g, de, fs.cos_max, gs_) : 0;
+            const int da = ang_a ? angle_decide(g, de, fa.cos_max, ga) : 0;
+            const int dc = ang_c ? angle_decide(g, de, fc.cos_max, gc) : 0;
+            if ((ds | da | dc) < 0) {
+                const float fwd = dot(me.dir, dvd(offset, sqrtf(dsq)));
+                in_s = in_s || (ds < 0 ? fwd > fs.cos_max : ds > 0);
+                in_a = in_a || (da < 0 ? fwd > fa.cos_max : da > 0);
+                in_c = in_c || (dc < 0 ? fwd > fc.cos_max : dc > 0);
+            } else {
+                in_s = in_s || ds > 0;
+                in_a = in_a || da > 0;
+                in_c = in_c || dc > 0;
+            }
+        }
         if (need & NEED_SEP) {
-            if ((d < fs.min_d) || (ang_s && fwd > fs.cos_max)) {
+            if (in_s) {
                 a.sep.sum = add(a.sep.sum, dvd(offset, -dsq));
                 a.sep.n++;
             }
         }
         if (need & NEED_ALI) {
-            if ((d < fa.min_d) || (ang_a && fwd > fa.cos_max)) {
+            if (in_a) {
                 a.ali.sum = add(a.ali.sum, bdir);
                 a.ali.n++;
             }
         }
         if (need & NEED_COH) {
-            if ((d < fc.min_d) || (ang_c && fwd > fc.cos_max)) {
+            if (in_c) {
                 a.coh.sum = add(a.coh.sum, bpos);
                 a.coh.n++;
             }
@@ -179,7 +202,7 @@ __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned n
     // the KNN distance equals d unless the neighbour moved after the KNN
     // (avoid-walls); the caller passes it then, else -1
     if (need & NEED_CLOSE)
-        close_add(a.close, me, p.min_sep, knn_d < 0.f ? d : knn_d, bpos, bradius);
+        close_add(a.close, me, p.min_sep, knn_d < 0.f ? sqrtf(dsq) : knn_d, bpos, bradius);
 }
 
 // Behaviours order[first..] in order, then nothing else.  fetch(rank, pos,
@@ -407,6 +430,8 @@ __global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) 
 }
 
 // ---- whole step without walls -------------------------------------------------------
+constexpr unsigned kNbrChunk = 4;
+
 // NEEDC: the behaviours that read the neighbour list, fixed at compile time
 // (kNeedRuntime: taken from p.need).
 constexpr unsigned kNeedRuntime = ~0u;
@@ -430,32 +455,74 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
         const unsigned base = agent_knn<KMAX, ENUM, EXACT, FLAT>(L, p, s, it, pos, id, sc, box, col, bd);
         if (base == UINT_MAX) return;
-        float4 f4v;
-        Self me = load_rest(L.B, s, pos, f4v);
-        unsigned applied = p.clear_applied ? 0u : u(f4v.z);
-        V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
-        const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali),
-                          fc = flock_params(p.coh);
-        Accs a;
-        init_accs(a, p);
         const bool need_dir = need & (NEED_ALI | NEED_AVOID);
         const bool need_rad = need & (NEED_AVOID | NEED_CLOSE);
+        // the neighbour pass reads position, heading, speed and radius; the
+        // rest of the state is loaded after it, so it is not held through it
+        Self me;
+        me.pos = pos;
+        {
+            const float4 f1 = L.B.f[1][s];
+            me.dir = v3(f1);
+            me.speed = f1.w;
+            me.radius = need_rad ? reinterpret_cast<const float*>(L.B.f[2] + s)[3] : 0.f;
+        }
+        const FlockParams fs = flock_params(p.sep, p.sep_dsq), fa = flock_params(p.ali, p.ali_dsq),
+                          fc = flock_params(p.coh, p.coh_dsq);
+        const AngleGate gs_ = angle_gate(me.dir, fs.cos_max), ga = angle_gate(me.dir, fa.cos_max),
+                        gc = angle_gate(me.dir, fc.cos_max);
+        Accs a;
+        init_accs(a, p);
         unsigned* rec_knn = L.rec_knn ? L.rec_knn + size_t(id) * p.k : nullptr;
         unsigned r = 0;
-        for (; r < p.k; ++r) {
-            const unsigned bs = col[(base + r) * bd];
-            if (bs == UINT_MAX) break;
-            const float4 b0 = L.B.f[0][bs];
-            const float4 b1 = need_dir ? L.B.f[1][bs] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float br = need_rad ? L.B.f[2][bs].w : 0.f;
-            if (rec_knn) rec_knn[r] = u(b0.w);
-            accumulate(a, p, need, fs, fa, fc, me, r, -1.f, v3(b0), v3(b1), b1.w, br);
+        // Neighbours kNbrChunk at a time: their loads are issued together, so
+        // the pass waits on a chunk's gathers once instead of on every
+        // neighbour's.  The list is filled from rank 0, so the first empty
+        // entry ends it; accumulation stays in list order.
+        for (bool more = true; more && r < p.k;) {
+            unsigned bs[kNbrChunk];
+            float4 b0[kNbrChunk], b1[kNbrChunk];
+            float br[kNbrChunk];
+#pragma unroll
+            for (unsigned j = 0; j < kNbrChunk; ++j)
+                bs[j] = r + j < p.k ? col[(base + r + j) * bd] : UINT_MAX;
+#pragma unroll
+            for (unsigned j = 0; j < kNbrChunk; ++j) {
+                const bool ok = bs[j] != UINT_MAX;
+                b0[j] = ok ? L.B.f[0][bs[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+                b1[j] = ok && need_dir ? L.B.f[1][bs[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+                br[j] = ok && need_rad ? reinterpret_cast<const float*>(L.B.f[2] + bs[j])[3] : 0.f;
+            }
+#pragma unroll
+            for (unsigned j = 0; j < kNbrChunk; ++j) {
+                if (bs[j] == UINT_MAX) {
+                    more = false;
+                    break;
+                }
+                if (rec_knn) rec_knn[r] = u(b0[j].w);
+                accumulate(a, p, need, fs, fa, fc, gs_, ga, gc, me, r, -1.f, v3(b0[j]), v3(b1[j]),
+                           b1[j].w, br[j]);
+                ++r;
+            }
         }
         if (rec_knn) {
             for (; r < p.k; ++r) rec_knn[r] = UINT_MAX;
             L.rec_pos[id] = make_float4(me.pos.x, me.pos.y, me.pos.z, me.speed);
             L.rec_dir[id] = make_float4(me.dir.x, me.dir.y, me.dir.z, 0.f);
         }
+        float4 f4v;
+        {
+            const float4 f2 = L.B.f[2][s], f3 = L.B.f[3][s];
+            f4v = L.B.f[4][s];
+            me.side = v3(f2);
+            me.radius = f2.w;
+            me.up = v3(f3);
+            me.mass = f3.w;
+            me.max_speed = f4v.x;
+            me.max_force = f4v.y;
+        }
+        unsigned applied = p.clear_applied ? 0u : u(f4v.z);
+        V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
         finish_all(a, p, 0, fs, fa, fc, me, applied, steer,
                    [&](unsigned rank, V3& bp, V3& bh, float& bsp) {
                        const unsigned bs = col[(base + rank) * bd];
@@ -551,7 +618,10 @@ __global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev
     me.radius = w0.w;
     me.dir = v3(w1);
     me.speed = w1.w;
-    const FlockParams fs = flock_params(p.sep), fa = flock_params(p.ali), fc = flock_params(p.coh);
+    const FlockParams fs = flock_params(p.sep, p.sep_dsq), fa = flock_params(p.ali, p.ali_dsq),
+                      fc = flock_params(p.coh, p.coh_dsq);
+    const AngleGate gs_ = angle_gate(me.dir, fs.cos_max), ga = angle_gate(me.dir, fa.cos_max),
+                    gc = angle_gate(me.dir, fc.cos_max);
     Accs a;
     init_accs(a, p);
     const bool need_dir = need & (NEED_ALI | NEED_AVOID);
@@ -561,7 +631,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev
         const float4 b0 = L.w0[bs];
         const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
-        accumulate(a, p, need, fs, fa, fc, me, i, kd, v3(b0), v3(b1), b1.w, b0.w);
+        accumulate(a, p, need, fs, fa, fc, gs_, ga, gc, me, i, kd, v3(b0), v3(b1), b1.w, b0.w);
     }
     const float4 w2 = L.w2[s];
     const float4 f2 = L.B.f[2][s], f3 = L.B.f[3][s], f4v = L.B.f[4][s];

@@ -321,10 +321,11 @@ def knn_capacity(group) -> int:
 
 
 def step_launches(group, walls: bool) -> int:
-    """Kernel launches of one fused step: the counting-sort scan (3), the
-    permute, the fused kernel (two with walls), the exact redo, and with the
-    streaming scan (capacity 128 or 256) the warp-per-agent exact lists."""
-    return 3 + 1 + (2 if walls else 1) + 1 + (1 if knn_capacity(group) > 64 else 0)
+    """Kernel launches of one fused step: the counting-sort scan (one
+    single-pass launch), the permute, the fused kernel (two with walls), the
+    exact redo, and with the streaming scan (capacity 128 or 256) the
+    warp-per-agent exact lists."""
+    return 1 + 1 + (2 if walls else 1) + 1 + (1 if knn_capacity(group) > 64 else 0)
 
 
 class Batch:

@@ -434,7 +434,9 @@ gs_status gs_rollout_backward(gs_rollout r, const float* adj_position, const flo
  * agent; zeroed on return).  Adds the adjoints of its inputs to adj_*_in
  * (float4 per agent) and per-block sums of d loss / d weights to
  * weight_partials (4 floats per block of 256 agents: separation, alignment,
- * cohesion, unused).  Asynchronous on `stream`. */
+ * cohesion, unused).  Deterministic: no float atomics; each agent's terms
+ * are summed in a fixed order.  Its scratch is allocated and freed on
+ * `stream` (stream-ordered).  Asynchronous on `stream`. */
 gs_status gs_flock_adjoint_step(const float* position_speed, const float* heading,
                                 const unsigned* knn, unsigned n, unsigned k,
                                 const float* max_speed, const float* max_force, const float* mass,

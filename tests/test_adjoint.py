@@ -148,6 +148,9 @@ def test_adjoint_matches_finite_differences_65536_boids():
 
 
 def test_checkpoint_interval_does_not_change_gradients():
+    """The recomputed segments equal the forward pass bit for bit and the
+    adjoint sums in a fixed order, so every checkpoint interval gives the same
+    gradients exactly."""
     steps = 16
     s, p = case(4096, 60.0, 128.0, steps, seed=5)
     target = target_positions(s, p, steps)
@@ -157,8 +160,25 @@ def test_checkpoint_interval_does_not_change_gradients():
         if base is None:
             base = (gv, gw)
             continue
-        assert rel_err(gw, base[1]) < 1e-5
-        assert rel_err(gv, base[0]) < 1e-5
+        np.testing.assert_array_equal(gw, base[1])
+        np.testing.assert_array_equal(gv, base[0])
+
+
+def test_backward_passes_are_bit_identical():
+    """No float atomics in the adjoint: the neighbour terms of each agent are
+    gathered through the reverse-KNN index and added in ascending edge order,
+    so two backward passes of one rollout (65,536 boids, k = 16, 24 steps,
+    checkpoints every 8) give the same gradients bit for bit."""
+    steps = 24
+    s = sc.boids_cube(65536, size=200.0, seed=0)
+    p = sc.boids_params(k=16, world=256.0, cell=4.0)
+    r = ah.Runner(s, p, steps, 8)
+    final = r.forward(None, W_EVAL)
+    g_final = torch.from_numpy(2.0 * (final - 0.5 * final) / (3 * s.n))
+    first = [None if t is None else t.numpy().copy() for t in r.backward(g_final, want_p0=True)]
+    second = [None if t is None else t.numpy().copy() for t in r.backward(g_final, want_p0=True)]
+    for a, b in zip(first, second):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_adjoint_step_entry_point_matches_rollout():
@@ -201,8 +221,9 @@ def test_adjoint_step_entry_point_matches_rollout():
     torch.cuda.synchronize()
     gw = wpart.view(-1, 4)[:, :3].double().sum(0).cpu().numpy()
     assert rel_err(gw, gw_r) < 1e-5
-    assert rel_err(lv_in[:, :3].cpu().numpy(), gv_r) < 1e-5
-    assert rel_err(lp_in[:, :3].cpu().numpy(), gp_r) < 1e-5
+    # the same kernels on the same inputs, summed in the same fixed order
+    np.testing.assert_array_equal(lv_in[:, :3].cpu().numpy(), gv_r)
+    np.testing.assert_array_equal(lp_in[:, :3].cpu().numpy(), gp_r)
     assert float(lp_out.abs().max()) == 0.0
 
 
