@@ -502,14 +502,19 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     # autotune cell size, block shape and KNN capacity on the scenes themselves
     t0 = time.perf_counter()
     if args.fixed_config:
-        tr = autotune.TuneResult(params=base, block=256, capacity=0, ms_per_step=0.0)
+        tr = autotune.TuneResult(params=base, block=256, capacity=0, ms_per_step=0.0,
+                                 persistent=args.persistent)
     else:
         tr = autotune.tune_batched(states, gaps, base, walls_rows)
     tune_s = time.perf_counter() - t0
     p = tr.params
+    def configure(grp, capacity=None):
+        gs.set_block(grp, tr.block)
+        gs.set_knn_capacity(grp, tr.capacity if capacity is None else capacity)
+        gs.set_persistent(grp, tr.persistent)
+
     b = autotune.batch_for(states, gaps, p, walls_rows)
-    gs.set_block(b.group, tr.block)
-    gs.set_knn_capacity(b.group, tr.capacity)
+    configure(b.group)
     stream = torch.cuda.ExternalStream(b.group.stream)
 
     # warm-up, then K timed steps (one graph replay each, state resident in HBM)
@@ -533,6 +538,23 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     phases = phase_times(lib, b.group, lambda k: b.step(p, k), max(3, min(args.steps, 10)))
     launches_per_step = gs.step_launches(b.group, True)
     measured_cap = gs.knn_capacity(b.group)  # the scan the resident steps used
+    # both forms of the step on the same batch: separate launches (one graph
+    # replay per step) and one persistent launch per step
+    forms = {}
+    for pers in (False, True):
+        gs.set_persistent(b.group, pers)
+        gs.set_knn_capacity(b.group, measured_cap)
+        b.step(p, 3)
+        b.group.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            b.step(p, 1)
+        f1.record(stream)
+        f1.synchronize()
+        forms["persistent" if pers else "separate"] = {
+            "ms_per_step": f0.elapsed_time(f1) / args.steps,
+            "launches_per_step": gs.step_launches(b.group, True)}
     del b
 
     # the same scenes, one gs_step call per scene per step (same grid, block,
@@ -550,8 +572,7 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
             grp = gs.AgentGroup(p.k, s.n, stream=first.stream if (shared and first) else None)
             first = first or grp
             grp.upload(s)
-            gs.set_block(grp, tr.block)
-            gs.set_knn_capacity(grp, tr.capacity)
+            configure(grp)
             groups.append((grp, bins, walls))
         for grp, bins, walls in groups:
             gs.step(grp, bins, walls, p, args.warmup)
@@ -571,9 +592,8 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
 
     total = args.warmup + ps_steps
     b2 = autotune.batch_for(states, gaps, p, walls_rows)
-    gs.set_block(b2.group, tr.block)
-    gs.set_knn_capacity(b2.group, tr.capacity)
-    per_scene, identical = None, None
+    configure(b2.group)
+    per_scene, identical, identical_other = None, None, None
     if not args.no_per_scene:
         per_seq, per_seq_ms, groups = per_scene_run(shared=True)
         del groups
@@ -583,6 +603,15 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
         got = b2.download()
         want = AgentState.concat([grp.download() for grp, _, _ in per])
         identical = all(np.array_equal(getattr(got, k), getattr(want, k)) for k in got.names())
+        # the other form of the step gives the same state
+        b3 = autotune.batch_for(states, gaps, p, walls_rows)
+        configure(b3.group, measured_cap)
+        gs.set_persistent(b3.group, not tr.persistent)
+        b3.step(p, total)
+        got3 = b3.download()
+        identical_other = all(np.array_equal(getattr(got3, k), getattr(want, k))
+                              for k in got3.names())
+        del b3
         del per
         per_scene = {
             "value": per_seq, "unit": "agent-steps/s", "steps": ps_steps,
@@ -626,10 +655,9 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     parts = []
     for lo, hi in zip(cuts[:-1], cuts[1:]):
         bp = autotune.batch_for(states[lo:hi], gaps[lo:hi], p, walls_rows)
-        gs.set_block(bp.group, tr.block)
         # a fixed capacity (the host-stepping graph needs one): the one the
         # resident batch used
-        gs.set_knn_capacity(bp.group, tr.capacity or measured_cap or 256)
+        configure(bp.group, tr.capacity or measured_cap or 256)
         parts.append(bp)
     # one step from the initial state: the parts equal the single batch
     for k in hio.names():
@@ -700,11 +728,13 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
         "data": "synthetic",
         "config": batched_config(p, len(states), n, world),
         "tuned": {"block": tr.block, "knn_capacity": tr.capacity or "auto",
-                  "cell": p.world_size[0] / p.world_cells[0]},
+                  "cell": p.world_size[0] / p.world_cells[0], "persistent": tr.persistent},
+        "forms": forms,
         "per_scene": per_scene,
         "identical_to_per_scene": None if identical is None else {
             "equal": bool(identical), "steps": total,
-            "compared": "every state array of every agent"},
+            "compared": "every state array of every agent",
+            "other_form_equal": bool(identical_other)},
         "autotune": {"seconds": tune_s, "trials": tr.trials},
         "adjoint": adjoint,
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
@@ -1034,6 +1064,8 @@ def main():
                     help="batched workload: scene ranges overlapped in the end-to-end run")
     ap.add_argument("--no-per-scene", action="store_true",
                     help="batched workload: skip the per-scene baselines")
+    ap.add_argument("--persistent", action="store_true",
+                    help="batched workload with --fixed-config: one persistent launch per step")
     ap.add_argument("--no-sub", action="store_true",
                     help="batched workload: skip the large-flock and brute-force records")
     ap.add_argument("--large-steps", type=int, default=200,

@@ -11,7 +11,7 @@ from .groups import (  # noqa: F401
     batches_step_host, pinned_state, MultiGroupParams, multigroup_step,
     antiPenetrationWall, updateGroupWithAntiPenetration,
     findKNearestNeighbors, findKNearestNeighborsBruteForce, findKNearestNeighborsGroups,
-    set_block, set_graphs,
+    set_barrier_limit, set_block, set_graphs, set_persistent,
     knn_capacity, set_knn_capacity, step, step_host, step_launches, steerForAlignment,
     steerForCohesion,
     steerForSeek, steerForSeparation, steerToAvoidNeighbors, steerToAvoidWalls, steerToFollowPath,

@@ -79,6 +79,8 @@ SIGNATURES = {
     "gs_group_set_profiling": [_vp, _i],
     "gs_group_phase_times": [_vp, _fp, _up, _u],
     "gs_group_exact_redos": [_vp, _up],
+    "gs_group_set_persistent": [_vp, C.c_int],
+    "gs_group_set_barrier_limit": [_vp, _u],
     "gs_knn_create": [_u, _u, C.POINTER(_vp)],
     "gs_knn_destroy": [_vp],
     "gs_knn_download": [_vp, _vp, _up, _fp],

@@ -28,10 +28,12 @@
 //   cohesion    g_q / n_members to each member's position
 //   alignment   g_q / n_members to each member's heading, turned into a
 //               velocity adjoint with (I - d d^T) / |v|
-// A second kernel gives each agent the sum of its own terms and of the terms
-// of every edge that points at it, found through a reverse-KNN index (edges
-// bucketed by their target) and added in ascending edge order.  No float
-// atomics: two backward passes give the same gradients bit for bit.
+// A kernel with one thread per edge files every edge in its target's bucket
+// (kBucket slots per agent taken with an integer atomic, an overflow list
+// past that).  The gather gives each agent the sum of its own terms and of
+// the terms of every edge that points at it, added in ascending edge order
+// whatever order the bucket was filled in.  No float atomics: two backward passes give the same
+// gradients bit for bit.
 // The derivative of the world wrap is the identity.
 #include <cfloat>
 #include <climits>
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(kAdjBlock) k_flock_adjoint(AdjointLaunch A, St
                 const V3 dj = v3(A.dir[j]);
                 if (Pj.w > 0.f) gvj = dvd(sub(g_ali, mul(dj, dot(dj, g_ali))), Pj.w);
             }
-            const size_t e = size_t(i) * A.k + r;
+            const unsigned e = i * A.k + r;
             A.edge_p[e] = f4z(gpj);
             A.edge_v[e] = f4z(gvj);
         }
@@ -210,47 +212,40 @@ __global__ void __launch_bounds__(kAdjBlock) k_flock_adjoint(AdjointLaunch A, St
     }
 }
 
-// ---- reverse-KNN index of the recorded lists -------------------------------------
-// In-degree of every agent (edges e = i * k + r whose target knn[e] is an agent).
-__global__ void k_rev_count(const unsigned* __restrict__ knn, unsigned n, unsigned k,
-                            unsigned* __restrict__ indeg) {
-    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (e >= size_t(n) * k) return;
-    const unsigned j = knn[e];
-    if (j < n) atomicAdd(indeg + j, 1u);
-}
-
-// Edges bucketed by target: redge[rstart[j] ..) holds the edges into j, in
-// the order the atomics hand out (the gather sorts each bucket).  fill is
-// zero on entry and holds the in-degrees on exit.
-__global__ void k_rev_fill(const unsigned* __restrict__ knn, unsigned n, unsigned k,
-                           const unsigned* __restrict__ rstart, unsigned* __restrict__ fill,
-                           unsigned* __restrict__ redge) {
-    const size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (e >= size_t(n) * k) return;
-    const unsigned j = knn[e];
-    if (j < n) redge[rstart[j] + atomicAdd(fill + j, 1u)] = unsigned(e);
+// Files edge e = i * k + r in the bucket of its target knn[e].
+__global__ void __launch_bounds__(kAdjBlock) k_bucket_edges(AdjointLaunch A) {
+    const unsigned e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= A.n * A.k) return;
+    const unsigned j = A.knn[e];
+    if (j >= A.n) return;
+    const unsigned slot = atomicAdd(A.fill + j, 1u);
+    if (slot < kBucket) {
+        A.bucket[size_t(j) * kBucket + slot] = e;
+    } else {
+        const unsigned o = atomicAdd(A.fill + A.n, 1u);
+        A.ovf[2 * size_t(o)] = j;
+        A.ovf[2 * size_t(o) + 1] = e;
+    }
 }
 
 // Agent j's input adjoints: its own terms, then the terms of the edges into
-// it in ascending edge order, added to lp_out / lv_out.  Buckets of up to
-// kGatherSort edges are sorted in a local array; longer ones (not met in
-// practice: in-degrees stay near k) are walked by repeated minimum search.
-constexpr unsigned kGatherSort = 64;
-
+// it in ascending edge order, added to lp_out / lv_out.  Up to kBucket edges
+// (in-degrees stay near k) are sorted in a local array; an agent with more
+// walks its bucket and the overflow list by repeated minimum search.
 __global__ void __launch_bounds__(kAdjBlock) k_adjoint_gather(AdjointLaunch A) {
     const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= A.n) return;
-    const unsigned lo = A.rstart[j], hi = A.rstart[j + 1], deg = hi - lo;
+    const unsigned deg = A.fill[j];
+    const unsigned* bk = A.bucket + size_t(j) * kBucket;
     V3 gp = v3(A.own_p[j]), gv = v3(A.own_v[j]);
     auto add_edge = [&](unsigned e) {
         gp = add(gp, v3(A.edge_p[e]));
         gv = add(gv, v3(A.edge_v[e]));
     };
-    if (deg <= kGatherSort) {
-        unsigned es[kGatherSort];
+    if (deg <= kBucket) {
+        unsigned es[kBucket];
         for (unsigned t = 0; t < deg; ++t) {  // insertion sort, ascending
-            const unsigned e = A.redge[lo + t];
+            const unsigned e = bk[t];
             unsigned q = t;
             while (q > 0 && es[q - 1] > e) {
                 es[q] = es[q - 1];
@@ -260,11 +255,17 @@ __global__ void __launch_bounds__(kAdjBlock) k_adjoint_gather(AdjointLaunch A) {
         }
         for (unsigned t = 0; t < deg; ++t) add_edge(es[t]);
     } else {
+        const unsigned n_ovf = A.fill[A.n];
         unsigned last = 0;
         for (unsigned t = 0; t < deg; ++t) {
             unsigned best = UINT_MAX;
-            for (unsigned q = lo; q < hi; ++q) {
-                const unsigned e = A.redge[q];
+            for (unsigned q = 0; q < kBucket; ++q) {
+                const unsigned e = bk[q];
+                if ((t == 0 || e > last) && e < best) best = e;
+            }
+            for (unsigned q = 0; q < n_ovf; ++q) {
+                if (A.ovf[2 * size_t(q)] != j) continue;
+                const unsigned e = A.ovf[2 * size_t(q) + 1];
                 if ((t == 0 || e > last) && e < best) best = e;
             }
             add_edge(best);
@@ -282,8 +283,8 @@ unsigned adjoint_blocks(unsigned n) { return n ? (n + kAdjBlock - 1) / kAdjBlock
 
 size_t adjoint_scratch_bytes(unsigned n, unsigned k) {
     const size_t nk = size_t(n) * k;
-    return nk * 32 + size_t(n) * 32 + (size_t(n) + 1) * 8 + nk * 4 +
-           (size_t(scan_tile_count(n + 1)) + 1) * 4 + 8 * 256;
+    return nk * 32 + size_t(n) * 32 + (size_t(n) + 1) * 4 + size_t(n) * kBucket * 4 + nk * 8 +
+           6 * 256;
 }
 
 // Carves the scratch of one adjoint step out of `base` (adjoint_scratch_bytes).
@@ -300,25 +301,20 @@ void adjoint_scratch_bind(AdjointLaunch& A, void* base, unsigned n, unsigned k) 
     o = align(o + size_t(n) * 16);
     A.own_v = reinterpret_cast<float4*>(b + o);
     o = align(o + size_t(n) * 16);
-    A.indeg = reinterpret_cast<unsigned*>(b + o);
+    A.fill = reinterpret_cast<unsigned*>(b + o);
     o = align(o + (size_t(n) + 1) * 4);
-    A.rstart = reinterpret_cast<unsigned*>(b + o);
-    o = align(o + (size_t(n) + 1) * 4);
-    A.redge = reinterpret_cast<unsigned*>(b + o);
-    o = align(o + nk * 4);
-    A.tile = reinterpret_cast<unsigned*>(b + o);
+    A.bucket = reinterpret_cast<unsigned*>(b + o);
+    o = align(o + size_t(n) * kBucket * 4);
+    A.ovf = reinterpret_cast<unsigned*>(b + o);
 }
 
 gs_status launch_flock_adjoint(const AdjointLaunch& A, const StepDev& p, cudaStream_t st) {
     if (A.k == 0 || A.k > 32) return fail(GS_ERR_INVALID_ARG, "adjoint needs 1 <= k <= 32");
     if (A.n == 0) return GS_OK;
-    const size_t nk = size_t(A.n) * A.k;
-    const unsigned eb = unsigned((nk + kAdjBlock - 1) / kAdjBlock);
-    // reverse-KNN index of this step's lists
-    GS_CUDA(cudaMemsetAsync(A.indeg, 0, (size_t(A.n) + 1) * 4, st));
-    k_rev_count<<<eb, kAdjBlock, 0, st>>>(A.knn, A.n, A.k, A.indeg);
-    GS_TRY(scan_counts(A.indeg, A.rstart, A.n, A.tile, st));  // zeroes indeg
-    k_rev_fill<<<eb, kAdjBlock, 0, st>>>(A.knn, A.n, A.k, A.rstart, A.indeg, A.redge);
+    if (size_t(A.n) * A.k > 0xffffffffull) return fail(GS_ERR_INVALID_ARG, "too many KNN edges");
+    // bucket fill counts and the overflow count start at zero
+    GS_CUDA(cudaMemsetAsync(A.fill, 0, (size_t(A.n) + 1) * 4, st));
+    k_bucket_edges<<<adjoint_blocks(A.n * A.k), kAdjBlock, 0, st>>>(A);
     // each agent's terms and its edges' terms, then the gather
     k_flock_adjoint<<<adjoint_blocks(A.n), kAdjBlock, 0, st>>>(A, p);
     k_adjoint_gather<<<adjoint_blocks(A.n), kAdjBlock, 0, st>>>(A);

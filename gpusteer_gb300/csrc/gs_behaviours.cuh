@@ -73,6 +73,12 @@ __device__ __forceinline__ float d_estimate(float dsq) {
     return (dsq >= 0x1p-60f && dsq <= 0x1p60f) ? r : __int_as_float(0x7fffffff);
 }
 
+// The reference's f = dot(dir, offset / d), d = sqrtf(dsq), out of line: the
+// gate decides almost every test, so this stays out of the unrolled loops.
+static __device__ __noinline__ float forward_component(V3 dir, V3 offset, float dsq) {
+    return dot(dir, dvd(offset, sqrtf(dsq)));
+}
+
 // 1: f > c; 0: f <= c; -1: undecided (the caller evaluates the reference's
 // expression).  g = dot(dir, offset), de = d_estimate(dsq).
 __device__ __forceinline__ int angle_decide(float g, float de, float c, AngleGate gate) {

@@ -53,8 +53,7 @@ static void release_fused(gs_group g) {
     dfree(g->retry_count);
     dfree(g->retry_knn);
     dfree(g->d_stat);
-    dfree(g->scan_state);
-    g->scan_state_cells = 0;
+    dfree(g->d_bar);
     db_release(g->fdb);
     g->fused_k_alloc = 0;
 }
@@ -803,8 +802,9 @@ static gs_status check_device_flags(gs_group g) {
     GS_CUDA(cudaStreamSynchronize(g->stream));
     if (flags) {
         GS_CUDA(cudaMemsetAsync(g->d_err, 0, sizeof(unsigned), g->stream));
-        if (flags & kErrScanTimeout)
-            return fail(GS_ERR_TIMEOUT, "fused step: a wait in the cell scan ran out (state void)");
+        if (flags & kErrBarrierTimeout)
+            return fail(GS_ERR_TIMEOUT,
+                        "persistent step: a grid barrier wait ran out (state void; upload again)");
         return fail(GS_ERR_STATE, "fused step: inconsistent cell counts (state not updated)");
     }
     return GS_OK;
@@ -1560,6 +1560,8 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         GS_TRY(dalloc(&g->retry_count, 1));
         GS_TRY(dalloc(&g->retry_knn, size_t(std::min<size_t>(n, kRetryListCap)) * kRetryListK));
         GS_TRY(dalloc(&g->d_stat, 1));
+        GS_TRY(dalloc(&g->d_bar, 2));
+        GS_CUDA(cudaMemset(g->d_bar, 0, 2 * sizeof(unsigned)));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
         GS_CUDA(cudaMemset(g->retry_count, 0, sizeof(unsigned)));
         GS_CUDA(cudaDeviceSynchronize());
@@ -1570,13 +1572,6 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         g->scene_alloc = n_scenes;
     }
     if (g->fdb.cells != C) GS_TRY(db_reserve(g->fdb, 0, C));
-    if (g->scan_state_cells != C) {
-        dfree(g->scan_state);
-        GS_TRY(dalloc(&g->scan_state, scan_state_bytes(C)));
-        GS_CUDA(cudaMemset(g->scan_state, 0, scan_state_bytes(C)));
-        GS_CUDA(cudaDeviceSynchronize());
-        g->scan_state_cells = C;
-    }
     if (walls && (!g->w0 || g->fused_k_alloc < k)) {
         const size_t n = g->capacity;
         dfree(g->w0);
@@ -1612,12 +1607,26 @@ struct WallsDev {
     const unsigned* cell_start = nullptr;
 };
 
-// One step's launches: scan, permute, fused (+ exact redo).
+// One step's launches: scan, permute, fused (+ exact redo); or, for a
+// supported step with the persistent form on, one launch for all of them.
 static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, unsigned C,
                            PhaseHook* hook) {
     cudaStream_t st = g->stream;
+    if (d.persistent && persistent_supported(d)) {
+        PersistLaunch P;
+        P.start = g->fdb.start;
+        P.tile = g->fdb.tile;
+        P.C = C;
+        P.T = scan_tile_count(C);
+        P.bar = g->d_bar;
+        P.limit = d.bar_limit;
+        if (hook) hook->mark(2, true);
+        GS_TRY(fused_step_persistent(L, d, P, st));
+        if (hook) hook->mark(2, false);
+        return GS_OK;
+    }
     if (hook) hook->mark(0, true);
-    GS_TRY(scan_counts_onepass(g->fdb.count, g->fdb.start, C, g->scan_state, g->d_err, st));
+    GS_TRY(scan_counts2(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
     if (hook) hook->mark(0, false);
     if (hook) hook->mark(1, true);
     GS_TRY(fused_permute(L, d.wrap_mode, d.dirty != 0, st));
@@ -1709,6 +1718,9 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
     FusedLaunch L;
     bool dirty = false;
     g->frame_cells = 0;
+    // part of the graph key: a changed form or limit captures again
+    d.persistent = g->persistent ? 1u : 0u;
+    d.bar_limit = g->bar_limit ? g->bar_limit : kBarrierPollsDefault;
     GS_TRY(fused_setup(g, d, grid, C, agent_scene, w, L, dirty));
     Profiler prof(g);
     PhaseHook* hook = g->profiling ? &prof : nullptr;
@@ -1798,6 +1810,18 @@ gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_p
     GS_TRY(gs_group_upload(g, in, n));
     GS_TRY(gs_step(g, bins, walls, p, steps));
     return gs_group_download(g, out);
+}
+
+gs_status gs_group_set_persistent(gs_group g, int enable) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    g->persistent = enable != 0;
+    return GS_OK;
+}
+
+gs_status gs_group_set_barrier_limit(gs_group g, unsigned polls) {
+    if (!g) return fail(GS_ERR_INVALID_ARG, "null group");
+    g->bar_limit = polls;
+    return GS_OK;
 }
 
 gs_status gs_group_set_graphs(gs_group g, int enable) {

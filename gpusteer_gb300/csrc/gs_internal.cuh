@@ -186,8 +186,9 @@ struct gs_group_s {
     bool accum_dirty;      // steering / applied may be non-zero
     int pending_wrap;      // wrap mode the pending cell counts were taken with
     unsigned fused_k_alloc;
-    unsigned char* scan_state;  // single-pass scan control and tile words (scan_state_bytes)
-    unsigned scan_state_cells;  // C it is sized for
+    bool persistent;       // run supported steps as one persistent launch
+    unsigned bar_limit;    // its barrier poll limit (0: default)
+    unsigned* d_bar;       // its grid barrier (2 words)
     // phase profiling (gs_group_set_profiling)
     bool profiling;
     std::vector<cudaEvent_t>* prof_events;  // pairs of (start, stop) per recorded phase

@@ -13,75 +13,20 @@
 
 #include "gs_behaviours.cuh"
 #include "gs_knn.cuh"
+#include "gs_scan.cuh"
 
 #include "gs_launch.h"
 
 namespace gs {
 
-// ---- exclusive scan -----------------------------------------------------------------
-constexpr unsigned kScanItems = 16;
-constexpr unsigned kScanTile = kBlock * kScanItems;
-
+// ---- exclusive scan (device code in gs_scan.cuh) ----------------------------------
 unsigned scan_tile_count(unsigned C) { return (C + kScanTile - 1) / kScanTile; }
-
-__device__ __forceinline__ unsigned block_exclusive_sum(unsigned v, unsigned* warp_sums,
-                                                        unsigned& total) {
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= unsigned(o)) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned w = lane < kBlock / 32 ? warp_sums[lane] : 0u;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= unsigned(o)) w += y;
-        }
-        if (lane < kBlock / 32) warp_sums[lane] = w;
-    }
-    __syncthreads();
-    total = warp_sums[kBlock / 32 - 1];
-    const unsigned before = warp ? warp_sums[warp - 1] : 0u;
-    __syncthreads();
-    return before + x - v;
-}
-
-// Loads tile t of count[] into shared memory (coalesced), returns this
-// thread's run of kScanItems consecutive items through `items`.
-__device__ __forceinline__ void load_tile(const unsigned* count, unsigned C, unsigned t,
-                                          unsigned* sh, unsigned items[kScanItems]) {
-    const unsigned base = t * kScanTile;
-#pragma unroll
-    for (unsigned j = 0; j < kScanItems; ++j) {
-        const unsigned i = j * kBlock + threadIdx.x;
-        sh[i + i / 32] = (base + i < C) ? count[base + i] : 0u;
-    }
-    __syncthreads();
-#pragma unroll
-    for (unsigned j = 0; j < kScanItems; ++j) {
-        const unsigned i = threadIdx.x * kScanItems + j;
-        items[j] = sh[i + i / 32];
-    }
-    __syncthreads();
-}
 
 __global__ void __launch_bounds__(kBlock) k_scan_reduce(const unsigned* __restrict__ count,
                                                         unsigned C, unsigned* __restrict__ tile) {
     __shared__ unsigned sh[kScanTile + kScanTile / 32];
     __shared__ unsigned ws[kBlock / 32];
-    unsigned items[kScanItems];
-    load_tile(count, C, blockIdx.x, sh, items);
-    unsigned s = 0;
-#pragma unroll
-    for (unsigned j = 0; j < kScanItems; ++j) s += items[j];
-    unsigned total;
-    block_exclusive_sum(s, ws, total);
-    if (threadIdx.x == 0) tile[blockIdx.x] = total;
+    scan_reduce_tile(count, C, blockIdx.x, sh, ws, tile);
 }
 
 // One block scans the tile totals in place (exclusive) and writes start[C].
@@ -162,130 +107,28 @@ gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* ti
     return GS_OK;
 }
 
-// ---- single-pass exclusive scan (the fused engine's counting sort) ---------------
-// Decoupled look-back: each block takes the next tile by ticket, so it only
-// ever waits on tiles that blocks already running hold; it publishes its tile
-// sum, then walks back over its predecessors' published words, 32 at a time,
-// until it meets one that carries an inclusive prefix, and publishes its own.
-// A word is (epoch:30 | flag:2 | value:32).  The epoch lives on the device
-// and the last block of each scan advances it (and resets the ticket), so
-// words left by earlier scans read as not ready without being cleared, also
-// across CUDA graph replays.  Every wait is bounded: a block that waits too
-// long sets kErrScanTimeout in err and goes on (the step is then void and the
-// host reports GS_ERR_TIMEOUT).  One launch reads each count once and writes
-// start and the zeroed count, against three launches and two reads.
-constexpr unsigned long long kScanAgg = 1ull << 32, kScanInc = 2ull << 32;
-constexpr unsigned kScanSpinLimit = 1u << 20;
-
-__device__ __forceinline__ unsigned long long ld_volatile64(const unsigned long long* p) {
-    return *reinterpret_cast<const volatile unsigned long long*>(p);
-}
-
-__global__ void __launch_bounds__(kBlock) k_scan_onepass(unsigned* __restrict__ count, unsigned C,
-                                                         unsigned* __restrict__ start,
-                                                         unsigned long long* state, ScanCtl* ctl,
-                                                         unsigned T, unsigned* __restrict__ err) {
+// ---- two-launch exclusive scan (the fused engine's counting sort) ----------------
+// k_scan_reduce writes each tile's total; then every block of k_scan_apply_prefix
+// sums the totals of the tiles before its own (a few thousand words from L2)
+// and writes its tile's starts.  Two launches instead of three (no one-block
+// pass over the tile totals) and no block ever waits on another.
+__global__ void __launch_bounds__(kBlock) k_scan_apply_prefix(unsigned* __restrict__ count,
+                                                              unsigned C,
+                                                              const unsigned* __restrict__ tile,
+                                                              unsigned* __restrict__ start,
+                                                              unsigned T) {
     __shared__ unsigned sh[kScanTile + kScanTile / 32];
     __shared__ unsigned ws[kBlock / 32];
-    __shared__ unsigned s_tile, s_epoch, s_prefix;
-    if (threadIdx.x == 0) {
-        s_tile = atomicAdd(&ctl->ticket, 1u);
-        s_epoch = *reinterpret_cast<volatile unsigned*>(&ctl->epoch);
-    }
-    __syncthreads();
-    const unsigned t = s_tile;
-    const unsigned long long ep = static_cast<unsigned long long>(s_epoch & 0x3fffffffu) << 34;
-    unsigned items[kScanItems];
-    load_tile(count, C, t, sh, items);
-    unsigned sum = 0;
-#pragma unroll
-    for (unsigned j = 0; j < kScanItems; ++j) sum += items[j];
-    unsigned total;
-    unsigned run = block_exclusive_sum(sum, ws, total);
-    if (threadIdx.x < 32) {
-        const unsigned lane = threadIdx.x;
-        if (lane == 0)
-            *reinterpret_cast<volatile unsigned long long*>(state + t) =
-                ep | (t == 0 ? kScanInc : kScanAgg) | total;
-        unsigned prefix = 0;
-        if (t > 0) {
-            int hi = int(t) - 1;  // the window is tiles hi, hi - 1, ..., hi - 31
-            for (;;) {
-                const int idx = hi - int(lane);
-                unsigned long long w = ep | kScanInc;  // before tile 0: an inclusive 0
-                if (idx >= 0) {
-                    unsigned spins = 0;
-                    for (;;) {
-                        w = ld_volatile64(state + idx);
-                        if ((w >> 34) == (ep >> 34) && (w & (3ull << 32)) != 0) break;
-                        if (++spins > kScanSpinLimit) {
-                            atomicOr(err, kErrScanTimeout);
-                            w = ep | kScanInc;
-                            break;
-                        }
-                        __nanosleep(64);
-                    }
-                }
-                const unsigned inc = __ballot_sync(0xffffffffu, (w & kScanInc) != 0);
-                const int first = inc ? __ffs(inc) - 1 : 32;  // the nearest inclusive word
-                unsigned part = int(lane) <= first ? unsigned(w) : 0u;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                prefix += part;
-                if (inc) break;
-                hi -= 32;
-            }
-        }
-        if (lane == 0) {
-            if (t > 0)
-                *reinterpret_cast<volatile unsigned long long*>(state + t) =
-                    ep | kScanInc | (prefix + total);
-            s_prefix = prefix;
-        }
-    }
-    __syncthreads();
-    run += s_prefix;
-#pragma unroll
-    for (unsigned j = 0; j < kScanItems; ++j) {
-        const unsigned i = threadIdx.x * kScanItems + j;
-        sh[i + i / 32] = run;
-        run += items[j];
-    }
-    __syncthreads();
-    const unsigned base = t * kScanTile;
-#pragma unroll
-    for (unsigned j = 0; j < kScanItems; ++j) {
-        const unsigned i = j * kBlock + threadIdx.x;
-        if (base + i < C) {
-            start[base + i] = sh[i + i / 32];
-            count[base + i] = 0u;
-        }
-    }
-    if (threadIdx.x == 0) {
-        if (t == T - 1) start[C] = s_prefix + total;
-        // the last block to finish readies the control block for the next scan
-        __threadfence();
-        if (atomicAdd(&ctl->done, 1u) == T - 1) {
-            ctl->ticket = 0;
-            ctl->done = 0;
-            atomicAdd(&ctl->epoch, 1u);
-        }
-    }
+    scan_apply_tile(count, C, tile, start, T, blockIdx.x, sh, ws);
 }
 
-unsigned long long* scan_state_words(void* scan_state) {
-    return reinterpret_cast<unsigned long long*>(static_cast<char*>(scan_state) + sizeof(ScanCtl));
-}
-
-size_t scan_state_bytes(unsigned C) { return sizeof(ScanCtl) + size_t(scan_tile_count(C)) * 8; }
-
-gs_status scan_counts_onepass(unsigned* count, unsigned* start, unsigned C, void* scan_state,
-                              unsigned* err, cudaStream_t st) {
+gs_status scan_counts2(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
+                       cudaStream_t st) {
     const unsigned T = scan_tile_count(C);
     if (T == 0) return GS_OK;
-    k_scan_onepass<<<T, kBlock, 0, st>>>(count, C, start, scan_state_words(scan_state),
-                                         static_cast<ScanCtl*>(scan_state), T, err);
-    GS_LAUNCHED("scan_onepass");
+    k_scan_reduce<<<T, kBlock, 0, st>>>(count, C, tile);
+    k_scan_apply_prefix<<<T, kBlock, 0, st>>>(count, C, tile, start, T);
+    GS_LAUNCHED("scan2");
     return GS_OK;
 }
 

@@ -149,6 +149,25 @@ __device__ __forceinline__ bool boundary_unsure(unsigned last, unsigned out_min)
 // The listed slots out[r * stride] (r < k, in key order, UINT_MAX after the
 // last neighbour) against the exact (distance, index) order, for the adjacent
 // entries whose T are within one unit (the others are ordered by their keys).
+// The exact comparisons of the near pairs (bit i: entries i - 1 and i of the
+// register list, first listed entry at register `first`), out of line: few
+// agents have any.
+static __device__ __noinline__ bool near_pairs_check(unsigned near, int first, V3 p,
+                                                     const float4* __restrict__ pos_id,
+                                                     const unsigned* out, unsigned stride) {
+    while (near) {
+        const int i = __ffs(int(near)) - 1;
+        near &= near - 1;
+        const unsigned r = unsigned(i - first);
+        const float4 qa = __ldg(pos_id + out[(r - 1) * stride]);
+        const float4 qb = __ldg(pos_id + out[r * stride]);
+        if (!knn_less(distance(p, v3(qa)), __float_as_uint(qa.w), distance(p, v3(qb)),
+                      __float_as_uint(qb.w)))
+            return false;
+    }
+    return true;
+}
+
 template <int KMAX, unsigned EBITS>
 __device__ __forceinline__ bool near_pairs_ordered(const unsigned (&key)[KMAX], int k, V3 p,
                                                    const float4* __restrict__ pos_id,
@@ -158,17 +177,7 @@ __device__ __forceinline__ bool near_pairs_ordered(const unsigned (&key)[KMAX], 
     for (int i = 1; i < KMAX; ++i)
         if (i > KMAX - k && key[i] != KEY32_EMPTY && (key[i] >> EBITS) < (key[i - 1] >> EBITS) + 2u)
             near |= 1u << i;
-    while (near) {
-        const int i = __ffs(near) - 1;
-        near &= near - 1;
-        const unsigned r = unsigned(i - (KMAX - k));
-        const float4 qa = __ldg(pos_id + out[(r - 1) * stride]);
-        const float4 qb = __ldg(pos_id + out[r * stride]);
-        if (!knn_less(distance(p, v3(qa)), __float_as_uint(qa.w), distance(p, v3(qb)),
-                      __float_as_uint(qb.w)))
-            return false;
-    }
-    return true;
+    return near == 0 || near_pairs_check(near, KMAX - k, p, pos_id, out, stride);
 }
 
 template <int KMAX>

@@ -11,16 +11,10 @@ namespace gs {
 gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
                       cudaStream_t st);
 unsigned scan_tile_count(unsigned C);
-// The same scan in one launch (decoupled look-back), for the fused engine.
-// scan_state: scan_state_bytes(C) bytes, zeroed once when allocated; err gets
-// kErrScanTimeout if a wait ran out.
-struct ScanCtl {
-    unsigned ticket, done, epoch, pad;
-};
-constexpr unsigned kErrScanTimeout = 4u;
-size_t scan_state_bytes(unsigned C);
-gs_status scan_counts_onepass(unsigned* count, unsigned* start, unsigned C, void* scan_state,
-                              unsigned* err, cudaStream_t st);
+// The same scan in two launches (tile totals, then each block sums the
+// totals before its tile): the fused engine's counting sort.
+gs_status scan_counts2(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
+                       cudaStream_t st);
 // Allocates db for C cells and n agents (keeps existing buffers when large enough).
 gs_status db_reserve(Database& db, unsigned n, unsigned C);
 void db_release(Database& db);
@@ -152,12 +146,28 @@ struct StepDev {
     unsigned enum_cap;  // candidate capacity of the fast KNN scan (32, 64: collecting; 128, 256: streaming)
     unsigned block;     // threads per block of the fused launches (0: 256)
     unsigned flat;      // the grid is one cell high (y): boxes hold 3 rows of cells
+    unsigned persistent;  // run a supported step as one persistent launch
+    unsigned bar_limit;   // its barrier poll limit
     PathDev path;       // path following (GS_B_FOLLOW_PATH)
     float path_time, w_path;
     unsigned mask_path;
 };
 constexpr unsigned NEED_SEP = 1, NEED_ALI = 2, NEED_COH = 4, NEED_AVOID = 8, NEED_CLOSE = 16,
                    NEED_WALLS = 32;
+// Bits of the fused step's device error word.
+constexpr unsigned kErrCounts = 1u;          // inconsistent cell counts
+constexpr unsigned kErrBarrierTimeout = 2u;  // a persistent step's barrier wait ran out
+
+// The persistent step's extra arguments: the scan's writable starts and tile
+// totals, the barrier words (zeroed before each launch) and the poll limit.
+struct PersistLaunch {
+    unsigned* start;
+    unsigned* tile;
+    unsigned C, T;
+    unsigned* bar;  // 2 words
+    unsigned limit;
+};
+constexpr unsigned kBarrierPollsDefault = 1u << 23;  // about a second of 100 ns polls
 
 // The exact redo's precomputed neighbour lists: kRetryListK slots per entry
 // (the largest KMAX), for up to kRetryListCap entries per step.
@@ -205,6 +215,11 @@ gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStr
 struct PhaseHook {
     virtual void mark(int phase, bool begin) = 0;
 };
+// The wall/rest step as one cooperative persistent launch (see gs_step.cu);
+// persistent_supported tells which steps have that build.
+bool persistent_supported(const StepDev& p);
+gs_status fused_step_persistent(const FusedLaunch& L, const StepDev& p, const PersistLaunch& P,
+                                cudaStream_t st);
 gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st,
                      PhaseHook* hook = nullptr);
 // slot_of: capacity words of scratch (each agent's slot, then the gather).
@@ -223,10 +238,13 @@ struct AdjointLaunch {
     float4 *lp_out, *lv_out;  // d loss / d (position, velocity) before the step; +=
     float* wpart;             // [blocks * 4] per-block sums: separation, alignment, cohesion
     unsigned n, k;
-    // scratch (adjoint_scratch_bind): per-edge and own terms, reverse-KNN index
+    // scratch (adjoint_scratch_bind): per-edge and own terms; per target agent
+    // its fill count (fill[n]: overflow count) and kBucket edge slots; the
+    // overflow list of (target, edge) pairs
     float4 *edge_p, *edge_v, *own_p, *own_v;
-    unsigned *indeg, *rstart, *redge, *tile;
+    unsigned *fill, *bucket, *ovf;
 };
+constexpr unsigned kBucket = 48;
 unsigned adjoint_blocks(unsigned n);
 size_t adjoint_scratch_bytes(unsigned n, unsigned k);
 void adjoint_scratch_bind(AdjointLaunch& A, void* base, unsigned n, unsigned k);

@@ -23,6 +23,7 @@
 // (plugins/BoidsGroup.cpp:606-637, plugins/ChokePointNew.cpp:586-630).
 #include "gs_behaviours.cuh"
 #include "gs_knn.cuh"
+#include "gs_scan.cuh"
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -94,16 +95,11 @@ gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellran
 }
 
 // A (slot i) -> B (slot start[cell] + rank), wrapping the position.
-__global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n,
-                                                    const uint2* __restrict__ cellrank,
-                                                    const unsigned* __restrict__ start,
-                                                    const Scene* __restrict__ scenes,
-                                                    int wrap_mode, int dirty,
-                                                    unsigned* __restrict__ err,
-                                                    unsigned* __restrict__ retry_count) {
-    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) *retry_count = 0u;  // the fused launch that follows refills it
-    if (i >= n) return;
+__device__ __forceinline__ void permute_agent(const Fused& A, const Fused& B, unsigned n,
+                                              const uint2* __restrict__ cellrank,
+                                              const unsigned* __restrict__ start,
+                                              const Scene* __restrict__ scenes, int wrap_mode,
+                                              int dirty, unsigned* __restrict__ err, unsigned i) {
     const uint2 cr = cellrank[i];
     const unsigned dst = start[cr.x] + cr.y;
     if (dst >= n) {  // inconsistent counts: record and write nothing
@@ -120,6 +116,19 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
     B.f[3][dst] = A.f[3][i];
     B.f[4][dst] = f4v;
     if (dirty) B.f[5][dst] = A.f[5][i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n,
+                                                    const uint2* __restrict__ cellrank,
+                                                    const unsigned* __restrict__ start,
+                                                    const Scene* __restrict__ scenes,
+                                                    int wrap_mode, int dirty,
+                                                    unsigned* __restrict__ err,
+                                                    unsigned* __restrict__ retry_count) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *retry_count = 0u;  // the fused launch that follows refills it
+    if (i >= n) return;
+    permute_agent(A, B, n, cellrank, start, scenes, wrap_mode, dirty, err, i);
 }
 
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st) {
@@ -169,7 +178,7 @@ __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned n
             const int da = ang_a ? angle_decide(g, de, fa.cos_max, ga) : 0;
             const int dc = ang_c ? angle_decide(g, de, fc.cos_max, gc) : 0;
             if ((ds | da | dc) < 0) {
-                const float fwd = dot(me.dir, dvd(offset, sqrtf(dsq)));
+                const float fwd = forward_component(me.dir, offset, dsq);
                 in_s = in_s || (ds < 0 ? fwd > fs.cos_max : ds > 0);
                 in_a = in_a || (da < 0 ? fwd > fa.cos_max : da > 0);
                 in_c = in_c || (dc < 0 ? fwd > fc.cos_max : dc > 0);
@@ -282,10 +291,27 @@ __device__ __forceinline__ Self load_rest(const Fused& B, unsigned s, V3 pos, fl
 }
 
 // ---- KNN of one agent (fast path, or exact redo) ----------------------------------
+// The exact (distance, index) list of one agent out of line: the collecting
+// scan's kernels call it for the rare agents whose fast scan could not vouch
+// for its order (or overflowed the tables), so its 64-bit list takes neither
+// registers nor instruction cache from the common path.
+template <int KMAX>
+static __device__ __noinline__ void knn_exact_out_of_line(int k, V3 p, unsigned self_id,
+                                                          const Grid& g, Box b,
+                                                          unsigned cell_offset,
+                                                          const unsigned* __restrict__ start,
+                                                          const float4* __restrict__ pos_id,
+                                                          unsigned* col, unsigned stride) {
+    knn_neighbours_exact<KMAX>(k, p, self_id, g, b, cell_offset, start, pos_id, col, stride);
+}
+
 // Writes the agent's neighbour slots in (distance, index) order to its shared
-// column: at col[(ENUM + r) * bd] on the fast path, col[r * bd] on the exact
-// path; returns the column offset of entry 0, or UINT_MAX when the fast path
-// gave up and the agent was appended to the retry list.
+// column: at col[(ENUM + r) * bd] on the collecting scan's fast path,
+// col[r * bd] otherwise; returns the column offset of entry 0.  After the
+// collecting scan (sparse boxes: a few agents per step give up, mostly
+// distance ties) the agent is redone inline; after the streaming scan it is
+// appended to the retry list for the warp-per-agent search and the redo
+// launch, and UINT_MAX is returned.
 template <int KMAX, unsigned ENUM, bool EXACT, bool FLAT>
 __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDev& p, unsigned s,
                                               unsigned it, V3 pos, unsigned id, const Scene& sc,
@@ -310,9 +336,14 @@ __device__ __forceinline__ unsigned agent_knn(const FusedLaunch& L, const StepDe
         if (knn_neighbours_stream<KMAX, EBITS, FLAT>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
                                                L.start, L.B.f[0], col, bd))
             return 0;
-    } else if (knn_neighbours_fast<KMAX, ENUM>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
-                                               L.start, L.B.f[0], col, col + ENUM * bd, bd)) {
-        return ENUM;
+    } else {
+        if (knn_neighbours_fast<KMAX, ENUM>(int(p.k), pos, id, sc.grid, box, sc.cell_offset,
+                                            L.start, L.B.f[0], col, col + ENUM * bd, bd))
+            return ENUM;
+        knn_exact_out_of_line<KMAX>(int(p.k), pos, id, sc.grid, box, sc.cell_offset, L.start,
+                                    L.B.f[0], col, bd);
+        atomicAdd(L.retry_count, 1u);  // counted (gs_group_exact_redos), not listed
+        return 0;
     }
     L.retry[atomicAdd(L.retry_count, 1u)] = s;
     return UINT_MAX;
@@ -354,18 +385,15 @@ __device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, u
 // streaming scan only (crowded boxes, where the serial pass is long).
 constexpr unsigned kRetryWarpKeys = 256;
 
+// The warp's entries e = first, first + stride, ...; keys / slots: the
+// warp's kRetryWarpKeys-entry shared tables.
 template <int KMAX>
-__global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) {
-    __shared__ unsigned long long sk[kBlock / 32][kRetryWarpKeys];
-    __shared__ unsigned ss[kBlock / 32][kRetryWarpKeys];
-    const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    const unsigned nw = gridDim.x * (blockDim.x >> 5);
+__device__ __forceinline__ void retry_lists(const FusedLaunch& L, const StepDev& p, unsigned first,
+                                            unsigned stride, unsigned long long* keys,
+                                            unsigned* slots) {
+    const unsigned lane = threadIdx.x & 31u;
     const unsigned count = min(*L.retry_count, L.retry_cap);
-    unsigned long long* keys = sk[w];
-    unsigned* slots = ss[w];
-    // warp w of block b takes entries w * gridDim.x + b, + nw, ...: a few
-    // hundred entries land one per block across every SM
-    for (unsigned e = w * gridDim.x + blockIdx.x; e < count; e += nw) {
+    for (unsigned e = first; e < count; e += stride) {
         const unsigned s = L.retry[e];
         const float4 f0 = L.B.f[0][s];
         const V3 pos = v3(f0);
@@ -429,8 +457,19 @@ __global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) 
     }
 }
 
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) {
+    __shared__ unsigned long long sk[kBlock / 32][kRetryWarpKeys];
+    __shared__ unsigned ss[kBlock / 32][kRetryWarpKeys];
+    const unsigned w = threadIdx.x >> 5;
+    // warp w of block b takes entries w * gridDim.x + b, + nw, ...: a few
+    // hundred entries land one per block across every SM
+    retry_lists<KMAX>(L, p, w * gridDim.x + blockIdx.x, gridDim.x * (blockDim.x >> 5), sk[w],
+                      ss[w]);
+}
+
 // ---- whole step without walls -------------------------------------------------------
-constexpr unsigned kNbrChunk = 4;
+constexpr unsigned kNbrChunk = 2;
 
 // NEEDC: the behaviours that read the neighbour list, fixed at compile time
 // (kNeedRuntime: taken from p.need).
@@ -538,15 +577,12 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
 }
 
 // ---- wall phase: KNN, wall KNN and avoid-walls ---------------------------------------
-template <int KMAX, int KW, unsigned ENUM, bool EXACT, bool FLAT = false>
-__global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDev p) {
-    extern __shared__ unsigned sh_col[];
-    const unsigned bd = blockDim.x;
-    unsigned* col = sh_col + threadIdx.x;
-    const unsigned step = EXACT ? gridDim.x * blockDim.x : 0u;
-    for (unsigned it = first_agent<EXACT>();; it += step) {
-        unsigned s;
-        if (!next_agent<EXACT>(L, it, s)) return;
+// Agent in slot s (entry `it` of the retry list on the exact path); col: the
+// thread's shared column (stride bd).
+template <int KMAX, int KW, unsigned ENUM, bool EXACT, bool FLAT>
+__device__ __forceinline__ void walls_agent(const FusedLaunch& L, const StepDev& p, unsigned s,
+                                            unsigned it, unsigned* col, unsigned bd) {
+    {
         const float4 f0 = L.B.f[0][s];
         const V3 pos = v3(f0);
         const unsigned id = u(f0.w), scene = load_scene(L.B, s);
@@ -597,6 +633,19 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
         L.w0[s] = make_float4(me.pos.x, me.pos.y, me.pos.z, me.radius);
         L.w1[s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
         L.w2[s] = make_float4(steer.x, steer.y, steer.z, fb(applied));
+    }
+}
+
+template <int KMAX, int KW, unsigned ENUM, bool EXACT, bool FLAT = false>
+__global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDev p) {
+    extern __shared__ unsigned sh_col[];
+    const unsigned bd = blockDim.x;
+    unsigned* col = sh_col + threadIdx.x;
+    const unsigned step = EXACT ? gridDim.x * blockDim.x : 0u;
+    for (unsigned it = first_agent<EXACT>();; it += step) {
+        unsigned s;
+        if (!next_agent<EXACT>(L, it, s)) return;
+        walls_agent<KMAX, KW, ENUM, EXACT, FLAT>(L, p, s, it, col, bd);
         if (!EXACT) return;
     }
 }
@@ -606,10 +655,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_fused_walls(FusedLaunch L, StepDe
 // gathers, and the extra resident warps hide more of that than the spills
 // cost (0.604 -> 0.585 ms per 256-scene step against four blocks).
 template <int KMAX, unsigned NEEDC>
-__global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev p) {
+__device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& p, unsigned s) {
     const unsigned need = NEEDC == kNeedRuntime ? p.need : NEEDC;
-    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= L.n) return;
     // the neighbour pass reads position, radius, heading and speed only; the
     // rest of the state is loaded after it, so it is not held through the pass
     const float4 w0 = L.w0[s], w1 = L.w1[s];
@@ -656,6 +703,12 @@ __global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev
     store_next(L, s, me, id, scene, sc, p.wrap_mode);
 }
 
+template <int KMAX, unsigned NEEDC>
+__global__ void __launch_bounds__(kBlock, 5) k_fused_rest(FusedLaunch L, StepDev p) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < L.n) rest_agent<KMAX, NEEDC>(L, p, s);
+}
+
 // Opts a kernel into more than 48 KiB of dynamic shared memory, once per
 // kernel (outside any stream capture: the first launch of a kernel is never
 // captured, see gs_capi.cu).
@@ -689,12 +742,11 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
     const size_t smem = ENUM > 64 ? size_t(KMAX > 8 ? KMAX : 8) * bs * sizeof(unsigned)
                                   : size_t(2 * ENUM) * bs * sizeof(unsigned);
     const size_t smem_x = size_t(KMAX > 8 ? KMAX : 8) * kBlock * sizeof(unsigned);
-    // The warp-per-agent exact lists pay off for crowded boxes (the streaming
-    // scan, 40-250 candidates); with the collecting scan (sparse boxes, mostly
-    // distance ties among a dozen candidates) the redo thread's own search is
-    // shorter than the extra launch, and the redo reads no stored lists.
-    FusedLaunch Lx = L;
-    if (ENUM <= 64) Lx.retry_cap = 0;
+    // The warp-per-agent exact lists and the redo launch serve the streaming
+    // scan (crowded boxes, 40-250 candidates); the collecting scan's kernels
+    // redo their few agents inline (sparse boxes, mostly distance ties among
+    // a dozen candidates), which costs less than a launch of one agent's
+    // latency.
     if (p.need & NEED_WALLS) {
         if (hook) hook->mark(2, true);
         // flat grids (one cell high) have a 3-row build of the streaming scan
@@ -710,8 +762,10 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
             GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
             k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
         }
-        if (ENUM > 64) k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
-        k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(Lx, p);
+        if (ENUM > 64) {
+            k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
+            k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
+        }
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
         // the choke-point step (separation and neighbour avoidance) has its own build
@@ -741,8 +795,10 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
             }
         }
         if (!done) k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
-        if (ENUM > 64) k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
-        k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(Lx, p);
+        if (ENUM > 64) {
+            k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
+            k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
+        }
         if (hook) hook->mark(2, false);
     }
     GS_LAUNCHED("fused_step");
@@ -756,6 +812,150 @@ static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream
     if (p.enum_cap <= 64) return launch_fused_k<KMAX, 64>(L, p, st, hook);
     if (p.enum_cap <= 128) return launch_fused_k<KMAX, 128>(L, p, st, hook);
     return launch_fused_k<KMAX, 256>(L, p, st, hook);
+}
+
+// ---- the wall/rest step in one persistent launch ----------------------------------
+// One cooperative launch runs every phase of the step - the scan's tile totals
+// and starts, the permute, the wall phase, the warp-per-agent exact lists, the
+// exact redo and the rest phase - over a grid of co-resident blocks.  Each
+// phase is a grid-stride loop over the same device functions the separate
+// kernels run, so the results are the same bit for bit; a grid-wide barrier
+// separates the phases.  Every barrier wait is bounded: a block that polls
+// more than P.limit times, or sees that another block gave up, sets
+// kErrBarrierTimeout and returns.  A block passes a barrier only once every
+// block has arrived there, i.e. finished the phase before it, so a step that
+// gives up never feeds a phase half-written input; the step is void and the
+// host reports GS_ERR_TIMEOUT.
+struct GridBarrier {
+    unsigned count, gen;
+};
+
+__device__ __forceinline__ unsigned ld_volatile(const unsigned* a) {
+    return *reinterpret_cast<const volatile unsigned*>(a);
+}
+
+__device__ bool grid_sync(GridBarrier* bar, unsigned limit, unsigned* err) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned gen = ld_volatile(&bar->gen);
+        __threadfence();
+        if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            unsigned polls = 0;
+            while (ld_volatile(&bar->gen) == gen) {
+                if (++polls > limit || (ld_volatile(err) & kErrBarrierTimeout)) {
+                    atomicOr(err, kErrBarrierTimeout);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int KMAX>
+constexpr size_t persistent_smem() {
+    constexpr size_t scan = (kScanTile + kScanTile / 32 + kBlock / 32) * sizeof(unsigned);
+    constexpr size_t cols = size_t(KMAX) * kBlock * sizeof(unsigned);
+    constexpr size_t retry = (kBlock / 32) * kRetryWarpKeys * (sizeof(unsigned long long) + 4);
+    return scan > cols ? (scan > retry ? scan : retry) : (cols > retry ? cols : retry);
+}
+
+template <int KMAX, unsigned ENUM, unsigned NEEDC>
+__global__ void __launch_bounds__(kBlock, 4) k_step_persistent(FusedLaunch L, StepDev p,
+                                                               PersistLaunch P) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(P.bar);
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    // scan: tile totals, then starts (zeroing the counts)
+    unsigned* sh = reinterpret_cast<unsigned*>(sm);
+    unsigned* ws = sh + kScanTile + kScanTile / 32;
+    for (unsigned t = blockIdx.x; t < P.T; t += gridDim.x)
+        scan_reduce_tile(L.count, P.C, t, sh, ws, P.tile);
+    if (!grid_sync(bar, P.limit, L.err)) return;
+    for (unsigned t = blockIdx.x; t < P.T; t += gridDim.x)
+        scan_apply_tile(L.count, P.C, P.tile, P.start, P.T, t, sh, ws);
+    if (!grid_sync(bar, P.limit, L.err)) return;
+    // permute A -> B
+    if (gtid == 0) *L.retry_count = 0u;
+    for (unsigned i = gtid; i < L.n; i += nthreads)
+        permute_agent(L.A, L.B, L.n, L.cellrank, P.start, L.scenes, p.wrap_mode, p.dirty, L.err, i);
+    if (!grid_sync(bar, P.limit, L.err)) return;
+    // wall phase
+    unsigned* col = reinterpret_cast<unsigned*>(sm) + threadIdx.x;
+    for (unsigned s = gtid; s < L.n; s += nthreads)
+        walls_agent<KMAX, 8, ENUM, false, true>(L, p, s, s, col, kBlock);
+    if (!grid_sync(bar, P.limit, L.err)) return;
+    // exact lists of the redo entries, one warp per entry
+    {
+        const unsigned w = threadIdx.x >> 5;
+        unsigned long long* keys = reinterpret_cast<unsigned long long*>(sm) + w * kRetryWarpKeys;
+        unsigned* slots = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned long long*>(sm) +
+                                                      (kBlock / 32) * kRetryWarpKeys) +
+                          w * kRetryWarpKeys;
+        retry_lists<KMAX>(L, p, w * gridDim.x + blockIdx.x, gridDim.x * (kBlock / 32), keys,
+                          slots);
+    }
+    if (!grid_sync(bar, P.limit, L.err)) return;
+    // exact redo, entries spread block-fastest over the grid
+    {
+        const unsigned count = *L.retry_count;
+        for (unsigned it = threadIdx.x * gridDim.x + blockIdx.x; it < count; it += nthreads)
+            walls_agent<KMAX, 8, 32, true, false>(L, p, L.retry[it], it, col, kBlock);
+    }
+    if (!grid_sync(bar, P.limit, L.err)) return;
+    // rest phase
+    for (unsigned s = gtid; s < L.n; s += nthreads) rest_agent<KMAX, NEEDC>(L, p, s);
+}
+
+bool persistent_supported(const StepDev& p) {
+    return (p.need & NEED_WALLS) && p.enum_cap > 64 && p.k > 8 && p.k <= 16 && p.flat &&
+           p.knw <= 8;
+}
+
+template <unsigned ENUM, unsigned NEEDC>
+static gs_status launch_persistent_k(const FusedLaunch& L, const StepDev& p,
+                                     const PersistLaunch& P, cudaStream_t st) {
+    auto kern = k_step_persistent<16, ENUM, NEEDC>;
+    constexpr size_t smem = persistent_smem<16>();
+    GS_TRY(allow_smem(kern, smem));
+    int dev = 0, sms = 0, per_sm = 0;
+    GS_CUDA(cudaGetDevice(&dev));
+    GS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, smem));
+    if (per_sm < 1) return fail(GS_ERR_UNSUPPORTED, "the persistent step does not fit on an SM");
+    const unsigned grid = unsigned(per_sm) * unsigned(sms);
+    // the barrier starts from zero on every launch, also after a step that gave up
+    GS_CUDA(cudaMemsetAsync(P.bar, 0, sizeof(GridBarrier), st));
+    FusedLaunch l = L;
+    StepDev q = p;
+    PersistLaunch pp = P;
+    void* args[] = {&l, &q, &pp};
+    GS_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid),
+                                        dim3(kBlock), args, smem, st));
+    return GS_OK;
+}
+
+gs_status fused_step_persistent(const FusedLaunch& L, const StepDev& p, const PersistLaunch& P,
+                                cudaStream_t st) {
+    if (L.n == 0) return GS_OK;
+    if (!persistent_supported(p)) return fail(GS_ERR_UNSUPPORTED, "no persistent build for this step");
+    const bool sep_avoid = (p.need & kNeedList) == (NEED_SEP | NEED_AVOID);
+    if (p.enum_cap <= 128)
+        return sep_avoid ? launch_persistent_k<128, NEED_SEP | NEED_AVOID>(L, p, P, st)
+                         : launch_persistent_k<128, kNeedRuntime>(L, p, P, st);
+    return sep_avoid ? launch_persistent_k<256, NEED_SEP | NEED_AVOID>(L, p, P, st)
+                     : launch_persistent_k<256, kNeedRuntime>(L, p, P, st);
 }
 
 gs_status fused_step(const FusedLaunch& L, const StepDev& p, cudaStream_t st, PhaseHook* hook) {

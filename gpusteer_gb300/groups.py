@@ -282,8 +282,9 @@ class WallGroup:
 class _GroupRef:
     """A non-owning view of a group handle (e.g. a batch's underlying group)."""
 
-    def __init__(self, handle):
+    def __init__(self, handle, k: int):
         self._h = handle
+        self.k = int(k)
 
     @property
     def handle(self):
@@ -307,6 +308,21 @@ def set_block(group, threads: int) -> None:
     call("gs_group_set_block", group.handle, int(threads))
 
 
+def set_persistent(group, enable: bool) -> None:
+    """One persistent launch per supported step (avoid-walls first, 9 <= k <=
+    16, a flat world, the streaming KNN scan) instead of separate launches;
+    results equal the separate launches bit for bit."""
+    call("gs_group_set_persistent", group.handle, int(bool(enable)))
+    group.persistent = bool(enable)
+
+
+def set_barrier_limit(group, polls: int) -> None:
+    """Polls a persistent step's barrier wait makes before it gives up (0:
+    the default); a step that gave up is void and the next synchronize raises
+    GS_ERR_TIMEOUT."""
+    call("gs_group_set_barrier_limit", group.handle, int(polls))
+
+
 def set_knn_capacity(group, capacity: int) -> None:
     """0 = from the crowd's density; 32/64 collecting scan; 128/256 streaming."""
     call("gs_group_set_knn_capacity", group.handle, int(capacity))
@@ -321,11 +337,14 @@ def knn_capacity(group) -> int:
 
 
 def step_launches(group, walls: bool) -> int:
-    """Kernel launches of one fused step: the counting-sort scan (one
-    single-pass launch), the permute, the fused kernel (two with walls), the
-    exact redo, and with the streaming scan (capacity 128 or 256) the
-    warp-per-agent exact lists."""
-    return 1 + 1 + (2 if walls else 1) + 1 + (1 if knn_capacity(group) > 64 else 0)
+    """Kernel launches of one fused step: the counting-sort scan (two), the
+    permute, the fused kernel (two with walls), and with the streaming scan
+    (capacity 128 or 256) the warp-per-agent exact lists and the exact redo
+    (the collecting scan redoes its rare agents inline)."""
+    cap = knn_capacity(group)
+    if getattr(group, "persistent", False) and walls and cap > 64 and 8 < group.k <= 16:
+        return 1
+    return 2 + 1 + (2 if walls else 1) + (2 if cap > 64 else 0)
 
 
 class Batch:
@@ -346,7 +365,7 @@ class Batch:
         self.cells_per_scene = int(np.prod(np.asarray(world_cells, np.uint64)))
         g = C.c_void_p()
         call("gs_batch_group", h, C.byref(g))
-        self.group = _GroupRef(g)
+        self.group = _GroupRef(g, k)
 
     @property
     def handle(self):

@@ -170,6 +170,19 @@ gs_status gs_group_set_profiling(gs_group g, int enable);
  * scan could not vouch for (exact distance ties, crowded boxes) and that the
  * exact path redid; waits for the group's stream. */
 gs_status gs_group_exact_redos(gs_group g, unsigned* count);
+/* One persistent launch per fused step (no counterpart in the reference,
+ * which launches one kernel per behaviour): the scan, permute, wall phase,
+ * exact lists, exact redo and rest phase of a step with avoid-walls first,
+ * 9 <= k <= 16, a flat world (one cell high) and the streaming KNN scan
+ * (capacity 128 or 256) run in one cooperative launch with grid-wide
+ * barriers between the phases; the results equal the separate launches bit
+ * for bit.  Other steps keep the separate launches.  Off by default. */
+gs_status gs_group_set_persistent(gs_group g, int enable);
+/* Polls a barrier wait of the persistent step makes before it gives up (0:
+ * the default, about a second).  A step whose wait ran out is void: the
+ * group must be uploaded again, and gs_group_synchronize (or the next call
+ * that returns host data) reports GS_ERR_TIMEOUT. */
+gs_status gs_group_set_barrier_limit(gs_group g, unsigned polls);
 gs_status gs_group_phase_times(gs_group g, float* ms, unsigned* launches, unsigned cap);
 
 /* ---- KNNData: KNNData(nSize, nK) (KNNData.cu) ---------------------------------- */

@@ -488,8 +488,8 @@ def test_knn_capacity_reads_back():
     assert gs.knn_capacity(g) == 0
     gs.step(g, bins, walls, p, 1)
     assert gs.knn_capacity(g) in (128, 256)
-    # single-pass scan, permute, wall phase, warp-per-agent lists, redo, rest phase
-    assert gs.step_launches(g, True) == 6
+    # two scan launches, permute, wall phase, warp-per-agent lists, redo, rest phase
+    assert gs.step_launches(g, True) == 7
     gs.set_knn_capacity(g, 64)
     assert gs.knn_capacity(g) == 64
     assert gs.step_launches(g, True) == 5
@@ -729,6 +729,63 @@ def test_batched_scene_matches_oracle():
         ol.run(want, p, 12, walls=walls)
         assert_state(got.subset(slice(off, off + s.n)), want, skip_side=want.speed == 0)
         off += s.n
+
+
+def test_persistent_step_equals_separate_launches():
+    """One cooperative persistent launch per step (scan, permute, wall phase,
+    exact lists, redo and rest phase between grid-wide barriers) equals the
+    separate launches bit for bit, with graphs on and off, resumed across
+    calls."""
+    states, gaps = sc.batched_chokepoint(7, seed=3, n_range=(300, 3000))
+    p = sc.chokepoint_params(world=256.0, cell=2.0)
+    want = per_scene(states, gaps, p, 15)
+    for graphs in (True, False):
+        b = batch_setup(states, gaps, p, graphs=graphs)
+        gs.set_knn_capacity(b.group, 256)
+        gs.set_persistent(b.group, True)
+        b.step(p, 5)
+        b.step(p, 10)
+        assert_state(b.download(), want)
+        assert gs.step_launches(b.group, True) == 1
+
+
+def test_persistent_step_through_the_redo_routes():
+    """A crowd of about 20 agents per cell (184 candidates per box, past the
+    streaming scan's 128): most agents go through the persistent step's
+    warp-per-agent lists and redo phase; the result is the oracle's."""
+    p = sc.chokepoint_params()
+    bins, walls = choke_walls(p)
+    s = sc.chokepoint_agents(4000, x_range=(-14.0, 14.0), z_range=(20.0, 48.0), seed=6)
+    g = group_of(s, p.k)
+    gs.set_knn_capacity(g, 128)
+    gs.set_persistent(g, True)
+    gs.step(g, bins, walls, p, 3)
+    want = s.copy()
+    ol.run(want, p, 3, walls=walls.download())
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
+def test_persistent_barrier_timeout_is_reported():
+    """A grid barrier whose wait runs out (a limit of one poll) makes every
+    block return without feeding the next phase; synchronize reports
+    GS_ERR_TIMEOUT and the group steps correctly again after an upload."""
+    p = sc.chokepoint_params()
+    bins, walls = choke_walls(p)
+    s = sc.chokepoint_agents(10000, seed=0)
+    g = group_of(s, p.k)
+    gs.set_knn_capacity(g, 256)
+    gs.set_persistent(g, True)
+    gs.set_barrier_limit(g, 1)
+    gs.step(g, bins, walls, p, 1)
+    with pytest.raises(gs.GpuSteerError) as e:
+        g.synchronize()
+    assert e.value.status == 4  # GS_ERR_TIMEOUT
+    gs.set_barrier_limit(g, 0)
+    g.upload(s)
+    gs.step(g, bins, walls, p, 2)
+    want = s.copy()
+    ol.run(want, p, 2, walls=walls.download())
+    assert_state(g.download(), want, skip_side=want.speed == 0)
 
 
 def test_graph_replay_equals_eager_single_group():
