@@ -672,13 +672,45 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
     Accs a;
     init_accs(a, p);
     const bool need_dir = need & (NEED_ALI | NEED_AVOID);
-    for (unsigned i = 0; i < p.k; ++i) {
+    // Neighbour avoidance runs as a second pass over the neighbours whose
+    // approach time may fall in its window (about a fifth in a crowd); the
+    // others leave its accumulator unchanged, so the result is the same.  A
+    // warp then runs the exact test as often as its busiest lane needs it,
+    // not once per list entry.
+    // Neighbours kNbrChunk at a time: their slots, then their gathers, are
+    // issued together.
+    unsigned exact_avoid = 0;
+    for (unsigned i0 = 0; i0 < p.k; i0 += kNbrChunk) {
+        unsigned bs[kNbrChunk];
+        float4 b0[kNbrChunk], b1[kNbrChunk];
+#pragma unroll
+        for (unsigned j = 0; j < kNbrChunk; ++j)
+            bs[j] = i0 + j < p.k ? L.knn_slot[size_t(i0 + j) * L.n + s] : UINT_MAX;
+#pragma unroll
+        for (unsigned j = 0; j < kNbrChunk; ++j) {
+            const bool ok = bs[j] != UINT_MAX;
+            b0[j] = ok ? L.w0[bs[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+            b1[j] = ok && need_dir ? L.w1[bs[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (unsigned j = 0; j < kNbrChunk; ++j) {
+            if (bs[j] == UINT_MAX) break;
+            const unsigned i = i0 + j;
+            const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
+            accumulate(a, p, need & ~NEED_AVOID, fs, fa, fc, gs_, ga, gc, me, i, kd, v3(b0[j]),
+                       v3(b1[j]), b1[j].w, b0[j].w);
+            if ((need & NEED_AVOID) &&
+                avoid_time_may_fall_in(me, p.min_time_col, v3(b0[j]), v3(b1[j]), b1[j].w))
+                exact_avoid |= 1u << i;
+        }
+        if (bs[kNbrChunk - 1] == UINT_MAX) break;
+    }
+    while (exact_avoid) {
+        const unsigned i = unsigned(__ffs(int(exact_avoid)) - 1);
+        exact_avoid &= exact_avoid - 1;
         const unsigned bs = L.knn_slot[size_t(i) * L.n + s];
-        if (bs == UINT_MAX) break;
-        const float4 b0 = L.w0[bs];
-        const float4 b1 = need_dir ? L.w1[bs] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
-        accumulate(a, p, need, fs, fa, fc, gs_, ga, gc, me, i, kd, v3(b0), v3(b1), b1.w, b0.w);
+        const float4 b0 = L.w0[bs], b1 = L.w1[bs];
+        avoid_lite_add(a.avoid, me, i, v3(b0), v3(b1), b1.w, b0.w);
     }
     const float4 w2 = L.w2[s];
     const float4 f2 = L.B.f[2][s], f3 = L.B.f[3][s], f4v = L.B.f[4][s];
