@@ -353,6 +353,7 @@ static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev&
     for (unsigned o = 0; o < p->n_order; ++o) {
         const unsigned b = p->order[o];
         d.order[o] = b;
+        d.order_packed |= (b & 7u) << (3u * o);
         switch (b) {
             case GS_B_AVOID_WALLS:
                 if (o != 0)

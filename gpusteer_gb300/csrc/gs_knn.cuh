@@ -273,6 +273,8 @@ __device__ __forceinline__ void collect_one(unsigned s, V3 p, unsigned self_id,
     }
 }
 
+constexpr unsigned kCollectChunk = 4;
+
 // Collects every candidate of `box` into the tables; returns the count (which
 // exceeds ENUM when the tables overflowed).
 template <unsigned ENUM>
@@ -309,19 +311,20 @@ __device__ __forceinline__ unsigned collect_box(V3 p, unsigned self_id, const Gr
         }
         if (total > ENUM) return total;  // overflow: the exact path redoes the agent
         // compacted in place (self and non-finite candidates dropped): entry
-        // e is written only after entries up to e were read.  Four at a
-        // time: the four slots, then the four positions, are loaded before
-        // any key is formed, so their loads overlap.
-        for (unsigned j0 = 0; j0 < total; j0 += 4) {
-            unsigned sl[4];
-            float4 q[4];
+        // e is written only after entries up to e were read.  kCollectChunk
+        // at a time: the slots, then the positions, are loaded before any key
+        // is formed, so their loads overlap.
+        for (unsigned j0 = 0; j0 < total; j0 += kCollectChunk) {
+            unsigned sl[kCollectChunk];
+            float4 q[kCollectChunk];
 #pragma unroll
-            for (unsigned u = 0; u < 4; ++u) sl[u] = j0 + u < total ? slot_tab[(j0 + u) * stride] : 0u;
+            for (unsigned u = 0; u < kCollectChunk; ++u)
+                sl[u] = j0 + u < total ? slot_tab[(j0 + u) * stride] : 0u;
 #pragma unroll
-            for (unsigned u = 0; u < 4; ++u)
+            for (unsigned u = 0; u < kCollectChunk; ++u)
                 q[u] = j0 + u < total ? __ldg(pos_id + sl[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-            for (unsigned u = 0; u < 4; ++u) {
+            for (unsigned u = 0; u < kCollectChunk; ++u) {
                 if (j0 + u >= total) break;
                 const unsigned bits = __float_as_uint(dist_sq(p, v3(q[u])));
                 if (__float_as_uint(q[u].w) != self_id && bits <= 0x7f7fffffu) {

@@ -140,6 +140,7 @@ struct StepDev {
     float w_avoid;
     unsigned mask_avoid;
     unsigned order[8];
+    unsigned order_packed;  // order[o] in bits 3o .. 3o+2 (codes 1..7)
     unsigned n_order;
     float dt;
     unsigned need;      // NEED_* bits

@@ -216,26 +216,38 @@ __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned n
 
 // Behaviours order[first..] in order, then nothing else.  fetch(rank, pos,
 // dir, speed) reads neighbour list entry `rank` again (neighbour avoidance).
+// A runtime loop over the packed order (3 bits per entry), so each
+// behaviour's code appears once in the kernel rather than once per order
+// slot; `need` drops the code of behaviours a specialised kernel never runs.
 template <class Fetch>
-__device__ __forceinline__ void finish_all(const Accs& a, const StepDev& p, unsigned first,
-                                           const FlockParams& fs, const FlockParams& fa,
-                                           const FlockParams& fc, const Self& me,
-                                           unsigned& applied, V3& steer, Fetch&& fetch) {
-#pragma unroll
-    for (unsigned o = 0; o < 8; ++o) {
-        if (o < first || o >= p.n_order) continue;
-        switch (p.order[o]) {
-            case GS_B_SEPARATION: flock_finish(0, a.sep, fs, me, applied, steer); break;
-            case GS_B_ALIGNMENT: flock_finish(1, a.ali, fa, me, applied, steer); break;
-            case GS_B_COHESION: flock_finish(2, a.coh, fc, me, applied, steer); break;
+__device__ __forceinline__ void finish_all(const Accs& a, const StepDev& p, unsigned need,
+                                           unsigned first, const FlockParams& fs,
+                                           const FlockParams& fa, const FlockParams& fc,
+                                           const Self& me, unsigned& applied, V3& steer,
+                                           Fetch&& fetch) {
+#pragma unroll 1
+    for (unsigned o = first; o < p.n_order; ++o) {
+        switch ((p.order_packed >> (3u * o)) & 7u) {
+            case GS_B_SEPARATION:
+                if (need & NEED_SEP) flock_finish(0, a.sep, fs, me, applied, steer);
+                break;
+            case GS_B_ALIGNMENT:
+                if (need & NEED_ALI) flock_finish(1, a.ali, fa, me, applied, steer);
+                break;
+            case GS_B_COHESION:
+                if (need & NEED_COH) flock_finish(2, a.coh, fc, me, applied, steer);
+                break;
             case GS_B_SEEK:
                 seek_finish(v3(p.seek_target[0], p.seek_target[1], p.seek_target[2]), p.w_seek,
                             p.mask_seek, me, applied, steer);
                 break;
             case GS_B_AVOID_NEIGHBORS:
-                if (p.avoid_close) close_finish(a.close, p.w_avoid, p.mask_avoid, applied, steer);
-                avoid_finish(avoid_lite_full(a.avoid, fetch), p.w_avoid, p.mask_avoid, me,
-                             applied, steer);
+                if (need & NEED_AVOID) {
+                    if (p.avoid_close)
+                        close_finish(a.close, p.w_avoid, p.mask_avoid, applied, steer);
+                    avoid_finish(avoid_lite_full(a.avoid, fetch), p.w_avoid, p.mask_avoid, me,
+                                 applied, steer);
+                }
                 break;
             case GS_B_FOLLOW_PATH:
                 follow_path_finish(p.path, p.path_time, p.w_path, p.mask_path, me, applied, steer);
@@ -469,7 +481,8 @@ __global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) 
 }
 
 // ---- whole step without walls -------------------------------------------------------
-constexpr unsigned kNbrChunk = 2;
+constexpr unsigned kNbrChunk = 1;  // measured best for the flock (2: +2.5 %, 4: +9 %)
+constexpr unsigned kRestChunk = 2;  // the rest phase's (1: +7 %, 4: +33 %, spills)
 
 // NEEDC: the behaviours that read the neighbour list, fixed at compile time
 // (kNeedRuntime: taken from p.need).
@@ -562,7 +575,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_fused(FusedLaunch L, StepDev p) {
         }
         unsigned applied = p.clear_applied ? 0u : u(f4v.z);
         V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
-        finish_all(a, p, 0, fs, fa, fc, me, applied, steer,
+        finish_all(a, p, need, 0, fs, fa, fc, me, applied, steer,
                    [&](unsigned rank, V3& bp, V3& bh, float& bsp) {
                        const unsigned bs = col[(base + rank) * bd];
                        const float4 b0 = L.B.f[0][bs], b1 = L.B.f[1][bs];
@@ -677,23 +690,23 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
     // others leave its accumulator unchanged, so the result is the same.  A
     // warp then runs the exact test as often as its busiest lane needs it,
     // not once per list entry.
-    // Neighbours kNbrChunk at a time: their slots, then their gathers, are
+    // Neighbours kRestChunk at a time: their slots, then their gathers, are
     // issued together.
     unsigned exact_avoid = 0;
-    for (unsigned i0 = 0; i0 < p.k; i0 += kNbrChunk) {
-        unsigned bs[kNbrChunk];
-        float4 b0[kNbrChunk], b1[kNbrChunk];
+    for (unsigned i0 = 0; i0 < p.k; i0 += kRestChunk) {
+        unsigned bs[kRestChunk];
+        float4 b0[kRestChunk], b1[kRestChunk];
 #pragma unroll
-        for (unsigned j = 0; j < kNbrChunk; ++j)
+        for (unsigned j = 0; j < kRestChunk; ++j)
             bs[j] = i0 + j < p.k ? L.knn_slot[size_t(i0 + j) * L.n + s] : UINT_MAX;
 #pragma unroll
-        for (unsigned j = 0; j < kNbrChunk; ++j) {
+        for (unsigned j = 0; j < kRestChunk; ++j) {
             const bool ok = bs[j] != UINT_MAX;
             b0[j] = ok ? L.w0[bs[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
             b1[j] = ok && need_dir ? L.w1[bs[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
-        for (unsigned j = 0; j < kNbrChunk; ++j) {
+        for (unsigned j = 0; j < kRestChunk; ++j) {
             if (bs[j] == UINT_MAX) break;
             const unsigned i = i0 + j;
             const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
@@ -703,7 +716,7 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
                 avoid_time_may_fall_in(me, p.min_time_col, v3(b0[j]), v3(b1[j]), b1[j].w))
                 exact_avoid |= 1u << i;
         }
-        if (bs[kNbrChunk - 1] == UINT_MAX) break;
+        if (bs[kRestChunk - 1] == UINT_MAX) break;
     }
     while (exact_avoid) {
         const unsigned i = unsigned(__ffs(int(exact_avoid)) - 1);
@@ -722,7 +735,7 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
     const unsigned id = u(reinterpret_cast<const float*>(L.B.f[0] + s)[3]), scene = u(f4v.w);
     unsigned applied = u(w2.w);
     V3 steer = v3(w2);
-    finish_all(a, p, 1, fs, fa, fc, me, applied, steer,
+    finish_all(a, p, need, 1, fs, fa, fc, me, applied, steer,
                [&](unsigned rank, V3& bp, V3& bh, float& bsp) {
                    const unsigned bs = L.knn_slot[size_t(rank) * L.n + s];
                    const float4 b0 = L.w0[bs], b1 = L.w1[bs];
