@@ -268,13 +268,14 @@ __device__ __forceinline__ void init_accs(Accs& a, const StepDev& p) {
 __device__ __forceinline__ void store_next(const FusedLaunch& L, unsigned s, const Self& me,
                                            unsigned id, unsigned scene, const Scene& sc,
                                            int wrap_mode) {
+    // the cell count's atomic first: its round trip overlaps the state stores
+    unsigned cell;
+    const unsigned rank = count_next(sc, me.pos, wrap_mode, L.count, cell);
     L.A.f[0][s] = make_float4(me.pos.x, me.pos.y, me.pos.z, fb(id));
     L.A.f[1][s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
     L.A.f[2][s] = make_float4(me.side.x, me.side.y, me.side.z, me.radius);
     L.A.f[3][s] = make_float4(me.up.x, me.up.y, me.up.z, me.mass);
     L.A.f[4][s] = make_float4(me.max_speed, me.max_force, fb(0u), fb(scene));
-    unsigned cell;
-    const unsigned rank = count_next(sc, me.pos, wrap_mode, L.count, cell);
     L.cellrank[s] = make_uint2(cell, rank);
 }
 
