@@ -165,6 +165,19 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            if not self.lines:
+                # a timed region shorter than the sampling period: one reading
+                # right after it
+                try:
+                    out = subprocess.run(
+                        ["nvidia-smi", "-i", str(self.index),
+                         "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
+                         "--format=csv,noheader,nounits"],
+                        capture_output=True, text=True, timeout=10).stdout
+                    self.lines = [ln.strip() for ln in out.splitlines() if ln.strip()]
+                    self.after = True
+                except (OSError, subprocess.TimeoutExpired):
+                    pass
 
     def summary(self):
         sm, mx, reasons = [], [], set()
@@ -183,8 +196,11 @@ class ClockSampler:
                     reasons.add(name)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if getattr(self, "after", False):
+            out["sampled"] = "once, right after the timed region (shorter than the 200 ms period)"
+        return out
 
 
 # ---- distributed plumbing ---------------------------------------------------------
