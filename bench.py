@@ -707,7 +707,7 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     floor_ms = copy_floor_ms([s.n for s in states], cuts)
     adjoint = adjoint_timing() if not args.no_adjoint else None
     # the other throughput configurations, as records of this line
-    large = brute = None
+    large = brute = choke = boids = None
     if not args.no_sub:
         sub = argparse.Namespace(**vars(args))
         sub.workload, sub.steps, sub.warmup = "large", args.large_steps, args.large_warmup
@@ -716,6 +716,16 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
         sub = argparse.Namespace(**vars(args))
         sub.workload, sub.steps, sub.warmup = "brute", 5, 3
         brute = gpu_brute_line(sub, dist, rank, world, local_rank)
+        sub = argparse.Namespace(**vars(args))
+        sub.workload, sub.steps, sub.warmup, sub.block = "chokepoint", 500, 10, None
+        sub.cpu_seconds = min(args.cpu_seconds, 3.0)
+        choke = gpu_single_line(sub, dist, rank, world, local_rank)
+        sub = argparse.Namespace(**vars(args))
+        sub.workload, sub.steps, sub.warmup, sub.block = "boids", 100, 10, None
+        sub.cpu_seconds = min(args.cpu_seconds, 3.0)
+        boids = gpu_single_line(sub, dist, rank, world, local_rank)
+        if boids is not None:
+            boids["bruteforce_dropin"] = boids_bruteforce_dropin(100, 10)
     if rank != 0:
         return None
     peak, peak_src = read_peaks()
@@ -780,8 +790,50 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
         "cpu_baseline": cpu,
         "large_flock": large,
         "brute": brute,
+        "chokepoint": choke,
+        "boids": boids,
     }
     return line
+
+
+def boids_bruteforce_dropin(steps: int, warmup: int) -> dict:
+    """Config 1 through brute-force KNN: 4,096 boids, k = 7, the drop-in call
+    sequence of BoidsGroupBruteForce's update (wrap, brute-force KNN,
+    separation, cohesion, alignment, update), `steps` steps timed with CUDA
+    events on the group's stream after `warmup`."""
+    import torch
+
+    import gpusteer_gb300 as gs
+    from gpusteer_gb300 import scenario as sc
+
+    p = sc.boids_params(k=7)
+    s = sc.boids_sphere(4096, seed=0)
+    g = gs.AgentGroup(p.k, s.n)
+    g.upload(s)
+    knn = gs.KNNData(s.n, p.k)
+    stream = torch.cuda.ExternalStream(g.stream)
+
+    def frame():
+        gs.wrapWorld(g, p.world_size, p.wrap_mode)
+        gs.findKNearestNeighborsBruteForce(g, knn, g)
+        gs.steerForSeparation(g, knn, g, p.sep_min, p.sep_max, p.sep_cos, p.w_sep, p.mask_sep)
+        gs.steerForCohesion(g, knn, g, p.coh_min, p.coh_max, p.coh_cos, p.w_coh, p.mask_coh)
+        gs.steerForAlignment(g, knn, g, p.ali_min, p.ali_max, p.ali_cos, p.w_ali, p.mask_ali)
+        gs.updateGroup(g, p.dt)
+
+    for _ in range(warmup):
+        frame()
+    g.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        frame()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"ms_per_step": ms, "value": s.n / (ms / 1e3), "unit": "agent-steps/s", "steps": steps,
+            "calls": "gs_wrap_world, gs_knn_bruteforce, gs_steer_for_separation / cohesion / "
+                     "alignment, gs_update_group per step (per-function launches)"}
 
 
 def copy_floor_ms(agents, cuts, reps: int = 5) -> float:
@@ -970,6 +1022,8 @@ def gpu_single_line(args, dist, rank, world, local_rank):
     walls = gs.WallGroup(walls_rows, bins=bins, knw=p.knw) if walls_rows is not None else None
     group = gs.AgentGroup(p.k, n)
     group.upload(state)
+    if getattr(args, "block", None):
+        gs.set_block(group, args.block)
     stream = torch.cuda.ExternalStream(group.stream)
     has_walls = walls is not None
 
@@ -1080,6 +1134,8 @@ def main():
                     help="batched workload: scene ranges overlapped in the end-to-end run")
     ap.add_argument("--no-per-scene", action="store_true",
                     help="batched workload: skip the per-scene baselines")
+    ap.add_argument("--block", type=int, default=None,
+                    help="large/chokepoint/boids workloads: threads per block of the fused launches")
     ap.add_argument("--persistent", action="store_true",
                     help="batched workload with --fixed-config: one persistent launch per step")
     ap.add_argument("--no-sub", action="store_true",
