@@ -518,8 +518,8 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     # autotune cell size, block shape and KNN capacity on the scenes themselves
     t0 = time.perf_counter()
     if args.fixed_config:
-        tr = autotune.TuneResult(params=base, block=256, capacity=0, ms_per_step=0.0,
-                                 persistent=args.persistent)
+        tr = autotune.TuneResult(params=base, block=args.block or 256, capacity=0,
+                                 ms_per_step=0.0, persistent=args.persistent)
     else:
         tr = autotune.tune_batched(states, gaps, base, walls_rows)
     tune_s = time.perf_counter() - t0
@@ -1135,7 +1135,8 @@ def main():
     ap.add_argument("--no-per-scene", action="store_true",
                     help="batched workload: skip the per-scene baselines")
     ap.add_argument("--block", type=int, default=None,
-                    help="large/chokepoint/boids workloads: threads per block of the fused launches")
+                    help="threads per block of the fused launches (large/chokepoint/boids "
+                         "workloads, and the batched workload with --fixed-config)")
     ap.add_argument("--persistent", action="store_true",
                     help="batched workload with --fixed-config: one persistent launch per step")
     ap.add_argument("--no-sub", action="store_true",
