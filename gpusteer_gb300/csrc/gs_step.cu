@@ -393,19 +393,25 @@ __device__ __forceinline__ bool next_agent(const FusedLaunch& L, unsigned& it, u
 // indices), a candidate is listed only below KEY_EMPTY, the agent itself is
 // skipped, and empty ranks hold UINT_MAX.  A redo entry costs a few
 // arg-min rounds of latency instead of one thread's serial pass over every
-// candidate.  Entries with more than kRetryWarpKeys candidates are marked
-// kRetryNotListed and searched by the redo's own thread.  Launched after the
-// streaming scan only (crowded boxes, where the serial pass is long).
+// candidate.  Launched after the streaming scan only (crowded boxes, where
+// the serial pass is long).
 constexpr unsigned kRetryWarpKeys = 256;
 
 // The warp's entries e = first, first + stride, ...; keys / slots: the
-// warp's kRetryWarpKeys-entry shared tables.
-template <int KMAX>
+// warp's kRetryWarpKeys-entry shared tables.  TO_SLOTS: the step with
+// avoid-walls, whose wall phase finished every agent but the redo agents'
+// lists (avoid-walls does not read the agent's own neighbours): each list
+// goes straight to knn_slot (and its KNN distances to knn_dist when
+// avoid-close-neighbours reads them), and lane 0 searches an entry of more
+// than kRetryWarpKeys candidates itself, so no redo launch follows.
+// Otherwise the first retry_cap entries' lists go to retry_knn for the redo
+// launch.
+template <int KMAX, bool TO_SLOTS>
 __device__ __forceinline__ void retry_lists(const FusedLaunch& L, const StepDev& p, unsigned first,
                                             unsigned stride, unsigned long long* keys,
                                             unsigned* slots) {
     const unsigned lane = threadIdx.x & 31u;
-    const unsigned count = min(*L.retry_count, L.retry_cap);
+    const unsigned count = TO_SLOTS ? *L.retry_count : min(*L.retry_count, L.retry_cap);
     for (unsigned e = first; e < count; e += stride) {
         const unsigned s = L.retry[e];
         const float4 f0 = L.B.f[0][s];
@@ -434,9 +440,25 @@ __device__ __forceinline__ void retry_lists(const FusedLaunch& L, const StepDev&
             }
         }
         __syncwarp();
-        unsigned* out = L.retry_knn + size_t(e) * kRetryListK;
+        unsigned* out = TO_SLOTS ? nullptr : L.retry_knn + size_t(e) * kRetryListK;
+        const bool dists = TO_SLOTS && (p.need & NEED_CLOSE);
         if (total > kRetryWarpKeys) {
-            if (lane == 0) out[0] = kRetryNotListed;
+            if (lane == 0) {
+                if (TO_SLOTS) {
+                    // the exact list into the warp's slot table, then out
+                    knn_neighbours_exact<KMAX>(int(p.k), pos, id, sc.grid, b, sc.cell_offset,
+                                               L.start, L.B.f[0], slots, 1u);
+                    for (unsigned r = 0; r < p.k; ++r) {
+                        const unsigned bs = slots[r];
+                        L.knn_slot[size_t(r) * L.n + s] = bs;
+                        if (dists)
+                            L.knn_dist[size_t(r) * L.n + s] =
+                                bs == UINT_MAX ? FLT_MAX : distance(pos, v3(L.B.f[0][bs]));
+                    }
+                } else {
+                    out[0] = kRetryNotListed;
+                }
+            }
             __syncwarp();
             continue;
         }
@@ -462,7 +484,13 @@ __device__ __forceinline__ void retry_lists(const FusedLaunch& L, const StepDev&
             // every lane holds the same (best, bj): the keys are unique
             const bool listed = best < KEY_EMPTY;
             if (lane == 0) {
-                out[r] = listed ? slots[bj] : UINT_MAX;
+                const unsigned bs = listed ? slots[bj] : UINT_MAX;
+                if (TO_SLOTS) {
+                    L.knn_slot[size_t(r) * L.n + s] = bs;
+                    if (dists) L.knn_dist[size_t(r) * L.n + s] = listed ? key_dist(best) : FLT_MAX;
+                } else {
+                    out[r] = bs;
+                }
                 if (listed) keys[bj] = ~0ull;
             }
             __syncwarp();
@@ -470,15 +498,15 @@ __device__ __forceinline__ void retry_lists(const FusedLaunch& L, const StepDev&
     }
 }
 
-template <int KMAX>
+template <int KMAX, bool TO_SLOTS>
 __global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) {
     __shared__ unsigned long long sk[kBlock / 32][kRetryWarpKeys];
     __shared__ unsigned ss[kBlock / 32][kRetryWarpKeys];
     const unsigned w = threadIdx.x >> 5;
     // warp w of block b takes entries w * gridDim.x + b, + nw, ...: a few
     // hundred entries land one per block across every SM
-    retry_lists<KMAX>(L, p, w * gridDim.x + blockIdx.x, gridDim.x * (blockDim.x >> 5), sk[w],
-                      ss[w]);
+    retry_lists<KMAX, TO_SLOTS>(L, p, w * gridDim.x + blockIdx.x,
+                                gridDim.x * (blockDim.x >> 5), sk[w], ss[w]);
 }
 
 // ---- whole step without walls -------------------------------------------------------
@@ -604,13 +632,15 @@ __device__ __forceinline__ void walls_agent(const FusedLaunch& L, const StepDev&
         unsigned ix, iy, iz;
         cell_coords(sc.grid, pos, ix, iy, iz);
         const Box box = cell_box(sc.grid, ix, iy, iz, p.r);
+        // a redo agent (base UINT_MAX: on the retry list) still gets its wall
+        // behaviour here, which does not read its own neighbours; the
+        // warp-per-agent search writes its list
         const unsigned base = agent_knn<KMAX, ENUM, EXACT, FLAT>(L, p, s, it, pos, id, sc, box, col, bd);
-        if (base == UINT_MAX) return;
         float4 f4v;
         Self me = load_rest(L.B, s, pos, f4v);
         unsigned applied = p.clear_applied ? 0u : u(f4v.z);
         V3 steer = p.dirty ? v3(L.B.f[5][s]) : v3(0.f, 0.f, 0.f);
-        for (unsigned r = 0; r < p.k; ++r) {
+        for (unsigned r = 0; r < p.k && base != UINT_MAX; ++r) {
             const unsigned bs = col[(base + r) * bd];
             L.knn_slot[size_t(r) * L.n + s] = bs;
             // the KNN distance (before any wall correction moves agents),
@@ -788,11 +818,11 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
     const size_t smem = ENUM > 64 ? size_t(KMAX > 8 ? KMAX : 8) * bs * sizeof(unsigned)
                                   : size_t(2 * ENUM) * bs * sizeof(unsigned);
     const size_t smem_x = size_t(KMAX > 8 ? KMAX : 8) * kBlock * sizeof(unsigned);
-    // The warp-per-agent exact lists and the redo launch serve the streaming
-    // scan (crowded boxes, 40-250 candidates); the collecting scan's kernels
-    // redo their few agents inline (sparse boxes, mostly distance ties among
-    // a dozen candidates), which costs less than a launch of one agent's
-    // latency.
+    // The warp-per-agent exact lists (and, without walls, the redo launch)
+    // serve the streaming scan (crowded boxes, 40-250 candidates); the
+    // collecting scan's kernels redo their few agents inline (sparse boxes,
+    // mostly distance ties among a dozen candidates), which costs less than a
+    // launch of one agent's latency.
     if (p.need & NEED_WALLS) {
         if (hook) hook->mark(2, true);
         // flat grids (one cell high) have a 3-row build of the streaming scan
@@ -808,10 +838,8 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
             GS_TRY(allow_smem(k_fused_walls<KMAX, 8, ENUM, false>, smem));
             k_fused_walls<KMAX, 8, ENUM, false><<<nb, bs, smem, st>>>(L, p);
         }
-        if (ENUM > 64) {
-            k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
-            k_fused_walls<KMAX, 8, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
-        }
+        // the redo agents' exact lists, straight into the neighbour lists
+        if (ENUM > 64) k_knn_retry<KMAX, true><<<nb_retry, kBlock, 0, st>>>(L, p);
         if (hook) hook->mark(2, false);
         if (hook) hook->mark(3, true);
         // the choke-point step (separation and neighbour avoidance) has its own build
@@ -842,7 +870,7 @@ static gs_status launch_fused_k(const FusedLaunch& L, const StepDev& p, cudaStre
         }
         if (!done) k_fused<KMAX, ENUM, false><<<nb, bs, smem, st>>>(L, p);
         if (ENUM > 64) {
-            k_knn_retry<KMAX><<<nb_retry, kBlock, 0, st>>>(L, p);
+            k_knn_retry<KMAX, false><<<nb_retry, kBlock, 0, st>>>(L, p);
             k_fused<KMAX, 32, true><<<nb_retry, kBlock, smem_x, st>>>(L, p);
         }
         if (hook) hook->mark(2, false);
@@ -862,8 +890,8 @@ static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream
 
 // ---- the wall/rest step in one persistent launch ----------------------------------
 // One cooperative launch runs every phase of the step - the scan's tile totals
-// and starts, the permute, the wall phase, the warp-per-agent exact lists, the
-// exact redo and the rest phase - over a grid of co-resident blocks.  Each
+// and starts, the permute, the wall phase, the warp-per-agent exact lists and
+// the rest phase - over a grid of co-resident blocks.  Each
 // phase is a grid-stride loop over the same device functions the separate
 // kernels run, so the results are the same bit for bit; a grid-wide barrier
 // separates the phases.  Every barrier wait is bounded: a block that polls
@@ -949,15 +977,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_step_persistent(FusedLaunch L, St
         unsigned* slots = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned long long*>(sm) +
                                                       (kBlock / 32) * kRetryWarpKeys) +
                           w * kRetryWarpKeys;
-        retry_lists<KMAX>(L, p, w * gridDim.x + blockIdx.x, gridDim.x * (kBlock / 32), keys,
-                          slots);
-    }
-    if (!grid_sync(bar, P.limit, L.err)) return;
-    // exact redo, entries spread block-fastest over the grid
-    {
-        const unsigned count = *L.retry_count;
-        for (unsigned it = threadIdx.x * gridDim.x + blockIdx.x; it < count; it += nthreads)
-            walls_agent<KMAX, 8, 32, true, false>(L, p, L.retry[it], it, col, kBlock);
+        retry_lists<KMAX, true>(L, p, w * gridDim.x + blockIdx.x, gridDim.x * (kBlock / 32),
+                                keys, slots);
     }
     if (!grid_sync(bar, P.limit, L.err)) return;
     // rest phase

@@ -172,7 +172,7 @@ gs_status gs_group_set_profiling(gs_group g, int enable);
 gs_status gs_group_exact_redos(gs_group g, unsigned* count);
 /* One persistent launch per fused step (no counterpart in the reference,
  * which launches one kernel per behaviour): the scan, permute, wall phase,
- * exact lists, exact redo and rest phase of a step with avoid-walls first,
+ * exact lists and rest phase of a step with avoid-walls first,
  * 9 <= k <= 16, a flat world (one cell high) and the streaming KNN scan
  * (capacity 128 or 256) run in one cooperative launch with grid-wide
  * barriers between the phases; the results equal the separate launches bit

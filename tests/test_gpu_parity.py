@@ -488,8 +488,8 @@ def test_knn_capacity_reads_back():
     assert gs.knn_capacity(g) == 0
     gs.step(g, bins, walls, p, 1)
     assert gs.knn_capacity(g) in (128, 256)
-    # two scan launches, permute, wall phase, warp-per-agent lists, redo, rest phase
-    assert gs.step_launches(g, True) == 7
+    # two scan launches, permute, wall phase, warp-per-agent lists, rest phase
+    assert gs.step_launches(g, True) == 6
     gs.set_knn_capacity(g, 64)
     assert gs.knn_capacity(g) == 64
     assert gs.step_launches(g, True) == 5
