@@ -317,6 +317,7 @@ static gs_status validate_step(const gs_step_params* p, gs_walls walls, StepDev&
     std::memset(&d, 0, sizeof(d));
     d.k = p->k;
     d.flat = p->world_cells[1] == 1 ? 1u : 0u;
+    d.scan_reach = scan_reach_tiles(p->world_cells, p->search_radius);
     d.knw = p->knw;
     d.r = p->search_radius;
     d.wrap_mode = p->wrap_mode;
@@ -1317,7 +1318,7 @@ gs_status gs_cell_density(gs_group g, gs_bins bins, unsigned* counts) {
     GS_TRY(diag_scratch(g, size_t(C) * 4, &d));
     const gs_status s = src == DIAG_DB
                             ? launch_cell_density(g->db, static_cast<unsigned*>(d), g->stream)
-                            : launch_frame_cell_density(g->fdb.start, C,
+                            : launch_frame_cell_density(g->fdb.start, g->fdb.live, C,
                                                         static_cast<unsigned*>(d), g->stream);
     return diag_copy_out(g, counts, d, size_t(C) * 4, s);
 }
@@ -1336,7 +1337,8 @@ gs_status gs_cell_avg_velocity(gs_group g, gs_bins bins, float* avg3) {
     if (src == DIAG_DB) {
         s = launch_cell_avg_velocity(g->db, g->direction, g->speed, out, g->stream);
     } else {
-        s = launch_frame_cell_avg_velocity(g->fdb.start, C, g->A.f[0], g->A.f[1], out, g->stream);
+        s = launch_frame_cell_avg_velocity(g->fdb.start, g->fdb.live, C, g->A.f[0], g->A.f[1],
+                                           out, g->stream);
     }
     return diag_copy_out(g, avg3, d, size_t(C) * 12, s);
 }
@@ -1608,6 +1610,13 @@ struct WallsDev {
     const unsigned* cell_start = nullptr;
 };
 
+// Zeroes the fused engine's counts and tile totals before a recount.
+static gs_status clear_counts(gs_group g, unsigned C, cudaStream_t st) {
+    GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
+    GS_CUDA(cudaMemsetAsync(g->fdb.tile, 0, size_t(scan_tile_count(C)) * 4, st));
+    return GS_OK;
+}
+
 // One step's launches: scan, permute, fused (+ exact redo); or, for a
 // supported step with the persistent form on, one launch for all of them.
 static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, unsigned C,
@@ -1617,6 +1626,7 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
         PersistLaunch P;
         P.start = g->fdb.start;
         P.tile = g->fdb.tile;
+        P.live = g->fdb.live;
         P.C = C;
         P.T = scan_tile_count(C);
         P.bar = g->d_bar;
@@ -1627,7 +1637,8 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
         return GS_OK;
     }
     if (hook) hook->mark(0, true);
-    GS_TRY(scan_counts2(g->fdb.count, g->fdb.start, C, g->fdb.tile, st));
+    GS_TRY(scan_counts_sparse(g->fdb.count, g->fdb.start, C, g->fdb.tile, g->fdb.live,
+                              d.scan_reach, st));
     if (hook) hook->mark(0, false);
     if (hook) hook->mark(1, true);
     GS_TRY(fused_permute(L, d.wrap_mode, d.dirty != 0, st));
@@ -1650,14 +1661,15 @@ static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned 
     if (!g->fused_current) {
         dirty = g->accum_dirty;
         // counts left pending by an earlier fused step no longer apply
-        GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
+        GS_TRY(clear_counts(g, C, st));
         GS_TRY(fused_from_reference(view(g), agent_scene, g->d_scene, g->A, g->cellrank,
-                                    g->fdb.count, d.wrap_mode, dirty, st));
+                                    g->fdb.count, g->fdb.tile, d.wrap_mode, dirty, st));
         g->fused_current = true;
     } else if (std::memcmp(&g->fdb.grid, &grid, sizeof(Grid)) != 0 || !g->fdb.valid ||
                g->pending_wrap != d.wrap_mode) {
-        GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
-        GS_TRY(fused_recount(g->A, g->n, g->d_scene, g->cellrank, g->fdb.count, d.wrap_mode, st));
+        GS_TRY(clear_counts(g, C, st));
+        GS_TRY(fused_recount(g->A, g->n, g->d_scene, g->cellrank, g->fdb.count, g->fdb.tile,
+                             d.wrap_mode, st));
     }
     g->fdb.grid = grid;
     g->fdb.valid = true;
@@ -1689,6 +1701,8 @@ static void fill_launch(gs_group g, const StepDev& d, const WallsDev& w, FusedLa
     L.B = g->B;
     L.cellrank = g->cellrank;
     L.count = g->fdb.count;
+    L.tile = g->fdb.tile;
+    L.tiles = scan_tile_count(g->fdb.cells);
     L.start = g->fdb.start;
     L.scenes = g->d_scene;
     L.n = g->n;
@@ -2065,9 +2079,9 @@ static gs_status io_upload(IoPart& q) { return upload_enqueue(q.b->g, &q.hi, q.b
 static gs_status io_compute_and_download(IoPart& q, unsigned steps, bool in_place) {
     gs_group g = q.b->g;
     cudaStream_t st = g->stream;
-    GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(q.Ct) * 4, st));
+    GS_TRY(clear_counts(g, q.Ct, st));
     GS_TRY(fused_from_reference(view(g), q.b->agent_scene, g->d_scene, g->A, g->cellrank,
-                                g->fdb.count, q.d.wrap_mode, true, st));
+                                g->fdb.count, g->fdb.tile, q.d.wrap_mode, true, st));
     for (unsigned i = 0; i < steps; ++i) {
         StepDev di = q.d;
         di.dirty = i == 0 ? 1 : 0;
@@ -2235,7 +2249,8 @@ gs_status gs_batch_cell_density(gs_batch b, unsigned* counts) {
     void* d = nullptr;
     GS_TRY(diag_scratch(g, size_t(Ct) * 4, &d));
     const gs_status s =
-        launch_frame_cell_density(g->fdb.start, Ct, static_cast<unsigned*>(d), g->stream);
+        launch_frame_cell_density(g->fdb.start, g->fdb.live, Ct, static_cast<unsigned*>(d),
+                                  g->stream);
     return diag_copy_out(g, counts, d, size_t(Ct) * 4, s);
 }
 
@@ -2246,8 +2261,9 @@ gs_status gs_batch_cell_avg_velocity(gs_batch b, float* avg3) {
     gs_group g = b->g;
     void* d = nullptr;
     GS_TRY(diag_scratch(g, size_t(Ct) * 12, &d));
-    const gs_status s = launch_frame_cell_avg_velocity(g->fdb.start, Ct, g->A.f[0], g->A.f[1],
-                                                       static_cast<float3*>(d), g->stream);
+    const gs_status s =
+        launch_frame_cell_avg_velocity(g->fdb.start, g->fdb.live, Ct, g->A.f[0], g->A.f[1],
+                                       static_cast<float3*>(d), g->stream);
     return diag_copy_out(g, avg3, d, size_t(Ct) * 12, s);
 }
 

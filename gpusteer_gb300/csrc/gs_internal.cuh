@@ -107,7 +107,8 @@ struct Database {
     float4* pos_id = nullptr;   // [n] (position.xyz, agent index bits) of slot
     unsigned* start = nullptr;  // [C + 1]
     unsigned* count = nullptr;  // [C] zero between uses
-    unsigned* tile = nullptr;   // scan scratch
+    unsigned* tile = nullptr;   // scan scratch; the fused engine's exact tile totals
+    unsigned* live = nullptr;   // [T] tiles the fused engine's last scan wrote
     unsigned agent_cap = 0;     // agents the per-agent arrays hold, where tracked
     bool valid = false;
     Grid grid{};

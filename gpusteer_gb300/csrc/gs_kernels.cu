@@ -107,29 +107,40 @@ gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* ti
     return GS_OK;
 }
 
-// ---- two-launch exclusive scan (the fused engine's counting sort) ----------------
-// k_scan_reduce writes each tile's total; then every block of k_scan_apply_prefix
-// sums the totals of the tiles before its own (a few thousand words from L2)
-// and writes its tile's starts.  Two launches instead of three (no one-block
-// pass over the tile totals) and no block ever waits on another.
-__global__ void __launch_bounds__(kBlock) k_scan_apply_prefix(unsigned* __restrict__ count,
+// ---- the fused engine's counting-sort scan: one launch, tiles near agents ---------
+// The counting atomics add each tile's total as they go, so no reduce pass
+// reads the counts; every block sums the totals of the tiles before its own (a
+// few thousand words from L2) and writes its tile's starts, and no block
+// waits on another (scan_apply_sparse_tile).
+__global__ void __launch_bounds__(kBlock) k_scan_apply_sparse(unsigned* __restrict__ count,
                                                               unsigned C,
                                                               const unsigned* __restrict__ tile,
                                                               unsigned* __restrict__ start,
-                                                              unsigned T) {
+                                                              unsigned T, unsigned reach,
+                                                              unsigned* __restrict__ live) {
     __shared__ unsigned sh[kScanTile + kScanTile / 32];
     __shared__ unsigned ws[kBlock / 32];
-    scan_apply_tile(count, C, tile, start, T, blockIdx.x, sh, ws);
+    scan_apply_sparse_tile(count, C, tile, start, T, blockIdx.x, reach, live, sh, ws);
 }
 
-gs_status scan_counts2(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
-                       cudaStream_t st) {
+gs_status scan_counts_sparse(unsigned* count, unsigned* start, unsigned C, const unsigned* tile,
+                             unsigned* live, unsigned reach, cudaStream_t st) {
     const unsigned T = scan_tile_count(C);
     if (T == 0) return GS_OK;
-    k_scan_reduce<<<T, kBlock, 0, st>>>(count, C, tile);
-    k_scan_apply_prefix<<<T, kBlock, 0, st>>>(count, C, tile, start, T);
-    GS_LAUNCHED("scan2");
+    k_scan_apply_sparse<<<T, kBlock, 0, st>>>(count, C, tile, start, T, reach, live);
+    GS_LAUNCHED("scan_sparse");
     return GS_OK;
+}
+
+unsigned scan_reach_tiles(const unsigned wc[3], unsigned r) {
+    // labels are x + z wc0 + y wc0 wc2: a box of radius r reads starts at
+    // most rx + rz wc0 + ry wc0 wc2 + 1 labels from its centre cell (the +1:
+    // the start after a row's last cell)
+    auto reach = [&](unsigned n) { return std::min<unsigned long long>(r, n ? n - 1 : 0); };
+    const unsigned long long d = reach(wc[0]) + reach(wc[2]) * wc[0] +
+                                 reach(wc[1]) * (unsigned long long)wc[0] * wc[2] + 1;
+    const unsigned long long t = (d + kScanTile - 1) / kScanTile;
+    return t > 0xffffffffull ? 0xffffffffu : unsigned(t);
 }
 
 // ---- database -----------------------------------------------------------------------
@@ -138,10 +149,14 @@ gs_status db_reserve(Database& db, unsigned n, unsigned C) {
         dfree(db.start);
         dfree(db.count);
         dfree(db.tile);
+        dfree(db.live);
         GS_TRY(dalloc(&db.start, size_t(C) + 1));
         GS_TRY(dalloc(&db.count, C));
         GS_TRY(dalloc(&db.tile, scan_tile_count(C) + 1));
+        GS_TRY(dalloc(&db.live, scan_tile_count(C) + 1));
         GS_CUDA(cudaMemset(db.count, 0, size_t(C) * sizeof(unsigned)));
+        GS_CUDA(cudaMemset(db.tile, 0, (size_t(scan_tile_count(C)) + 1) * sizeof(unsigned)));
+        GS_CUDA(cudaMemset(db.live, 0, (size_t(scan_tile_count(C)) + 1) * sizeof(unsigned)));
         // the counts are used next on a non-blocking stream
         GS_CUDA(cudaDeviceSynchronize());
         db.cells = C;
@@ -164,6 +179,7 @@ void db_release(Database& db) {
     dfree(db.start);
     dfree(db.count);
     dfree(db.tile);
+    dfree(db.live);
     db.cells = 0;
     db.agent_cap = 0;
     db.valid = false;
@@ -568,10 +584,16 @@ gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, 
 }
 
 // ---- ExtractData diagnostics (ProcessData.cu:132-237) -------------------------------------
+// live (the fused engine's frame, may be null): tiles whose starts the last
+// scan wrote; a cell of another tile is empty.
+__device__ __forceinline__ bool frame_cell_live(const unsigned* live, unsigned c) {
+    return live == nullptr || live[c / kScanTile] != 0u;
+}
+
 __global__ void k_cell_density(const unsigned* __restrict__ start, unsigned C,
-                               unsigned* __restrict__ out) {
+                               const unsigned* __restrict__ live, unsigned* __restrict__ out) {
     const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < C) out[c] = start[c + 1] - start[c];
+    if (c < C) out[c] = frame_cell_live(live, c) ? start[c + 1] - start[c] : 0u;
 }
 
 // A cell's agents are added in ascending index, the order the reference's
@@ -605,12 +627,14 @@ __global__ void k_cell_avg_velocity(const unsigned* __restrict__ start,
 // in f0.w, heading and speed in f1).  A cell's agents belong to one scene, so
 // ascending index is the reference's order here too.
 __global__ void k_cell_avg_velocity_frame(const unsigned* __restrict__ start, unsigned C,
+                                          const unsigned* __restrict__ live,
                                           const float4* __restrict__ f0,
                                           const float4* __restrict__ f1,
                                           float3* __restrict__ out) {
     const unsigned c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
-    const unsigned s0 = start[c], s1 = start[c + 1];
+    const bool on = frame_cell_live(live, c);
+    const unsigned s0 = on ? start[c] : 0u, s1 = on ? start[c + 1] : 0u;
     V3 sum = v3(0.f, 0.f, 0.f);
     unsigned last = 0;
     for (unsigned t = 0; t < s1 - s0; ++t) {
@@ -630,25 +654,26 @@ __global__ void k_cell_avg_velocity_frame(const unsigned* __restrict__ start, un
     out[c] = make_float3(avg.x, avg.y, avg.z);
 }
 
-gs_status launch_frame_cell_density(const unsigned* start, unsigned C, unsigned* out,
-                                    cudaStream_t st) {
+gs_status launch_frame_cell_density(const unsigned* start, const unsigned* live, unsigned C,
+                                    unsigned* out, cudaStream_t st) {
     if (C == 0) return GS_OK;
-    k_cell_density<<<blocks_for(C), kBlock, 0, st>>>(start, C, out);
+    k_cell_density<<<blocks_for(C), kBlock, 0, st>>>(start, C, live, out);
     GS_LAUNCHED("cell_density");
     return GS_OK;
 }
 
-gs_status launch_frame_cell_avg_velocity(const unsigned* start, unsigned C, const float4* f0,
-                                         const float4* f1, float3* out, cudaStream_t st) {
+gs_status launch_frame_cell_avg_velocity(const unsigned* start, const unsigned* live,
+                                         unsigned C, const float4* f0, const float4* f1,
+                                         float3* out, cudaStream_t st) {
     if (C == 0) return GS_OK;
-    k_cell_avg_velocity_frame<<<blocks_for(C), kBlock, 0, st>>>(start, C, f0, f1, out);
+    k_cell_avg_velocity_frame<<<blocks_for(C), kBlock, 0, st>>>(start, C, live, f0, f1, out);
     GS_LAUNCHED("cell_avg_velocity");
     return GS_OK;
 }
 
 gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st) {
     if (db.cells == 0) return GS_OK;
-    k_cell_density<<<blocks_for(db.cells), kBlock, 0, st>>>(db.start, db.cells, out);
+    k_cell_density<<<blocks_for(db.cells), kBlock, 0, st>>>(db.start, db.cells, nullptr, out);
     GS_LAUNCHED("cell_density");
     return GS_OK;
 }

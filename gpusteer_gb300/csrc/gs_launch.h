@@ -11,10 +11,14 @@ namespace gs {
 gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
                       cudaStream_t st);
 unsigned scan_tile_count(unsigned C);
-// The same scan in two launches (tile totals, then each block sums the
-// totals before its tile): the fused engine's counting sort.
-gs_status scan_counts2(unsigned* count, unsigned* start, unsigned C, unsigned* tile,
-                       cudaStream_t st);
+// The fused engine's scan in one launch: tile[] holds exact tile totals
+// (added by the counting atomics), and only tiles within `reach` tiles of an
+// occupied one get starts (live[t] = 1) and zeroed counts.
+gs_status scan_counts_sparse(unsigned* count, unsigned* start, unsigned C, const unsigned* tile,
+                             unsigned* live, unsigned reach, cudaStream_t st);
+// Tiles (of the scan) between a cell and the farthest start its box of
+// radius r reads, on a grid of wc cells.
+unsigned scan_reach_tiles(const unsigned wc[3], unsigned r);
 // Allocates db for C cells and n agents (keeps existing buffers when large enough).
 gs_status db_reserve(Database& db, unsigned n, unsigned C);
 void db_release(Database& db);
@@ -56,11 +60,13 @@ gs_status launch_wrap(float4* pos, unsigned n, const float ws[3], int mode, cuda
 gs_status launch_cell_density(const Database& db, unsigned* out, cudaStream_t st);
 gs_status launch_cell_avg_velocity(const Database& db, const float4* dir, const float* speed,
                                    float3* out, cudaStream_t st);
-// The same diagnostics over a fused step's frame (start-of-step buckets, new state in A).
-gs_status launch_frame_cell_density(const unsigned* start, unsigned C, unsigned* out,
-                                    cudaStream_t st);
-gs_status launch_frame_cell_avg_velocity(const unsigned* start, unsigned C, const float4* f0,
-                                         const float4* f1, float3* out, cudaStream_t st);
+// The same diagnostics over a fused step's frame (start-of-step buckets, new
+// state in A; live: the tiles whose starts the step's scan wrote).
+gs_status launch_frame_cell_density(const unsigned* start, const unsigned* live, unsigned C,
+                                    unsigned* out, cudaStream_t st);
+gs_status launch_frame_cell_avg_velocity(const unsigned* start, const unsigned* live,
+                                         unsigned C, const float4* f0, const float4* f1,
+                                         float3* out, cudaStream_t st);
 
 struct GroupView {
     float4 *position, *direction, *steering;
@@ -147,6 +153,7 @@ struct StepDev {
     unsigned enum_cap;  // candidate capacity of the fast KNN scan (32, 64: collecting; 128, 256: streaming)
     unsigned block;     // threads per block of the fused launches (0: 256)
     unsigned flat;      // the grid is one cell high (y): boxes hold 3 rows of cells
+    unsigned scan_reach;  // scan_reach_tiles of the step's grid and radius
     unsigned persistent;  // run a supported step as one persistent launch
     unsigned bar_limit;   // its barrier poll limit
     PathDev path;       // path following (GS_B_FOLLOW_PATH)
@@ -164,6 +171,7 @@ constexpr unsigned kErrBarrierTimeout = 2u;  // a persistent step's barrier wait
 struct PersistLaunch {
     unsigned* start;
     unsigned* tile;
+    unsigned* live;
     unsigned C, T;
     unsigned* bar;  // 2 words
     unsigned limit;
@@ -180,6 +188,10 @@ struct FusedLaunch {
     Fused A, B;
     uint2* cellrank;
     unsigned* count;
+    // [tiles] exact totals of count per scan tile: zeroed by the permute,
+    // added by the counting atomics
+    unsigned* tile;
+    unsigned tiles;
     const unsigned* start;
     const Scene* scenes;
     unsigned n;
@@ -205,11 +217,13 @@ struct FusedLaunch {
     unsigned* rec_knn;  // [n * k] neighbour indices, row-major, UINT_MAX after the last
 };
 
+// Both count each agent's cell into count[] and its scan tile's total into
+// tile[] (zeroed beforehand, like count[]).
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
-                               Fused A, uint2* cellrank, unsigned* count, int wrap_mode,
-                               bool dirty, cudaStream_t st);
+                               Fused A, uint2* cellrank, unsigned* count, unsigned* tile,
+                               int wrap_mode, bool dirty, cudaStream_t st);
 gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
-                        unsigned* count, int wrap_mode, cudaStream_t st);
+                        unsigned* count, unsigned* tile, int wrap_mode, cudaStream_t st);
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st);
 // `phase` (may be null) brackets each launch: phase(i, true) before and
 // phase(i, false) after the launch of phase i.

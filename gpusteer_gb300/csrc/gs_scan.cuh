@@ -109,4 +109,29 @@ __device__ __forceinline__ void scan_apply_tile(unsigned* __restrict__ count, un
     __syncthreads();
 }
 
+// The fused engine's scan, over tiles near agents only.  tile[] holds each
+// tile's exact total, added by the counting atomics themselves (no reduce
+// pass); the step reads the starts of cells at most `reach` tiles from an
+// agent's own tile (its box's rows, scan_reach_tiles).  So tile t's starts
+// are written, and its counts zeroed, only when a tile within `reach` of it
+// holds agents; live[t] records which.  The other tiles' counts are already
+// zero and their starts, stale, are not read.  reach >= kBlock / 2: every
+// tile is written.
+__device__ __forceinline__ void scan_apply_sparse_tile(unsigned* __restrict__ count, unsigned C,
+                                                       const unsigned* __restrict__ tile,
+                                                       unsigned* __restrict__ start, unsigned T,
+                                                       unsigned t, unsigned reach,
+                                                       unsigned* __restrict__ live, unsigned* sh,
+                                                       unsigned* ws) {
+    unsigned v = reach >= kBlock / 2 ? 1u : 0u;
+    if (!v && threadIdx.x <= 2 * reach) {
+        const long long u = (long long)t - (long long)reach + (long long)threadIdx.x;
+        if (u >= 0 && u < (long long)T) v = tile[u];
+    }
+    const int need = __syncthreads_or(v != 0u);
+    if (threadIdx.x == 0) live[t] = need ? 1u : 0u;
+    if (!need) return;
+    scan_apply_tile(count, C, tile, start, T, t, sh, ws);
+}
+
 }  // namespace gs

@@ -3,7 +3,8 @@
 // State lives in bucketed order in two ping-pong sets of six float4 streams
 // (Fused A and B, layout in gs_internal.cuh).  One step is
 //   scan      exclusive scan of the per-cell counts gathered by the previous
-//             step (or by fused_from_reference), zeroing the counts;
+//             step (or by fused_from_reference), zeroing the counts, over the
+//             cells near agents (the counting also keeps per-tile totals);
 //   permute   A -> B into bucketed order, applying the world wrap
 //             (WrapWorldCUDAKernel) on the way;
 //   fused     one thread per agent of B: binned KNN over B's own bucketed
@@ -35,10 +36,22 @@ namespace gs {
 __device__ __forceinline__ unsigned u(float x) { return __float_as_uint(x); }
 __device__ __forceinline__ float fb(unsigned x) { return __uint_as_float(x); }
 
+// Adds 1 to the scan tile total of `cell`, once per group of active lanes in
+// the same tile (a warp's agents are mostly in one).
+__device__ __forceinline__ void add_to_tile(unsigned* tile, unsigned cell) {
+    const unsigned t = cell / kScanTile;
+    const unsigned peers = __match_any_sync(__activemask(), t);
+    if ((threadIdx.x & 31u) == unsigned(__ffs(int(peers)) - 1))
+        atomicAdd(tile + t, unsigned(__popc(int(peers))));
+}
+
+// The agent's cell for the next step's counting sort: counted (the old count
+// is its rank in the cell) and added to its tile's total.
 __device__ __forceinline__ unsigned count_next(const Scene& sc, V3 pos, int wrap_mode,
-                                               unsigned* count, unsigned& cell) {
+                                               unsigned* count, unsigned* tile, unsigned& cell) {
     const V3 wp = wrap_world(pos, sc.grid.ws, wrap_mode);
     cell = sc.cell_offset + cell_of(sc.grid, wp);
+    add_to_tile(tile, cell);
     return atomicAdd(count + cell, 1u);
 }
 
@@ -46,7 +59,7 @@ __device__ __forceinline__ unsigned count_next(const Scene& sc, V3 pos, int wrap
 __global__ void k_from_reference(GroupView g, const unsigned* __restrict__ agent_scene,
                                  const Scene* __restrict__ scenes, Fused A,
                                  uint2* __restrict__ cellrank, unsigned* __restrict__ count,
-                                 int wrap_mode, int dirty) {
+                                 unsigned* __restrict__ tile, int wrap_mode, int dirty) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
     const unsigned si = agent_scene ? agent_scene[i] : 0u;
@@ -61,35 +74,35 @@ __global__ void k_from_reference(GroupView g, const unsigned* __restrict__ agent
     A.f[4][i] = make_float4(g.max_speed[i], g.max_force[i], fb(g.applied[i]), fb(si));
     if (dirty) A.f[5][i] = g.steering[i];
     unsigned cell;
-    const unsigned rank = count_next(sc, v3(p), wrap_mode, count, cell);
+    const unsigned rank = count_next(sc, v3(p), wrap_mode, count, tile, cell);
     cellrank[i] = make_uint2(cell, rank);
 }
 
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
-                               Fused A, uint2* cellrank, unsigned* count, int wrap_mode,
-                               bool dirty, cudaStream_t st) {
+                               Fused A, uint2* cellrank, unsigned* count, unsigned* tile,
+                               int wrap_mode, bool dirty, cudaStream_t st) {
     if (g.n == 0) return GS_OK;
     k_from_reference<<<blocks_for(g.n), kBlock, 0, st>>>(g, agent_scene, scenes, A, cellrank,
-                                                         count, wrap_mode, dirty ? 1 : 0);
+                                                         count, tile, wrap_mode, dirty ? 1 : 0);
     GS_LAUNCHED("fused_from_reference");
     return GS_OK;
 }
 
 __global__ void k_recount(Fused A, unsigned n, const Scene* __restrict__ scenes,
                           uint2* __restrict__ cellrank, unsigned* __restrict__ count,
-                          int wrap_mode) {
+                          unsigned* __restrict__ tile, int wrap_mode) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Scene sc = scenes[u(A.f[4][i].w)];
     unsigned cell;
-    const unsigned rank = count_next(sc, v3(A.f[0][i]), wrap_mode, count, cell);
+    const unsigned rank = count_next(sc, v3(A.f[0][i]), wrap_mode, count, tile, cell);
     cellrank[i] = make_uint2(cell, rank);
 }
 
 gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
-                        unsigned* count, int wrap_mode, cudaStream_t st) {
+                        unsigned* count, unsigned* tile, int wrap_mode, cudaStream_t st) {
     if (n == 0) return GS_OK;
-    k_recount<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, cellrank, count, wrap_mode);
+    k_recount<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, cellrank, count, tile, wrap_mode);
     GS_LAUNCHED("fused_recount");
     return GS_OK;
 }
@@ -124,9 +137,12 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
                                                     const Scene* __restrict__ scenes,
                                                     int wrap_mode, int dirty,
                                                     unsigned* __restrict__ err,
-                                                    unsigned* __restrict__ retry_count) {
+                                                    unsigned* __restrict__ retry_count,
+                                                    unsigned* __restrict__ tile, unsigned tiles) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *retry_count = 0u;  // the fused launch that follows refills it
+    // the scan has read the tile totals; the step's counting adds them anew
+    for (unsigned t = i; t < tiles; t += gridDim.x * blockDim.x) tile[t] = 0u;
     if (i >= n) return;
     permute_agent(A, B, n, cellrank, start, scenes, wrap_mode, dirty, err, i);
 }
@@ -134,7 +150,8 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st) {
     if (L.n == 0) return GS_OK;
     k_permute<<<blocks_for(L.n), kBlock, 0, st>>>(L.A, L.B, L.n, L.cellrank, L.start, L.scenes,
-                                                  wrap_mode, dirty ? 1 : 0, L.err, L.retry_count);
+                                                  wrap_mode, dirty ? 1 : 0, L.err, L.retry_count,
+                                                  L.tile, L.tiles);
     GS_LAUNCHED("fused_permute");
     return GS_OK;
 }
@@ -270,7 +287,7 @@ __device__ __forceinline__ void store_next(const FusedLaunch& L, unsigned s, con
                                            int wrap_mode) {
     // the cell count's atomic first: its round trip overlaps the state stores
     unsigned cell;
-    const unsigned rank = count_next(sc, me.pos, wrap_mode, L.count, cell);
+    const unsigned rank = count_next(sc, me.pos, wrap_mode, L.count, L.tile, cell);
     L.A.f[0][s] = make_float4(me.pos.x, me.pos.y, me.pos.z, fb(id));
     L.A.f[1][s] = make_float4(me.dir.x, me.dir.y, me.dir.z, me.speed);
     L.A.f[2][s] = make_float4(me.side.x, me.side.y, me.side.z, me.radius);
@@ -889,9 +906,9 @@ static gs_status launch_fused(const FusedLaunch& L, const StepDev& p, cudaStream
 }
 
 // ---- the wall/rest step in one persistent launch ----------------------------------
-// One cooperative launch runs every phase of the step - the scan's tile totals
-// and starts, the permute, the wall phase, the warp-per-agent exact lists and
-// the rest phase - over a grid of co-resident blocks.  Each
+// One cooperative launch runs every phase of the step - the scan's starts, the
+// permute, the wall phase, the warp-per-agent exact lists and the rest phase -
+// over a grid of co-resident blocks.  Each
 // phase is a grid-stride loop over the same device functions the separate
 // kernels run, so the results are the same bit for bit; a grid-wide barrier
 // separates the phases.  Every barrier wait is bounded: a block that polls
@@ -951,17 +968,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_step_persistent(FusedLaunch L, St
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(P.bar);
     const unsigned nthreads = gridDim.x * blockDim.x;
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    // scan: tile totals, then starts (zeroing the counts)
+    // scan: starts of the tiles near agents (zeroing their counts), from the
+    // tile totals the counting atomics added
     unsigned* sh = reinterpret_cast<unsigned*>(sm);
     unsigned* ws = sh + kScanTile + kScanTile / 32;
     for (unsigned t = blockIdx.x; t < P.T; t += gridDim.x)
-        scan_reduce_tile(L.count, P.C, t, sh, ws, P.tile);
+        scan_apply_sparse_tile(L.count, P.C, P.tile, P.start, P.T, t, p.scan_reach, P.live, sh,
+                               ws);
     if (!grid_sync(bar, P.limit, L.err)) return;
-    for (unsigned t = blockIdx.x; t < P.T; t += gridDim.x)
-        scan_apply_tile(L.count, P.C, P.tile, P.start, P.T, t, sh, ws);
-    if (!grid_sync(bar, P.limit, L.err)) return;
-    // permute A -> B
+    // permute A -> B; the tile totals start again for the step's counting
     if (gtid == 0) *L.retry_count = 0u;
+    for (unsigned t = gtid; t < P.T; t += nthreads) P.tile[t] = 0u;
     for (unsigned i = gtid; i < L.n; i += nthreads)
         permute_agent(L.A, L.B, L.n, L.cellrank, P.start, L.scenes, p.wrap_mode, p.dirty, L.err, i);
     if (!grid_sync(bar, P.limit, L.err)) return;

@@ -337,7 +337,7 @@ def knn_capacity(group) -> int:
 
 
 def step_launches(group, walls: bool) -> int:
-    """Kernel launches of one fused step: the counting-sort scan (two), the
+    """Kernel launches of one fused step: the counting-sort scan, the
     permute, the fused kernel (two with walls), and with the streaming scan
     (capacity 128 or 256) the warp-per-agent exact lists, plus, without
     walls, the exact redo (with walls the lists go straight to the second
@@ -346,7 +346,7 @@ def step_launches(group, walls: bool) -> int:
     if getattr(group, "persistent", False) and walls and cap > 64 and 8 < group.k <= 16:
         return 1
     redo = (1 if walls else 2) if cap > 64 else 0
-    return 2 + 1 + (2 if walls else 1) + redo
+    return 1 + 1 + (2 if walls else 1) + redo
 
 
 class Batch:

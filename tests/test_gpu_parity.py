@@ -488,17 +488,17 @@ def test_knn_capacity_reads_back():
     assert gs.knn_capacity(g) == 0
     gs.step(g, bins, walls, p, 1)
     assert gs.knn_capacity(g) in (128, 256)
-    # two scan launches, permute, wall phase, warp-per-agent lists, rest phase
-    assert gs.step_launches(g, True) == 6
+    # scan, permute, wall phase, warp-per-agent lists, rest phase
+    assert gs.step_launches(g, True) == 5
     gs.set_knn_capacity(g, 64)
     assert gs.knn_capacity(g) == 64
-    assert gs.step_launches(g, True) == 5
+    assert gs.step_launches(g, True) == 4
     s = sc.boids_sphere(4096, seed=0)
     pb = sc.boids_params(k=7)
     fb = group_of(s, pb.k)
     gs.step(fb, gs.KNNBinData(pb.world_cells, pb.world_size, 1), None, pb, 1)
     assert gs.knn_capacity(fb) in (32, 64)
-    assert gs.step_launches(fb, False) == 4
+    assert gs.step_launches(fb, False) == 3
 
 
 @pytest.mark.parametrize("capacity", [128, 256])
