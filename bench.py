@@ -508,6 +508,7 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     import gpusteer_gb300 as gs
     from gpusteer_gb300 import autotune
     from gpusteer_gb300._lib import check
+    from gpusteer_gb300.state import AgentState
 
     lib = gs.load()
     check(lib.gs_set_device(local_rank))
@@ -519,7 +520,8 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     t0 = time.perf_counter()
     if args.fixed_config:
         tr = autotune.TuneResult(params=base, block=args.block or 256, capacity=0,
-                                 ms_per_step=0.0, persistent=args.persistent)
+                                 ms_per_step=0.0, persistent=args.persistent,
+                                 parts=max(1, args.parts))
     else:
         tr = autotune.tune_batched(states, gaps, base, walls_rows)
     tune_s = time.perf_counter() - t0
@@ -532,27 +534,53 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     b = autotune.batch_for(states, gaps, p, walls_rows)
     configure(b.group)
     stream = torch.cuda.ExternalStream(b.group.stream)
+    # the timed batches: the scenes in tr.parts consecutive ranges, each a
+    # batch on its own stream, stepped concurrently (one batch when 1)
+    run = [b] if tr.parts <= 1 else autotune.batch_parts(states, gaps, p, walls_rows, tr.parts)
+    for x in run:
+        configure(x.group)
+    streams = [torch.cuda.ExternalStream(x.group.stream) for x in run]
 
-    # warm-up, then K timed steps (one graph replay each, state resident in HBM)
-    b.step(p, args.warmup)
-    b.group.synchronize()
+    # warm-up, then K timed steps (one graph replay per batch each, state
+    # resident in HBM); the other streams start after ev0 and ev1 waits for
+    # all of them
+    for x in run:
+        x.step(p, args.warmup)
+    for x in run:
+        x.group.synchronize()
     barrier(dist)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clocks:
         torch.cuda.synchronize()
         torch.cuda.profiler.start()  # ncu --profile-from-start off sees the timed steps only
-        ev0.record(stream)
+        ev0.record(streams[0])
+        for st_ in streams[1:]:
+            st_.wait_event(ev0)
         for _ in range(args.steps):
-            b.step(p, 1)
-        ev1.record(stream)
+            for x in run:
+                x.step(p, 1)
+        for st_ in streams[1:]:
+            done = torch.cuda.Event()
+            done.record(st_)
+            streams[0].wait_event(done)
+        ev1.record(streams[0])
         ev1.synchronize()
         torch.cuda.profiler.stop()
         torch.cuda.synchronize()
     barrier(dist)
     ms_max = allreduce_max(dist, ev0.elapsed_time(ev1))
     value = n * args.steps * world / (ms_max / 1e3)
+    parts_identical = None
+    if len(run) > 1:
+        # the parts against the whole batch stepped as often
+        b.step(p, args.warmup + args.steps)
+        want = b.download()
+        got = AgentState.concat([x.download() for x in run])
+        parts_identical = all(np.array_equal(getattr(got, k), getattr(want, k))
+                              for k in got.names())
+    del run
     phases = phase_times(lib, b.group, lambda k: b.step(p, k), max(3, min(args.steps, 10)))
-    launches_per_step = gs.step_launches(b.group, True)
+    launches_per_step = gs.step_launches(b.group, True) * max(1, tr.parts)
     measured_cap = gs.knn_capacity(b.group)  # the scan the resident steps used
     # both forms of the step on the same batch: separate launches (one graph
     # replay per step) and one persistent launch per step
@@ -603,8 +631,6 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
             grp.synchronize()
         el = allreduce_max(dist, time.perf_counter() - t0)
         return n * ps_steps * world / el, 1e3 * el / ps_steps, groups
-
-    from gpusteer_gb300.state import AgentState
 
     total = args.warmup + ps_steps
     b2 = autotune.batch_for(states, gaps, p, walls_rows)
@@ -664,12 +690,10 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
     e2e_one = n * e2e_steps * world / one_s
     # the parts: scene ranges of about equal agent counts
     K = max(1, min(args.e2e_parts, len(states)))
-    cum = np.cumsum([s.n for s in states])
-    cuts = [0] + [int(np.searchsorted(cum, n * i / K, side="right")) for i in range(1, K)] + \
-        [len(states)]
-    cuts = sorted(set(cuts))
+    ranges = autotune.scene_cuts(states, K)
+    cuts = [lo for lo, _ in ranges] + [ranges[-1][1]]
     parts = []
-    for lo, hi in zip(cuts[:-1], cuts[1:]):
+    for lo, hi in ranges:
         bp = autotune.batch_for(states[lo:hi], gaps[lo:hi], p, walls_rows)
         # a fixed capacity (the host-stepping graph needs one): the one the
         # resident batch used
@@ -754,7 +778,11 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
         "data": "synthetic",
         "config": batched_config(p, len(states), n, world),
         "tuned": {"block": tr.block, "knn_capacity": tr.capacity or "auto",
-                  "cell": p.world_size[0] / p.world_cells[0], "persistent": tr.persistent},
+                  "cell": p.world_size[0] / p.world_cells[0], "persistent": tr.persistent,
+                  "parts": tr.parts},
+        "parts": {"count": tr.parts, "identical_to_one_batch": parts_identical,
+                  "launch": "the scenes in consecutive ranges of about equal agent counts, "
+                            "each a batch on its own stream, stepped concurrently"},
         "forms": forms,
         "per_scene": per_scene,
         "identical_to_per_scene": None if identical is None else {
@@ -1137,6 +1165,9 @@ def main():
     ap.add_argument("--block", type=int, default=None,
                     help="threads per block of the fused launches (large/chokepoint/boids "
                          "workloads, and the batched workload with --fixed-config)")
+    ap.add_argument("--parts", type=int, default=1,
+                    help="batched workload with --fixed-config: scene ranges stepped "
+                         "concurrently, each a batch on its own stream")
     ap.add_argument("--persistent", action="store_true",
                     help="batched workload with --fixed-config: one persistent launch per step")
     ap.add_argument("--no-sub", action="store_true",
