@@ -376,9 +376,11 @@ GS_HD void avoid_lite_add(AvoidLite& a, const Self& s, unsigned rank, V3 bpos, V
 // h - min_t |rv|^2 > 2^-14 (S + min_t |rv|^2) proves t > min_t, each margin
 // hundreds of times the rounding bound.  Outside the guarded ranges (tiny or
 // huge magnitudes, rs = 0, NaN) it answers true and the exact test runs.
-GS_HD bool avoid_time_may_fall_in(const Self& s, float min_t, V3 bpos, V3 bdir, float bspeed) {
+// The caller passes rp = s.pos - bpos as the negated offset bpos - s.pos it
+// already has: the same values (only the sign of an exact zero can differ,
+// which no comparison here sees).
+GS_HD bool avoid_time_may_fall_in(const Self& s, float min_t, V3 rp, V3 bdir, float bspeed) {
     const V3 rv = sub(mul(bdir, bspeed), mul(s.dir, s.speed));
-    const V3 rp = sub(s.pos, bpos);
     const float ss = dot(rv, rv);
     const float h = dot(rv, rp);
     const float S = (fabsf(rv.x * rp.x) + fabsf(rv.y * rp.y)) + fabsf(rv.z * rp.z);

@@ -761,7 +761,8 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
             accumulate(a, p, need & ~NEED_AVOID, fs, fa, fc, gs_, ga, gc, me, i, kd, v3(b0[j]),
                        v3(b1[j]), b1[j].w, b0[j].w);
             if ((need & NEED_AVOID) &&
-                avoid_time_may_fall_in(me, p.min_time_col, v3(b0[j]), v3(b1[j]), b1[j].w))
+                avoid_time_may_fall_in(me, p.min_time_col, neg(sub(v3(b0[j]), me.pos)), v3(b1[j]),
+                                       b1[j].w))
                 exact_avoid |= 1u << i;
         }
         if (bs[kRestChunk - 1] == UINT_MAX) break;
