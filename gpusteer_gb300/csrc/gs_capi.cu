@@ -245,24 +245,20 @@ static gs_status walls_db(gs_walls w, const Grid& grid, unsigned C, cudaStream_t
 }
 
 // Candidate capacity of the fused KNN scan from the crowd's density.  The
-// crowd is taken as a Poisson scatter of lambda agents per cell over some
-// region of cells: then agents / occupied cells = lambda / (1 - exp(-lambda)),
-// solved for lambda by bisection, and an agent sees m = lambda * (2r+1)^d
-// candidates on average.  32 (collecting scan) when m is at least four
-// standard deviations below 32, else the streaming scan with 128 or 256
-// candidates.  Agents beyond the capacity take the exact redo path, so this
-// only affects speed.
-static unsigned knn_capacity(unsigned n, unsigned occupied, const Grid& g, unsigned r) {
+// other agents in an agent's own cell, averaged over the agents, are
+// lambda = sum c (c - 1) / n over the cell counts c (for a Poisson scatter of
+// lambda agents per cell this is lambda itself; averaged over agents, not
+// cells, so the dense scenes of a batch count by their agents), and an agent
+// sees m = lambda * (2r+1)^d candidates on average.  32 (collecting scan)
+// when m is at least four standard deviations below 32, else the streaming
+// scan with 128 or 256 candidates.  Agents beyond the capacity take the
+// exact redo path, so this only affects speed (a batch whose densest scenes
+// passed 128 candidates per box ran 3.7 times slower on 128 than on 256).
+static unsigned knn_capacity(unsigned n, unsigned long long sumsq, const Grid& g, unsigned r) {
     double box = 1.0;
     for (int a = 0; a < 3; ++a) box *= double(std::min<unsigned>(2 * r + 1, g.wc[a]));
-    const double ratio = occupied ? double(n) / double(occupied) : 1.0;
-    double lo = 0.0, hi = std::max(ratio, 1e-9);
-    for (int it = 0; it < 60; ++it) {
-        const double mid = 0.5 * (lo + hi);
-        const double f = mid > 1e-12 ? mid / (1.0 - std::exp(-mid)) : 1.0;
-        (f < ratio ? lo : hi) = mid;
-    }
-    const double m = 0.5 * (lo + hi) * box;
+    const double lambda = n ? (double(sumsq) - double(n)) / double(n) : 0.0;
+    const double m = std::max(lambda, 0.0) * box;
     const double top = m + 4.0 * std::sqrt(m) + 1.0;
     if (top <= 32.0) return 32u;
     return top <= 128.0 ? 128u : 256u;
@@ -1562,7 +1558,7 @@ static gs_status reserve_fused(gs_group g, unsigned C, bool walls, unsigned k, u
         GS_TRY(dalloc(&g->slot_of, n));
         GS_TRY(dalloc(&g->retry_count, 1));
         GS_TRY(dalloc(&g->retry_knn, size_t(std::min<size_t>(n, kRetryListCap)) * kRetryListK));
-        GS_TRY(dalloc(&g->d_stat, 1));
+        GS_TRY(dalloc(&g->d_stat, 4));
         GS_TRY(dalloc(&g->d_bar, 2));
         GS_CUDA(cudaMemset(g->d_bar, 0, 2 * sizeof(unsigned)));
         GS_CUDA(cudaMemset(g->d_err, 0, sizeof(unsigned)));
@@ -1681,8 +1677,9 @@ static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned 
             std::memcmp(&g->auto_cap_grid, &grid, sizeof(Grid)) != 0) {
             // one synchronising read per upload or grid change
             unsigned occupied = 0;
-            GS_TRY(count_occupied(g->fdb.count, C, g->d_stat, &occupied, st));
-            g->auto_cap = knn_capacity(g->n, occupied, grid, d.r);
+            unsigned long long sumsq = 0;
+            GS_TRY(count_occupied(g->fdb.count, C, g->d_stat, &occupied, &sumsq, st));
+            g->auto_cap = knn_capacity(g->n, sumsq, grid, d.r);
             g->auto_cap_grid = grid;
             g->auto_cap_r = d.r;
             g->auto_cap_valid = true;

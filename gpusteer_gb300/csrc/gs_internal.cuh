@@ -167,7 +167,7 @@ struct gs_group_s {
     unsigned* slot_of;     // [capacity] each agent's slot (conversion to the reference layout)
     unsigned* retry_count;
     unsigned* retry_knn;   // [min(capacity, kRetryListCap) * kRetryListK] exact-redo lists
-    unsigned* d_stat;      // one word of scratch for device-side statistics
+    unsigned* d_stat;      // four words of scratch for device-side statistics
     // candidate capacity of the fused KNN scan: knn_cap fixed by the caller
     // (gs_group_set_knn_capacity), else auto_cap, measured from the crowd's
     // density when the state is uploaded or the grid changes

@@ -265,8 +265,9 @@ size_t adjoint_scratch_bytes(unsigned n, unsigned k);
 void adjoint_scratch_bind(AdjointLaunch& A, void* base, unsigned n, unsigned k);
 gs_status launch_flock_adjoint(const AdjointLaunch& A, const StepDev& p, cudaStream_t st);
 
-// Number of non-zero entries of count[0..C), read back to the host (syncs st).
+// Number of non-zero entries of count[0..C) and the sum of their squares,
+// read back to the host (syncs st); d_tmp: 4 words of device scratch.
 gs_status count_occupied(const unsigned* count, unsigned C, unsigned* d_tmp, unsigned* h_out,
-                         cudaStream_t st);
+                         unsigned long long* h_sumsq, cudaStream_t st);
 
 }  // namespace gs

@@ -26,6 +26,7 @@
 #include "gs_knn.cuh"
 #include "gs_scan.cuh"
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -1096,26 +1097,42 @@ gs_status fused_to_reference(Fused A, unsigned n, const Scene* scenes, unsigned*
 
 namespace gs {
 
+// Occupied cells and the sum of squared cell counts (out[0], and the 64-bit
+// word at out + 2).
 __global__ void k_count_occupied(const unsigned* __restrict__ count, unsigned C,
                                  unsigned* __restrict__ out) {
     unsigned local = 0;
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x)
-        local += count[i] != 0u;
+    unsigned long long sq = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+        const unsigned c = count[i];
+        local += c != 0u;
+        sq += (unsigned long long)c * c;
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
+    for (int o = 16; o > 0; o >>= 1) {
+        local += __shfl_down_sync(0xffffffffu, local, o);
+        sq += __shfl_down_sync(0xffffffffu, sq, o);
+    }
+    if ((threadIdx.x & 31) == 0 && local) {
+        atomicAdd(out, local);
+        atomicAdd(reinterpret_cast<unsigned long long*>(out + 2), sq);
+    }
 }
 
 gs_status count_occupied(const unsigned* count, unsigned C, unsigned* d_tmp, unsigned* h_out,
-                         cudaStream_t st) {
+                         unsigned long long* h_sumsq, cudaStream_t st) {
     *h_out = 0;
+    *h_sumsq = 0;
     if (C == 0) return GS_OK;
-    GS_CUDA(cudaMemsetAsync(d_tmp, 0, sizeof(unsigned), st));
+    GS_CUDA(cudaMemsetAsync(d_tmp, 0, 4 * sizeof(unsigned), st));
     const unsigned nb = std::min(blocks_for(C, kBlock), 8u * 152u);
     k_count_occupied<<<nb, kBlock, 0, st>>>(count, C, d_tmp);
     GS_LAUNCHED("count_occupied");
-    GS_CUDA(cudaMemcpyAsync(h_out, d_tmp, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    unsigned h[4];
+    GS_CUDA(cudaMemcpyAsync(h, d_tmp, sizeof(h), cudaMemcpyDeviceToHost, st));
     GS_CUDA(cudaStreamSynchronize(st));
+    *h_out = h[0];
+    std::memcpy(h_sumsq, h + 2, sizeof(*h_sumsq));
     return GS_OK;
 }
 

@@ -501,6 +501,21 @@ def test_knn_capacity_reads_back():
     assert gs.step_launches(fb, False) == 3
 
 
+@pytest.mark.parametrize("cell,want", [(2.0, 128), (3.0, 256)])
+def test_knn_capacity_follows_the_dense_scenes_of_a_batch(cell, want):
+    """The automatic capacity weighs cells by their agents: a batch whose
+    densest scenes see more than 128 candidates per box (cell 3.0) takes the
+    256-candidate scan, the same scenes at cell 2.0 the 128-candidate one."""
+    states, gaps = sc.batched_chokepoint(24, seed=0)
+    p = sc.chokepoint_params(cell=cell)
+    b = gs.Batch([s.n for s in states], p.k, p.world_cells, p.world_size, p.search_radius)
+    for i, gap in enumerate(gaps):
+        b.set_walls(i, sc.chokepoint_walls(gap))
+    b.upload(AgentState.concat(states))
+    b.step(p, 1)
+    assert gs.knn_capacity(b.group) == want
+
+
 @pytest.mark.parametrize("capacity", [128, 256])
 def test_flat_streaming_scan_without_walls(capacity):
     """A 2D crowd (grid one cell high) without walls: the 3-row build of the
