@@ -63,6 +63,25 @@ def test_bins_reject_bad_grids(cells, size):
     assert e.value.status == 1
 
 
+@pytest.mark.parametrize("parts", [1, 2, 3, 4, 8, 300])
+def test_scene_cuts_cover_the_scenes_in_balanced_ranges(parts):
+    """The concurrent batches of the batched workload: consecutive scene
+    ranges covering every scene once, of about equal agent counts."""
+    from gpusteer_gb300 import autotune
+
+    states, _ = sc.batched_chokepoint(40, seed=3)
+    ranges = autotune.scene_cuts(states, parts)
+    assert ranges[0][0] == 0 and ranges[-1][1] == len(states)
+    assert all(a < b for a, b in ranges)
+    assert all(ranges[i][1] == ranges[i + 1][0] for i in range(len(ranges) - 1))
+    assert len(ranges) <= min(parts, len(states))
+    if parts <= 4:
+        agents = [sum(s.n for s in states[a:b]) for a, b in ranges]
+        n = sum(agents)
+        # each range ends at the first scene that reaches its share
+        assert max(agents) <= n / len(ranges) + max(s.n for s in states)
+
+
 def test_splitmix_stream_is_fixed():
     # first outputs of splitmix64 seeded with 0 (published test values)
     v = sc.splitmix64(0, 3)
