@@ -531,6 +531,31 @@ def test_flat_streaming_scan_without_walls(capacity):
     assert_state(g.download(), want, skip_side=want.speed == 0)
 
 
+@pytest.mark.parametrize("wide", [False, True])
+def test_scan_over_tiles_near_agents(wide):
+    """The step's scan writes starts only for the cell tiles within reach of
+    agents.  A flock in one corner of a large grid leaves most tiles empty
+    and unwritten; on a grid whose box spans more tiles than a block can
+    test (1024 x 4 x 1024 cells: y rows are a million labels apart) every
+    tile is written.  Both against the oracle over the steps' moves across
+    tiles."""
+    if wide:
+        p = sc.boids_params(k=16, world=2048.0, cell=2.0).replace(
+            world_size=(2048.0, 8.0, 2048.0), world_cells=(1024, 4, 1024))
+        s = sc.boids_sphere(4096, radius=30.0, seed=12)
+        s.position[:, 1] *= np.float32(0.1)  # a disc inside the 8-unit-high world
+    else:
+        p = sc.boids_params(k=16, world=512.0, cell=4.0)
+        s = sc.boids_sphere(8192, radius=30.0, seed=12)
+        s.position[:, :3] += np.float32(200.0)
+    bins = gs.KNNBinData(p.world_cells, p.world_size, 1)
+    g = group_of(s, p.k)
+    gs.step(g, bins, None, p, 6)
+    want = s.copy()
+    ol.run(want, p, 6)
+    assert_state(g.download(), want, skip_side=want.speed == 0)
+
+
 def test_streaming_scan_in_3d_matches_oracle():
     s = sc.boids_sphere(20000, radius=25.0, seed=8)
     p = sc.boids_params(k=16, world=64.0, cell=2.0)
