@@ -771,6 +771,30 @@ def test_batched_scene_matches_oracle():
         off += s.n
 
 
+@pytest.mark.parametrize("capacity", [0, 128])
+def test_ragged_batch_with_empty_and_single_agent_scenes(capacity):
+    """Scenes of 0, 1, 17 and 3,000 agents in one batch (and an empty last
+    scene): every non-empty scene equals the oracle stepped alone."""
+    counts = [0, 1, 17, 3000, 0]
+    states = [sc.chokepoint_agents(n, seed=40 + i) for i, n in enumerate(counts)]
+    gaps = [10.0, 7.5, 20.0, 12.5, 30.0]
+    p = sc.chokepoint_params(world=256.0, cell=2.0)
+    b = batch_setup(states, gaps, p)
+    gs.set_knn_capacity(b.group, capacity)
+    b.step(p, 15)
+    got = b.download()
+    assert got.n == sum(counts)
+    off = 0
+    for st, g in zip(states, gaps):
+        if st.n:
+            want = st.copy()
+            walls = ol.split_walls(*sc.walls_from_rows(sc.chokepoint_walls(g)), p.world_size,
+                                   p.world_cells)
+            ol.run(want, p, 15, walls=walls)
+            assert_state(got.subset(slice(off, off + st.n)), want, skip_side=want.speed == 0)
+        off += st.n
+
+
 def test_persistent_step_equals_separate_launches():
     """One cooperative persistent launch per step (scan, permute, wall phase,
     exact lists, redo and rest phase between grid-wide barriers) equals the
