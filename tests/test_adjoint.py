@@ -247,7 +247,7 @@ def test_fit_recovers_steering_weights():
         opt.step()
         sched.step()
         if first is None:
-            first = float(loss)
+            first = float(loss.detach())
     final = ah.GpuRollout.apply(v0, w.detach(), r)
     last = float(((final - target) ** 2).mean())
     assert last < 1e-2 * first, (first, last, w)
