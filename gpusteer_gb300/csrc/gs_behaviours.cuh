@@ -379,17 +379,21 @@ GS_HD void avoid_lite_add(AvoidLite& a, const Self& s, unsigned rank, V3 bpos, V
 // The caller passes rp = s.pos - bpos as the negated offset bpos - s.pos it
 // already has: the same values (only the sign of an exact zero can differ,
 // which no comparison here sees).
-GS_HD bool avoid_time_may_fall_in(const Self& s, float min_t, V3 rp, V3 bdir, float bspeed) {
-    const V3 rv = sub(mul(bdir, bspeed), mul(s.dir, s.speed));
-    const float ss = dot(rv, rv);
-    const float h = dot(rv, rp);
-    const float S = (fabsf(rv.x * rp.x) + fabsf(rv.y * rp.y)) + fabsf(rv.z * rp.z);
+// The decision from ss = dot(rv, rv), h = dot(rv, rp) and S.
+GS_HD bool avoid_time_window_test(float ss, float h, float S, float min_t) {
     if (!(ss >= 0x1p-60f && ss <= 0x1p60f && S >= 0x1p-60f && S <= 0x1p60f && min_t > 0.f &&
           min_t <= 0x1p30f))
         return true;
     if (h < -0x1p-14f * S) return false;
     const float msq = min_t * ss;
     return !(h - msq > 0x1p-14f * (S + msq));
+}
+GS_HD bool avoid_time_may_fall_in(const Self& s, float min_t, V3 rp, V3 bdir, float bspeed) {
+    const V3 rv = sub(mul(bdir, bspeed), mul(s.dir, s.speed));
+    const float ss = dot(rv, rv);
+    const float h = dot(rv, rp);
+    const float S = (fabsf(rv.x * rp.x) + fabsf(rv.y * rp.y)) + fabsf(rv.z * rp.z);
+    return avoid_time_window_test(ss, h, S, min_t);
 }
 
 // fetch(rank, pos, dir, speed) reads list entry `rank` as the pass saw it.

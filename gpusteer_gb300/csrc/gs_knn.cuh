@@ -263,6 +263,21 @@ __device__ __forceinline__ unsigned long long pack_xy(float x, float y) {
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
     return r;
 }
+__device__ __forceinline__ void unpack_xy(unsigned long long v, float& x, float& y) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long packed_sub(unsigned long long a,
+                                                         unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long packed_mul(unsigned long long a,
+                                                         unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ float dist_sq_xy2(unsigned long long pxy, float pz, float4 q) {
     const unsigned long long qxy = pack_xy(q.x, q.y);
     unsigned long long o, sq;

@@ -167,14 +167,13 @@ struct Accs {
 // `need` is p.need, or a compile-time mask equal to it in a kernel
 // specialised for one configuration (the unused accumulators then vanish).
 // gs, ga, gc: the agent's angle gates of the three flocking behaviours.
-__device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned need,
-                                           const FlockParams& fs, const FlockParams& fa,
-                                           const FlockParams& fc, AngleGate gs_, AngleGate ga,
-                                           AngleGate gc, const Self& me, unsigned rank,
-                                           float knn_d, V3 bpos, V3 bdir, float bspeed,
-                                           float bradius) {
-    const V3 offset = sub(bpos, me.pos);
-    const float dsq = dot(offset, offset);
+// offset = bpos - me.pos and dsq = dot(offset, offset), computed by the caller.
+__device__ __forceinline__ void accumulate_at(Accs& a, const StepDev& p, unsigned need,
+                                              const FlockParams& fs, const FlockParams& fa,
+                                              const FlockParams& fc, AngleGate gs_, AngleGate ga,
+                                              AngleGate gc, const Self& me, unsigned rank,
+                                              float knn_d, V3 offset, float dsq, V3 bpos,
+                                              V3 bdir, float bspeed, float bradius) {
     if (need & (NEED_SEP | NEED_ALI | NEED_COH)) {
         // inBoidNeighborhood (FlockingCommon.cuh:4-30) for the three flocking
         // behaviours, without its square root and divisions where they cannot
@@ -230,6 +229,61 @@ __device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned n
     // (avoid-walls); the caller passes it then, else -1
     if (need & NEED_CLOSE)
         close_add(a.close, me, p.min_sep, knn_d < 0.f ? sqrtf(dsq) : knn_d, bpos, bradius);
+}
+
+__device__ __forceinline__ void accumulate(Accs& a, const StepDev& p, unsigned need,
+                                           const FlockParams& fs, const FlockParams& fa,
+                                           const FlockParams& fc, AngleGate gs_, AngleGate ga,
+                                           AngleGate gc, const Self& me, unsigned rank,
+                                           float knn_d, V3 bpos, V3 bdir, float bspeed,
+                                           float bradius) {
+    const V3 offset = sub(bpos, me.pos);
+    accumulate_at(a, p, need, fs, fa, fc, gs_, ga, gc, me, rank, knn_d, offset,
+                  dot(offset, offset), bpos, bdir, bspeed, bradius);
+}
+
+// The rest phase's per-neighbour arithmetic with the x and y components in
+// packed f32x2 subtracts and multiplies (elementwise, rounded to nearest, not
+// contracted: the same operations in the same order, so the same bits).
+struct PackedSelf {
+    unsigned long long pos_xy, vel_xy;  // me.pos.xy, me.dir.xy * me.speed
+    float vel_z;
+};
+__device__ __forceinline__ PackedSelf packed_self(const Self& me) {
+    PackedSelf q;
+    q.pos_xy = pack_xy(me.pos.x, me.pos.y);
+    q.vel_xy = packed_mul(pack_xy(me.dir.x, me.dir.y), pack_xy(me.speed, me.speed));
+    q.vel_z = me.dir.z * me.speed;
+    return q;
+}
+// offset = bpos - me.pos (x and y also packed, in o_xy) and dot(offset, offset)
+__device__ __forceinline__ float packed_offset(const PackedSelf& q, const Self& me, float4 b0,
+                                               V3& off, unsigned long long& o_xy) {
+    o_xy = packed_sub(pack_xy(b0.x, b0.y), q.pos_xy);
+    unpack_xy(o_xy, off.x, off.y);
+    off.z = b0.z - me.pos.z;
+    float sx, sy;
+    unpack_xy(packed_mul(o_xy, o_xy), sx, sy);
+    return (sx + sy) + off.z * off.z;
+}
+// avoid_time_may_fall_in with rp = me.pos - bpos = -offset: h = dot(rv, rp)
+// is -dot(rv, offset) and S the same sum of magnitudes (negation is exact;
+// only the sign of a zero h can differ, which the comparisons do not see).
+__device__ __forceinline__ bool packed_avoid_time_may_fall_in(const PackedSelf& q,
+                                                              unsigned long long o_xy,
+                                                              float off_z, float min_t,
+                                                              float4 b1) {
+    const unsigned long long rv_xy =
+        packed_sub(packed_mul(pack_xy(b1.x, b1.y), pack_xy(b1.w, b1.w)), q.vel_xy);
+    const float rv_z = b1.z * b1.w - q.vel_z;
+    float sx, sy, hx, hy;
+    unpack_xy(packed_mul(rv_xy, rv_xy), sx, sy);
+    unpack_xy(packed_mul(rv_xy, o_xy), hx, hy);
+    const float hz = rv_z * off_z;
+    const float ss = (sx + sy) + rv_z * rv_z;
+    const float h = -((hx + hy) + hz);
+    const float S = (fabsf(hx) + fabsf(hy)) + fabsf(hz);
+    return avoid_time_window_test(ss, h, S, min_t);
 }
 
 // Behaviours order[first..] in order, then nothing else.  fetch(rank, pos,
@@ -742,6 +796,7 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
     // Neighbours kRestChunk at a time: their slots, then their gathers, are
     // issued together.
     unsigned exact_avoid = 0;
+    const PackedSelf pq = packed_self(me);
     for (unsigned i0 = 0; i0 < p.k; i0 += kRestChunk) {
         unsigned bs[kRestChunk];
         float4 b0[kRestChunk], b1[kRestChunk];
@@ -759,11 +814,13 @@ __device__ __forceinline__ void rest_agent(const FusedLaunch& L, const StepDev& 
             if (bs[j] == UINT_MAX) break;
             const unsigned i = i0 + j;
             const float kd = (need & NEED_CLOSE) ? L.knn_dist[size_t(i) * L.n + s] : -1.f;
-            accumulate(a, p, need & ~NEED_AVOID, fs, fa, fc, gs_, ga, gc, me, i, kd, v3(b0[j]),
-                       v3(b1[j]), b1[j].w, b0[j].w);
+            V3 off;
+            unsigned long long o_xy;
+            const float dsq = packed_offset(pq, me, b0[j], off, o_xy);
+            accumulate_at(a, p, need & ~NEED_AVOID, fs, fa, fc, gs_, ga, gc, me, i, kd, off, dsq,
+                          v3(b0[j]), v3(b1[j]), b1[j].w, b0[j].w);
             if ((need & NEED_AVOID) &&
-                avoid_time_may_fall_in(me, p.min_time_col, neg(sub(v3(b0[j]), me.pos)), v3(b1[j]),
-                                       b1[j].w))
+                packed_avoid_time_may_fall_in(pq, o_xy, off.z, p.min_time_col, b1[j]))
                 exact_avoid |= 1u << i;
         }
         if (bs[kRestChunk - 1] == UINT_MAX) break;
