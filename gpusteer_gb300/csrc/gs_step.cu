@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(kBlock) k_knn_retry(FusedLaunch L, StepDev p) 
 
 // ---- whole step without walls -------------------------------------------------------
 constexpr unsigned kNbrChunk = 1;  // measured best for the flock (2: +2.5 %, 4: +9 %)
-constexpr unsigned kRestChunk = 2;  // the rest phase's (1: +7 %, 4: +33 %, spills)
+constexpr unsigned kRestChunk = 2;  // the rest phase's (1: +7 %, 3: +6 %, 4: +12 %; spills)
 
 // NEEDC: the behaviours that read the neighbour list, fixed at compile time
 // (kNeedRuntime: taken from p.need).
