@@ -362,14 +362,15 @@ gs_status gs_group_set_graphs(gs_group g, int enable);
 gs_status gs_group_set_block(gs_group g, unsigned threads);
 /* Candidate capacity of the fused step's KNN scan: 32 or 64 (collecting
  * scan, for sparse crowds), 128 or 256 (streaming scan, for crowded cells),
- * or 0 (default: chosen from the crowd's density, measured once after each
- * upload).  Results do not depend on it: agents with more candidates are
+ * or 0 (default: chosen from the crowd's density, the agents in an agent's
+ * cell averaged over the agents, measured once after each upload).  Results do not depend on it: agents with more candidates are
  * redone by the exact scan.  Not part of the reference. */
 gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity);
 /* The capacity the fused step uses: the fixed one, else the one measured at
- * the last step (0 before the first).  With 128 or 256 a step makes one more
- * launch: the exact lists of the agents the fast scan hands to the redo,
- * found by one warp per agent. */
+ * the last step (0 before the first).  With 128 or 256 a step makes more
+ * launches: the exact lists of the agents the fast scan hands to the redo,
+ * found by one warp per agent (with avoid-walls they go straight into the
+ * neighbour lists; without, a redo launch then steps those agents). */
 gs_status gs_group_knn_capacity(gs_group g, unsigned* capacity);
 
 /* ---- batched scenes -------------------------------------------------------------
