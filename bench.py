@@ -812,7 +812,9 @@ def gpu_batched_line(args, dist, rank, world, local_rank):
                      "kernel": "k_fused_walls+k_fused_rest",
                      "algorithmic_bytes_per_launch": fbytes, "peak_source": peak_src},
         "phases_ms": phases,
-        "issue": issue_rate("batched", fused_ms, clocks.summary(), local_rank),
+        # the committed instruction count is the 256-scene workload's
+        "issue": (issue_rate("batched", fused_ms, clocks.summary(), local_rank)
+                  if len(states) == 256 else None),
         "step_model_gbs": step_model_bytes(n, p.k, cells * len(states)) /
                           (ms_max / args.steps / 1e3) / 1e9,
         "clocks": clocks.summary(),
