@@ -99,7 +99,7 @@ def grid_for(base: StepParams, cell: float) -> StepParams:
 
 
 def tune_batched(states, gaps, base: StepParams, walls_rows, cell_scales=(1.0, 1.25, 1.5),
-                 blocks=(128, 256), capacities=(0, 256), part_counts=(1, 2, 4), steps: int = 4,
+                 blocks=(128, 256), capacities=(0, 256), part_counts=(1, 2, 3, 4), steps: int = 4,
                  warmup: int = 2) -> TuneResult:
     """Times every (cell size, block, capacity, form) on the batch; cell
     sizes are the scenario's cell times `cell_scales` (all >= 1).  The
