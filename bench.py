@@ -901,7 +901,7 @@ def issue_rate(workload: str, kernel_ms: float, clocks: dict, device: int):
     """Warp instructions the dominant kernel(s) issue per launch (from the
     committed ncu capture, profiles/issue_<workload>.json) over what the SMs
     can issue in the measured time: SMs x 4 schedulers x median SM clock x
-    time.  An instruction-bound kernel is judged against this ceiling."""
+    time.  An instruction-bound kernel is measured against this ceiling."""
     path = REPO / "profiles" / f"issue_{workload}.json"
     if not path.exists() or not kernel_ms or not clocks.get("sm_mhz"):
         return None
