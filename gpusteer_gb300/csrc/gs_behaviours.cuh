@@ -364,22 +364,21 @@ GS_HD void avoid_lite_add(AvoidLite& a, const Self& s, unsigned rank, V3 bpos, V
         }
     }
 }
-// False only when the nearest-approach time of the neighbour (bpos, bdir,
-// bspeed) is provably outside [0, min_t): avoid_lite_add then leaves the
-// accumulator as it is (its window only narrows during the pass).  The
-// reference's time (nearest_approach_time, SteerToAvoidNeighborsCUDAKernel.cu:
-// 192-233) is t = fl(fl(dot(fl(rv / rs), rp)) / rs) with rs = sqrtf(dot(rv,
-// rv)); with the same rv, rp and P = rv . rp, S = sum |rv_i rp_i|, standard
-// error analysis gives |t - P / rs^2| <= gamma_6 S / rs^2 and rs^2 = |rv|^2
-// (1 + eta), |eta| <= 5u (u = 2^-24).  So h = dot(rv, rp) < -2^-14 S proves
-// t < 0 (nonzero: S >= 2^-60 and |rv|^2 <= 2^60 keep |t| above 2^-134), and
-// h - min_t |rv|^2 > 2^-14 (S + min_t |rv|^2) proves t > min_t, each margin
-// hundreds of times the rounding bound.  Outside the guarded ranges (tiny or
-// huge magnitudes, rs = 0, NaN) it answers true and the exact test runs.
-// The caller passes rp = s.pos - bpos as the negated offset bpos - s.pos it
-// already has: the same values (only the sign of an exact zero can differ,
-// which no comparison here sees).
-// The decision from ss = dot(rv, rv), h = dot(rv, rp) and S.
+// Neighbour avoidance's pre-test: false only when the nearest-approach time
+// of a neighbour is provably outside [0, min_t), so that avoid_lite_add
+// would leave the accumulator as it is (its window only narrows during the
+// pass).  From the relative velocity rv = bdir * bspeed - dir * speed and
+// rp = pos - bpos: ss = dot(rv, rv), h = dot(rv, rp) and S = sum |rv_i rp_i|.
+// The reference's time (nearest_approach_time, SteerToAvoidNeighborsCUDA
+// Kernel.cu:192-233) is t = fl(fl(dot(fl(rv / rs), rp)) / rs) with
+// rs = sqrtf(dot(rv, rv)); standard error analysis gives
+// |t - h / rs^2| <= gamma_6 S / rs^2 and rs^2 = |rv|^2 (1 + eta), |eta| <= 5u
+// (u = 2^-24).  So h < -2^-14 S proves t < 0 (nonzero: S >= 2^-60 and
+// |rv|^2 <= 2^60 keep |t| above 2^-134), and h - min_t |rv|^2 >
+// 2^-14 (S + min_t |rv|^2) proves t > min_t, each margin hundreds of times
+// the rounding bound.  Outside the guarded ranges (tiny or huge magnitudes,
+// rs = 0, NaN) it answers true and the exact test runs.  (The sign of a zero
+// h does not matter: no comparison here sees it.)
 GS_HD bool avoid_time_window_test(float ss, float h, float S, float min_t) {
     if (!(ss >= 0x1p-60f && ss <= 0x1p60f && S >= 0x1p-60f && S <= 0x1p60f && min_t > 0.f &&
           min_t <= 0x1p30f))
@@ -387,13 +386,6 @@ GS_HD bool avoid_time_window_test(float ss, float h, float S, float min_t) {
     if (h < -0x1p-14f * S) return false;
     const float msq = min_t * ss;
     return !(h - msq > 0x1p-14f * (S + msq));
-}
-GS_HD bool avoid_time_may_fall_in(const Self& s, float min_t, V3 rp, V3 bdir, float bspeed) {
-    const V3 rv = sub(mul(bdir, bspeed), mul(s.dir, s.speed));
-    const float ss = dot(rv, rv);
-    const float h = dot(rv, rp);
-    const float S = (fabsf(rv.x * rp.x) + fabsf(rv.y * rp.y)) + fabsf(rv.z * rp.z);
-    return avoid_time_window_test(ss, h, S, min_t);
 }
 
 // fetch(rank, pos, dir, speed) reads list entry `rank` as the pass saw it.

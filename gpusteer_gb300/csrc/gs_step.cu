@@ -266,9 +266,10 @@ __device__ __forceinline__ float packed_offset(const PackedSelf& q, const Self& 
     unpack_xy(packed_mul(o_xy, o_xy), sx, sy);
     return (sx + sy) + off.z * off.z;
 }
-// avoid_time_may_fall_in with rp = me.pos - bpos = -offset: h = dot(rv, rp)
-// is -dot(rv, offset) and S the same sum of magnitudes (negation is exact;
-// only the sign of a zero h can differ, which the comparisons do not see).
+// The avoidance pre-test (avoid_time_window_test) for rp = me.pos - bpos =
+// -offset: h = dot(rv, rp) is -dot(rv, offset) and S the same sum of
+// magnitudes (negation is exact; only the sign of a zero h can differ, which
+// the comparisons do not see).
 __device__ __forceinline__ bool packed_avoid_time_may_fall_in(const PackedSelf& q,
                                                               unsigned long long o_xy,
                                                               float off_z, float min_t,
