@@ -668,9 +668,12 @@ gs_status gs_group_upload(gs_group g, const gs_agent_arrays* h, unsigned n) {
         !h->max_speed || !h->max_force || !h->radius || !h->mass || !h->applied)
         return fail(GS_ERR_INVALID_ARG, "upload needs every array");
     GS_TRY(upload_enqueue(g, h, n));
+    // the automatic KNN capacity is measured again (a synchronising read)
+    // only when the agent count changes: stepping host state in a loop keeps
+    // its choice, which never changes results
+    if (n != g->n) g->auto_cap_valid = false;
     g->n = n;
     g->db.valid = false;
-    g->auto_cap_valid = false;
     touched(g);
     return GS_OK;
 }

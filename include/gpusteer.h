@@ -363,7 +363,8 @@ gs_status gs_group_set_block(gs_group g, unsigned threads);
 /* Candidate capacity of the fused step's KNN scan: 32 or 64 (collecting
  * scan, for sparse crowds), 128 or 256 (streaming scan, for crowded cells),
  * or 0 (default: chosen from the crowd's density, the agents in an agent's
- * cell averaged over the agents, measured once after each upload).  Results do not depend on it: agents with more candidates are
+ * cell averaged over the agents, measured at the first step after an upload
+ * that changes the agent count, or after a grid change).  Results do not depend on it: agents with more candidates are
  * redone by the exact scan.  Not part of the reference. */
 gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity);
 /* The capacity the fused step uses: the fixed one, else the one measured at
