@@ -1101,6 +1101,8 @@ def gpu_single_line(args, dist, rank, world, local_rank):
     e2e_s = allreduce_max(dist, time.perf_counter() - t0)
     e2e = n * e2e_steps * world / e2e_s
     bytes_state = n * (16 * 3 + 12 * 2 + 4 * 5 + 4)
+    # in place, the four per-agent constants no step changes are not copied back
+    bytes_back = bytes_state - n * 16
     for ptr in keep_in + keep_out:
         lib.gs_host_free(ptr)
 
@@ -1129,7 +1131,9 @@ def gpu_single_line(args, dist, rank, world, local_rank):
         "data": "synthetic",
         "config": single_config(args.workload, p, n, world),
         "e2e": {"value": e2e, "unit": "agent-steps/s", "h2d_bytes_per_step": bytes_state,
-                "d2h_bytes_per_step": bytes_state},
+                "d2h_bytes_per_step": bytes_back,
+                "api": "gs_step_host in place: page-locked host state copied in, one step, "
+                       "copied out (the per-agent constants stay on the host)"},
         "gpu_launches": gs.step_launches(group, has_walls) * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,

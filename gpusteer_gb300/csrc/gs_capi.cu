@@ -1822,9 +1822,16 @@ gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params
 gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
                        unsigned steps, const gs_agent_arrays* in, unsigned n,
                        const gs_agent_arrays* out) {
+    if (!g || !in || !out) return fail(GS_ERR_INVALID_ARG, "null argument");
     GS_TRY(gs_group_upload(g, in, n));
     GS_TRY(gs_step(g, bins, walls, p, steps));
-    return gs_group_download(g, out);
+    // in place, the per-agent constants no step changes (maxSpeed, maxForce,
+    // radius, mass) are already on the host and are not copied back
+    const bool in_place = out->max_speed == in->max_speed && out->max_force == in->max_force &&
+                          out->radius == in->radius && out->mass == in->mass;
+    GS_TRY(download_enqueue(g, out, in_place));
+    GS_CUDA(cudaStreamSynchronize(g->stream));
+    return check_device_flags(g);
 }
 
 gs_status gs_group_set_persistent(gs_group g, int enable) {

@@ -350,7 +350,9 @@ gs_status gs_anti_penetration_wall(gs_group g, gs_knn knw, gs_walls walls, float
 gs_status gs_step(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
                   unsigned steps);
 /* As gs_step but the state comes from and goes back to host arrays, each copy
- * on the group's stream (the reference's per-frame SyncDevice / SyncHost). */
+ * on the group's stream (the reference's per-frame SyncDevice / SyncHost).
+ * When `out` shares `in`'s maxSpeed, maxForce, radius and mass arrays, those
+ * constants (which no step changes) are not copied back. */
 gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_params* p,
                        unsigned steps, const gs_agent_arrays* in, unsigned n,
                        const gs_agent_arrays* out);

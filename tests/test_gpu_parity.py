@@ -626,6 +626,13 @@ def test_step_host_is_upload_step_download():
     want = s.copy()
     ol.run(want, p, 5)
     assert_state(out, want, skip_side=want.speed == 0)
+    # in place: the state stepped in its own arrays, five more steps one call
+    # at a time (the constants stay on the host)
+    inplace = want.copy()
+    for _ in range(5):
+        gs.step_host(g, bins, None, p, 1, inplace, inplace)
+    ol.run(want, p, 5)
+    assert_state(inplace, want, skip_side=want.speed == 0)
 
 
 def test_large_flock_two_steps_match_oracle():
