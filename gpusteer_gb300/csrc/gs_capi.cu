@@ -1609,10 +1609,9 @@ struct WallsDev {
     const unsigned* cell_start = nullptr;
 };
 
-// Zeroes the fused engine's counts and tile totals before a recount.
+// Zeroes the fused engine's counts before a recount.
 static gs_status clear_counts(gs_group g, unsigned C, cudaStream_t st) {
     GS_CUDA(cudaMemsetAsync(g->fdb.count, 0, size_t(C) * 4, st));
-    GS_CUDA(cudaMemsetAsync(g->fdb.tile, 0, size_t(scan_tile_count(C)) * 4, st));
     return GS_OK;
 }
 
@@ -1662,13 +1661,15 @@ static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned 
         // counts left pending by an earlier fused step no longer apply
         GS_TRY(clear_counts(g, C, st));
         GS_TRY(fused_from_reference(view(g), agent_scene, g->d_scene, g->A, g->cellrank,
-                                    g->fdb.count, g->fdb.tile, d.wrap_mode, dirty, st));
+                                    g->fdb.count, d.wrap_mode, dirty, st));
+        GS_TRY(scan_tile_totals(g->fdb.count, C, g->fdb.tile, st));
         g->fused_current = true;
     } else if (std::memcmp(&g->fdb.grid, &grid, sizeof(Grid)) != 0 || !g->fdb.valid ||
                g->pending_wrap != d.wrap_mode) {
         GS_TRY(clear_counts(g, C, st));
-        GS_TRY(fused_recount(g->A, g->n, g->d_scene, g->cellrank, g->fdb.count, g->fdb.tile,
-                             d.wrap_mode, st));
+        GS_TRY(fused_recount(g->A, g->n, g->d_scene, g->cellrank, g->fdb.count, d.wrap_mode,
+                             st));
+        GS_TRY(scan_tile_totals(g->fdb.count, C, g->fdb.tile, st));
     }
     g->fdb.grid = grid;
     g->fdb.valid = true;
@@ -2088,7 +2089,8 @@ static gs_status io_compute_and_download(IoPart& q, unsigned steps, bool in_plac
     cudaStream_t st = g->stream;
     GS_TRY(clear_counts(g, q.Ct, st));
     GS_TRY(fused_from_reference(view(g), q.b->agent_scene, g->d_scene, g->A, g->cellrank,
-                                g->fdb.count, g->fdb.tile, q.d.wrap_mode, true, st));
+                                g->fdb.count, q.d.wrap_mode, true, st));
+    GS_TRY(scan_tile_totals(g->fdb.count, q.Ct, g->fdb.tile, st));
     for (unsigned i = 0; i < steps; ++i) {
         StepDev di = q.d;
         di.dirty = i == 0 ? 1 : 0;

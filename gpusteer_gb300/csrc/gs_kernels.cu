@@ -108,8 +108,9 @@ gs_status scan_counts(unsigned* count, unsigned* start, unsigned C, unsigned* ti
 }
 
 // ---- the fused engine's counting-sort scan: one launch, tiles near agents ---------
-// The counting atomics add each tile's total as they go, so no reduce pass
-// reads the counts; every block sums the totals of the tiles before its own (a
+// The step's counting atomics add each tile's total as they go, so no reduce
+// pass reads the counts (only a whole recount, from the reference layout or
+// on a new grid, takes one); every block sums the totals of the tiles before its own (a
 // few thousand words from L2) and writes its tile's starts, and no block
 // waits on another (scan_apply_sparse_tile).
 __global__ void __launch_bounds__(kBlock) k_scan_apply_sparse(unsigned* __restrict__ count,
@@ -121,6 +122,14 @@ __global__ void __launch_bounds__(kBlock) k_scan_apply_sparse(unsigned* __restri
     __shared__ unsigned sh[kScanTile + kScanTile / 32];
     __shared__ unsigned ws[kBlock / 32];
     scan_apply_sparse_tile(count, C, tile, start, T, blockIdx.x, reach, live, sh, ws);
+}
+
+gs_status scan_tile_totals(const unsigned* count, unsigned C, unsigned* tile, cudaStream_t st) {
+    const unsigned T = scan_tile_count(C);
+    if (T == 0) return GS_OK;
+    k_scan_reduce<<<T, kBlock, 0, st>>>(count, C, tile);
+    GS_LAUNCHED("scan_tile_totals");
+    return GS_OK;
 }
 
 gs_status scan_counts_sparse(unsigned* count, unsigned* start, unsigned C, const unsigned* tile,

@@ -16,6 +16,10 @@ unsigned scan_tile_count(unsigned C);
 // occupied one get starts (live[t] = 1) and zeroed counts.
 gs_status scan_counts_sparse(unsigned* count, unsigned* start, unsigned C, const unsigned* tile,
                              unsigned* live, unsigned reach, cudaStream_t st);
+// tile[t] = the total of count[] over scan tile t (after a whole recount,
+// whose agents come in no spatial order: per-agent tile atomics would all
+// contend on a few hundred words).
+gs_status scan_tile_totals(const unsigned* count, unsigned C, unsigned* tile, cudaStream_t st);
 // Tiles (of the scan) between a cell and the farthest start its box of
 // radius r reads, on a grid of wc cells.
 unsigned scan_reach_tiles(const unsigned wc[3], unsigned r);
@@ -217,13 +221,13 @@ struct FusedLaunch {
     unsigned* rec_knn;  // [n * k] neighbour indices, row-major, UINT_MAX after the last
 };
 
-// Both count each agent's cell into count[] and its scan tile's total into
-// tile[] (zeroed beforehand, like count[]).
+// Both count each agent's cell into count[] (zeroed beforehand); the scan
+// tile totals follow from scan_tile_totals.
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
-                               Fused A, uint2* cellrank, unsigned* count, unsigned* tile,
-                               int wrap_mode, bool dirty, cudaStream_t st);
+                               Fused A, uint2* cellrank, unsigned* count, int wrap_mode,
+                               bool dirty, cudaStream_t st);
 gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
-                        unsigned* count, unsigned* tile, int wrap_mode, cudaStream_t st);
+                        unsigned* count, int wrap_mode, cudaStream_t st);
 gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st);
 // `phase` (may be null) brackets each launch: phase(i, true) before and
 // phase(i, false) after the launch of phase i.

@@ -110,8 +110,9 @@ __device__ __forceinline__ void scan_apply_tile(unsigned* __restrict__ count, un
 }
 
 // The fused engine's scan, over tiles near agents only.  tile[] holds each
-// tile's exact total, added by the counting atomics themselves (no reduce
-// pass); the step reads the starts of cells at most `reach` tiles from an
+// tile's exact total, added by the step's counting atomics themselves (after
+// a whole recount, whose agents come in no spatial order, by a reduce pass);
+// the step reads the starts of cells at most `reach` tiles from an
 // agent's own tile (its box's rows, scan_reach_tiles).  So tile t's starts
 // are written, and its counts zeroed, only when a tile within `reach` of it
 // holds agents; live[t] records which.  The other tiles' counts are already

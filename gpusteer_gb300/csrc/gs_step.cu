@@ -47,12 +47,13 @@ __device__ __forceinline__ void add_to_tile(unsigned* tile, unsigned cell) {
 }
 
 // The agent's cell for the next step's counting sort: counted (the old count
-// is its rank in the cell) and added to its tile's total.
+// is its rank in the cell) and, given tile totals (tile not null), added to
+// its tile's total.
 __device__ __forceinline__ unsigned count_next(const Scene& sc, V3 pos, int wrap_mode,
                                                unsigned* count, unsigned* tile, unsigned& cell) {
     const V3 wp = wrap_world(pos, sc.grid.ws, wrap_mode);
     cell = sc.cell_offset + cell_of(sc.grid, wp);
-    add_to_tile(tile, cell);
+    if (tile) add_to_tile(tile, cell);
     return atomicAdd(count + cell, 1u);
 }
 
@@ -60,7 +61,7 @@ __device__ __forceinline__ unsigned count_next(const Scene& sc, V3 pos, int wrap
 __global__ void k_from_reference(GroupView g, const unsigned* __restrict__ agent_scene,
                                  const Scene* __restrict__ scenes, Fused A,
                                  uint2* __restrict__ cellrank, unsigned* __restrict__ count,
-                                 unsigned* __restrict__ tile, int wrap_mode, int dirty) {
+                                 int wrap_mode, int dirty) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
     const unsigned si = agent_scene ? agent_scene[i] : 0u;
@@ -75,35 +76,35 @@ __global__ void k_from_reference(GroupView g, const unsigned* __restrict__ agent
     A.f[4][i] = make_float4(g.max_speed[i], g.max_force[i], fb(g.applied[i]), fb(si));
     if (dirty) A.f[5][i] = g.steering[i];
     unsigned cell;
-    const unsigned rank = count_next(sc, v3(p), wrap_mode, count, tile, cell);
+    const unsigned rank = count_next(sc, v3(p), wrap_mode, count, nullptr, cell);
     cellrank[i] = make_uint2(cell, rank);
 }
 
 gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const Scene* scenes,
-                               Fused A, uint2* cellrank, unsigned* count, unsigned* tile,
-                               int wrap_mode, bool dirty, cudaStream_t st) {
+                               Fused A, uint2* cellrank, unsigned* count, int wrap_mode,
+                               bool dirty, cudaStream_t st) {
     if (g.n == 0) return GS_OK;
     k_from_reference<<<blocks_for(g.n), kBlock, 0, st>>>(g, agent_scene, scenes, A, cellrank,
-                                                         count, tile, wrap_mode, dirty ? 1 : 0);
+                                                         count, wrap_mode, dirty ? 1 : 0);
     GS_LAUNCHED("fused_from_reference");
     return GS_OK;
 }
 
 __global__ void k_recount(Fused A, unsigned n, const Scene* __restrict__ scenes,
                           uint2* __restrict__ cellrank, unsigned* __restrict__ count,
-                          unsigned* __restrict__ tile, int wrap_mode) {
+                          int wrap_mode) {
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Scene sc = scenes[u(A.f[4][i].w)];
     unsigned cell;
-    const unsigned rank = count_next(sc, v3(A.f[0][i]), wrap_mode, count, tile, cell);
+    const unsigned rank = count_next(sc, v3(A.f[0][i]), wrap_mode, count, nullptr, cell);
     cellrank[i] = make_uint2(cell, rank);
 }
 
 gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
-                        unsigned* count, unsigned* tile, int wrap_mode, cudaStream_t st) {
+                        unsigned* count, int wrap_mode, cudaStream_t st) {
     if (n == 0) return GS_OK;
-    k_recount<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, cellrank, count, tile, wrap_mode);
+    k_recount<<<blocks_for(n), kBlock, 0, st>>>(A, n, scenes, cellrank, count, wrap_mode);
     GS_LAUNCHED("fused_recount");
     return GS_OK;
 }
