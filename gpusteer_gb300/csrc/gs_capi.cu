@@ -1639,7 +1639,7 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
                               d.scan_reach, st));
     if (hook) hook->mark(0, false);
     if (hook) hook->mark(1, true);
-    GS_TRY(fused_permute(L, d.wrap_mode, d.dirty != 0, st));
+    GS_TRY(fused_permute(L, d.wrap_mode, d.dirty != 0, d.fresh != 0, st));
     if (hook) hook->mark(1, false);
     GS_TRY(fused_step(L, d, st, hook));
     return GS_OK;
@@ -1647,17 +1647,36 @@ static gs_status step_body(gs_group g, const FusedLaunch& L, const StepDev& d, u
 
 static void fill_launch(gs_group g, const StepDev& d, const WallsDev& w, FusedLaunch& L);
 
+// Whether the first step after an upload permutes by a gather.  A scene's
+// agents in agent order scatter within the scene's slot range: a scene of a
+// few thousand agents (a few hundred KB) scatters into lines that stay in L2
+// until they are whole, and there the gather's extra pass only adds time.
+// Measured end to end: a 10,000-agent scene, and batched scenes of up to
+// 20,000, are as fast either way (within 1-2 %); a 1,048,576-agent flock
+// gains 5 % with the gather.
+constexpr unsigned kGatherPermuteMinAgents = 1u << 17;  // 12 MB of state per scene
+static bool gather_first_permute(gs_group g) {
+    unsigned most = 0;
+    if (g->h_scenes)
+        for (const Scene& sc : *g->h_scenes) most = std::max(most, sc.n_agents);
+    return most >= kGatherPermuteMinAgents;
+}
+
 // Brings the fused engine's bucketed state and pending cell counts up to
 // date for steps on `grid` and fills the launch block L; picks the KNN
 // capacity into d.  dirty: the first step must add the steering and applied
-// bits left by per-function calls.
+// bits left by per-function calls.  fresh: the bucketed state was just
+// rebuilt in agent order, from scenes large enough that the first step's
+// permute gathers.
 static gs_status fused_setup(gs_group g, StepDev& d, const Grid& grid, unsigned C,
                              const unsigned* agent_scene, const WallsDev& w, FusedLaunch& L,
-                             bool& dirty) {
+                             bool& dirty, bool& fresh) {
     cudaStream_t st = g->stream;
     dirty = false;
+    fresh = false;
     if (!g->fused_current) {
         dirty = g->accum_dirty;
+        fresh = gather_first_permute(g);
         // counts left pending by an earlier fused step no longer apply
         GS_TRY(clear_counts(g, C, st));
         GS_TRY(fused_from_reference(view(g), agent_scene, g->d_scene, g->A, g->cellrank,
@@ -1710,6 +1729,7 @@ static void fill_launch(gs_group g, const StepDev& d, const WallsDev& w, FusedLa
     L.err = g->d_err;
     L.retry = g->retry;
     L.retry_count = g->retry_count;
+    L.agent_at = g->slot_of;  // free during a step: fused_to_reference refills it
     L.retry_knn = g->retry_knn;
     L.retry_cap = unsigned(std::min<size_t>(g->capacity, kRetryListCap));
     if (d.need & NEED_WALLS) {
@@ -1732,31 +1752,35 @@ static gs_status fused_run(gs_group g, StepDev d, const Grid& grid, unsigned C,
                            const unsigned* agent_scene, const WallsDev& w, unsigned steps) {
     cudaStream_t st = g->stream;
     FusedLaunch L;
-    bool dirty = false;
+    bool dirty = false, fresh = false;
     g->frame_cells = 0;
     // part of the graph key: a changed form or limit captures again
     d.persistent = g->persistent ? 1u : 0u;
     d.bar_limit = g->bar_limit ? g->bar_limit : kBarrierPollsDefault;
-    GS_TRY(fused_setup(g, d, grid, C, agent_scene, w, L, dirty));
+    GS_TRY(fused_setup(g, d, grid, C, agent_scene, w, L, dirty, fresh));
     Profiler prof(g);
     PhaseHook* hook = g->profiling ? &prof : nullptr;
     unsigned step = 0;
-    // A step with steering carried in from per-function calls runs eagerly;
-    // so do all steps while profiling, and the first step of a new launch
-    // configuration (which also performs one-time kernel set-up).
+    // A step with steering carried in from per-function calls, or the first
+    // after an upload (its permute gathers), runs eagerly; so do all steps
+    // while profiling, and the first step of a new launch configuration
+    // (which also performs one-time kernel set-up).
     const bool cfg_same = g->graph_exec && std::memcmp(&g->graph_L, &L, sizeof(L)) == 0 &&
                           std::memcmp(&g->graph_d, &d, sizeof(d)) == 0 && g->graph_C == C;
     // The legacy default stream cannot be captured: a group on it runs eagerly.
     const bool graphs = g->use_graph && st != cudaStreamLegacy && st != nullptr;
-    if (dirty || hook || !graphs || !cfg_same) {
+    if (dirty || fresh || hook || !graphs || !cfg_same) {
         const unsigned eager = (hook || !graphs) ? steps : 1u;
         for (; step < eager && step < steps; ++step) {
             d.dirty = dirty ? 1 : 0;
+            d.fresh = fresh ? 1 : 0;
             GS_TRY(step_body(g, L, d, C, hook));
             dirty = false;
+            fresh = false;
         }
     }
     d.dirty = 0;
+    d.fresh = 0;
     if (step < steps) {
         if (!(g->graph_exec && std::memcmp(&g->graph_L, &L, sizeof(L)) == 0 &&
               std::memcmp(&g->graph_d, &d, sizeof(d)) == 0 && g->graph_C == C)) {
@@ -2094,6 +2118,7 @@ static gs_status io_compute_and_download(IoPart& q, unsigned steps, bool in_plac
     for (unsigned i = 0; i < steps; ++i) {
         StepDev di = q.d;
         di.dirty = i == 0 ? 1 : 0;
+        di.fresh = i == 0 && gather_first_permute(g) ? 1 : 0;
         GS_TRY(step_body(g, q.L, di, q.Ct, nullptr));
     }
     GS_TRY(fused_to_reference(g->A, g->n, g->d_scene, g->slot_of, view(g), st));
@@ -2501,10 +2526,11 @@ static gs_status rollout_record(gs_rollout r, unsigned c, StepDev d, const Grid&
     GS_TRY(put_scenes(g, std::vector<Scene>{sc}));
     d.block = g->block;
     FusedLaunch L;
-    bool dirty = false;
-    GS_TRY(fused_setup(g, d, grid, C, nullptr, WallsDev{}, L, dirty));
+    bool dirty = false, fresh = false;
+    GS_TRY(fused_setup(g, d, grid, C, nullptr, WallsDev{}, L, dirty, fresh));
     d.dirty = 0;
     for (unsigned j = 0; j < len; ++j) {
+        d.fresh = fresh && j == 0 ? 1u : 0u;
         FusedLaunch Lj = L;
         Lj.rec_pos = r->rec_pos + size_t(j) * r->cap;
         Lj.rec_dir = r->rec_dir + size_t(j) * r->cap;

@@ -160,6 +160,7 @@ struct StepDev {
     unsigned scan_reach;  // scan_reach_tiles of the step's grid and radius
     unsigned persistent;  // run a supported step as one persistent launch
     unsigned bar_limit;   // its barrier poll limit
+    unsigned fresh;       // A is in agent order (first step after an upload)
     PathDev path;       // path following (GS_B_FOLLOW_PATH)
     float path_time, w_path;
     unsigned mask_path;
@@ -208,6 +209,7 @@ struct FusedLaunch {
     unsigned* err;  // device flag: bit 0 = a bucketed slot fell outside [0, n)
     unsigned* retry;        // [n] slots the fast KNN handed to the exact redo
     unsigned* retry_count;  // zeroed by the permute launch of each step
+    unsigned* agent_at;     // [n] the fresh permute's slot -> agent map (scratch)
     // [retry_cap * kRetryListK] the exact neighbour slots of the first
     // retry_cap redo entries, written by the warp-per-agent exact search
     // (entry 0 = kRetryNotListed when that search left the entry to the
@@ -228,7 +230,10 @@ gs_status fused_from_reference(GroupView g, const unsigned* agent_scene, const S
                                bool dirty, cudaStream_t st);
 gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellrank,
                         unsigned* count, int wrap_mode, cudaStream_t st);
-gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st);
+// fresh: A is in agent order (the first step after an upload), permuted by a
+// gather through L.agent_at (two launches instead of one).
+gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, bool fresh,
+                        cudaStream_t st);
 // `phase` (may be null) brackets each launch: phase(i, true) before and
 // phase(i, false) after the launch of phase i.
 struct PhaseHook {

@@ -109,18 +109,10 @@ gs_status fused_recount(Fused A, unsigned n, const Scene* scenes, uint2* cellran
     return GS_OK;
 }
 
-// A (slot i) -> B (slot start[cell] + rank), wrapping the position.
-__device__ __forceinline__ void permute_agent(const Fused& A, const Fused& B, unsigned n,
-                                              const uint2* __restrict__ cellrank,
-                                              const unsigned* __restrict__ start,
-                                              const Scene* __restrict__ scenes, int wrap_mode,
-                                              int dirty, unsigned* __restrict__ err, unsigned i) {
-    const uint2 cr = cellrank[i];
-    const unsigned dst = start[cr.x] + cr.y;
-    if (dst >= n) {  // inconsistent counts: record and write nothing
-        atomicOr(err, 1u);
-        return;
-    }
+// A (slot i) -> B (slot dst), wrapping the position.
+__device__ __forceinline__ void move_agent(const Fused& A, const Fused& B,
+                                           const Scene* __restrict__ scenes, int wrap_mode,
+                                           int dirty, unsigned i, unsigned dst) {
     const float4 f0 = A.f[0][i];
     const float4 f4v = A.f[4][i];
     const Scene sc = scenes[u(f4v.w)];
@@ -131,6 +123,21 @@ __device__ __forceinline__ void permute_agent(const Fused& A, const Fused& B, un
     B.f[3][dst] = A.f[3][i];
     B.f[4][dst] = f4v;
     if (dirty) B.f[5][dst] = A.f[5][i];
+}
+
+// A (slot i) -> B (slot start[cell] + rank), wrapping the position.
+__device__ __forceinline__ void permute_agent(const Fused& A, const Fused& B, unsigned n,
+                                              const uint2* __restrict__ cellrank,
+                                              const unsigned* __restrict__ start,
+                                              const Scene* __restrict__ scenes, int wrap_mode,
+                                              int dirty, unsigned* __restrict__ err, unsigned i) {
+    const uint2 cr = cellrank[i];
+    const unsigned dst = start[cr.x] + cr.y;
+    if (dst >= n) {  // inconsistent counts: record and write nothing
+        atomicOr(err, kErrCounts);
+        return;
+    }
+    move_agent(A, B, scenes, wrap_mode, dirty, i, dst);
 }
 
 __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n,
@@ -149,8 +156,61 @@ __global__ void __launch_bounds__(kBlock) k_permute(Fused A, Fused B, unsigned n
     permute_agent(A, B, n, cellrank, start, scenes, wrap_mode, dirty, err, i);
 }
 
-gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, cudaStream_t st) {
+// The first step after an upload finds A in agent order, which
+// is a shuffle of the bucket order: there the scatter above stores each
+// agent's five float4 to scattered slots (partial-sector writes, about five
+// times the steady step's permute).  Instead, one scattered 4-byte store per
+// agent records which agent each slot takes, and the permute gathers:
+// scattered 16-byte reads, coalesced writes.
+__global__ void k_agent_at(unsigned n, const uint2* __restrict__ cellrank,
+                           const unsigned* __restrict__ start, unsigned* __restrict__ err,
+                           unsigned* __restrict__ agent_at) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 cr = cellrank[i];
+    const unsigned dst = start[cr.x] + cr.y;
+    if (dst >= n) {  // inconsistent counts: record and write nothing
+        atomicOr(err, kErrCounts);
+        return;
+    }
+    agent_at[dst] = i;
+}
+
+__global__ void __launch_bounds__(kBlock) k_permute_gather(Fused A, Fused B, unsigned n,
+                                                           const unsigned* __restrict__ agent_at,
+                                                           const Scene* __restrict__ scenes,
+                                                           int wrap_mode, int dirty,
+                                                           unsigned* __restrict__ err,
+                                                           unsigned* __restrict__ retry_count,
+                                                           unsigned* __restrict__ tile,
+                                                           unsigned tiles) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) *retry_count = 0u;
+    for (unsigned t = s; t < tiles; t += gridDim.x * blockDim.x) tile[t] = 0u;
+    if (s >= n) return;
+    // with consistent counts every slot below n was written just before;
+    // a slot left over from inconsistent ones (the error bit is set) may hold
+    // any word, so the index is checked before the reads
+    const unsigned i = agent_at[s];
+    if (i >= n) {
+        atomicOr(err, kErrCounts);
+        return;
+    }
+    move_agent(A, B, scenes, wrap_mode, dirty, i, s);
+}
+
+gs_status fused_permute(const FusedLaunch& L, int wrap_mode, bool dirty, bool fresh,
+                        cudaStream_t st) {
     if (L.n == 0) return GS_OK;
+    if (fresh) {
+        k_agent_at<<<blocks_for(L.n), kBlock, 0, st>>>(L.n, L.cellrank, L.start, L.err,
+                                                        L.agent_at);
+        k_permute_gather<<<blocks_for(L.n), kBlock, 0, st>>>(L.A, L.B, L.n, L.agent_at, L.scenes,
+                                                             wrap_mode, dirty ? 1 : 0, L.err,
+                                                             L.retry_count, L.tile, L.tiles);
+        GS_LAUNCHED("fused_permute");
+        return GS_OK;
+    }
     k_permute<<<blocks_for(L.n), kBlock, 0, st>>>(L.A, L.B, L.n, L.cellrank, L.start, L.scenes,
                                                   wrap_mode, dirty ? 1 : 0, L.err, L.retry_count,
                                                   L.tile, L.tiles);

@@ -357,7 +357,9 @@ gs_status gs_step_host(gs_group g, gs_bins bins, gs_walls walls, const gs_step_p
                        unsigned steps, const gs_agent_arrays* in, unsigned n,
                        const gs_agent_arrays* out);
 /* Replays one captured CUDA graph per fused step while the launch
- * configuration stays the same (default on).  Not part of the reference. */
+ * configuration stays the same (default on).  The first step after an
+ * upload of a scene of 131,072 agents or more runs eagerly: its permute
+ * gathers, in one more launch.  Not part of the reference. */
 gs_status gs_group_set_graphs(gs_group g, int enable);
 /* Threads per block of the fused-step launches: 64, 128 or 256 (default).
  * Results do not depend on it; the autotuner picks it. */
@@ -366,8 +368,9 @@ gs_status gs_group_set_block(gs_group g, unsigned threads);
  * scan, for sparse crowds), 128 or 256 (streaming scan, for crowded cells),
  * or 0 (default: chosen from the crowd's density, the agents in an agent's
  * cell averaged over the agents, measured at the first step after an upload
- * that changes the agent count, or after a grid change).  Results do not depend on it: agents with more candidates are
- * redone by the exact scan.  Not part of the reference. */
+ * that changes the agent count, or after a grid change).  Results do not
+ * depend on it: agents with more candidates are redone by the exact scan.
+ * Not part of the reference. */
 gs_status gs_group_set_knn_capacity(gs_group g, unsigned capacity);
 /* The capacity the fused step uses: the fixed one, else the one measured at
  * the last step (0 before the first).  With 128 or 256 a step makes more
