@@ -977,7 +977,10 @@ def gpu_brute_line(args, dist, rank, world, local_rank):
     barrier(dist)
     ms_max = allreduce_max(dist, ev0.elapsed_time(ev1))
     per = ms_max / args.steps
-    pairs = float(n) * (n - 1)
+    pairs_all = float(n) * (n - 1)
+    # the pairs the distance filter ran on: the bucketed scan skips chunks of
+    # candidates beyond every bound of a warp's queries
+    pairs = float(gs.bruteforce_pairs(g))
     tflops = 8.0 * pairs / (per / 1e3) / 1e12
     peak = fp32_peak_tflops()
     # end to end: positions up, lists down, every query
@@ -1014,8 +1017,11 @@ def gpu_brute_line(args, dist, rank, world, local_rank):
                 "h2d_bytes_per_step": n * 96, "d2h_bytes_per_step": n * k * 8},
         "gpu_launches": args.steps,
         "roofline": {"bound": "fp32", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
-                     "frac": tflops / peak, "traffic": None, "kernel": "k_knn_brute3",
+                     "frac": tflops / peak, "traffic": None, "kernel": "k_knn_brute3_bucketed",
                      "algorithmic_flops_per_launch": 8.0 * pairs,
+                     "pairs_evaluated": pairs, "pairs_all": pairs_all,
+                     "time": "the whole call (extent, seed databases and search, chunk "
+                             "boxes, scan)",
                      "peak_source": "measured here: cuBLAS SGEMM 8192^3 with TF32 off"},
         "issue": issue_rate("brute", per, clocks.summary(), local_rank),
         "clocks": clocks.summary(),

@@ -8,7 +8,7 @@ GroupSteerLibrary free functions), seeded scenarios and the build step.
 from ._lib import GpuSteerError, load  # noqa: F401
 from .groups import (  # noqa: F401
     AgentGroup, Batch, KNNBinData, KNNData, Path, Rollout, WallGroup, antiPenetrationAgents,
-    batches_step_host, pinned_state, MultiGroupParams, multigroup_step,
+    batches_step_host, bruteforce_pairs, pinned_state, MultiGroupParams, multigroup_step,
     antiPenetrationWall, updateGroupWithAntiPenetration,
     findKNearestNeighbors, findKNearestNeighborsBruteForce, findKNearestNeighborsGroups,
     set_barrier_limit, set_block, set_graphs, set_persistent,

@@ -99,6 +99,7 @@ SIGNATURES = {
     "gs_find_knn": [_vp, _vp, _vp, _vp, _u],
     "gs_find_knn_walls": [_vp, _vp, _vp, _vp, _u],
     "gs_knn_bruteforce": [_vp, _vp, _vp],
+    "gs_knn_bruteforce_pairs": [_vp, C.POINTER(C.c_ulonglong)],
     "gs_steer_for_separation": [_vp, _vp, _vp, _f, _f, _f, _f, _u],
     "gs_steer_for_alignment": [_vp, _vp, _vp, _f, _f, _f, _f, _u],
     "gs_steer_for_cohesion": [_vp, _vp, _vp, _f, _f, _f, _f, _u],

@@ -555,6 +555,7 @@ gs_status gs_group_destroy(gs_group g) {
     db_release(g->bf_a);
     db_release(g->bf_b);
     dfree(g->bf_tmp);
+    dfree(g->bf_boxes);
     if (g->diag) cudaFree(g->diag);
     if (g->ap) cudaFree(g->ap);
     if (g->read_ev) cudaEventDestroy(g->read_ev);
@@ -1204,12 +1205,16 @@ gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
     }
     cudaStream_t st = g->stream;
     const float* seed = nullptr;
+    g->bf_counted = false;
+    g->bf_pairs = (unsigned long long)g->n * other->n;
     // Seed every query's filter with the k-th distance among the candidates
     // of its 3 x 3 x 3 cells on an automatic grid: the k-th distance among a
     // subset of the candidates bounds the true one from above, so the full
-    // scan still sees every pair and gives the same lists.
+    // scan still sees every pair it needs and gives the same lists.  The
+    // scan then runs over the seed databases' bucketed arrays and skips
+    // chunks of candidates beyond every bound of a warp's queries.
     if (out->k <= 32 && g->n >= 4096 && other->n > out->k) {
-        if (!g->bf_tmp) GS_TRY(dalloc(&g->bf_tmp, 4));
+        if (!g->bf_tmp) GS_TRY(dalloc(&g->bf_tmp, 6));
         float ext[3];
         GS_TRY(abs_extent(other->position, other->n, g->bf_tmp, ext, st));
         Grid grid;
@@ -1227,12 +1232,47 @@ gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
                 GS_TRY(db_build(B, other->position, other->n, grid, st));
             }
             GS_TRY(launch_knn_binned(A, g->n, B, other == g, 1, out->k, out->idx, out->dist, st));
+            // A box of 3 x 3 x 3 cells at a corner or edge of the grid may hold
+            // fewer than k candidates; those queries search wider boxes (the
+            // others return at once), so that few scans start unbounded: an
+            // unbounded query of the bucketed scan inserts most candidates of
+            // the first stages and holds its block for the whole call.
+            GS_TRY(launch_knn_binned(A, g->n, B, other == g, 2, out->k, out->idx, out->dist, st,
+                                     true));
+            GS_TRY(launch_knn_binned(A, g->n, B, other == g, 4, out->k, out->idx, out->dist, st,
+                                     true));
             seed = out->dist + size_t(out->k - 1) * g->n;  // the k-th distance column
+            // chunk boxes of 64 candidates, then stage boxes of 32 chunks
+            const size_t chunks = (size_t(other->capacity) + 63) / 64;
+            const size_t boxes = chunks + (chunks + 31) / 32;
+            if (g->bf_boxes_cap < boxes) {
+                dfree(g->bf_boxes);
+                g->bf_boxes_cap = 0;
+                GS_TRY(dalloc(&g->bf_boxes, 2 * boxes));
+                g->bf_boxes_cap = boxes;
+            }
+            auto* evaluated = reinterpret_cast<unsigned long long*>(g->bf_tmp + 4);
+            GS_CUDA(cudaMemsetAsync(evaluated, 0, sizeof(unsigned long long), st));
+            GS_TRY(launch_knn_brute_bucketed(A.pos_id, g->n, B.pos_id, other->n, g->bf_boxes,
+                                             other == g, out->k, seed, evaluated, out->idx,
+                                             out->dist, st));
+            g->bf_counted = true;
+            return read_done(g, other);
         }
     }
     GS_TRY(launch_knn_brute(g->position, g->n, other->position, other->n, other == g, out->k,
                             seed, out->idx, out->dist, st));
     return read_done(g, other);
+}
+
+gs_status gs_knn_bruteforce_pairs(gs_group g, unsigned long long* pairs) {
+    if (!g || !pairs) return fail(GS_ERR_INVALID_ARG, "null argument");
+    *pairs = g->bf_pairs;
+    if (!g->bf_counted) return GS_OK;
+    GS_CUDA(cudaMemcpyAsync(pairs, g->bf_tmp + 4, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, g->stream));
+    GS_CUDA(cudaStreamSynchronize(g->stream));
+    return GS_OK;
 }
 
 static gs_status flock_call(int kind, gs_group g, gs_knn knn, gs_group other, float a, float b,

@@ -156,9 +156,14 @@ struct gs_group_s {
     float* knn_dist;       // [k * n]
     gs::Database fdb;      // counts / starts of the fused step
     // brute-force KNN's seed search: databases of the queries and of the
-    // other group on an automatic grid, and three words of scratch
+    // other group on an automatic grid; scratch (words 0-2: the extent,
+    // words 4-5: the pairs the filter ran on); the candidates' chunk boxes
     gs::Database bf_a, bf_b;
     unsigned* bf_tmp;
+    float4* bf_boxes;
+    size_t bf_boxes_cap;         // boxes bf_boxes holds
+    bool bf_counted;             // the last call counted its pairs in bf_tmp
+    unsigned long long bf_pairs; // else the pairs it ran on (n * m)
     gs::Scene* d_scene;    // scene table (one entry for a plain group)
     unsigned scene_alloc;
     std::vector<gs::Scene>* h_scenes;  // host copy of the table on the device

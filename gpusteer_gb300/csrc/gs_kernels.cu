@@ -235,15 +235,18 @@ gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid
 
 // ---- binned KNN, reference output layout (KNNBinningV2Kernel.cu:417-528) ----------
 // One thread per agent of A in bucketed order (neighbouring threads scan the
-// same cells); results go to idx/dist[a + i * nA].
+// same cells); results go to idx/dist[a + i * nA].  unfilled_only: only the
+// agents whose k-th entry is still empty (FLT_MAX) search, the others return.
 template <int KMAX>
 __global__ void __launch_bounds__(kBlock) k_knn_binned(
     const unsigned* __restrict__ a_sorted, const float4* __restrict__ a_pos_id, unsigned nA,
     const unsigned* __restrict__ b_start, const float4* __restrict__ b_pos_id, Grid g,
-    unsigned r, unsigned k, bool self, unsigned* __restrict__ idx, float* __restrict__ dist) {
+    unsigned r, unsigned k, bool self, bool unfilled_only, unsigned* __restrict__ idx,
+    float* __restrict__ dist) {
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nA) return;
     const unsigned a = a_sorted[s];
+    if (unfilled_only && dist[a + size_t(k - 1) * nA] != FLT_MAX) return;
     const V3 p = v3(a_pos_id[s]);
     unsigned ix, iy, iz;
     cell_coords(g, p, ix, iy, iz);
@@ -264,14 +267,14 @@ __global__ void __launch_bounds__(kBlock) k_knn_binned(
 template <int KMAX>
 static gs_status knn_binned_k(const Database& A, unsigned nA, const Database& B, bool self,
                               unsigned r, unsigned k, unsigned* idx, float* dist,
-                              cudaStream_t st) {
+                              cudaStream_t st, bool unfilled_only) {
     const size_t smem = size_t(2 * 64) * kBlock * sizeof(unsigned);
     if (smem > 48 * 1024)
         GS_CUDA(cudaFuncSetAttribute(k_knn_binned<KMAX>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     k_knn_binned<KMAX><<<blocks_for(nA), kBlock, smem, st>>>(A.sorted, A.pos_id, nA, B.start,
-                                                             B.pos_id, B.grid, r, k, self, idx,
-                                                             dist);
+                                                             B.pos_id, B.grid, r, k, self,
+                                                             unfilled_only, idx, dist);
     GS_LAUNCHED("knn_binned");
     return GS_OK;
 }
@@ -334,12 +337,13 @@ gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st) {
 }
 
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
-                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
-    if (nA == 0) return GS_OK;
-    if (k <= 8) return knn_binned_k<8>(A, nA, B, self, r, k, idx, dist, st);
-    if (k <= 16) return knn_binned_k<16>(A, nA, B, self, r, k, idx, dist, st);
-    if (k <= 32) return knn_binned_k<32>(A, nA, B, self, r, k, idx, dist, st);
-    return knn_binned_k<64>(A, nA, B, self, r, k, idx, dist, st);
+                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st,
+                            bool unfilled_only) {
+    if (nA == 0 || k == 0) return GS_OK;
+    if (k <= 8) return knn_binned_k<8>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
+    if (k <= 16) return knn_binned_k<16>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
+    if (k <= 32) return knn_binned_k<32>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
+    return knn_binned_k<64>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
 }
 
 // ---- brute-force KNN (KNNBruteForceCudaKernel.cu:207-283) ---------------------------
@@ -461,6 +465,54 @@ __device__ __forceinline__ float seed_prefilter(float d) {
     return __fmul_ru(__fmul_ru(d, d), 1.000004f);
 }
 
+// The warp's step over the staged candidates t0 .. t0 + 63 (each lane the
+// pair t0 + 2 lane, t0 + 2 lane + 1): the packed filter against every query
+// of the warp, then the exact insertion of the candidates that passed.  sid:
+// the staged candidates' indices (null: base + their position in the stage).
+__device__ __forceinline__ void brute_chunk(
+    const float* sx, const float* sy, const float* sz, const unsigned* sid, unsigned base,
+    unsigned t0, unsigned cnt, unsigned lane, bool self, unsigned k, const V3 (&q)[kBruteQW],
+    const unsigned (&qid)[kBruteQW], const unsigned long long (&px)[kBruteQW],
+    const unsigned long long (&py)[kBruteQW], const unsigned long long (&pz)[kBruteQW],
+    unsigned long long (&entry)[kBruteQW], float (&bound)[kBruteQW],
+    const float (&seed_bound)[kBruteQW]) {
+    const unsigned t = t0 + 2 * lane;
+    const unsigned long long x2 = *reinterpret_cast<const unsigned long long*>(sx + t);
+    const unsigned long long y2 = *reinterpret_cast<const unsigned long long*>(sy + t);
+    const unsigned long long z2 = *reinterpret_cast<const unsigned long long*>(sz + t);
+    bool hit0[kBruteQW], hit1[kBruteQW];
+    bool any = false;
+#pragma unroll
+    for (unsigned j = 0; j < kBruteQW; ++j) {
+        const unsigned long long dx = sub2(px[j], x2), dy = sub2(py[j], y2), dz = sub2(pz[j], z2);
+        float e0, e1;
+        unpack2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))), e0, e1);
+        hit0[j] = e0 <= bound[j];
+        hit1[j] = e1 <= bound[j];
+        any |= hit0[j] | hit1[j];
+    }
+    if (!__any_sync(0xffffffffu, any)) return;
+    // only the candidates that passed: the lane's first (h = 0) and second
+    // (h = 1) candidate have separate votes
+#pragma unroll
+    for (unsigned j = 0; j < kBruteQW; ++j) {
+#pragma unroll
+        for (unsigned h = 0; h < 2; ++h) {
+            unsigned m = __ballot_sync(0xffffffffu, h ? hit1[j] : hit0[j]);
+            while (m) {
+                const unsigned src = unsigned(__ffs(m)) - 1u;
+                m &= m - 1u;
+                const unsigned c = t0 + 2 * src + h;
+                if (c >= cnt) continue;
+                const unsigned id = sid ? sid[c] : base + c;
+                if (self && id == qid[j]) continue;
+                warp_list_insert(entry[j], bound[j], seed_bound[j], q[j], sx[c], sy[c], sz[c],
+                                 id, k, lane);
+            }
+        }
+    }
+}
+
 // seed (may be null): per query an upper bound of its k-th distance (the
 // k-th distance among any subset of the candidates is one); the filter then
 // starts at that bound instead of infinity, so a query's list takes little
@@ -473,11 +525,13 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned q0 = (blockIdx.x * kBruteWarps + warp) * kBruteQW;
     V3 q[kBruteQW];
+    unsigned qid[kBruteQW];
     unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW], entry[kBruteQW];
     float bound[kBruteQW], seed_bound[kBruteQW];
 #pragma unroll
     for (unsigned j = 0; j < kBruteQW; ++j) {
         const bool act = q0 + j < nA;
+        qid[j] = q0 + j;
         q[j] = act ? v3(posA[q0 + j]) : v3(0.f, 0.f, 0.f);
         px[j] = pack2(q[j].x, q[j].x);
         py[j] = pack2(q[j].y, q[j].y);
@@ -497,43 +551,9 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
         }
         __syncthreads();
         const unsigned cnt = min(kBruteTile, nB - base);
-        for (unsigned t0 = 0; t0 < cnt; t0 += 64) {
-            const unsigned t = t0 + 2 * lane;
-            const unsigned long long x2 = *reinterpret_cast<const unsigned long long*>(sx + t);
-            const unsigned long long y2 = *reinterpret_cast<const unsigned long long*>(sy + t);
-            const unsigned long long z2 = *reinterpret_cast<const unsigned long long*>(sz + t);
-            bool hit0[kBruteQW], hit1[kBruteQW];
-            bool any = false;
-#pragma unroll
-            for (unsigned j = 0; j < kBruteQW; ++j) {
-                const unsigned long long dx = sub2(px[j], x2), dy = sub2(py[j], y2),
-                                         dz = sub2(pz[j], z2);
-                float e0, e1;
-                unpack2(fma2(dz, dz, fma2(dy, dy, mul2(dx, dx))), e0, e1);
-                hit0[j] = e0 <= bound[j];
-                hit1[j] = e1 <= bound[j];
-                any |= hit0[j] | hit1[j];
-            }
-            if (!__any_sync(0xffffffffu, any)) continue;
-            // only the candidates that passed: the lane's first (h = 0) and
-            // second (h = 1) candidate have separate votes
-#pragma unroll
-            for (unsigned j = 0; j < kBruteQW; ++j) {
-#pragma unroll
-                for (unsigned h = 0; h < 2; ++h) {
-                    unsigned m = __ballot_sync(0xffffffffu, h ? hit1[j] : hit0[j]);
-                    while (m) {
-                        const unsigned src = unsigned(__ffs(m)) - 1u;
-                        m &= m - 1u;
-                        const unsigned c = t0 + 2 * src + h;
-                        const unsigned id = base + c;
-                        if (c >= cnt || (self && id == q0 + j)) continue;
-                        warp_list_insert(entry[j], bound[j], seed_bound[j], q[j], sx[c], sy[c],
-                                         sz[c], id, k, lane);
-                    }
-                }
-            }
-        }
+        for (unsigned t0 = 0; t0 < cnt; t0 += 64)
+            brute_chunk(sx, sy, sz, nullptr, base, t0, cnt, lane, self, k, q, qid, px, py, pz,
+                        entry, bound, seed_bound);
     }
 #pragma unroll
     for (unsigned j = 0; j < kBruteQW; ++j) {
@@ -543,6 +563,203 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
             dist[qq + size_t(lane) * nA] = key_dist(entry[j]);
         }
     }
+}
+
+// ---- brute force over bucketed candidates: chunks beyond every bound skipped ---------
+// With the seed's databases, queries and candidates are taken in bucket
+// order (the cell-sorted pos_id arrays: position and agent index), so a
+// warp's queries are neighbours and 64 consecutive candidates (a chunk) sit
+// in a few neighbouring cells.  Before each stage a lane tests one of the
+// stage's 32 chunks: the squared distance from each query of its warp to the
+// chunk's bounding box, in the reference's unfused operations.  Per axis the
+// gap to the box is fl(lo - q) or fl(q - hi), at most |fl(q - c)| for every
+// candidate c of the chunk (rounding is monotone), and squares and sums are
+// monotone too, so the box's squared distance is at most every candidate's
+// exact one: a chunk whose box lies beyond the filter bound of every query of
+// the warp holds no candidate the filter would pass, and the warp skips it
+// without changing a list.  The block stages only the chunks some warp needs.
+
+// Bounding box of each chunk of 64 consecutive slots: boxes[2c] = lower
+// corner, boxes[2c + 1] = upper corner (NaN coordinates ignored: such a
+// candidate's distance is NaN and never passes the filter).  With `merge`,
+// pos_id holds n such boxes and each output box covers 32 of them (a stage
+// of kBruteTile candidates).  One warp per output box.
+__global__ void k_chunk_boxes(const float4* __restrict__ pos_id, unsigned n, bool merge,
+                              float4* __restrict__ boxes) {
+    const unsigned c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const unsigned per = merge ? 32u : 64u;
+    if (c >= (n + per - 1) / per) return;  // warp-uniform
+    const float inf = __int_as_float(0x7f800000);
+    float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+    if (merge) {
+        const unsigned b = c * 32 + lane;
+        if (b < n) {
+            const float4 l = pos_id[2 * b], h = pos_id[2 * b + 1];
+            lo[0] = l.x;
+            lo[1] = l.y;
+            lo[2] = l.z;
+            hi[0] = h.x;
+            hi[1] = h.y;
+            hi[2] = h.z;
+        }
+    } else {
+#pragma unroll
+        for (unsigned h = 0; h < 2; ++h) {
+            const unsigned sl = c * 64 + 2 * lane + h;
+            if (sl < n) {
+                const float4 v = pos_id[sl];
+                lo[0] = fminf(lo[0], v.x);
+                lo[1] = fminf(lo[1], v.y);
+                lo[2] = fminf(lo[2], v.z);
+                hi[0] = fmaxf(hi[0], v.x);
+                hi[1] = fmaxf(hi[1], v.y);
+                hi[2] = fmaxf(hi[2], v.z);
+            }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    }
+    if (lane == 0) {
+        boxes[2 * c] = make_float4(lo[0], lo[1], lo[2], 0.f);
+        boxes[2 * c + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    }
+}
+
+// Squared distance from q to the box [lo, hi], as a lower bound of every
+// inside candidate's exact squared distance (same operation order as dot).
+__device__ __forceinline__ float box_dist_sq(V3 q, float4 lo, float4 hi) {
+    const V3 gap = v3(fmaxf(fmaxf(lo.x - q.x, q.x - hi.x), 0.f),
+                      fmaxf(fmaxf(lo.y - q.y, q.y - hi.y), 0.f),
+                      fmaxf(fmaxf(lo.z - q.z, q.z - hi.z), 0.f));
+    return dot(gap, gap);
+}
+
+// qpos / cpos: the queries' and candidates' bucketed (position, agent index)
+// arrays; seed: per agent index an upper bound of its k-th distance; the
+// lists go to idx / dist by agent index.  evaluated (may be null): adds the
+// (query, candidate) pairs the packed filter ran on.
+// sboxes: the boxes of the stages (32 chunks each), tested first, 32 stages
+// at a time, so that a block visits only the stages some query may need.
+__global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3_bucketed(
+    const float4* __restrict__ qpos, unsigned nA, const float4* __restrict__ cpos, unsigned nB,
+    const float4* __restrict__ boxes, const float4* __restrict__ sboxes, bool self, unsigned k,
+    const float* __restrict__ seed, unsigned long long* __restrict__ evaluated,
+    unsigned* __restrict__ idx, float* __restrict__ dist) {
+    __shared__ __align__(16) float sx[kBruteTile], sy[kBruteTile], sz[kBruteTile];
+    __shared__ unsigned sid[kBruteTile];
+    __shared__ unsigned wmask[kBruteWarps], smask[kBruteWarps];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned s0 = (blockIdx.x * kBruteWarps + warp) * kBruteQW;
+    V3 q[kBruteQW];
+    unsigned qid[kBruteQW];
+    unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW], entry[kBruteQW];
+    float bound[kBruteQW], seed_bound[kBruteQW];
+    unsigned active = 0;
+#pragma unroll
+    for (unsigned j = 0; j < kBruteQW; ++j) {
+        const float4 v = s0 + j < nA ? qpos[s0 + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        qid[j] = s0 + j < nA ? __float_as_uint(v.w) : UINT_MAX;
+        const bool act = qid[j] < nA;  // a slot holds an agent index below nA
+        active += act;
+        q[j] = v3(v);
+        px[j] = pack2(q[j].x, q[j].x);
+        py[j] = pack2(q[j].y, q[j].y);
+        pz[j] = pack2(q[j].z, q[j].z);
+        entry[j] = KEY_EMPTY;
+        seed_bound[j] = act ? seed_prefilter(seed[qid[j]]) : prefilter_bound(KEY_EMPTY);
+        bound[j] = act ? seed_bound[j] : -1.f;
+    }
+    const float inf = __int_as_float(0x7f800000);
+    const unsigned chunks = (nB + 63) / 64, stages = (nB + kBruteTile - 1) / kBruteTile;
+    for (unsigned sg = 0; sg < stages; sg += 32) {
+        // lane l: may stage sg + l hold a candidate some query of the warp
+        // would pass?  (bounds only fall, so the answer stays safe)
+        bool swant = false;
+        if (sg + lane < stages) {
+            const float4 lo = sboxes[2 * (sg + lane)], hi = sboxes[2 * (sg + lane) + 1];
+#pragma unroll
+            for (unsigned j = 0; j < kBruteQW; ++j) swant |= box_dist_sq(q[j], lo, hi) <= bound[j];
+        }
+        const unsigned sm = __ballot_sync(0xffffffffu, swant);
+        __syncthreads();  // the previous group's reads of smask are done
+        if (lane == 0) smask[warp] = sm;
+        __syncthreads();
+        unsigned visit = 0;
+#pragma unroll
+        for (unsigned w = 0; w < kBruteWarps; ++w) visit |= smask[w];
+        for (; visit; visit &= visit - 1u) {
+            const unsigned base = (sg + unsigned(__ffs(visit)) - 1u) * kBruteTile;
+            // lane l: may chunk base / 64 + l hold a candidate some query of the
+            // warp would pass?  (bounds only fall within the stage)
+            const unsigned ch = base / 64 + lane;
+            bool want = false;
+            if (ch < chunks) {
+                const float4 lo = boxes[2 * ch], hi = boxes[2 * ch + 1];
+#pragma unroll
+                for (unsigned j = 0; j < kBruteQW; ++j)
+                    want |= box_dist_sq(q[j], lo, hi) <= bound[j];
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, want);
+            __syncthreads();  // the previous stage's reads of the staged chunks are done
+            if (lane == 0) wmask[warp] = mask;
+            __syncthreads();
+            unsigned need = 0;
+#pragma unroll
+            for (unsigned w = 0; w < kBruteWarps; ++w) need |= wmask[w];
+            if (need == 0) continue;  // block-uniform
+            for (unsigned c = threadIdx.x; c < kBruteTile; c += blockDim.x) {
+                if (!((need >> (c / 64)) & 1u)) continue;
+                const float4 v =
+                    base + c < nB ? cpos[base + c] : make_float4(inf, inf, inf, 0.f);
+                sx[c] = v.x;
+                sy[c] = v.y;
+                sz[c] = v.z;
+                sid[c] = __float_as_uint(v.w);
+            }
+            __syncthreads();
+            if (evaluated && lane == 0 && mask)
+                atomicAdd(evaluated, (unsigned long long)__popc(mask) * 64u * active);
+            const unsigned cnt = min(kBruteTile, nB - base);
+            for (unsigned m = mask; m; m &= m - 1u)
+                brute_chunk(sx, sy, sz, sid, base, 64u * (unsigned(__ffs(m)) - 1u), cnt, lane,
+                            self, k, q, qid, px, py, pz, entry, bound, seed_bound);
+        }
+    }
+#pragma unroll
+    for (unsigned j = 0; j < kBruteQW; ++j) {
+        if (qid[j] < nA && lane < k) {
+            idx[qid[j] + size_t(lane) * nA] = key_id(entry[j]);
+            dist[qid[j] + size_t(lane) * nA] = key_dist(entry[j]);
+        }
+    }
+}
+
+gs_status launch_knn_brute_bucketed(const float4* qpos, unsigned nA, const float4* cpos,
+                                    unsigned nB, float4* boxes, bool self, unsigned k,
+                                    const float* seed, unsigned long long* evaluated,
+                                    unsigned* idx, float* dist, cudaStream_t st) {
+    if (nA == 0) return GS_OK;
+    if (k > 32 || seed == nullptr)
+        return fail(GS_ERR_UNSUPPORTED, "the bucketed brute force needs k <= 32 and a seed");
+    const unsigned chunks = (nB + 63) / 64, stages = (chunks + 31) / 32;
+    float4* sboxes = boxes + 2 * size_t(chunks);
+    if (chunks) {
+        k_chunk_boxes<<<(chunks * 32 + kBlock - 1) / kBlock, kBlock, 0, st>>>(cpos, nB, false,
+                                                                               boxes);
+        k_chunk_boxes<<<(stages * 32 + kBlock - 1) / kBlock, kBlock, 0, st>>>(boxes, chunks, true,
+                                                                               sboxes);
+    }
+    const unsigned per_block = kBruteWarps * kBruteQW;
+    k_knn_brute3_bucketed<<<(nA + per_block - 1) / per_block, kBruteWarps * 32, 0, st>>>(
+        qpos, nA, cpos, nB, boxes, sboxes, self, k, seed, evaluated, idx, dist);
+    GS_LAUNCHED("knn_brute_bucketed");
+    return GS_OK;
 }
 
 // Largest |coordinate| per axis of n positions, as float bits (non-negative

@@ -31,8 +31,11 @@ gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid
                    cudaStream_t st);
 
 // ---- per-function (drop-in) kernels -----------------------------------------
+// unfilled_only: only the agents of A whose k-th entry is still empty
+// (FLT_MAX, fewer than k neighbours found before) search again.
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
-                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
+                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st,
+                            bool unfilled_only = false);
 // Batched binned KNN over (A, B) database pairs of one grid (every group pair
 // of a MultiGroup frame): one launch, results as launch_knn_binned per pair.
 // 49 pairs (seven groups, every pair) keep the parameter block under 4 KiB.
@@ -57,6 +60,15 @@ gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st);
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
                            bool self, unsigned k, const float* seed, unsigned* idx, float* dist,
                            cudaStream_t st);
+// The same lists over bucketed queries and candidates (the seed databases'
+// pos_id arrays), skipping chunks of 64 candidates beyond every bound of a
+// warp's queries; k <= 32 and a seed.  boxes: 2 * (ceil(nB / 64) +
+// ceil(nB / 2048)) float4 of scratch (chunk, then stage boxes); evaluated
+// (may be null) adds the pairs the filter ran on.
+gs_status launch_knn_brute_bucketed(const float4* qpos, unsigned nA, const float4* cpos,
+                                    unsigned nB, float4* boxes, bool self, unsigned k,
+                                    const float* seed, unsigned long long* evaluated,
+                                    unsigned* idx, float* dist, cudaStream_t st);
 // Largest |coordinate| per axis of n positions (synchronises st); d_tmp3: 3 words.
 gs_status abs_extent(const float4* pos, unsigned n, unsigned* d_tmp3, float out[3],
                      cudaStream_t st);

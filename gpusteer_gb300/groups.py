@@ -573,6 +573,14 @@ def findKNearestNeighborsBruteForce(group: AgentGroup, knn: KNNData, other: Agen
     call("gs_knn_bruteforce", group.handle, knn.handle, other.handle)
 
 
+def bruteforce_pairs(group: AgentGroup) -> int:
+    """gs_knn_bruteforce_pairs: the (query, candidate) pairs the group's last
+    brute-force call ran its distance filter on."""
+    out = C.c_ulonglong(0)
+    call("gs_knn_bruteforce_pairs", group.handle, C.byref(out))
+    return out.value
+
+
 def steerForSeparation(group, knn, other, min_distance, max_distance, cos_max_angle, weight,
                        do_not_apply_with=0) -> None:
     call("gs_steer_for_separation", group.handle, knn.handle, other.handle, min_distance,

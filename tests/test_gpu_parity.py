@@ -154,6 +154,8 @@ def test_knn_bruteforce_matches_oracle_larger():
         oi, od = ol.knn_brute(p, p, True, k)
         np.testing.assert_array_equal(i, oi)
         np.testing.assert_array_equal(d, od)
+        # the bucketed scan skips most chunks of candidates
+        assert 0 < gs.bruteforce_pairs(A) < A.size * A.size // 4
 
 
 @pytest.mark.parametrize("k", [1, 8, 16, 24, 32, 40])
@@ -222,6 +224,7 @@ def test_knn_bruteforce_fewer_candidates_than_k():
     np.testing.assert_array_equal(i, oi)
     np.testing.assert_array_equal(d, od)
     assert (i.reshape(16, 70)[5:] == 0xFFFFFFFF).all()
+    assert gs.bruteforce_pairs(A) == 70 * 5  # a small call scans every pair
 
 
 # ---- behaviours, one per launch -----------------------------------------------------
