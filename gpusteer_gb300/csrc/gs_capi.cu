@@ -1231,17 +1231,13 @@ gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
                 B.agent_cap = other->capacity;
                 GS_TRY(db_build(B, other->position, other->n, grid, st));
             }
-            GS_TRY(launch_knn_binned(A, g->n, B, other == g, 1, out->k, out->idx, out->dist, st));
-            // A box of 3 x 3 x 3 cells at a corner or edge of the grid may hold
-            // fewer than k candidates; those queries search wider boxes (the
-            // others return at once), so that few scans start unbounded: an
-            // unbounded query of the bucketed scan inserts most candidates of
-            // the first stages and holds its block for the whole call.
-            GS_TRY(launch_knn_binned(A, g->n, B, other == g, 2, out->k, out->idx, out->dist, st,
-                                     true));
-            GS_TRY(launch_knn_binned(A, g->n, B, other == g, 4, out->k, out->idx, out->dist, st,
-                                     true));
-            seed = out->dist + size_t(out->k - 1) * g->n;  // the k-th distance column
+            // the seed goes to the k-th distance column, which the scan
+            // overwrites; a query whose box holds fewer than k candidates at
+            // every size tried starts unbounded (its block then takes the
+            // longest: it inserts most candidates of the first stages)
+            float* seed_col = out->dist + size_t(out->k - 1) * g->n;
+            GS_TRY(launch_brute_seed(A, g->n, B, other == g, out->k, seed_col, st));
+            seed = seed_col;
             // chunk boxes of 64 candidates, then stage boxes of 32 chunks
             const size_t chunks = (size_t(other->capacity) + 63) / 64;
             const size_t boxes = chunks + (chunks + 31) / 32;

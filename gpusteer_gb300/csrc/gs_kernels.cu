@@ -235,18 +235,15 @@ gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid
 
 // ---- binned KNN, reference output layout (KNNBinningV2Kernel.cu:417-528) ----------
 // One thread per agent of A in bucketed order (neighbouring threads scan the
-// same cells); results go to idx/dist[a + i * nA].  unfilled_only: only the
-// agents whose k-th entry is still empty (FLT_MAX) search, the others return.
+// same cells); results go to idx/dist[a + i * nA].
 template <int KMAX>
 __global__ void __launch_bounds__(kBlock) k_knn_binned(
     const unsigned* __restrict__ a_sorted, const float4* __restrict__ a_pos_id, unsigned nA,
     const unsigned* __restrict__ b_start, const float4* __restrict__ b_pos_id, Grid g,
-    unsigned r, unsigned k, bool self, bool unfilled_only, unsigned* __restrict__ idx,
-    float* __restrict__ dist) {
+    unsigned r, unsigned k, bool self, unsigned* __restrict__ idx, float* __restrict__ dist) {
     const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nA) return;
     const unsigned a = a_sorted[s];
-    if (unfilled_only && dist[a + size_t(k - 1) * nA] != FLT_MAX) return;
     const V3 p = v3(a_pos_id[s]);
     unsigned ix, iy, iz;
     cell_coords(g, p, ix, iy, iz);
@@ -267,14 +264,14 @@ __global__ void __launch_bounds__(kBlock) k_knn_binned(
 template <int KMAX>
 static gs_status knn_binned_k(const Database& A, unsigned nA, const Database& B, bool self,
                               unsigned r, unsigned k, unsigned* idx, float* dist,
-                              cudaStream_t st, bool unfilled_only) {
+                              cudaStream_t st) {
     const size_t smem = size_t(2 * 64) * kBlock * sizeof(unsigned);
     if (smem > 48 * 1024)
         GS_CUDA(cudaFuncSetAttribute(k_knn_binned<KMAX>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     k_knn_binned<KMAX><<<blocks_for(nA), kBlock, smem, st>>>(A.sorted, A.pos_id, nA, B.start,
-                                                             B.pos_id, B.grid, r, k, self,
-                                                             unfilled_only, idx, dist);
+                                                             B.pos_id, B.grid, r, k, self, idx,
+                                                             dist);
     GS_LAUNCHED("knn_binned");
     return GS_OK;
 }
@@ -337,13 +334,12 @@ gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st) {
 }
 
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
-                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st,
-                            bool unfilled_only) {
-    if (nA == 0 || k == 0) return GS_OK;
-    if (k <= 8) return knn_binned_k<8>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
-    if (k <= 16) return knn_binned_k<16>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
-    if (k <= 32) return knn_binned_k<32>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
-    return knn_binned_k<64>(A, nA, B, self, r, k, idx, dist, st, unfilled_only);
+                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st) {
+    if (nA == 0) return GS_OK;
+    if (k <= 8) return knn_binned_k<8>(A, nA, B, self, r, k, idx, dist, st);
+    if (k <= 16) return knn_binned_k<16>(A, nA, B, self, r, k, idx, dist, st);
+    if (k <= 32) return knn_binned_k<32>(A, nA, B, self, r, k, idx, dist, st);
+    return knn_binned_k<64>(A, nA, B, self, r, k, idx, dist, st);
 }
 
 // ---- brute-force KNN (KNNBruteForceCudaKernel.cu:207-283) ---------------------------
@@ -629,6 +625,88 @@ __global__ void k_chunk_boxes(const float4* __restrict__ pos_id, unsigned n, boo
         boxes[2 * c] = make_float4(lo[0], lo[1], lo[2], 0.f);
         boxes[2 * c + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
     }
+}
+
+// The scan's seed: per query (one thread each, in bucket order, so that
+// neighbouring threads read the same cells) the k-th smallest distance among
+// the other group's candidates in its 3 x 3 x 3 cells; in its 5 x 5 x 5, then
+// 9 x 9 x 9 cells when the smaller box holds fewer than k (grid corners and
+// edges); FLT_MAX when even that box does.  The k-th distance among a subset
+// of the candidates is at least the k-th among all of them, and an upper
+// bound is all the filter needs, so no list is kept: the k smallest squared
+// distances (the reference's unfused sum) stay in registers and one square
+// root is taken at the end (correctly rounded square roots keep their
+// order).  Candidates at an infinite or NaN distance never enter a list and
+// are not counted.  seed[a] by agent index.
+template <int KMAX>
+__global__ void __launch_bounds__(kBlock) k_brute_seed(const float4* __restrict__ a_pos_id,
+                                                       unsigned nA,
+                                                       const unsigned* __restrict__ b_start,
+                                                       const float4* __restrict__ b_pos_id,
+                                                       Grid g, unsigned k, bool self,
+                                                       float* __restrict__ seed) {
+    const unsigned s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nA) return;
+    const float4 v = a_pos_id[s];
+    const unsigned a = __float_as_uint(v.w);
+    if (a >= nA) return;
+    const V3 p = v3(v);
+    unsigned ix, iy, iz;
+    cell_coords(g, p, ix, iy, iz);
+    const float inf = __int_as_float(0x7f800000);
+    float kth = FLT_MAX;
+    for (unsigned r = 1; r <= 4; r *= 2) {
+        // the k smallest in top[KMAX - k .. KMAX - 1], ascending; the slots
+        // below hold -1 (below every distance) and never change
+        float top[KMAX];
+#pragma unroll
+        for (int i = 0; i < KMAX; ++i) top[i] = i < KMAX - int(k) ? -1.f : inf;
+        unsigned found = 0;
+        const Box b = cell_box(g, ix, iy, iz, r);
+        for (unsigned cy = b.y0; cy <= b.y1; ++cy) {
+            for (unsigned cz = b.z0; cz <= b.z1; ++cz) {
+                const unsigned s0 = __ldg(b_start + cell_label(g, b.x0, cy, cz));
+                const unsigned s1 = __ldg(b_start + cell_label(g, b.x1, cy, cz) + 1);
+                for (unsigned t = s0; t < s1; ++t) {
+                    const float4 q = __ldg(b_pos_id + t);
+                    if (self && __float_as_uint(q.w) == a) continue;
+                    const V3 o = sub(p, v3(q));
+                    const float d2 = dot(o, o);
+                    if (!(d2 < inf)) continue;
+                    ++found;
+                    if (d2 < top[KMAX - 1]) {
+#pragma unroll
+                        for (int i = KMAX - 1; i > 0; --i)
+                            top[i] = fminf(top[i], fmaxf(top[i - 1], d2));
+                        top[0] = fminf(top[0], d2);
+                    }
+                }
+            }
+        }
+        if (found >= k) {
+            kth = sqrtf(top[KMAX - 1]);
+            break;
+        }
+    }
+    seed[a] = kth;
+}
+
+gs_status launch_brute_seed(const Database& A, unsigned nA, const Database& B, bool self,
+                            unsigned k, float* seed, cudaStream_t st) {
+    if (nA == 0) return GS_OK;
+    if (k == 0 || k > 32)
+        return fail(GS_ERR_UNSUPPORTED, "the brute-force seed needs 1 <= k <= 32");
+    if (k <= 8)
+        k_brute_seed<8><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id, B.grid,
+                                                           k, self, seed);
+    else if (k <= 16)
+        k_brute_seed<16><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id,
+                                                            B.grid, k, self, seed);
+    else
+        k_brute_seed<32><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id,
+                                                            B.grid, k, self, seed);
+    GS_LAUNCHED("brute_seed");
+    return GS_OK;
 }
 
 // Squared distance from q to the box [lo, hi], as a lower bound of every

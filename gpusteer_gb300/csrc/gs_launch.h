@@ -31,11 +31,8 @@ gs_status db_build(Database& db, const float4* pos, unsigned n, const Grid& grid
                    cudaStream_t st);
 
 // ---- per-function (drop-in) kernels -----------------------------------------
-// unfilled_only: only the agents of A whose k-th entry is still empty
-// (FLT_MAX, fewer than k neighbours found before) search again.
 gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, bool self,
-                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st,
-                            bool unfilled_only = false);
+                            unsigned r, unsigned k, unsigned* idx, float* dist, cudaStream_t st);
 // Batched binned KNN over (A, B) database pairs of one grid (every group pair
 // of a MultiGroup frame): one launch, results as launch_knn_binned per pair.
 // 49 pairs (seven groups, every pair) keep the parameter block under 4 KiB.
@@ -60,6 +57,10 @@ gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st);
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
                            bool self, unsigned k, const float* seed, unsigned* idx, float* dist,
                            cudaStream_t st);
+// Per query of A (by agent index) an upper bound of its k-th distance to B's
+// agents: the k-th among the candidates of a box of cells (1 <= k <= 32).
+gs_status launch_brute_seed(const Database& A, unsigned nA, const Database& B, bool self,
+                            unsigned k, float* seed, cudaStream_t st);
 // The same lists over bucketed queries and candidates (the seed databases'
 // pos_id arrays), skipping chunks of 64 candidates beyond every bound of a
 // warp's queries; k <= 32 and a seed.  boxes: 2 * (ceil(nB / 64) +
