@@ -1213,7 +1213,7 @@ gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other) {
     // scan still sees every pair it needs and gives the same lists.  The
     // scan then runs over the seed databases' bucketed arrays and skips
     // chunks of candidates beyond every bound of a warp's queries.
-    if (out->k <= 32 && g->n >= 4096 && other->n > out->k) {
+    if (g->n >= 4096 && other->n > out->k) {
         if (!g->bf_tmp) GS_TRY(dalloc(&g->bf_tmp, 6));
         float ext[3];
         GS_TRY(abs_extent(other->position, other->n, g->bf_tmp, ext, st));

@@ -343,7 +343,6 @@ gs_status launch_knn_binned(const Database& A, unsigned nA, const Database& B, b
 }
 
 // ---- brute-force KNN (KNNBruteForceCudaKernel.cu:207-283) ---------------------------
-// Candidates are staged through shared memory in tiles of kBlock positions.
 // A candidate needs its square root only when its squared distance is within
 // a rounded-up bound of the current k-th distance squared: a larger squared
 // distance has a correctly rounded square root strictly above the k-th
@@ -353,51 +352,11 @@ __device__ __forceinline__ float prefilter_bound(unsigned long long thr) {
     return __fmul_ru(__fmul_ru(td, td), 1.000004f);
 }
 
-template <int KMAX>
-__global__ void __launch_bounds__(kBlock) k_knn_brute(const float4* __restrict__ posA,
-                                                      unsigned nA,
-                                                      const float4* __restrict__ posB,
-                                                      unsigned nB, bool self, unsigned k,
-                                                      unsigned* __restrict__ idx,
-                                                      float* __restrict__ dist) {
-    __shared__ float4 tile[kBlock];
-    const unsigned a = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = a < nA;
-    const V3 p = active ? v3(posA[a]) : v3(0.f, 0.f, 0.f);
-    KList<KMAX> L;
-    L.init(int(k));
-    float bound = prefilter_bound(L.key[KMAX - 1]);
-    for (unsigned base = 0; base < nB; base += kBlock) {
-        const unsigned j = base + threadIdx.x;
-        tile[threadIdx.x] = j < nB ? posB[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        __syncthreads();
-        const unsigned cnt = min(unsigned(kBlock), nB - base);
-        if (active) {
-            for (unsigned t = 0; t < cnt; ++t) {
-                const float4 q = tile[t];
-                const V3 o = sub(p, v3(q));
-                const float d2 = dot(o, o);
-                if (d2 <= bound) {
-                    const unsigned id = base + t;
-                    if (self && id == a) continue;
-                    L.insert(knn_key(sqrtf(d2), id), id);
-                    bound = prefilter_bound(L.key[KMAX - 1]);
-                }
-            }
-        }
-        __syncthreads();
-    }
-    if (!active) return;
-    L.for_each(int(k), [&](int r, unsigned long long key, unsigned) {
-        idx[a + size_t(r) * nA] = key_id(key);
-        dist[a + size_t(r) * nA] = key_dist(key);
-    });
-}
-
-// ---- brute force, FP32-pipe form (k <= 32) ----------------------------------------------
+// ---- brute force, FP32-pipe form (k <= 64) ----------------------------------------------
 // One warp serves kBruteQW queries and keeps each query's exact (distance,
-// index) top-k list spread over its lanes: lane r holds entry r, so the
-// list is sorted across the warp and its k-th key is one shuffle away.  The
+// index) top-k list spread over its lanes: lane r holds entry r (and entry
+// 32 + r for k > 32), so the list is sorted across the warp and its k-th key
+// is one shuffle away.  The
 // block stages kBruteTile candidates in shared memory as x / y / z arrays;
 // each lane takes two neighbouring candidates per step and computes their
 // squared distances to every query of its warp with packed f32x2 subtract,
@@ -441,19 +400,59 @@ __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigne
     return r;
 }
 
-// Inserts candidate (x, y, z, id) into the lane-distributed list `entry`
-// (lane r holds rank r < k) if its exact key is below the k-th; updates the
-// filter bound.  Every lane runs it with the same candidate.
-__device__ __forceinline__ void warp_list_insert(unsigned long long& entry, float& bound,
-                                                 float seed_bound, V3 q, float x, float y,
-                                                 float z, unsigned id, unsigned k,
-                                                 unsigned lane) {
+// A query's exact (distance, index) top-k list spread over the warp: lane r
+// holds rank r in e[0] and, with L = 2 (32 < k <= 64), rank 32 + r in e[1].
+// Ranks at or past k hold the empty key.
+template <int L>
+struct WarpList {
+    unsigned long long e[L];
+    __device__ __forceinline__ void init() {
+#pragma unroll
+        for (int h = 0; h < L; ++h) e[h] = KEY_EMPTY;
+    }
+    // the k-th key, on every lane (k is warp-uniform)
+    __device__ __forceinline__ unsigned long long kth(unsigned k) const {
+        if (L == 1 || k <= 32) return __shfl_sync(0xffffffffu, e[0], int(k) - 1);
+        return __shfl_sync(0xffffffffu, e[L - 1], int(k) - 33);
+    }
+};
+
+// Inserts candidate (x, y, z, id) into the lane-distributed list if its
+// exact key is below the k-th: each rank below k whose key is larger takes
+// the larger of the candidate and the rank before it (all from the old
+// list); updates the filter bound.  Every lane runs it with the same
+// candidate.
+template <int L>
+__device__ __forceinline__ void warp_list_insert(WarpList<L>& w, float& bound, float seed_bound,
+                                                 V3 q, float x, float y, float z, unsigned id,
+                                                 unsigned k, unsigned lane) {
     const unsigned long long key = knn_key(distance(q, v3(x, y, z)), id);
-    const unsigned long long kth = __shfl_sync(0xffffffffu, entry, int(k) - 1);
-    if (!(key < kth)) return;  // warp-uniform
-    const unsigned long long left = __shfl_up_sync(0xffffffffu, entry, 1);
-    if (lane < k && key < entry) entry = (lane == 0 || key > left) ? key : left;
-    bound = fminf(seed_bound, prefilter_bound(__shfl_sync(0xffffffffu, entry, int(k) - 1)));
+    if (!(key < w.kth(k))) return;  // warp-uniform
+    const unsigned long long left0 = __shfl_up_sync(0xffffffffu, w.e[0], 1);
+    if (L == 2) {
+        unsigned long long left1 = __shfl_up_sync(0xffffffffu, w.e[L - 1], 1);
+        const unsigned long long last0 = __shfl_sync(0xffffffffu, w.e[0], 31);
+        if (lane == 0) left1 = last0;  // rank 32 follows rank 31
+        if (32 + lane < k && key < w.e[L - 1]) w.e[L - 1] = key > left1 ? key : left1;
+    }
+    if (lane < k && key < w.e[0]) w.e[0] = (lane == 0 || key > left0) ? key : left0;
+    bound = fminf(seed_bound, prefilter_bound(w.kth(k)));
+}
+
+// Writes a warp list to idx / dist[a + rank * nA], ranks below k.
+template <int L>
+__device__ __forceinline__ void warp_list_store(const WarpList<L>& w, unsigned a, unsigned nA,
+                                                unsigned k, unsigned lane,
+                                                unsigned* __restrict__ idx,
+                                                float* __restrict__ dist) {
+#pragma unroll
+    for (int h = 0; h < L; ++h) {
+        const unsigned rank = 32u * h + lane;
+        if (rank < k) {
+            idx[a + size_t(rank) * nA] = key_id(w.e[h]);
+            dist[a + size_t(rank) * nA] = key_dist(w.e[h]);
+        }
+    }
 }
 
 // Rounded-up filter bound for a known upper bound d of the k-th distance.
@@ -465,12 +464,13 @@ __device__ __forceinline__ float seed_prefilter(float d) {
 // pair t0 + 2 lane, t0 + 2 lane + 1): the packed filter against every query
 // of the warp, then the exact insertion of the candidates that passed.  sid:
 // the staged candidates' indices (null: base + their position in the stage).
+template <int L>
 __device__ __forceinline__ void brute_chunk(
     const float* sx, const float* sy, const float* sz, const unsigned* sid, unsigned base,
     unsigned t0, unsigned cnt, unsigned lane, bool self, unsigned k, const V3 (&q)[kBruteQW],
     const unsigned (&qid)[kBruteQW], const unsigned long long (&px)[kBruteQW],
     const unsigned long long (&py)[kBruteQW], const unsigned long long (&pz)[kBruteQW],
-    unsigned long long (&entry)[kBruteQW], float (&bound)[kBruteQW],
+    WarpList<L> (&entry)[kBruteQW], float (&bound)[kBruteQW],
     const float (&seed_bound)[kBruteQW]) {
     const unsigned t = t0 + 2 * lane;
     const unsigned long long x2 = *reinterpret_cast<const unsigned long long*>(sx + t);
@@ -513,6 +513,7 @@ __device__ __forceinline__ void brute_chunk(
 // k-th distance among any subset of the candidates is one); the filter then
 // starts at that bound instead of infinity, so a query's list takes little
 // more than its k final entries.
+template <int L>
 __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
     const float4* __restrict__ posA, unsigned nA, const float4* __restrict__ posB, unsigned nB,
     bool self, unsigned k, const float* __restrict__ seed, unsigned* __restrict__ idx,
@@ -522,7 +523,8 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
     const unsigned q0 = (blockIdx.x * kBruteWarps + warp) * kBruteQW;
     V3 q[kBruteQW];
     unsigned qid[kBruteQW];
-    unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW], entry[kBruteQW];
+    unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW];
+    WarpList<L> entry[kBruteQW];
     float bound[kBruteQW], seed_bound[kBruteQW];
 #pragma unroll
     for (unsigned j = 0; j < kBruteQW; ++j) {
@@ -532,7 +534,7 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
         px[j] = pack2(q[j].x, q[j].x);
         py[j] = pack2(q[j].y, q[j].y);
         pz[j] = pack2(q[j].z, q[j].z);
-        entry[j] = KEY_EMPTY;
+        entry[j].init();
         seed_bound[j] = (act && seed) ? seed_prefilter(seed[q0 + j]) : prefilter_bound(KEY_EMPTY);
         bound[j] = act ? seed_bound[j] : -1.f;
     }
@@ -552,13 +554,8 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3(
                         entry, bound, seed_bound);
     }
 #pragma unroll
-    for (unsigned j = 0; j < kBruteQW; ++j) {
-        const unsigned qq = q0 + j;
-        if (qq < nA && lane < k) {
-            idx[qq + size_t(lane) * nA] = key_id(entry[j]);
-            dist[qq + size_t(lane) * nA] = key_dist(entry[j]);
-        }
-    }
+    for (unsigned j = 0; j < kBruteQW; ++j)
+        if (q0 + j < nA) warp_list_store(entry[j], q0 + j, nA, k, lane, idx, dist);
 }
 
 // ---- brute force over bucketed candidates: chunks beyond every bound skipped ---------
@@ -694,16 +691,19 @@ __global__ void __launch_bounds__(kBlock) k_brute_seed(const float4* __restrict_
 gs_status launch_brute_seed(const Database& A, unsigned nA, const Database& B, bool self,
                             unsigned k, float* seed, cudaStream_t st) {
     if (nA == 0) return GS_OK;
-    if (k == 0 || k > 32)
-        return fail(GS_ERR_UNSUPPORTED, "the brute-force seed needs 1 <= k <= 32");
+    if (k == 0 || k > 64)
+        return fail(GS_ERR_UNSUPPORTED, "the brute-force seed needs 1 <= k <= 64");
     if (k <= 8)
         k_brute_seed<8><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id, B.grid,
                                                            k, self, seed);
     else if (k <= 16)
         k_brute_seed<16><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id,
                                                             B.grid, k, self, seed);
-    else
+    else if (k <= 32)
         k_brute_seed<32><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id,
+                                                            B.grid, k, self, seed);
+    else
+        k_brute_seed<64><<<blocks_for(nA), kBlock, 0, st>>>(A.pos_id, nA, B.start, B.pos_id,
                                                             B.grid, k, self, seed);
     GS_LAUNCHED("brute_seed");
     return GS_OK;
@@ -724,6 +724,7 @@ __device__ __forceinline__ float box_dist_sq(V3 q, float4 lo, float4 hi) {
 // (query, candidate) pairs the packed filter ran on.
 // sboxes: the boxes of the stages (32 chunks each), tested first, 32 stages
 // at a time, so that a block visits only the stages some query may need.
+template <int L>
 __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3_bucketed(
     const float4* __restrict__ qpos, unsigned nA, const float4* __restrict__ cpos, unsigned nB,
     const float4* __restrict__ boxes, const float4* __restrict__ sboxes, bool self, unsigned k,
@@ -736,7 +737,8 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3_bucketed(
     const unsigned s0 = (blockIdx.x * kBruteWarps + warp) * kBruteQW;
     V3 q[kBruteQW];
     unsigned qid[kBruteQW];
-    unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW], entry[kBruteQW];
+    unsigned long long px[kBruteQW], py[kBruteQW], pz[kBruteQW];
+    WarpList<L> entry[kBruteQW];
     float bound[kBruteQW], seed_bound[kBruteQW];
     unsigned active = 0;
 #pragma unroll
@@ -749,7 +751,7 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3_bucketed(
         px[j] = pack2(q[j].x, q[j].x);
         py[j] = pack2(q[j].y, q[j].y);
         pz[j] = pack2(q[j].z, q[j].z);
-        entry[j] = KEY_EMPTY;
+        entry[j].init();
         seed_bound[j] = act ? seed_prefilter(seed[qid[j]]) : prefilter_bound(KEY_EMPTY);
         bound[j] = act ? seed_bound[j] : -1.f;
     }
@@ -810,12 +812,8 @@ __global__ void __launch_bounds__(kBruteWarps * 32) k_knn_brute3_bucketed(
         }
     }
 #pragma unroll
-    for (unsigned j = 0; j < kBruteQW; ++j) {
-        if (qid[j] < nA && lane < k) {
-            idx[qid[j] + size_t(lane) * nA] = key_id(entry[j]);
-            dist[qid[j] + size_t(lane) * nA] = key_dist(entry[j]);
-        }
-    }
+    for (unsigned j = 0; j < kBruteQW; ++j)
+        if (qid[j] < nA) warp_list_store(entry[j], qid[j], nA, k, lane, idx, dist);
 }
 
 gs_status launch_knn_brute_bucketed(const float4* qpos, unsigned nA, const float4* cpos,
@@ -823,8 +821,8 @@ gs_status launch_knn_brute_bucketed(const float4* qpos, unsigned nA, const float
                                     const float* seed, unsigned long long* evaluated,
                                     unsigned* idx, float* dist, cudaStream_t st) {
     if (nA == 0) return GS_OK;
-    if (k > 32 || seed == nullptr)
-        return fail(GS_ERR_UNSUPPORTED, "the bucketed brute force needs k <= 32 and a seed");
+    if (k == 0 || k > 64 || seed == nullptr)
+        return fail(GS_ERR_UNSUPPORTED, "the bucketed brute force needs 1 <= k <= 64 and a seed");
     const unsigned chunks = (nB + 63) / 64, stages = (chunks + 31) / 32;
     float4* sboxes = boxes + 2 * size_t(chunks);
     if (chunks) {
@@ -833,9 +831,13 @@ gs_status launch_knn_brute_bucketed(const float4* qpos, unsigned nA, const float
         k_chunk_boxes<<<(stages * 32 + kBlock - 1) / kBlock, kBlock, 0, st>>>(boxes, chunks, true,
                                                                                sboxes);
     }
-    const unsigned per_block = kBruteWarps * kBruteQW;
-    k_knn_brute3_bucketed<<<(nA + per_block - 1) / per_block, kBruteWarps * 32, 0, st>>>(
-        qpos, nA, cpos, nB, boxes, sboxes, self, k, seed, evaluated, idx, dist);
+    const unsigned per_block = kBruteWarps * kBruteQW, blocks = (nA + per_block - 1) / per_block;
+    if (k <= 32)
+        k_knn_brute3_bucketed<1><<<blocks, kBruteWarps * 32, 0, st>>>(
+            qpos, nA, cpos, nB, boxes, sboxes, self, k, seed, evaluated, idx, dist);
+    else
+        k_knn_brute3_bucketed<2><<<blocks, kBruteWarps * 32, 0, st>>>(
+            qpos, nA, cpos, nB, boxes, sboxes, self, k, seed, evaluated, idx, dist);
     GS_LAUNCHED("knn_brute_bucketed");
     return GS_OK;
 }
@@ -876,13 +878,14 @@ gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, 
                            bool self, unsigned k, const float* seed, unsigned* idx, float* dist,
                            cudaStream_t st) {
     if (nA == 0) return GS_OK;
-    if (k <= 32) {
-        const unsigned per_block = kBruteWarps * kBruteQW;
-        k_knn_brute3<<<(nA + per_block - 1) / per_block, kBruteWarps * 32, 0, st>>>(
-            posA, nA, posB, nB, self, k, seed, idx, dist);
-    } else {
-        k_knn_brute<64><<<blocks_for(nA), kBlock, 0, st>>>(posA, nA, posB, nB, self, k, idx, dist);
-    }
+    if (k == 0 || k > 64) return fail(GS_ERR_UNSUPPORTED, "brute force needs 1 <= k <= 64");
+    const unsigned per_block = kBruteWarps * kBruteQW, blocks = (nA + per_block - 1) / per_block;
+    if (k <= 32)
+        k_knn_brute3<1><<<blocks, kBruteWarps * 32, 0, st>>>(posA, nA, posB, nB, self, k, seed,
+                                                             idx, dist);
+    else
+        k_knn_brute3<2><<<blocks, kBruteWarps * 32, 0, st>>>(posA, nA, posB, nB, self, k, seed,
+                                                             idx, dist);
     GS_LAUNCHED("knn_brute");
     return GS_OK;
 }

@@ -53,17 +53,17 @@ struct KnnPairs {
     unsigned r, n_pairs;
 };
 gs_status launch_knn_binned_pairs(KnnPairs& P, cudaStream_t st);
-// seed (may be null, k <= 32 only): per query of A an upper bound of its k-th distance.
+// seed (may be null): per query of A an upper bound of its k-th distance.
 gs_status launch_knn_brute(const float4* posA, unsigned nA, const float4* posB, unsigned nB,
                            bool self, unsigned k, const float* seed, unsigned* idx, float* dist,
                            cudaStream_t st);
 // Per query of A (by agent index) an upper bound of its k-th distance to B's
-// agents: the k-th among the candidates of a box of cells (1 <= k <= 32).
+// agents: the k-th among the candidates of a box of cells (1 <= k <= 64).
 gs_status launch_brute_seed(const Database& A, unsigned nA, const Database& B, bool self,
                             unsigned k, float* seed, cudaStream_t st);
 // The same lists over bucketed queries and candidates (the seed databases'
 // pos_id arrays), skipping chunks of 64 candidates beyond every bound of a
-// warp's queries; k <= 32 and a seed.  boxes: 2 * (ceil(nB / 64) +
+// warp's queries; k <= 64 and a seed.  boxes: 2 * (ceil(nB / 64) +
 // ceil(nB / 2048)) float4 of scratch (chunk, then stage boxes); evaluated
 // (may be null) adds the pairs the filter ran on.
 gs_status launch_knn_brute_bucketed(const float4* qpos, unsigned nA, const float4* cpos,

@@ -270,9 +270,9 @@ gs_status gs_multigroup_step(const gs_group* groups, unsigned n_groups, gs_bins 
 gs_status gs_find_knn_walls(gs_group g, gs_knn out, gs_bins bins, gs_walls walls,
                             unsigned search_radius);
 /* KNNBruteForceCUDAV2 (KNNBruteForceCUDA.cu:163-187).  The lists are the
- * reference's for every pair of groups; with k <= 32 and 4,096 queries or
- * more the scan skips candidates that cannot enter a list (a seeded bound
- * and bucketed chunks), so a call evaluates far fewer than n * m pairs. */
+ * reference's for every pair of groups; with 4,096 queries or more the
+ * scan skips candidates that cannot enter a list (a seeded bound and
+ * bucketed chunks), so a call evaluates far fewer than n * m pairs. */
 gs_status gs_knn_bruteforce(gs_group g, gs_knn out, gs_group other);
 /* The (query, candidate) pairs the last gs_knn_bruteforce call of g ran its
  * distance filter on (n * m without the skipping scan).  Synchronises the

@@ -158,11 +158,12 @@ def test_knn_bruteforce_matches_oracle_larger():
         assert 0 < gs.bruteforce_pairs(A) < A.size * A.size // 4
 
 
-@pytest.mark.parametrize("k", [1, 8, 16, 24, 32, 40])
+@pytest.mark.parametrize("k", [1, 8, 16, 24, 32, 33, 40, 64])
 def test_knn_bruteforce_sizes_ties_and_cross_groups(k):
     """Group sizes that are not multiples of the 64-query block or of the
     eight candidate slices, an integer lattice with duplicated points (exact
-    distance ties, broken by the lower index), and a cross-group search."""
+    distance ties, broken by the lower index), and a cross-group search; k
+    past 32 keeps two list entries per lane."""
     rng = np.random.default_rng(k)
     g3 = np.stack(np.meshgrid(np.arange(9), np.arange(9), np.arange(9), indexing="ij"), -1)
     lat = g3.reshape(-1, 3).astype(np.float32) - 4.0
@@ -181,7 +182,7 @@ def test_knn_bruteforce_sizes_ties_and_cross_groups(k):
         np.testing.assert_array_equal(d, od)
 
 
-@pytest.mark.parametrize("k", [8, 16, 32])
+@pytest.mark.parametrize("k", [8, 16, 32, 48, 64])
 def test_knn_bruteforce_seeded_large_groups(k):
     """Groups of 4,096 and more take the seeded filter (k-th distance of a
     binned search on an automatic grid): a lattice with duplicates (ties), a
