@@ -396,3 +396,30 @@ def test_parameter_blocks_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for field, _ in cls._fields_:
             assert got[(cname, field)] == getattr(cls, field).offset, (cname, field)
+
+
+def test_chunk_box_distance_bounds_every_inside_candidate():
+    """The bucketed brute force skips a chunk of candidates when the squared
+    distance from a query to the chunk's bounding box, in the reference's
+    unfused binary32 operations, exceeds the filter bound.  That is safe
+    because the box's value is at most every inside candidate's exact squared
+    distance: per axis fl(lo - q) or fl(q - hi) is at most |fl(q - c)|
+    (rounding is monotone), and so are the squares and the sums.  Checked
+    here in float32 numpy arithmetic on boxes that are points, on ones that
+    straddle the query, and across magnitudes from 1e-3 to 1e18."""
+    rng = np.random.default_rng(5)
+    f = np.float32
+    for scale in (1e-3, 1.0, 512.0, 1e6, 1e18):
+        q = (rng.uniform(-1, 1, (4000, 3)) * scale).astype(f)
+        c = (rng.uniform(-1, 1, (4000, 32, 3)) * scale).astype(f)
+        c[::7] = c[::7, :1]                      # every candidate at one point
+        c[1::7] += q[1::7, None, :] - c[1::7, :1]  # the query on the box's corner
+        lo, hi = c.min(axis=1), c.max(axis=1)
+        zero = f(0)
+        gap = np.maximum(np.maximum(lo - q, q - hi), zero)
+        box = (gap[:, 0] * gap[:, 0] + gap[:, 1] * gap[:, 1]) + gap[:, 2] * gap[:, 2]
+        o = q[:, None, :] - c
+        d2 = (o[..., 0] * o[..., 0] + o[..., 1] * o[..., 1]) + o[..., 2] * o[..., 2]
+        assert box.dtype == np.float32 and d2.dtype == np.float32
+        finite = np.isfinite(d2)
+        assert (box[:, None] <= d2)[finite].all()
