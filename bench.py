@@ -1015,7 +1015,10 @@ def gpu_brute_line(args, dist, rank, world, local_rank):
         "config": brute_config(n, k, world),
         "e2e": {"value": n * e2e_steps * world / e2e_s, "unit": "agent-queries/s",
                 "h2d_bytes_per_step": n * 96, "d2h_bytes_per_step": n * k * 8},
-        "gpu_launches": args.steps,
+        # per call: the extent, the seed database (count, three scan
+        # launches, scatter), the seed, chunk and stage boxes, the scan
+        # (profiles/k_knn_brute3_65536_agents.md lists them)
+        "gpu_launches": 10 * args.steps,
         "roofline": {"bound": "fp32", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
                      "frac": tflops / peak, "traffic": None, "kernel": "k_knn_brute3_bucketed",
                      "algorithmic_flops_per_launch": 8.0 * pairs,

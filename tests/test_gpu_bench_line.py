@@ -36,3 +36,22 @@ def test_bench_line_keeps_the_contract():
     assert rf["bound"] == "hbm" and rf["peak"] > 0 and 0 < rf["frac"] < 1.5
     assert d["gpu_launches"] == d["forms"]["separate"]["launches_per_step"] * 2 * 4
     assert "sm_mhz" in d["clocks"]
+
+
+def test_brute_line_counts_the_pairs_it_filters():
+    """The brute-force workload's line: agent-queries/s of the 65,536-agent
+    call, with the pairs its distance filter ran on well below a full scan's
+    (the bucketed scan skips chunks beyond every bound) and its issue rate."""
+    cmd = [sys.executable, str(REPO / "bench.py"), "--workload", "brute", "--steps", "3",
+           "--warmup", "3", "--no-cpu"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["metric"] == "agent-queries/s" and d["value"] > 0
+    rf = d["roofline"]
+    assert 0 < rf["pairs_evaluated"] < rf["pairs_all"] / 10
+    assert rf["pairs_all"] == 65536.0 * 65535
+    assert d["issue"] is not None and 0 < d["issue"]["frac"] < 1.5
+    assert d["gpu_launches"] == 10 * 3  # ten launches per call
