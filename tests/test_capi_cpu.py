@@ -423,3 +423,103 @@ def test_chunk_box_distance_bounds_every_inside_candidate():
         assert box.dtype == np.float32 and d2.dtype == np.float32
         finite = np.isfinite(d2)
         assert (box[:, None] <= d2)[finite].all()
+
+
+def _ru_mul(a, b):
+    """binary32 a * b rounded up (the float64 product of two binary32 values
+    is exact)."""
+    prod = np.float64(a) * np.float64(b)
+    x = np.float32(prod)
+    return np.nextafter(x, np.float32(np.inf)) if np.float64(x) < prod else x
+
+
+def _bucketed_brute_lists(pos, k, per_axis):
+    """A restatement of the bucketed brute force's pruning for self searches:
+    per query the seed (k-th distance among the candidates of its 3 x 3 x 3
+    cells, widened to 5 x 5 x 5 and 9 x 9 x 9 when they hold fewer than k),
+    the filter bound rounded up from it, chunks of 64 bucketed candidates
+    skipped for a warp of four bucketed queries when their box's squared
+    distance exceeds every query's bound; then each query's (distance, index)
+    top k among the candidates of the chunks its warp kept."""
+    f = np.float32
+    p = pos[:, :3].astype(f)
+    n = p.shape[0]
+    lo_w, hi_w = p.min(0), p.max(0)
+    cell3 = np.clip(((p - lo_w) / (hi_w - lo_w + f(1e-3)) * per_axis).astype(np.int64), 0,
+                    per_axis - 1)
+    cell = (cell3[:, 1] * per_axis + cell3[:, 2]) * per_axis + cell3[:, 0]
+    order = np.argsort(cell, kind="stable")          # bucket order
+    bp, bc3 = p[order], cell3[order]
+
+    def dist(q, c):
+        o = q - c
+        return np.sqrt((o[..., 0] * o[..., 0] + o[..., 1] * o[..., 1]) + o[..., 2] * o[..., 2])
+
+    bound = np.empty(n, f)
+    for s in range(n):
+        for r in (1, 2, 4):
+            near = np.all(np.abs(bc3 - bc3[s]) <= r, axis=1)
+            near[s] = False
+            d = dist(bp[s], bp[near])
+            if d.size >= k:
+                kth = np.partition(d, k - 1)[k - 1]
+                bound[s] = _ru_mul(_ru_mul(kth, kth), f(1.000004))
+                break
+        else:
+            bound[s] = np.inf
+    chunks = (n + 63) // 64
+    clo = np.stack([bp[c * 64:(c + 1) * 64].min(0) for c in range(chunks)])
+    chi = np.stack([bp[c * 64:(c + 1) * 64].max(0) for c in range(chunks)])
+    out_idx = np.empty((k, n), np.uint32)
+    out_dist = np.empty((k, n), f)
+    kept = 0
+    for w0 in range(0, n, 4):
+        qs = range(w0, min(w0 + 4, n))
+        keep = np.zeros(chunks, bool)
+        for s in qs:
+            gap = np.maximum(np.maximum(clo - bp[s], bp[s] - chi), f(0))
+            box = (gap[:, 0] * gap[:, 0] + gap[:, 1] * gap[:, 1]) + gap[:, 2] * gap[:, 2]
+            keep |= box <= bound[s]
+        kept += int(keep.sum())
+        cand = np.concatenate([np.arange(c * 64, min(c * 64 + 64, n))
+                               for c in np.flatnonzero(keep)])
+        for s in qs:
+            c = cand[cand != s]
+            d = dist(bp[s], bp[c])
+            ids = order[c].astype(np.uint32)
+            pick = np.lexsort((ids, d))[:k]
+            a = order[s]
+            out_idx[:, a] = ids[pick]
+            out_dist[:, a] = d[pick]
+    return out_idx.reshape(-1), out_dist.reshape(-1), kept / (chunks * ((n + 3) // 4))
+
+
+@pytest.mark.parametrize("case", ["cube", "lattice", "flat", "clusters"])
+def test_bucketed_brute_force_pruning_keeps_every_list(case):
+    """The bucketed brute force's seed and chunk skipping, restated on the CPU,
+    give the oracle's full-scan lists: uniform, lattice with duplicated
+    points (distance ties broken by the lower index), flat 2D crowd and
+    tight clusters, at k = 8, 16 and 40."""
+    rng = np.random.default_rng(11)
+    if case == "cube":
+        pos = sc.boids_cube(2500, size=64.0, seed=3).position
+    elif case == "lattice":
+        g3 = np.stack(np.meshgrid(*(np.arange(12),) * 3, indexing="ij"), -1)
+        lat = g3.reshape(-1, 3).astype(np.float32) - 6.0
+        lat = np.concatenate([lat, lat[::5]])
+        pos = np.zeros((lat.shape[0], 4), np.float32)
+        pos[:, :3] = lat
+    elif case == "flat":
+        pos = sc.chokepoint_agents(2500, seed=4).position
+    else:
+        centres = rng.uniform(-200, 200, (6, 3))
+        pts = centres[rng.integers(0, 6, 2400)] + rng.normal(0, 2.0, (2400, 3))
+        pos = np.zeros((2400, 4), np.float32)
+        pos[:, :3] = pts
+    pos = np.ascontiguousarray(pos, np.float32)
+    for k in (8, 16, 40):
+        want_i, want_d = ol.knn_brute(pos, pos, True, k)
+        got_i, got_d, kept = _bucketed_brute_lists(pos, k, per_axis=11)
+        np.testing.assert_array_equal(got_i, want_i)
+        np.testing.assert_array_equal(got_d, want_d)
+        assert kept < 0.5, kept  # the pruning is not vacuous
